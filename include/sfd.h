@@ -1,0 +1,200 @@
+/*
+ * sfd.h -- C ABI of the GB300 boundary-integral engine (libsfd.so).
+ *
+ * Drop-in replacement for the CuSuperHelium Roberts-1983 boundary-integral
+ * right-hand side and its RK4 time step.  Plain C types only: host pointers,
+ * device pointers (as void*), sizes.  All functions return 0 on success and a
+ * negative SFD_ERR_* code on failure; sfd_last_error() gives the message of the
+ * calling thread's last failure.  Nothing here exits the process.
+ *
+ * Two groups of entry points:
+ *  1. Reference-compatible exports: the exact signatures the reference's
+ *     ctypes layer binds (CuSuperHelium/Python/integration/rhs.py:93-350),
+ *     with the reference's SI-unit handling (adimensionalizeProperties,
+ *     CuSuperHelium/CuSuperHelium/Export.cu:1222-1246) and finite-depth helium
+ *     physics.  Each declaration cites the reference export it replaces.
+ *  2. Engine API (sfd_*): a persistent handle that owns device buffers, so a
+ *     time loop pays set-up once; nondimensional units; water or helium per
+ *     surface; uneven-N batches; FP64 or mixed precision.
+ */
+#ifndef SFD_H
+#define SFD_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+#define SFD_BOOL bool
+extern "C" {
+#else
+#define SFD_BOOL _Bool
+#endif
+
+/* ------------------------------------------------------------ error codes */
+#define SFD_OK 0
+#define SFD_ERR_INVALID (-1)     /* bad argument (null pointer, unsupported size, ...) */
+#define SFD_ERR_CUDA (-2)        /* a CUDA runtime call failed                          */
+#define SFD_ERR_NUMERICS (-3)    /* non-finite values or solver breakdown (see status)  */
+#define SFD_ERR_NO_DEVICE (-4)   /* no usable CUDA device                               */
+
+/* ------------------------------------------------------------ physics */
+#define SFD_WATER 0              /* WaterBoundaryProblem  (createMKernel path)          */
+#define SFD_HELIUM 1             /* HeliumBoundaryProblem (createFiniteDepthMKernel)    */
+
+#define SFD_PRECISION_FP64 0     /* every stage in FP64 (LU without exchanges)          */
+#define SFD_PRECISION_MIXED 1    /* FP32 preconditioner + double-float/FP64 refinement  */
+
+/* per-surface status bits (sfd_get_status) */
+#define SFD_STATUS_NONFINITE 0x1u
+#define SFD_STATUS_PIVOT_SWAP 0x2u      /* |l_ij| > 1: partial pivoting would have exchanged rows */
+#define SFD_STATUS_ZERO_PIVOT 0x4u
+#define SFD_STATUS_REFINE_STALL 0x8u
+
+/* Nondimensional physics of one surface; mirrors the fields of
+ * ProblemProperties (CuSuperHelium/CuSuperHelium/ProblemProperties.hpp:5-32)
+ * that the hot path reads, plus explicit A3 and g. */
+typedef struct sfd_problem {
+    int physics;          /* SFD_WATER or SFD_HELIUM                                     */
+    int infinite_depth;   /* helium: drop the image terms (ProblemProperties.infinite_depth) */
+    double rho;           /* water density ratio (the configs use 0)                     */
+    double depth;         /* helium film thickness h                                     */
+    double A3;            /* helium van der Waals constant; <= 0 selects the reference's h^4/3 */
+    double gravity;       /* water g; <= 0 selects 1                                     */
+    double U;             /* uniform stream (linear part of phi only; the configs use 0) */
+    double kappa;         /* surface tension (helium Bernoulli variant; 0 = off)         */
+    int use_expansions;   /* helium Bernoulli as a series in y (createM.cuh:171-193)      */
+    int expansion_order;  /* 1..3                                                        */
+} sfd_problem;
+
+typedef struct sfd_options {
+    int precision;        /* SFD_PRECISION_FP64 or SFD_PRECISION_MIXED                   */
+    int refine_iters;     /* mixed: correction iterations per RK stage (default 3)       */
+    int refactor_every;   /* mixed: rebuild the preconditioner every k RK4 steps (1)     */
+    int use_graphs;       /* capture one RK4 step in a CUDA graph (1)                    */
+    int device;           /* CUDA device ordinal (0)                                     */
+} sfd_options;
+
+typedef struct sfd_engine sfd_engine;
+
+/* ------------------------------------------------------------ engine API */
+void sfd_default_options(sfd_options* opts);
+void sfd_default_problem(sfd_problem* prob);   /* water, rho = 0, g = 1 */
+
+/* Create an engine for `nsurf` surfaces with n[s] nodes each (1 <= n <= 8192).
+ * `problems` holds one entry per surface (or one entry for all when
+ * `shared_problem` != 0).  Replaces the constructor chain
+ * BoundaryProblem -> BaseBoundaryIntegralCalculator<N,batch> ->
+ * AutonomousRungeKuttaStepper<std_complex,2N>
+ * (BaseBoundaryIntegrator.cuh:88-108, AutonomousRungeKuttaStepper.cuh:91-105). */
+int sfd_create(const int* n, int nsurf, const sfd_problem* problems, int shared_problem,
+               const sfd_options* opts, sfd_engine** out);
+int sfd_destroy(sfd_engine* e);
+/* Use a caller stream (0 = the engine's own). */
+int sfd_set_stream(sfd_engine* e, void* cuda_stream);
+int sfd_total_nodes(const sfd_engine* e);
+
+/* State = concatenated per-surface nodes, SoA: x[ntot], y[ntot], phi[ntot]. */
+int sfd_set_state_host(sfd_engine* e, const double* x, const double* y, const double* phi);
+int sfd_get_state_host(sfd_engine* e, double* x, double* y, double* phi);
+/* Same with device pointers (each ntot doubles). */
+int sfd_set_state_device(sfd_engine* e, const void* x, const void* y, const void* phi);
+int sfd_get_state_device(sfd_engine* e, void* x, void* y, void* phi);
+/* Device address of the engine's resident state [x | y | phi] (3 * ntot doubles). */
+int sfd_state_device_ptr(sfd_engine* e, void** state);
+
+/* One RHS evaluation of the current state (BaseBoundaryIntegralCalculator::run,
+ * BaseBoundaryIntegrator.cuh:137-314): dx, dy = lower-fluid velocity
+ * (dz/dt), dphi = Bernoulli right-hand side.  Optional diagnostics (nullable):
+ * a = vortex strength, zp / zpp = interleaved complex z', z'' (per index). */
+int sfd_rhs_host(sfd_engine* e, double* dx, double* dy, double* dphi, double* a, double* zp, double* zpp);
+/* Same on device pointers: state_in and rhs_out are [x|y|phi] / [dx|dy|dphi]. */
+int sfd_rhs_device(sfd_engine* e, const void* state_in, void* rhs_out);
+
+/* `steps` classic RK4 steps of size dt on the resident state
+ * (AutonomousRungeKuttaStepper<std_complex,2N>::runStep, :123-307). */
+int sfd_rk4_steps(sfd_engine* e, double dt, int steps);
+/* Enqueue without waiting for completion (timed loops). */
+int sfd_rk4_steps_async(sfd_engine* e, double dt, int steps);
+int sfd_synchronize(sfd_engine* e);
+
+/* Invariants of the current state, 5 doubles per surface: kinetic, potential
+ * (gravitational or van der Waals), surface, volume flux (Energies.cuh:136-204)
+ * and mass = sum y x'.  `kappa` scales the surface energy as in the reference. */
+int sfd_invariants(sfd_engine* e, double kappa, double* out);
+
+/* Per-surface status words (SFD_STATUS_* bits), max |l_ij| of the last
+ * factorisation and max |residual| of the last refinement (each nullable). */
+int sfd_get_status(sfd_engine* e, unsigned int* status, double* lmax, double* rnorm);
+int sfd_clear_status(sfd_engine* e);
+
+/* Number of kernel launches the engine issued since creation (graph replays
+ * count every kernel node). */
+long long sfd_kernel_launches(const sfd_engine* e);
+
+/* Per-kernel-class device time: while enabled, RK4 steps run eagerly (no
+ * graph) and every kernel launch is bracketed by CUDA events on the engine
+ * stream; sfd_profile_read returns accumulated milliseconds and launch counts
+ * per class (names from sfd_profile_class_name; 15 classes). */
+#define SFD_PROFILE_CLASSES 15
+int sfd_profile(sfd_engine* e, int enable);
+int sfd_profile_read(sfd_engine* e, double* ms, long long* counts, int nclass);
+const char* sfd_profile_class_name(int cls);
+
+const char* sfd_last_error(void);
+const char* sfd_version(void);
+
+/* Precision used by the reference-compatible exports below (default FP64). */
+int sfd_set_default_precision(int precision);
+
+/* ------------------------------------------------------------ reference-compatible exports */
+/* CuSuperHelium/CuSuperHelium/Export.cuh:31 (Export.cu:560-599, :194-265). */
+int calculateRHSFromVectors(const double* x, const double* y, const double* phi, double* vx, double* vy,
+                            double* rhsPhi, double L, double rho, double kappa, double depth, size_t N);
+/* Export.cuh:30 */
+int calculateRHS256FromVectors(const double* x, const double* y, const double* phi, double* vx, double* vy,
+                               double* rhsPhi, double L, double rho, double kappa, double depth);
+/* Export.cuh:33 */
+int calculateRHS2048FromVectors(const double* x, const double* y, const double* phi, double* vx, double* vy,
+                                double* rhsPhi, double L, double rho, double kappa, double depth);
+/* Export.cuh:51 (Export.cu:520-557): inputs concatenated per surface (256 each). */
+int calculateRHS256FromVectorsBatched(const double* x, const double* y, const double* phi, double* vx, double* vy,
+                                      double* rhsPhi, double L, double rho, double kappa, double depth,
+                                      int batchSize);
+/* Export.cuh:48 (Export.cu:279-349): complex Z, phi (interleaved re, im);
+ * Zp / Zpp may be NULL. */
+int calculateVorticities256FromVectors(const double* Z, const double* phi, double* a, double* Zp, double* Zpp,
+                                       double L, double rho, double kappa, double depth);
+/* Export.cuh:49 (Export.cu:351-384): spectral first derivative of 256 complex
+ * samples (no linear part, no 2 pi / N scale). */
+int calculateDerivativeFFT256(const double* input, double* output);
+
+/* SimProperties / RK4SolverOptions (CuSuperHelium/CuSuperHelium/ExportTypes.cuh:8-40). */
+typedef struct SimProperties {
+    double L;
+    double rho;
+    double kappa;
+    double depth;
+    SFD_BOOL use_expansions;
+    int expansion_order;
+    SFD_BOOL infinite_depth;
+} SimProperties;
+typedef struct RK4SolverOptions {
+    double timeStep;
+    double t0;
+    double t1;
+    SFD_BOOL returnTrajectory;
+} RK4SolverOptions;
+
+/* Export.cuh:69 (Export.cu:767-770 is a stub there that returns 0 without
+ * integrating; this one integrates).  initialState = [x | y | phi] (3N);
+ * statesOut receives the initial state and the state after every step when
+ * returnTrajectory, else only the final state; free with the next function. */
+int integrateSimulationRK4(double* initialState, double** statesOut, size_t* statesCount, double** timesOut,
+                           size_t* timesCount, SimProperties* simProperties, RK4SolverOptions* rkOptions, size_t N);
+/* Export.cuh:70 */
+int integrateSimulationRK4_freeMemory(double* statesOut, double* timesOut);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SFD_H */

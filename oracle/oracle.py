@@ -1,0 +1,237 @@
+"""ctypes front end of the CPU FP64 oracle (sfd_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() and by
+bench.py's CPU-baseline leg, always as the checker.  The product library never
+imports this module.
+
+The oracle restates the reference's FP64 boundary-integral path
+(CuSuperHelium/CuSuperHelium/*.cuh); each C function cites the routine it
+follows.  Problems are described by :class:`Problem` (nondimensional units).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from dataclasses import dataclass
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_SRC = os.path.join(_HERE, "sfd_oracle.c")
+_BUILD = os.path.join(_HERE, "_build")
+_LIB_PATH = os.path.join(_BUILD, "libsfd_oracle.so")
+
+WATER = 0
+HELIUM = 1
+
+
+class _CProblem(ctypes.Structure):
+    _fields_ = [
+        ("physics", ctypes.c_int),
+        ("rho", ctypes.c_double),
+        ("depth", ctypes.c_double),
+        ("vdw", ctypes.c_double),
+        ("gravity", ctypes.c_double),
+        ("U", ctypes.c_double),
+        ("infinite_depth", ctypes.c_int),
+    ]
+
+
+@dataclass
+class Problem:
+    """Nondimensional physics of one surface.
+
+    physics: WATER (createMKernel path) or HELIUM (finite-depth path).
+    A3: van der Waals constant; None means the reference's fixed h^4/3.
+    """
+
+    physics: int = WATER
+    rho: float = 0.0
+    depth: float = 1.0
+    A3: float | None = None
+    gravity: float = 1.0
+    U: float = 0.0
+    infinite_depth: bool = False
+
+    @property
+    def vdw(self) -> float:
+        if self.A3 is None:
+            return self.depth / 3.0
+        return self.A3 / self.depth ** 3
+
+    def to_c(self) -> _CProblem:
+        return _CProblem(self.physics, self.rho, self.depth, self.vdw, self.gravity, self.U,
+                         1 if self.infinite_depth else 0)
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle into oracle/_build (gcc, OpenMP, no -march flags)."""
+    os.makedirs(_BUILD, exist_ok=True)
+    if force or not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(_SRC):
+        tmp = _LIB_PATH + f".tmp{os.getpid()}"
+        subprocess.check_call(["gcc", "-O2", "-fopenmp", "-fPIC", "-shared", "-std=c11",
+                               "-o", tmp, _SRC, "-lm"])
+        os.replace(tmp, _LIB_PATH)
+    return _LIB_PATH
+
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        path = build()
+        L = ctypes.CDLL(path)
+        dp = ctypes.POINTER(ctypes.c_double)
+        ip = ctypes.POINTER(ctypes.c_int)
+        pp = ctypes.POINTER(_CProblem)
+        L.orc_fft.argtypes = [ctypes.c_int, dp, ctypes.c_int]
+        L.orc_fft_derivative.argtypes = [ctypes.c_int, dp, dp, ctypes.c_int, ctypes.c_double]
+        L.orc_zphi_derivative.argtypes = [ctypes.c_int, dp, dp, ctypes.c_double, ctypes.c_double, dp, dp, dp]
+        L.orc_create_M_water.argtypes = [ctypes.c_int, dp, dp, dp, ctypes.c_double, dp]
+        L.orc_create_M_helium.argtypes = [ctypes.c_int, dp, dp, dp, ctypes.c_double, ctypes.c_int, dp]
+        L.orc_lu_factor.argtypes = [ctypes.c_int, dp, ip]
+        L.orc_lu_factor.restype = ctypes.c_int
+        L.orc_lu_solve.argtypes = [ctypes.c_int, dp, ip, dp]
+        L.orc_velocities.argtypes = [ctypes.c_int, dp, dp, dp, dp, dp, ctypes.c_int, ctypes.c_double,
+                                     ctypes.c_int, ctypes.c_int, dp]
+        L.orc_rhs_phi_water.argtypes = [ctypes.c_int, dp, dp, dp, ctypes.c_double, ctypes.c_double, dp]
+        L.orc_rhs_phi_helium.argtypes = [ctypes.c_int, dp, dp, ctypes.c_double, ctypes.c_double, dp]
+        L.orc_rhs.argtypes = [pp, ctypes.c_int, dp, dp, dp, dp, dp, dp, dp, dp, dp]
+        L.orc_rhs.restype = ctypes.c_int
+        L.orc_rk4_step.argtypes = [pp, ctypes.c_int, ctypes.c_double, dp, dp, dp]
+        L.orc_rk4_step.restype = ctypes.c_int
+        L.orc_rk4_steps.argtypes = [pp, ctypes.c_int, ctypes.c_double, ctypes.c_int, dp, dp, dp]
+        L.orc_rk4_steps.restype = ctypes.c_int
+        L.orc_invariants.argtypes = [pp, ctypes.c_int, dp, dp, dp, dp, dp, ctypes.c_double, dp]
+        L.orc_cot_green.argtypes = [ctypes.c_double] * 4 + [dp]
+        L.orc_set_threads.argtypes = [ctypes.c_int]
+        L.orc_set_threads.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _f64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _c128(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.complex128)
+
+
+def cot_green(zk: complex, zj: complex) -> complex:
+    out = np.empty(2)
+    lib().orc_cot_green(zk.real, zk.imag, zj.real, zj.imag, _dp(out))
+    return complex(out[0], out[1])
+
+
+def set_threads(n: int) -> int:
+    return lib().orc_set_threads(int(n))
+
+
+def fft(data, inverse: bool = False) -> np.ndarray:
+    d = _c128(data).copy()
+    lib().orc_fft(d.size, _dp(d), 1 if inverse else -1)
+    return d
+
+
+def fft_derivative(data, second: bool = False, scale: float = 1.0) -> np.ndarray:
+    d = _c128(data)
+    out = np.empty_like(d)
+    lib().orc_fft_derivative(d.size, _dp(d), _dp(out), 1 if second else 0, float(scale))
+    return out
+
+
+def zphi_derivative(Z, Phi, rho: float = 0.0, U: float = 0.0):
+    Z = _c128(Z)
+    Phi = _c128(Phi)
+    n = Z.size
+    Zp = np.empty(n, np.complex128)
+    PhP = np.empty(n, np.complex128)
+    Zpp = np.empty(n, np.complex128)
+    lib().orc_zphi_derivative(n, _dp(Z), _dp(Phi), rho, U, _dp(Zp), _dp(PhP), _dp(Zpp))
+    return Zp, PhP, Zpp
+
+
+def create_M(problem: Problem, Z, Zp, Zpp) -> np.ndarray:
+    """Row-major M (row k, column j)."""
+    Z, Zp, Zpp = _c128(Z), _c128(Zp), _c128(Zpp)
+    n = Z.size
+    M = np.empty((n, n), np.float64)
+    if problem.physics == WATER:
+        lib().orc_create_M_water(n, _dp(Z), _dp(Zp), _dp(Zpp), problem.rho, _dp(M))
+    else:
+        lib().orc_create_M_helium(n, _dp(Z), _dp(Zp), _dp(Zpp), problem.depth,
+                                  1 if problem.infinite_depth else 0, _dp(M))
+    return M
+
+
+def lu_solve(M, b):
+    A = _f64(M).copy()
+    x = _f64(b).copy()
+    n = x.size
+    piv = np.empty(n, np.int32)
+    info = lib().orc_lu_factor(n, _dp(A), piv.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
+    lib().orc_lu_solve(n, _dp(A), piv.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _dp(x))
+    return x, info
+
+
+def velocities(problem: Problem, Z, Zp, Zpp, a, ap, lower: bool = True) -> np.ndarray:
+    Z, Zp, Zpp, ap = _c128(Z), _c128(Zp), _c128(Zpp), _c128(ap)
+    a = _f64(a)
+    n = Z.size
+    vel = np.empty(n, np.complex128)
+    lib().orc_velocities(n, _dp(Z), _dp(Zp), _dp(Zpp), _dp(a), _dp(ap),
+                         1 if problem.physics == HELIUM else 0, problem.depth,
+                         1 if problem.infinite_depth else 0, 1 if lower else 0, _dp(vel))
+    return vel
+
+
+def rhs_phi_water(Z, vlow, vup, rho: float = 0.0, g: float = 1.0) -> np.ndarray:
+    Z, vlow, vup = _c128(Z), _c128(vlow), _c128(vup)
+    out = np.empty(Z.size, np.float64)
+    lib().orc_rhs_phi_water(Z.size, _dp(Z), _dp(vlow), _dp(vup), rho, g, _dp(out))
+    return out
+
+
+def rhs_phi_helium(Z, vlow, h: float, vdw: float) -> np.ndarray:
+    Z, vlow = _c128(Z), _c128(vlow)
+    out = np.empty(Z.size, np.float64)
+    lib().orc_rhs_phi_helium(Z.size, _dp(Z), _dp(vlow), h, vdw, _dp(out))
+    return out
+
+
+def rhs(problem: Problem, x, y, phi, diagnostics: bool = False):
+    """One RHS evaluation: returns (dx, dy, dphi[, a, zp, zpp]) and the LU info."""
+    x, y, phi = _f64(x), _f64(y), _f64(phi)
+    n = x.size
+    dx, dy, dphi, a = (np.empty(n) for _ in range(4))
+    zp = np.empty(n, np.complex128)
+    zpp = np.empty(n, np.complex128)
+    cp = problem.to_c()
+    info = lib().orc_rhs(ctypes.byref(cp), n, _dp(x), _dp(y), _dp(phi), _dp(dx), _dp(dy), _dp(dphi),
+                         _dp(a), _dp(zp), _dp(zpp))
+    if diagnostics:
+        return (dx, dy, dphi, a, zp, zpp), info
+    return (dx, dy, dphi), info
+
+
+def rk4_steps(problem: Problem, x, y, phi, dt: float, steps: int):
+    x, y, phi = _f64(x).copy(), _f64(y).copy(), _f64(phi).copy()
+    cp = problem.to_c()
+    info = lib().orc_rk4_steps(ctypes.byref(cp), x.size, float(dt), int(steps), _dp(x), _dp(y), _dp(phi))
+    return (x, y, phi), info
+
+
+def invariants(problem: Problem, x, y, phi, u, v, kappa: float = 0.0) -> np.ndarray:
+    x, y, phi, u, v = _f64(x), _f64(y), _f64(phi), _f64(u), _f64(v)
+    out = np.empty(5)
+    cp = problem.to_c()
+    lib().orc_invariants(ctypes.byref(cp), x.size, _dp(x), _dp(y), _dp(phi), _dp(u), _dp(v), kappa, _dp(out))
+    return out

@@ -1,0 +1,125 @@
+"""ctypes binding of libsfd.so (include/sfd.h).
+
+The binding fails loudly when the compiled library is absent: there is no CPU
+fallback anywhere in the product path.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+from ctypes import POINTER, c_bool, c_char_p, c_double, c_int, c_longlong, c_size_t, c_uint, c_void_p
+
+from . import build as _build
+
+WATER = 0
+HELIUM = 1
+PRECISION_FP64 = 0
+PRECISION_MIXED = 1
+
+STATUS_NONFINITE = 0x1
+STATUS_PIVOT_SWAP = 0x2
+STATUS_ZERO_PIVOT = 0x4
+STATUS_REFINE_STALL = 0x8
+PROFILE_CLASSES = 15
+
+
+class SfdProblem(ctypes.Structure):
+    _fields_ = [("physics", c_int), ("infinite_depth", c_int), ("rho", c_double), ("depth", c_double),
+                ("A3", c_double), ("gravity", c_double), ("U", c_double), ("kappa", c_double),
+                ("use_expansions", c_int), ("expansion_order", c_int)]
+
+
+class SfdOptions(ctypes.Structure):
+    _fields_ = [("precision", c_int), ("refine_iters", c_int), ("refactor_every", c_int),
+                ("use_graphs", c_int), ("device", c_int)]
+
+
+class SimProperties(ctypes.Structure):
+    """ExportTypes.cuh:8-20 (the field order the reference's rhs.py binds)."""
+    _fields_ = [("L", c_double), ("rho", c_double), ("kappa", c_double), ("depth", c_double),
+                ("use_expansions", c_bool), ("expansion_order", c_int), ("infinite_depth", c_bool)]
+
+
+class RK4SolverOptions(ctypes.Structure):
+    """ExportTypes.cuh:35-40."""
+    _fields_ = [("timeStep", c_double), ("t0", c_double), ("t1", c_double), ("returnTrajectory", c_bool)]
+
+
+_dp = POINTER(c_double)
+_SIGS = {
+    "sfd_default_options": (None, [POINTER(SfdOptions)]),
+    "sfd_default_problem": (None, [POINTER(SfdProblem)]),
+    "sfd_create": (c_int, [POINTER(c_int), c_int, POINTER(SfdProblem), c_int, POINTER(SfdOptions), POINTER(c_void_p)]),
+    "sfd_destroy": (c_int, [c_void_p]),
+    "sfd_set_stream": (c_int, [c_void_p, c_void_p]),
+    "sfd_total_nodes": (c_int, [c_void_p]),
+    "sfd_set_state_host": (c_int, [c_void_p, _dp, _dp, _dp]),
+    "sfd_get_state_host": (c_int, [c_void_p, _dp, _dp, _dp]),
+    "sfd_set_state_device": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    "sfd_get_state_device": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    "sfd_state_device_ptr": (c_int, [c_void_p, POINTER(c_void_p)]),
+    "sfd_rhs_host": (c_int, [c_void_p, _dp, _dp, _dp, _dp, _dp, _dp]),
+    "sfd_rhs_device": (c_int, [c_void_p, c_void_p, c_void_p]),
+    "sfd_rk4_steps": (c_int, [c_void_p, c_double, c_int]),
+    "sfd_rk4_steps_async": (c_int, [c_void_p, c_double, c_int]),
+    "sfd_synchronize": (c_int, [c_void_p]),
+    "sfd_invariants": (c_int, [c_void_p, c_double, _dp]),
+    "sfd_get_status": (c_int, [c_void_p, POINTER(c_uint), _dp, _dp]),
+    "sfd_clear_status": (c_int, [c_void_p]),
+    "sfd_kernel_launches": (c_longlong, [c_void_p]),
+    "sfd_profile": (c_int, [c_void_p, c_int]),
+    "sfd_profile_read": (c_int, [c_void_p, _dp, POINTER(c_longlong), c_int]),
+    "sfd_profile_class_name": (c_char_p, [c_int]),
+    "sfd_last_error": (c_char_p, []),
+    "sfd_version": (c_char_p, []),
+    "sfd_set_default_precision": (c_int, [c_int]),
+    "calculateRHSFromVectors": (c_int, [_dp] * 6 + [c_double] * 4 + [c_size_t]),
+    "calculateRHS256FromVectors": (c_int, [_dp] * 6 + [c_double] * 4),
+    "calculateRHS2048FromVectors": (c_int, [_dp] * 6 + [c_double] * 4),
+    "calculateRHS256FromVectorsBatched": (c_int, [_dp] * 6 + [c_double] * 4 + [c_int]),
+    "calculateVorticities256FromVectors": (c_int, [_dp] * 5 + [c_double] * 4),
+    "calculateDerivativeFFT256": (c_int, [_dp, _dp]),
+    "integrateSimulationRK4": (c_int, [_dp, POINTER(_dp), POINTER(c_size_t), POINTER(_dp), POINTER(c_size_t),
+                                       POINTER(SimProperties), POINTER(RK4SolverOptions), c_size_t]),
+    "integrateSimulationRK4_freeMemory": (c_int, [_dp, _dp]),
+}
+
+_lib = None
+
+
+def header_symbols() -> list[str]:
+    """Function names declared in include/sfd.h."""
+    txt = open(os.path.join(_build.ROOT, "include", "sfd.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    names = re.findall(r"^\s*(?:[A-Za-z_][A-Za-z0-9_]*[\s*]+)+([A-Za-z_][A-Za-z0-9_]*)\s*\(", txt, flags=re.M)
+    return sorted(set(n for n in names if n not in ("if", "while", "return")))
+
+
+def load(build_if_missing: bool = True) -> ctypes.CDLL:
+    """Load (building first if needed) libsfd.so and bind every export."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if not os.path.exists(path) or not _build.up_to_date():
+        if not build_if_missing:
+            raise RuntimeError(f"libsfd.so not built at {path}; run superfluid_dynamics_gb300.build.build()")
+        _build.build()
+    L = ctypes.CDLL(path)
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+class SfdError(RuntimeError):
+    pass
+
+
+def check(rc: int) -> None:
+    if rc != 0:
+        msg = load().sfd_last_error()
+        raise SfdError(f"sfd error {rc}: {msg.decode() if msg else ''}")

@@ -1,0 +1,1040 @@
+// sfd_api.cu -- engine orchestration and the C ABI (include/sfd.h).
+//
+// One engine = one batch of surfaces resident in HBM.  An RHS evaluation is
+//   spectral derivatives -> node prep -> solve (FP64 LU, or mixed: FP32
+//   Gauss-Jordan preconditioner + double-float refinement) -> a' -> velocity
+//   and Bernoulli,
+// all enqueued on the engine stream with no host synchronisation; one RK4
+// step (4 evaluations + stage combines) is captured once into a CUDA graph and
+// replayed.  Host code never touches the per-stage data.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/sfd.h"
+#include "sfd_engine.cuh"
+#include "sfd_kernels.cuh"
+#include "sfd_solve.cuh"
+
+enum {
+  SFD_K_OTHER = 0,
+  SFD_K_SPECTRAL,
+  SFD_K_NODE,
+  SFD_K_SUMS64,
+  SFD_K_SUMSDF,
+  SFD_K_SUMS32,
+  SFD_K_EPILOGUE,
+  SFD_K_ASSEMBLE,
+  SFD_K_DIAG,
+  SFD_K_PANEL,
+  SFD_K_UPDATE,
+  SFD_K_TRSV,
+  SFD_K_GEMV,
+  SFD_K_VELOCITY,
+  SFD_K_RK4,
+  SFD_NCLASS
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+int g_default_precision = SFD_PRECISION_FP64;
+
+int set_error(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+int sfd_fail(cudaError_t e) { return set_error(SFD_ERR_CUDA, "CUDA error: %s", cudaGetErrorString(e)); }
+
+#define CK(expr)                                                                                        \
+  do {                                                                                                  \
+    cudaError_t _e = (expr);                                                                            \
+    if (_e != cudaSuccess)                                                                              \
+      return set_error(SFD_ERR_CUDA, "%s failed: %s (%s:%d)", #expr, cudaGetErrorString(_e), __FILE__, \
+                       __LINE__);                                                                       \
+  } while (0)
+
+template <typename T>
+cudaError_t dalloc(T** p, size_t count) {
+  *p = nullptr;
+  if (count == 0) return cudaSuccess;
+  return cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T));
+}
+
+// exp(-2 pi i e / n), computed in long double (80- or 128-bit) and rounded.
+std::vector<cd> twiddles(int n) {
+  std::vector<cd> t(n);
+  const long double two_pi = 6.283185307179586476925286766559005768L;
+  for (int e = 0; e < n; ++e) {
+    long double ang = two_pi * (long double)e / (long double)n;
+    t[e] = cd{(double)cosl(ang), (double)(-sinl(ang))};
+  }
+  // exact values at the quarter points
+  if (n % 4 == 0) {
+    t[0] = {1.0, 0.0};
+    t[n / 4] = {0.0, -1.0};
+    t[n / 2] = {-1.0, 0.0};
+    t[3 * n / 4] = {0.0, 1.0};
+  } else if (n % 2 == 0) {
+    t[0] = {1.0, 0.0};
+    t[n / 2] = {-1.0, 0.0};
+  } else {
+    t[0] = {1.0, 0.0};
+  }
+  return t;
+}
+
+// radices: 4s, then a 2, then odd primes ascending
+bool factorize(int n, std::vector<int>& rad) {
+  rad.clear();
+  while (n % 4 == 0) { rad.push_back(4); n /= 4; }
+  while (n % 2 == 0) { rad.push_back(2); n /= 2; }
+  for (int p = 3; n > 1; p += 2) {
+    while (n % p == 0) { rad.push_back(p); n /= p; }
+    if (p > 8192) return false;
+  }
+  return (int)rad.size() <= SFD_MAX_RADICES;
+}
+
+}  // namespace
+
+struct sfd_engine {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaStream_t own_stream = nullptr;
+  sfd_options opt{};
+  int nsurf = 0, ntot = 0, max_n = 0, max_np = 0, max_chunks = 0;
+  long long mat_elems = 0, panel_elems = 0;
+  bool any_rho = false;
+  std::vector<SurfaceDesc> hs;
+  SurfaceDesc* d_surf = nullptr;
+  int* d_node_surf = nullptr;
+  std::map<int, cd*> d_tw;
+  // work lists
+  int2* d_jobs_first = nullptr; int njobs_first = 0;
+  int2* d_jobs_ap = nullptr; int njobs_ap = 0;
+  int4* d_sum_items = nullptr; int nsum = 0;
+  int4* d_asm_tiles = nullptr; int nasm = 0;
+  int2* d_gemv_rows = nullptr; int ngemv = 0;
+  long long* d_poff = nullptr;
+  int max_blocks64 = 0, max_blocks128 = 0;
+  // state (each 3 * ntot): [x | y | phi]
+  double *y0 = nullptr, *ys = nullptr, *kacc = nullptr, *kcur = nullptr;
+  // stage data
+  cd *zp = nullptr, *zpp = nullptr, *ap = nullptr;
+  double *phip = nullptr, *a = nullptr, *r = nullptr, *delta = nullptr, *phi_im = nullptr;
+  NodeData nd{};
+  cd *part_s = nullptr, *part_t = nullptr, *cacc = nullptr, *dacc = nullptr, *vel_low1 = nullptr;
+  double* part_a = nullptr;
+  unsigned int* status = nullptr;
+  double *lmax = nullptr, *rnorm = nullptr, *inv_out = nullptr;
+  // matrices
+  double* m64 = nullptr;
+  float* m32 = nullptr;
+  float *pbuf = nullptr, *rbuf = nullptr, *cbuf = nullptr;
+  // graphs
+  cudaGraphExec_t g_step[2] = {nullptr, nullptr};
+  double g_dt = 0.0;
+  int g_kernels[2] = {0, 0};
+  long long step_count = 0;
+  long long launches = 0;
+  bool have_precond = false;
+  // per-kernel-class timing (eager launches only)
+  bool profile = false;
+  struct Pending {
+    int cls;
+    cudaEvent_t a, b;
+  };
+  std::vector<Pending> pending;
+  std::vector<cudaEvent_t> event_pool;
+  double class_ms[SFD_NCLASS] = {};
+  long long class_count[SFD_NCLASS] = {};
+};
+
+namespace {
+
+// ------------------------------------------------------------------ enqueue helpers
+int launch_check(sfd_engine* e) {
+  cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) return set_error(SFD_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString(err));
+  e->launches++;
+  return 0;
+}
+
+cudaEvent_t get_event(sfd_engine* e) {
+  if (!e->event_pool.empty()) {
+    cudaEvent_t ev = e->event_pool.back();
+    e->event_pool.pop_back();
+    return ev;
+  }
+  cudaEvent_t ev = nullptr;
+  cudaEventCreate(&ev);
+  return ev;
+}
+
+// Collect finished profile intervals (called after a stream synchronisation).
+void drain_profile(sfd_engine* e) {
+  for (auto& p : e->pending) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+      e->class_ms[p.cls] += ms;
+      e->class_count[p.cls] += 1;
+    }
+    e->event_pool.push_back(p.a);
+    e->event_pool.push_back(p.b);
+  }
+  e->pending.clear();
+}
+
+// LAUNCHC(e, class, launch-expression): launch, check, count, and when
+// profiling bracket the launch with events on the engine stream.
+#define LAUNCHC(e, cls, ...)                                     \
+  do {                                                           \
+    cudaEvent_t _ea = nullptr, _eb = nullptr;                    \
+    if ((e)->profile) {                                          \
+      _ea = get_event(e);                                        \
+      _eb = get_event(e);                                        \
+      cudaEventRecord(_ea, (e)->stream);                         \
+    }                                                            \
+    __VA_ARGS__;                                                 \
+    int _rc = launch_check(e);                                   \
+    if (_rc) return _rc;                                         \
+    if ((e)->profile) {                                          \
+      cudaEventRecord(_eb, (e)->stream);                         \
+      (e)->pending.push_back({(cls), _ea, _eb});                 \
+    }                                                            \
+  } while (0)
+#define LAUNCH(e, ...) LAUNCHC(e, SFD_K_OTHER, __VA_ARGS__)
+
+inline int blocks_for(long long n, int t) { return (int)((n + t - 1) / t); }
+
+int enqueue_sums(sfd_engine* e, int prec, const double* weights) {
+  SumArgs A{e->d_surf, e->d_sum_items, e->nsurf, e->ntot, e->nd.w, e->nd.p, weights, e->part_s, e->part_t, e->part_a};
+  int cls = prec == SFD_PREC_F64 ? SFD_K_SUMS64 : prec == SFD_PREC_DF ? SFD_K_SUMSDF : SFD_K_SUMS32;
+  LAUNCHC(e, cls, sfd_launch_sums(prec, A, e->nsum, e->stream));
+  return 0;
+}
+
+int enqueue_epilogue(sfd_engine* e, const double* weights, int mode, bool track_norm) {
+  EpiArgs E{e->d_surf, e->d_node_surf, e->nsurf, e->ntot, e->part_s, e->part_t, e->part_a, weights, e->nd.w,
+            e->zp, e->nd.mdiag, e->phip, e->cacc, e->dacc, e->r, track_norm ? e->rnorm : nullptr};
+  LAUNCHC(e, SFD_K_EPILOGUE, k_sum_epilogue<<<blocks_for(e->ntot, 256), 256, 0, e->stream>>>(E, mode));
+  return 0;
+}
+
+int enqueue_precond(sfd_engine* e) {
+  const int nb = e->max_np / 128;
+  LAUNCHC(e, SFD_K_ASSEMBLE, sfd_launch_assemble32(e->d_surf, e->d_asm_tiles, e->nasm, e->nd.w, e->nd.p, e->zp, e->nd.mdiag, e->m32,
+                                  e->stream));
+  const int tiles = e->max_np / 64;
+  for (int kb = 0; kb < nb; ++kb) {
+    LAUNCHC(e, SFD_K_DIAG, k_gj_diag<<<e->nsurf, 512, 128 * 129 * sizeof(float), e->stream>>>(e->d_surf, e->nsurf, kb, e->m32,
+                                                                                  e->pbuf, e->status));
+    LAUNCHC(e, SFD_K_PANEL, k_gj_panel<<<dim3(tiles, 1, e->nsurf), 256, 0, e->stream>>>(e->d_surf, e->nsurf, kb, e->m32, e->pbuf,
+                                                                          e->rbuf, e->cbuf, e->d_poff));
+    LAUNCHC(e, SFD_K_UPDATE, k_gj_update<<<dim3(tiles, tiles, e->nsurf), 256, 0, e->stream>>>(e->d_surf, e->nsurf, kb, e->m32,
+                                                                               e->pbuf, e->rbuf, e->cbuf, e->d_poff));
+  }
+  return 0;
+}
+
+// First half of an RHS evaluation (calculateVorticities,
+// BaseBoundaryIntegrator.cuh:275-306): z', z'', phi', M a = phi' and the
+// boundary sums C, D of the solution.
+int enqueue_solve(sfd_engine* e, const double* st, const double* phi_im, bool refactor) {
+  const int nt = e->ntot;
+  const double *x = st, *y = st + nt, *phi = st + 2 * nt;
+  DerivArgs D{e->d_surf, e->nsurf, x, y, phi, phi_im, e->a, e->zp, e->zpp, e->phip, e->ap};
+  LAUNCHC(e, SFD_K_SPECTRAL, sfd_launch_spectral(D, e->d_jobs_first, e->njobs_first, e->max_n, e->stream));
+  LAUNCHC(e, SFD_K_NODE, k_node_prep<<<blocks_for(nt, 256), 256, 0, e->stream>>>(e->d_surf, e->d_node_surf, nt, x, y, e->zp,
+                                                                     e->zpp, e->nd));
+  if (e->opt.precision == SFD_PRECISION_FP64) {
+    LAUNCHC(e, SFD_K_ASSEMBLE, sfd_launch_assemble64(e->d_surf, e->d_asm_tiles, e->nasm, e->nd.w, e->nd.p, e->zp, e->nd.mdiag,
+                                    e->m64, e->stream));
+    const int nb = e->max_np / 64;
+    for (int kb = 0; kb < nb; ++kb) {
+      LAUNCHC(e, SFD_K_DIAG, k_lu64_diag<<<e->nsurf, 256, 0, e->stream>>>(e->d_surf, e->nsurf, kb, e->m64, e->status, e->lmax));
+      int rem = nb - kb - 1;
+      if (rem > 0) {
+        LAUNCHC(e, SFD_K_PANEL, k_lu64_trsm<<<dim3(rem, 2, e->nsurf), 64, 0, e->stream>>>(e->d_surf, e->nsurf, kb, e->m64, e->lmax));
+        LAUNCHC(e, SFD_K_UPDATE, k_lu64_gemm<<<dim3(rem, rem, e->nsurf), 256, 0, e->stream>>>(e->d_surf, e->nsurf, kb, e->m64));
+      }
+    }
+    LAUNCHC(e, SFD_K_TRSV, k_lu64_solve<<<e->nsurf, 256, e->max_np * sizeof(double), e->stream>>>(e->d_surf, e->m64, e->phip,
+                                                                                       e->a));
+    int rc = enqueue_sums(e, SFD_PREC_F64, e->a);
+    if (rc) return rc;
+    rc = enqueue_epilogue(e, e->a, 0, true);
+    if (rc) return rc;
+  } else {
+    if (refactor || !e->have_precond) {
+      int rc = enqueue_precond(e);
+      if (rc) return rc;
+      e->have_precond = true;
+    }
+    // a0 = X phi'; accurate residual; FP32 corrections
+    LAUNCHC(e, SFD_K_GEMV, k_gemv<<<e->ngemv, 256, 0, e->stream>>>(e->d_surf, e->d_gemv_rows, e->m32, e->phip, e->a));
+    int rc = enqueue_sums(e, SFD_PREC_DF, e->a);
+    if (rc) return rc;
+    rc = enqueue_epilogue(e, e->a, 0, e->opt.refine_iters == 0);
+    if (rc) return rc;
+    for (int it = 0; it < e->opt.refine_iters; ++it) {
+      LAUNCHC(e, SFD_K_GEMV, k_gemv<<<e->ngemv, 256, 0, e->stream>>>(e->d_surf, e->d_gemv_rows, e->m32, e->r, e->delta));
+      LAUNCH(e, k_axpy_inplace<<<blocks_for(nt, 256), 256, 0, e->stream>>>(nt, e->a, e->delta));
+      rc = enqueue_sums(e, SFD_PREC_F32, e->delta);
+      if (rc) return rc;
+      rc = enqueue_epilogue(e, e->delta, 1, it == e->opt.refine_iters - 1);
+      if (rc) return rc;
+    }
+  }
+  return 0;
+}
+
+// One RHS evaluation: state [x|y|phi] -> out [dx|dy|dphi].
+int enqueue_rhs(sfd_engine* e, const double* st, double* out, bool refactor) {
+  int rc = enqueue_solve(e, st, nullptr, refactor);
+  if (rc) return rc;
+  const int nt = e->ntot;
+  const double* y = st + nt;
+  DerivArgs D{e->d_surf, e->nsurf, st, y, st + 2 * nt, nullptr, e->a, e->zp, e->zpp, e->phip, e->ap};
+  // a' and the velocity / Bernoulli epilogue
+  LAUNCHC(e, SFD_K_SPECTRAL, sfd_launch_spectral(D, e->d_jobs_ap, e->njobs_ap, e->max_n, e->stream));
+  VelArgs V{e->d_surf, e->d_node_surf, e->nsurf, nt, e->cacc, e->dacc, e->a, e->ap, e->nd.v1low, e->nd.v1up,
+            e->nd.v2, y, e->zp, e->zpp, e->vel_low1, out, out + nt, out + 2 * nt, e->status};
+  if (e->any_rho) LAUNCHC(e, SFD_K_VELOCITY, k_velocity_node1<<<1, 32, 0, e->stream>>>(V));
+  LAUNCHC(e, SFD_K_VELOCITY, k_velocity_bernoulli<<<blocks_for(nt, 256), 256, 0, e->stream>>>(V));
+  return 0;
+}
+
+int enqueue_step(sfd_engine* e, double dt, bool refactor) {
+  const int n3 = 3 * e->ntot;
+  const int nb = blocks_for(n3, 256);
+  const double wk[4] = {1.0, 2.0, 2.0, 1.0};
+  const double cy[4] = {dt * 0.5, dt * 0.5, dt, 0.0};
+  for (int s = 0; s < 4; ++s) {
+    const double* in = s == 0 ? e->y0 : e->ys;
+    int rc = enqueue_rhs(e, in, e->kcur, refactor && s == 0);
+    if (rc) return rc;
+    LAUNCHC(e, SFD_K_RK4, k_rk4_stage<<<nb, 256, 0, e->stream>>>(n3, e->y0, e->kcur, e->kacc, s < 3 ? e->ys : nullptr, wk[s],
+                                                       cy[s], s == 0));
+  }
+  LAUNCHC(e, SFD_K_RK4, k_rk4_final<<<nb, 256, 0, e->stream>>>(n3, e->y0, e->kacc, dt / 6.0));
+  return 0;
+}
+
+void destroy_graphs(sfd_engine* e) {
+  for (int i = 0; i < 2; ++i)
+    if (e->g_step[i]) {
+      cudaGraphExecDestroy(e->g_step[i]);
+      e->g_step[i] = nullptr;
+    }
+}
+
+int build_graph(sfd_engine* e, double dt, int variant) {
+  cudaGraph_t g = nullptr;
+  long long before = e->launches;
+  bool had = e->have_precond;
+  if (variant == 0) e->have_precond = true;  // capture the no-refactor variant as such
+  CK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = enqueue_step(e, dt, variant == 1);
+  cudaError_t ce = cudaStreamEndCapture(e->stream, &g);
+  e->have_precond = had;
+  e->launches = before;
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (ce != cudaSuccess) return sfd_fail(ce);
+  size_t nn = 0;
+  cudaGraphGetNodes(g, nullptr, &nn);
+  e->g_kernels[variant] = (int)nn;
+  ce = cudaGraphInstantiate(&e->g_step[variant], g, 0);
+  cudaGraphDestroy(g);
+  if (ce != cudaSuccess) return sfd_fail(ce);
+  return 0;
+}
+
+int run_steps(sfd_engine* e, double dt, int steps) {
+  if (steps < 0) return set_error(SFD_ERR_INVALID, "negative step count");
+  CK(cudaSetDevice(e->device));
+  const bool mixed = e->opt.precision == SFD_PRECISION_MIXED;
+  const int every = std::max(1, e->opt.refactor_every);
+  if (e->opt.use_graphs && !e->profile) {
+    if (e->g_dt != dt) {
+      destroy_graphs(e);
+      e->g_dt = dt;
+    }
+    for (int s = 0; s < steps; ++s) {
+      int variant = (!mixed || (e->step_count % every) == 0 || !e->have_precond) ? 1 : 0;
+      if (!mixed) variant = 1;
+      if (!e->g_step[variant]) {
+        int rc = build_graph(e, dt, variant);
+        if (rc) return rc;
+      }
+      CK(cudaGraphLaunch(e->g_step[variant], e->stream));
+      e->launches += e->g_kernels[variant];
+      if (variant == 1 && mixed) e->have_precond = true;
+      e->step_count++;
+    }
+  } else {
+    for (int s = 0; s < steps; ++s) {
+      bool refactor = !mixed || (e->step_count % every) == 0;
+      int rc = enqueue_step(e, dt, refactor);
+      if (rc) return rc;
+      e->step_count++;
+    }
+  }
+  return 0;
+}
+
+void free_engine(sfd_engine* e) {
+  if (!e) return;
+  cudaSetDevice(e->device);
+  if (e->stream) cudaStreamSynchronize(e->stream);
+  destroy_graphs(e);
+  void* ptrs[] = {e->d_surf, e->d_node_surf, e->d_jobs_first, e->d_jobs_ap, e->d_sum_items, e->d_asm_tiles,
+                  e->d_gemv_rows, e->d_poff, e->y0, e->ys, e->kacc, e->kcur, e->zp, e->zpp, e->ap, e->phip, e->a,
+                  e->r, e->delta, e->phi_im, e->nd.w, e->nd.p, e->nd.mdiag, e->nd.v1low, e->nd.v1up, e->nd.v2,
+                  e->part_s, e->part_t, e->cacc, e->dacc, e->vel_low1, e->part_a, e->status, e->lmax, e->rnorm,
+                  e->inv_out, e->m64, e->m32, e->pbuf, e->rbuf, e->cbuf};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  drain_profile(e);
+  for (cudaEvent_t ev : e->event_pool) cudaEventDestroy(ev);
+  for (auto& kv : e->d_tw) cudaFree(kv.second);
+  if (e->own_stream) cudaStreamDestroy(e->own_stream);
+  delete e;
+}
+
+int fill_surface(SurfaceDesc& S, const sfd_problem& p) {
+  S.physics = p.physics;
+  S.infinite_depth = p.infinite_depth ? 1 : 0;
+  S.rho = p.rho;
+  S.depth = p.depth;
+  S.gravity = p.gravity > 0 ? p.gravity : 1.0;
+  S.U = p.U;
+  S.kappa = p.kappa;
+  S.expansion_order = p.expansion_order;
+  S.bern_variant = 0;
+  if (p.physics != SFD_WATER && p.physics != SFD_HELIUM) return set_error(SFD_ERR_INVALID, "unknown physics %d", p.physics);
+  if (p.physics == SFD_HELIUM) {
+    if (!(p.depth > 0)) return set_error(SFD_ERR_INVALID, "helium needs depth > 0 (got %g)", p.depth);
+    S.vdw = p.A3 > 0 ? p.A3 / (p.depth * p.depth * p.depth) : p.depth / 3.0;  // createM.cuh:113
+    if (p.use_expansions) S.bern_variant = 1;      // HeliumBoundaryProblem.cuh:140-148
+    else if (p.kappa != 0.0) S.bern_variant = 2;
+  } else {
+    S.vdw = 0.0;
+  }
+  return 0;
+}
+
+}  // namespace
+
+// ====================================================================== C ABI
+extern "C" {
+
+void sfd_default_options(sfd_options* o) {
+  if (!o) return;
+  o->precision = SFD_PRECISION_MIXED;
+  o->refine_iters = 3;
+  o->refactor_every = 1;
+  o->use_graphs = 1;
+  o->device = 0;
+}
+
+void sfd_default_problem(sfd_problem* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->physics = SFD_WATER;
+  p->depth = 1.0;
+  p->gravity = 1.0;
+}
+
+const char* sfd_last_error(void) { return g_last_error.c_str(); }
+const char* sfd_version(void) { return "sfd-gb300 0.1 (sm_103a)"; }
+
+int sfd_set_default_precision(int precision) {
+  if (precision != SFD_PRECISION_FP64 && precision != SFD_PRECISION_MIXED)
+    return set_error(SFD_ERR_INVALID, "unknown precision %d", precision);
+  g_default_precision = precision;
+  return 0;
+}
+
+int sfd_create(const int* n, int nsurf, const sfd_problem* problems, int shared_problem, const sfd_options* opts,
+               sfd_engine** out) {
+  if (!out || !n || !problems || nsurf <= 0) return set_error(SFD_ERR_INVALID, "sfd_create: bad arguments");
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    return set_error(SFD_ERR_NO_DEVICE, "no CUDA device available");
+  sfd_engine* e = new sfd_engine();
+  if (opts) e->opt = *opts;
+  else sfd_default_options(&e->opt);
+  if (e->opt.precision != SFD_PRECISION_FP64 && e->opt.precision != SFD_PRECISION_MIXED) {
+    delete e;
+    return set_error(SFD_ERR_INVALID, "unknown precision %d", e->opt.precision);
+  }
+  if (e->opt.refine_iters < 0) e->opt.refine_iters = 0;
+  e->device = e->opt.device;
+  if (e->device < 0 || e->device >= ndev) {
+    delete e;
+    return set_error(SFD_ERR_INVALID, "device %d out of range", e->opt.device);
+  }
+  int rc = 0;
+#define CKE(expr)                   \
+  do {                              \
+    cudaError_t _e = (expr);        \
+    if (_e != cudaSuccess) {        \
+      rc = sfd_fail(_e);            \
+      free_engine(e);               \
+      return rc;                    \
+    }                               \
+  } while (0)
+  CKE(cudaSetDevice(e->device));
+  CKE(cudaStreamCreateWithFlags(&e->own_stream, cudaStreamNonBlocking));
+  e->stream = e->own_stream;
+  e->nsurf = nsurf;
+  e->hs.resize(nsurf);
+  long long off = 0, moff = 0, poff = 0;
+  std::vector<long long> h_poff(nsurf);
+  for (int s = 0; s < nsurf; ++s) {
+    int ns = n[s];
+    if (ns < 1 || ns > 8192) {
+      free_engine(e);
+      return set_error(SFD_ERR_INVALID, "surface %d: n = %d outside 1..8192", s, ns);
+    }
+    SurfaceDesc& S = e->hs[s];
+    std::memset(&S, 0, sizeof(S));
+    S.n = ns;
+    S.off = (int)off;
+    S.moff = moff;
+    rc = fill_surface(S, problems[shared_problem ? 0 : s]);
+    if (rc) {
+      free_engine(e);
+      return rc;
+    }
+    std::vector<int> rad;
+    if (!factorize(ns, rad)) {
+      free_engine(e);
+      return set_error(SFD_ERR_INVALID, "surface %d: n = %d has too many factors", s, ns);
+    }
+    S.nrad = (int)rad.size();
+    for (size_t i = 0; i < rad.size(); ++i) S.rad[i] = rad[i];
+    if (!e->d_tw.count(ns)) {
+      std::vector<cd> t = twiddles(ns);
+      cd* d = nullptr;
+      CKE(dalloc(&d, ns));
+      e->d_tw[ns] = d;
+      CKE(cudaMemcpy(d, t.data(), ns * sizeof(cd), cudaMemcpyHostToDevice));
+    }
+    S.tw = e->d_tw[ns];
+    if (S.physics == 0 && S.rho != 0.0) e->any_rho = true;
+    int np = pad_n(ns);
+    h_poff[s] = poff;
+    poff += 128LL * np;
+    off += ns;
+    moff += (long long)np * np;
+    e->max_n = std::max(e->max_n, ns);
+    e->max_np = std::max(e->max_np, np);
+    e->max_chunks = std::max(e->max_chunks, (ns + kSumChunk - 1) / kSumChunk);
+  }
+  if (off > (1LL << 30)) {
+    free_engine(e);
+    return set_error(SFD_ERR_INVALID, "too many nodes");
+  }
+  e->ntot = (int)off;
+  e->mat_elems = moff;
+  e->panel_elems = poff;
+  const int nt = e->ntot;
+  // work lists
+  std::vector<int> node_surf(nt);
+  std::vector<int2> jf, ja;
+  std::vector<int4> items, tiles;
+  std::vector<int2> rows;
+  for (int s = 0; s < nsurf; ++s) {
+    const SurfaceDesc& S = e->hs[s];
+    for (int k = 0; k < S.n; ++k) node_surf[S.off + k] = s;
+    jf.push_back({s, SFD_JOB_ZP});
+    jf.push_back({s, SFD_JOB_ZPP});
+    jf.push_back({s, SFD_JOB_PHIP});
+    ja.push_back({s, SFD_JOB_AP});
+    int nch = (S.n + kSumChunk - 1) / kSumChunk;
+    for (int t0 = 0; t0 < S.n; t0 += kSumTargets)
+      for (int c = 0; c < nch; ++c) items.push_back({s, t0, c * kSumChunk, c});
+    int np = pad_n(S.n);
+    for (int r0 = 0; r0 < np; r0 += 64)
+      for (int c0 = 0; c0 < np; c0 += 64) tiles.push_back({s, r0, c0, 0});
+    for (int r0 = 0; r0 < S.n; r0 += 8) rows.push_back({s, r0});
+  }
+  e->njobs_first = (int)jf.size();
+  e->njobs_ap = (int)ja.size();
+  e->nsum = (int)items.size();
+  e->nasm = (int)tiles.size();
+  e->ngemv = (int)rows.size();
+  CKE(dalloc(&e->d_surf, nsurf));
+  CKE(cudaMemcpy(e->d_surf, e->hs.data(), nsurf * sizeof(SurfaceDesc), cudaMemcpyHostToDevice));
+  CKE(dalloc(&e->d_node_surf, nt));
+  CKE(cudaMemcpy(e->d_node_surf, node_surf.data(), nt * sizeof(int), cudaMemcpyHostToDevice));
+  CKE(dalloc(&e->d_jobs_first, jf.size()));
+  CKE(cudaMemcpy(e->d_jobs_first, jf.data(), jf.size() * sizeof(int2), cudaMemcpyHostToDevice));
+  CKE(dalloc(&e->d_jobs_ap, ja.size()));
+  CKE(cudaMemcpy(e->d_jobs_ap, ja.data(), ja.size() * sizeof(int2), cudaMemcpyHostToDevice));
+  CKE(dalloc(&e->d_sum_items, items.size()));
+  CKE(cudaMemcpy(e->d_sum_items, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice));
+  CKE(dalloc(&e->d_asm_tiles, tiles.size()));
+  CKE(cudaMemcpy(e->d_asm_tiles, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice));
+  CKE(dalloc(&e->d_gemv_rows, rows.size()));
+  CKE(cudaMemcpy(e->d_gemv_rows, rows.data(), rows.size() * sizeof(int2), cudaMemcpyHostToDevice));
+  CKE(dalloc(&e->d_poff, nsurf));
+  CKE(cudaMemcpy(e->d_poff, h_poff.data(), nsurf * sizeof(long long), cudaMemcpyHostToDevice));
+  // buffers
+  CKE(dalloc(&e->y0, 3LL * nt));
+  CKE(dalloc(&e->ys, 3LL * nt));
+  CKE(dalloc(&e->kacc, 3LL * nt));
+  CKE(dalloc(&e->kcur, 3LL * nt));
+  CKE(dalloc(&e->zp, nt));
+  CKE(dalloc(&e->zpp, nt));
+  CKE(dalloc(&e->ap, nt));
+  CKE(dalloc(&e->phip, nt));
+  CKE(dalloc(&e->a, nt));
+  CKE(dalloc(&e->r, nt));
+  CKE(dalloc(&e->delta, nt));
+  CKE(dalloc(&e->nd.w, nt));
+  CKE(dalloc(&e->nd.p, nt));
+  CKE(dalloc(&e->nd.mdiag, nt));
+  CKE(dalloc(&e->nd.v1low, nt));
+  CKE(dalloc(&e->nd.v1up, nt));
+  CKE(dalloc(&e->nd.v2, nt));
+  CKE(dalloc(&e->part_s, (long long)e->max_chunks * nt));
+  CKE(dalloc(&e->part_t, (long long)e->max_chunks * nt));
+  CKE(dalloc(&e->part_a, (long long)e->max_chunks * nsurf));
+  CKE(dalloc(&e->cacc, nt));
+  CKE(dalloc(&e->dacc, nt));
+  CKE(dalloc(&e->vel_low1, 1));
+  CKE(dalloc(&e->status, nsurf));
+  CKE(dalloc(&e->lmax, nsurf));
+  CKE(dalloc(&e->rnorm, nsurf));
+  CKE(dalloc(&e->inv_out, 5LL * nsurf));
+  CKE(cudaMemset(e->status, 0, nsurf * sizeof(unsigned int)));
+  CKE(cudaMemset(e->lmax, 0, nsurf * sizeof(double)));
+  CKE(cudaMemset(e->rnorm, 0, nsurf * sizeof(double)));
+  CKE(cudaMemset(e->y0, 0, 3LL * nt * sizeof(double)));
+  CKE(cudaMemset(e->nd.p, 0, nt * sizeof(cd)));
+  CKE(cudaMemset(e->dacc, 0, nt * sizeof(cd)));
+  CKE(cudaMemset(e->part_t, 0, (long long)e->max_chunks * nt * sizeof(cd)));
+  if (e->opt.precision == SFD_PRECISION_FP64) {
+    CKE(dalloc(&e->m64, e->mat_elems));
+  } else {
+    CKE(dalloc(&e->m32, e->mat_elems));
+    CKE(dalloc(&e->pbuf, (long long)nsurf * 128 * 128));
+    CKE(dalloc(&e->rbuf, e->panel_elems));
+    CKE(dalloc(&e->cbuf, e->panel_elems));
+  }
+  CKE(sfd_fft_configure());
+  CKE(cudaFuncSetAttribute(k_gj_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, 128 * 129 * (int)sizeof(float)));
+  CKE(cudaFuncSetAttribute(k_lu64_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, 8320 * (int)sizeof(double)));
+#undef CKE
+  *out = e;
+  return 0;
+}
+
+int sfd_destroy(sfd_engine* e) {
+  free_engine(e);
+  return 0;
+}
+
+int sfd_set_stream(sfd_engine* e, void* st) {
+  if (!e) return set_error(SFD_ERR_INVALID, "null engine");
+  destroy_graphs(e);
+  e->stream = st ? (cudaStream_t)st : e->own_stream;
+  return 0;
+}
+
+int sfd_total_nodes(const sfd_engine* e) { return e ? e->ntot : 0; }
+
+int sfd_set_state_host(sfd_engine* e, const double* x, const double* y, const double* phi) {
+  if (!e || !x || !y || !phi) return set_error(SFD_ERR_INVALID, "null argument");
+  CK(cudaSetDevice(e->device));
+  size_t b = e->ntot * sizeof(double);
+  CK(cudaMemcpyAsync(e->y0, x, b, cudaMemcpyHostToDevice, e->stream));
+  CK(cudaMemcpyAsync(e->y0 + e->ntot, y, b, cudaMemcpyHostToDevice, e->stream));
+  CK(cudaMemcpyAsync(e->y0 + 2 * e->ntot, phi, b, cudaMemcpyHostToDevice, e->stream));
+  CK(cudaStreamSynchronize(e->stream));
+  return 0;
+}
+
+int sfd_get_state_host(sfd_engine* e, double* x, double* y, double* phi) {
+  if (!e || !x || !y || !phi) return set_error(SFD_ERR_INVALID, "null argument");
+  CK(cudaSetDevice(e->device));
+  size_t b = e->ntot * sizeof(double);
+  CK(cudaMemcpyAsync(x, e->y0, b, cudaMemcpyDeviceToHost, e->stream));
+  CK(cudaMemcpyAsync(y, e->y0 + e->ntot, b, cudaMemcpyDeviceToHost, e->stream));
+  CK(cudaMemcpyAsync(phi, e->y0 + 2 * e->ntot, b, cudaMemcpyDeviceToHost, e->stream));
+  CK(cudaStreamSynchronize(e->stream));
+  return 0;
+}
+
+int sfd_set_state_device(sfd_engine* e, const void* x, const void* y, const void* phi) {
+  if (!e || !x || !y || !phi) return set_error(SFD_ERR_INVALID, "null argument");
+  CK(cudaSetDevice(e->device));
+  size_t b = e->ntot * sizeof(double);
+  CK(cudaMemcpyAsync(e->y0, x, b, cudaMemcpyDeviceToDevice, e->stream));
+  CK(cudaMemcpyAsync(e->y0 + e->ntot, y, b, cudaMemcpyDeviceToDevice, e->stream));
+  CK(cudaMemcpyAsync(e->y0 + 2 * e->ntot, phi, b, cudaMemcpyDeviceToDevice, e->stream));
+  return 0;
+}
+
+int sfd_get_state_device(sfd_engine* e, void* x, void* y, void* phi) {
+  if (!e || !x || !y || !phi) return set_error(SFD_ERR_INVALID, "null argument");
+  CK(cudaSetDevice(e->device));
+  size_t b = e->ntot * sizeof(double);
+  CK(cudaMemcpyAsync(x, e->y0, b, cudaMemcpyDeviceToDevice, e->stream));
+  CK(cudaMemcpyAsync(y, e->y0 + e->ntot, b, cudaMemcpyDeviceToDevice, e->stream));
+  CK(cudaMemcpyAsync(phi, e->y0 + 2 * e->ntot, b, cudaMemcpyDeviceToDevice, e->stream));
+  return 0;
+}
+
+int sfd_state_device_ptr(sfd_engine* e, void** state) {
+  if (!e || !state) return set_error(SFD_ERR_INVALID, "null argument");
+  *state = e->y0;
+  return 0;
+}
+
+int sfd_rhs_device(sfd_engine* e, const void* state_in, void* rhs_out) {
+  if (!e || !state_in || !rhs_out) return set_error(SFD_ERR_INVALID, "null argument");
+  CK(cudaSetDevice(e->device));
+  return enqueue_rhs(e, (const double*)state_in, (double*)rhs_out, true);
+}
+
+int sfd_rhs_host(sfd_engine* e, double* dx, double* dy, double* dphi, double* a, double* zp, double* zpp) {
+  if (!e || !dx || !dy || !dphi) return set_error(SFD_ERR_INVALID, "null argument");
+  CK(cudaSetDevice(e->device));
+  int rc = enqueue_rhs(e, e->y0, e->kcur, true);
+  if (rc) return rc;
+  size_t b = e->ntot * sizeof(double);
+  CK(cudaMemcpyAsync(dx, e->kcur, b, cudaMemcpyDeviceToHost, e->stream));
+  CK(cudaMemcpyAsync(dy, e->kcur + e->ntot, b, cudaMemcpyDeviceToHost, e->stream));
+  CK(cudaMemcpyAsync(dphi, e->kcur + 2 * e->ntot, b, cudaMemcpyDeviceToHost, e->stream));
+  if (a) CK(cudaMemcpyAsync(a, e->a, b, cudaMemcpyDeviceToHost, e->stream));
+  if (zp) CK(cudaMemcpyAsync(zp, e->zp, 2 * b, cudaMemcpyDeviceToHost, e->stream));
+  if (zpp) CK(cudaMemcpyAsync(zpp, e->zpp, 2 * b, cudaMemcpyDeviceToHost, e->stream));
+  CK(cudaStreamSynchronize(e->stream));
+  return 0;
+}
+
+int sfd_rk4_steps_async(sfd_engine* e, double dt, int steps) {
+  if (!e) return set_error(SFD_ERR_INVALID, "null engine");
+  return run_steps(e, dt, steps);
+}
+
+int sfd_synchronize(sfd_engine* e) {
+  if (!e) return set_error(SFD_ERR_INVALID, "null engine");
+  CK(cudaSetDevice(e->device));
+  CK(cudaStreamSynchronize(e->stream));
+  if (e->profile) drain_profile(e);
+  return 0;
+}
+
+int sfd_profile(sfd_engine* e, int enable) {
+  if (!e) return set_error(SFD_ERR_INVALID, "null engine");
+  CK(cudaSetDevice(e->device));
+  CK(cudaStreamSynchronize(e->stream));
+  drain_profile(e);
+  e->profile = enable != 0;
+  for (int i = 0; i < SFD_NCLASS; ++i) {
+    e->class_ms[i] = 0.0;
+    e->class_count[i] = 0;
+  }
+  return 0;
+}
+
+int sfd_profile_read(sfd_engine* e, double* ms, long long* counts, int nclass) {
+  if (!e || !ms || !counts) return set_error(SFD_ERR_INVALID, "null argument");
+  CK(cudaSetDevice(e->device));
+  CK(cudaStreamSynchronize(e->stream));
+  drain_profile(e);
+  for (int i = 0; i < nclass && i < SFD_NCLASS; ++i) {
+    ms[i] = e->class_ms[i];
+    counts[i] = e->class_count[i];
+  }
+  return 0;
+}
+
+const char* sfd_profile_class_name(int cls) {
+  static const char* names[SFD_NCLASS] = {"other", "spectral_deriv", "node_prep", "boundary_sums_fp64",
+                                          "boundary_sums_df", "boundary_sums_fp32", "sum_epilogue", "assemble",
+                                          "factor_diag", "factor_panel", "factor_update", "lu_trsv", "gemv",
+                                          "velocity_bernoulli", "rk4_combine"};
+  return (cls >= 0 && cls < SFD_NCLASS) ? names[cls] : "";
+}
+
+int sfd_rk4_steps(sfd_engine* e, double dt, int steps) {
+  int rc = sfd_rk4_steps_async(e, dt, steps);
+  if (rc) return rc;
+  return sfd_synchronize(e);
+}
+
+int sfd_invariants(sfd_engine* e, double kappa, double* out) {
+  if (!e || !out) return set_error(SFD_ERR_INVALID, "null argument");
+  CK(cudaSetDevice(e->device));
+  int rc = enqueue_rhs(e, e->y0, e->kcur, true);
+  if (rc) return rc;
+  const int nt = e->ntot;
+  LAUNCH(e, k_invariants<<<e->nsurf, 256, 0, e->stream>>>(e->d_surf, e->y0, e->y0 + nt, e->y0 + 2 * nt, e->zp, e->kcur,
+                                                            e->kcur + nt, kappa, e->inv_out));
+  CK(cudaMemcpyAsync(out, e->inv_out, 5 * e->nsurf * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+  CK(cudaStreamSynchronize(e->stream));
+  return 0;
+}
+
+int sfd_get_status(sfd_engine* e, unsigned int* status, double* lmax, double* rnorm) {
+  if (!e) return set_error(SFD_ERR_INVALID, "null engine");
+  CK(cudaSetDevice(e->device));
+  CK(cudaStreamSynchronize(e->stream));
+  if (status) CK(cudaMemcpy(status, e->status, e->nsurf * sizeof(unsigned int), cudaMemcpyDeviceToHost));
+  if (lmax) CK(cudaMemcpy(lmax, e->lmax, e->nsurf * sizeof(double), cudaMemcpyDeviceToHost));
+  if (rnorm) CK(cudaMemcpy(rnorm, e->rnorm, e->nsurf * sizeof(double), cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+int sfd_clear_status(sfd_engine* e) {
+  if (!e) return set_error(SFD_ERR_INVALID, "null engine");
+  CK(cudaSetDevice(e->device));
+  CK(cudaMemsetAsync(e->status, 0, e->nsurf * sizeof(unsigned int), e->stream));
+  CK(cudaMemsetAsync(e->lmax, 0, e->nsurf * sizeof(double), e->stream));
+  CK(cudaMemsetAsync(e->rnorm, 0, e->nsurf * sizeof(double), e->stream));
+  return 0;
+}
+
+long long sfd_kernel_launches(const sfd_engine* e) { return e ? e->launches : 0; }
+
+}  // extern "C"
+
+// ====================================================================== reference-compatible exports
+namespace {
+
+constexpr double kPi = 3.14159265358979323846;
+constexpr double kAlphaHamaker = 3.5e-24;  // constants.cuh:15
+constexpr double kRhoHelium = 150.0;       // Export.cuh:82 default
+
+struct NondimProps {
+  double depth, rho, kappa, base_time;
+};
+
+// adimensionalizeProperties (Export.cu:1222-1246) without the console output.
+NondimProps adimensionalize(double L, double rho, double kappa, double depth) {
+  NondimProps p;
+  double base_length = L / (2.0 * kPi);
+  double base_acc = 3 * kAlphaHamaker / std::pow(depth, 4);
+  p.base_time = std::sqrt(base_length / base_acc);
+  double stf = kRhoHelium * base_length * base_length * base_length / (p.base_time * p.base_time);
+  p.kappa = kappa / stf;
+  p.depth = depth / base_length;
+  p.rho = rho / kRhoHelium;
+  return p;
+}
+
+sfd_problem helium_problem(const NondimProps& np, bool use_exp = false, int order = 1, bool inf = false) {
+  sfd_problem p;
+  sfd_default_problem(&p);
+  p.physics = SFD_HELIUM;
+  p.depth = np.depth;
+  p.rho = np.rho;
+  p.kappa = np.kappa;
+  p.A3 = 0.0;  // the reference's fixed h^4 / 3
+  p.use_expansions = use_exp ? 1 : 0;
+  p.expansion_order = order;
+  p.infinite_depth = inf ? 1 : 0;
+  return p;
+}
+
+int make_engine(int n, int batch, const sfd_problem& p, sfd_engine** e) {
+  sfd_options o;
+  sfd_default_options(&o);
+  o.precision = g_default_precision;
+  o.use_graphs = 0;
+  std::vector<int> ns(batch, n);
+  return sfd_create(ns.data(), batch, &p, 1, &o, e);
+}
+
+int rhs_from_vectors(const double* x, const double* y, const double* phi, double* vx, double* vy, double* rhsPhi,
+                     double L, double rho, double kappa, double depth, int n, int batch) {
+  if (!x || !y || !phi || !vx || !vy || !rhsPhi) return set_error(SFD_ERR_INVALID, "null argument");
+  sfd_engine* e = nullptr;
+  int rc = make_engine(n, batch, helium_problem(adimensionalize(L, rho, kappa, depth)), &e);
+  if (rc) return rc;
+  rc = sfd_set_state_host(e, x, y, phi);
+  if (!rc) rc = sfd_rhs_host(e, vx, vy, rhsPhi, nullptr, nullptr, nullptr);
+  sfd_destroy(e);
+  return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int calculateRHSFromVectors(const double* x, const double* y, const double* phi, double* vx, double* vy,
+                            double* rhsPhi, double L, double rho, double kappa, double depth, size_t N) {
+  if (N < 1 || N > 8192) return set_error(SFD_ERR_INVALID, "unsupported particle number %zu (1..8192)", N);
+  return rhs_from_vectors(x, y, phi, vx, vy, rhsPhi, L, rho, kappa, depth, (int)N, 1);
+}
+
+int calculateRHS256FromVectors(const double* x, const double* y, const double* phi, double* vx, double* vy,
+                               double* rhsPhi, double L, double rho, double kappa, double depth) {
+  return rhs_from_vectors(x, y, phi, vx, vy, rhsPhi, L, rho, kappa, depth, 256, 1);
+}
+
+int calculateRHS2048FromVectors(const double* x, const double* y, const double* phi, double* vx, double* vy,
+                                double* rhsPhi, double L, double rho, double kappa, double depth) {
+  return rhs_from_vectors(x, y, phi, vx, vy, rhsPhi, L, rho, kappa, depth, 2048, 1);
+}
+
+int calculateRHS256FromVectorsBatched(const double* x, const double* y, const double* phi, double* vx, double* vy,
+                                      double* rhsPhi, double L, double rho, double kappa, double depth,
+                                      int batchSize) {
+  if (batchSize < 1) return set_error(SFD_ERR_INVALID, "unsupported batch size %d", batchSize);
+  return rhs_from_vectors(x, y, phi, vx, vy, rhsPhi, L, rho, kappa, depth, 256, batchSize);
+}
+
+int calculateVorticities256FromVectors(const double* Z, const double* phi, double* a, double* Zp, double* Zpp,
+                                       double L, double rho, double kappa, double depth) {
+  if (!Z || !phi || !a) return set_error(SFD_ERR_INVALID, "null argument");
+  const int n = 256;
+  sfd_engine* e = nullptr;
+  int rc = make_engine(n, 1, helium_problem(adimensionalize(L, rho, kappa, depth)), &e);
+  if (rc) return rc;
+  std::vector<double> x(n), y(n), ph(n), phi_im(n), dx(n), dy(n), dp(n);
+  for (int i = 0; i < n; ++i) {
+    x[i] = Z[2 * i];
+    y[i] = Z[2 * i + 1];
+    ph[i] = phi[2 * i];
+    phi_im[i] = phi[2 * i + 1];
+  }
+  bool imag = false;
+  for (int i = 0; i < n; ++i) imag |= phi_im[i] != 0.0;
+  rc = sfd_set_state_host(e, x.data(), y.data(), ph.data());
+  if (!rc && imag) {
+    // the reference transforms the complex phi as given (SimulationRunner.cuh:245-251)
+    if (cudaMalloc(&e->phi_im, n * sizeof(double)) != cudaSuccess ||
+        cudaMemcpy(e->phi_im, phi_im.data(), n * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
+      rc = set_error(SFD_ERR_CUDA, "phi_im upload failed");
+  }
+  if (!rc) rc = enqueue_solve(e, e->y0, e->phi_im, true);
+  if (!rc) {
+    cudaStreamSynchronize(e->stream);
+    if (cudaMemcpy(a, e->a, n * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) rc = SFD_ERR_CUDA;
+    if (!rc && Zp) cudaMemcpy(Zp, e->zp, n * sizeof(cd), cudaMemcpyDeviceToHost);
+    if (!rc && Zpp) cudaMemcpy(Zpp, e->zpp, n * sizeof(cd), cudaMemcpyDeviceToHost);
+  }
+  sfd_destroy(e);
+  return rc;
+}
+
+int calculateDerivativeFFT256(const double* input, double* output) {
+  if (!input || !output) return set_error(SFD_ERR_INVALID, "null argument");
+  const int n = 256;
+  sfd_problem p;
+  sfd_default_problem(&p);
+  sfd_engine* e = nullptr;
+  int rc = make_engine(n, 1, p, &e);
+  if (rc) return rc;
+  std::vector<double> re(n), im(n);
+  for (int i = 0; i < n; ++i) {
+    re[i] = input[2 * i];
+    im[i] = input[2 * i + 1];
+  }
+  rc = sfd_set_state_host(e, re.data(), im.data(), re.data());
+  if (!rc) {
+    int2 job{0, SFD_JOB_RAW};
+    int2* dj = nullptr;
+    if (cudaMalloc(&dj, sizeof(int2)) != cudaSuccess) rc = SFD_ERR_CUDA;
+    if (!rc) cudaMemcpy(dj, &job, sizeof(int2), cudaMemcpyHostToDevice);
+    const int nt = e->ntot;
+    DerivArgs D{e->d_surf, e->nsurf, e->y0, e->y0 + nt, e->y0 + 2 * nt, nullptr, e->a, e->zp, e->zpp, e->phip, e->ap};
+    if (!rc && sfd_launch_spectral(D, dj, 1, n, e->stream) != cudaSuccess) rc = SFD_ERR_CUDA;
+    if (!rc) {
+      cudaStreamSynchronize(e->stream);
+      if (cudaMemcpy(output, e->ap, n * sizeof(cd), cudaMemcpyDeviceToHost) != cudaSuccess) rc = SFD_ERR_CUDA;
+    }
+    if (dj) cudaFree(dj);
+    if (rc == SFD_ERR_CUDA) set_error(rc, "calculateDerivativeFFT256: CUDA failure");
+  }
+  sfd_destroy(e);
+  return rc;
+}
+
+int integrateSimulationRK4(double* initialState, double** statesOut, size_t* statesCount, double** timesOut,
+                           size_t* timesCount, SimProperties* sp, RK4SolverOptions* ro, size_t N) {
+  if (!initialState || !statesOut || !statesCount || !timesOut || !timesCount || !sp || !ro)
+    return set_error(SFD_ERR_INVALID, "null argument");
+  if (N < 1 || N > 8192) return set_error(SFD_ERR_INVALID, "unsupported N %zu", N);
+  NondimProps np = adimensionalize(sp->L, sp->rho, sp->kappa, sp->depth);
+  // adimensionalizeRK4SolverOptions (Export.cu:1212-1219)
+  double dt = ro->timeStep / np.base_time, t0 = ro->t0 / np.base_time, t1 = ro->t1 / np.base_time;
+  if (!(dt > 0)) return set_error(SFD_ERR_INVALID, "timeStep must be > 0");
+  size_t steps = (size_t)((t1 - t0) / dt);  // runEvolution (AutonomousRungeKuttaStepper.cuh:421)
+  sfd_engine* e = nullptr;
+  int rc = make_engine((int)N, 1, helium_problem(np, sp->use_expansions, sp->expansion_order, sp->infinite_depth), &e);
+  if (rc) return rc;
+  e->opt.use_graphs = 1;
+  const size_t n3 = 3 * N;
+  size_t nstates = ro->returnTrajectory ? steps + 1 : 1;
+  double* states = (double*)std::malloc(nstates * n3 * sizeof(double));
+  double* times = ro->returnTrajectory ? (double*)std::malloc(nstates * sizeof(double)) : nullptr;
+  if (!states || (ro->returnTrajectory && !times)) {
+    std::free(states);
+    std::free(times);
+    sfd_destroy(e);
+    return set_error(SFD_ERR_INVALID, "host allocation failed");
+  }
+  rc = sfd_set_state_host(e, initialState, initialState + N, initialState + 2 * N);
+  double t = t0;
+  if (!rc && ro->returnTrajectory) {
+    std::memcpy(states, initialState, n3 * sizeof(double));
+    times[0] = t;
+  }
+  for (size_t s = 0; s < steps && !rc; ++s) {
+    rc = sfd_rk4_steps_async(e, dt, 1);
+    t += dt;
+    if (!rc && ro->returnTrajectory) {
+      double* dst = states + (s + 1) * n3;
+      rc = sfd_get_state_host(e, dst, dst + N, dst + 2 * N);
+      times[s + 1] = t;
+    }
+  }
+  if (!rc && !ro->returnTrajectory) rc = sfd_get_state_host(e, states, states + N, states + 2 * N);
+  sfd_destroy(e);
+  if (rc) {
+    std::free(states);
+    std::free(times);
+    return rc;
+  }
+  *statesOut = states;
+  *statesCount = nstates;
+  *timesOut = times;
+  *timesCount = ro->returnTrajectory ? nstates : 0;
+  return 0;
+}
+
+int integrateSimulationRK4_freeMemory(double* statesOut, double* timesOut) {
+  std::free(statesOut);
+  std::free(timesOut);
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,51 @@
+// sfd_engine.cuh -- device-visible descriptors shared by the engine kernels.
+#pragma once
+#include "sfd_common.cuh"
+
+#define SFD_MAX_RADICES 24
+
+// One surface of a (possibly uneven) batch.  All node arrays of the batch are
+// concatenated; surface s owns [off, off + n).  Dense per-surface matrices are
+// concatenated too; surface s owns [moff, moff + n*n) stored row-major
+// (row k = target node, column j = source node).
+struct SurfaceDesc {
+  int n;
+  int off;
+  long long moff;
+  int physics;          // 0 water, 1 helium
+  int infinite_depth;   // helium without image terms
+  double rho;           // water density ratio
+  double depth;         // helium film thickness h
+  double vdw;           // A3 / h^3 (the reference fixes h / 3)
+  double gravity;       // water g
+  double U;             // uniform stream (only the linear part of phi uses it)
+  double kappa;         // surface tension (helium Bernoulli variant)
+  int bern_variant;     // 0 standard, 1 series expansion (createM.cuh:171-193), 2 surface tension (:200-211)
+  int expansion_order;
+  const cd* tw;         // forward FFT twiddles exp(-2 pi i e / n), e in [0, n)
+  int nrad;
+  int rad[SFD_MAX_RADICES];
+};
+
+// Spectral-derivative job kinds (one CTA per job).
+enum : int {
+  SFD_JOB_ZP = 0,   // z' from x - 2 pi j/N + i y
+  SFD_JOB_ZPP = 1,  // z''
+  SFD_JOB_PHIP = 2, // phi' (real part kept)
+  SFD_JOB_AP = 3,   // a' (complex kept)
+  SFD_JOB_RAW = 4,  // d/dj of (x + i y) with no linear part and no 2 pi/N scale -> ap
+};
+
+struct DerivArgs {
+  const SurfaceDesc* surf;
+  int nsurf;
+  const double* x;
+  const double* y;
+  const double* phi;
+  const double* phi_im;  // imaginary part of a complex phi input (nullable)
+  const double* a;
+  cd* zp;
+  cd* zpp;
+  double* phip;
+  cd* ap;
+};

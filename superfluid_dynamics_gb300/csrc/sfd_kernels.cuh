@@ -1,0 +1,87 @@
+// sfd_kernels.cuh -- launch-argument structs and kernel declarations.
+#pragma once
+#include "sfd_engine.cuh"
+
+enum : int { SFD_PREC_F64 = 0, SFD_PREC_DF = 1, SFD_PREC_F32 = 2 };
+
+constexpr int kSumThreads = 256;  // threads per CTA of the boundary sums
+constexpr int kSumTargets = 256;  // targets per CTA
+constexpr int kSumChunk = 512;    // sources per CTA (shared-memory chunk)
+
+struct NodeData {
+  cd* w;        // exp(i z)
+  cd* p;        // exp(i z) e^{-h} (helium image kernel)
+  double* mdiag;
+  cd* v1low;    // V1_kk lower fluid (no image term)
+  cd* v1up;     // V1_kk upper fluid
+  cd* v2;       // V2_k
+};
+
+struct SumArgs {
+  const SurfaceDesc* surf;
+  const int4* items;
+  int nsurf;
+  int ntot;
+  const cd* w;
+  const cd* p;
+  const double* a;
+  cd* part_s;
+  cd* part_t;
+  double* part_a;
+};
+
+struct EpiArgs {
+  const SurfaceDesc* surf;
+  const int* node_surf;
+  int nsurf;
+  int ntot;
+  const cd* part_s;
+  const cd* part_t;
+  const double* part_a;
+  const double* a;
+  const cd* w;
+  const cd* zp;
+  const double* mdiag;
+  const double* phip;
+  cd* cacc;
+  cd* dacc;
+  double* r;
+  double* rnorm;  // per-surface max |r| (nullable)
+};
+
+struct VelArgs {
+  const SurfaceDesc* surf;
+  const int* node_surf;
+  int nsurf;
+  int ntot;
+  const cd* cacc;
+  const cd* dacc;
+  const double* a;
+  const cd* ap;
+  const cd* v1low;
+  const cd* v1up;
+  const cd* v2;
+  const double* y;
+  const cd* zp;
+  const cd* zpp;
+  cd* vel_low1;
+  double* dx;
+  double* dy;
+  double* dphi;
+  unsigned int* status;
+};
+
+__global__ void k_node_prep(const SurfaceDesc* surf, const int* node_surf, int ntot, const double* x,
+                            const double* y, const cd* zp, const cd* zpp, NodeData nd);
+cudaError_t sfd_launch_sums(int prec, const SumArgs& A, int nitems, cudaStream_t st);
+__global__ void k_sum_epilogue(EpiArgs E, int mode);
+__global__ void k_velocity_bernoulli(VelArgs V);
+__global__ void k_velocity_node1(VelArgs V);
+__global__ void k_rk4_stage(int n3, const double* y0, const double* k, double* kacc, double* ystage, double wk,
+                            double cy, int first);
+__global__ void k_rk4_final(int n3, double* y0, const double* kacc, double c);
+__global__ void k_invariants(const SurfaceDesc* surf, const double* x, const double* y, const double* phi,
+                             const cd* zp, const double* u, const double* v, double kappa, double* out);
+
+cudaError_t sfd_launch_spectral(const DerivArgs& A, const int2* jobs, int njobs, int max_n, cudaStream_t st);
+cudaError_t sfd_fft_configure();

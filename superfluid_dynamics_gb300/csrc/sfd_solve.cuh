@@ -1,0 +1,23 @@
+// sfd_solve.cuh -- dense-solver kernels (padded per-surface matrices).
+#pragma once
+#include "sfd_engine.cuh"
+
+// per-surface matrices are padded to a multiple of 128 rows/columns
+__host__ __device__ __forceinline__ int pad_n(int n) { return (n + 127) / 128 * 128; }
+
+cudaError_t sfd_launch_assemble64(const SurfaceDesc* surf, const int4* tiles, int ntiles, const cd* w, const cd* p,
+                                  const cd* zp, const double* mdiag, double* mat, cudaStream_t st);
+cudaError_t sfd_launch_assemble32(const SurfaceDesc* surf, const int4* tiles, int ntiles, const cd* w, const cd* p,
+                                  const cd* zp, const double* mdiag, float* mat, cudaStream_t st);
+__global__ void k_lu64_diag(const SurfaceDesc* surf, int nsurf, int kb, double* mat, unsigned int* status,
+                            double* lmax);
+__global__ void k_lu64_trsm(const SurfaceDesc* surf, int nsurf, int kb, double* mat, double* lmax);
+__global__ void k_lu64_gemm(const SurfaceDesc* surf, int nsurf, int kb, double* mat);
+__global__ void k_lu64_solve(const SurfaceDesc* surf, const double* mat, const double* b, double* x);
+__global__ void k_gj_diag(const SurfaceDesc* surf, int nsurf, int kb, float* mat, float* pbuf, unsigned int* status);
+__global__ void k_gj_panel(const SurfaceDesc* surf, int nsurf, int kb, const float* mat, const float* pbuf,
+                           float* rbuf, float* cbuf, const long long* poff);
+__global__ void k_gj_update(const SurfaceDesc* surf, int nsurf, int kb, float* mat, const float* pbuf,
+                            const float* rbuf, const float* cbuf, const long long* poff);
+__global__ void k_gemv(const SurfaceDesc* surf, const int2* rowblk, const float* mat, const double* v, double* y);
+__global__ void k_axpy_inplace(int n, double* a, const double* d);

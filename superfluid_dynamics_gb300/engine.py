@@ -1,0 +1,330 @@
+"""Host-side interface over the C ABI.
+
+`Engine` owns one batch of surfaces resident on the GPU.  The classes below it
+mirror the reference's C++ solver/stepper interface so code written against the
+reference reads the same here:
+
+  reference (CuSuperHelium/CuSuperHelium)              here
+  -------------------------------------------------    ---------------------------------
+  WaterBoundaryProblem<N,B>   (WaterBoundaryProblem.cuh:7-40)    WaterBoundaryProblem
+  HeliumBoundaryProblem<N,B>  (HeliumBoundaryProblem.cuh:6-47)   HeliumBoundaryProblem
+  BaseBoundaryIntegralCalculator<N,B>::run / calculateVorticities
+                              (BaseBoundaryIntegrator.cuh:137-314) BoundaryIntegralCalculator
+  AutonomousRungeKuttaStepper<std_complex,2N>
+                              (AutonomousRungeKuttaStepper.cuh:24-437) AutonomousRungeKuttaStepper
+  SimulationManager (Python/integration/rhs.py:68-365)            SimulationManager
+
+Arrays are float64 numpy arrays (host) or device pointers (ints) for the
+device-side calls.  Errors raise SfdError; nothing falls back to the CPU.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from ._lib import HELIUM, PRECISION_FP64, PRECISION_MIXED, WATER, SfdError, check
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _f64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+@dataclass
+class Physics:
+    """Nondimensional physics of one surface (sfd_problem)."""
+
+    physics: int = WATER
+    rho: float = 0.0
+    depth: float = 1.0
+    A3: float | None = None        # None: the reference's h^4 / 3
+    gravity: float = 1.0
+    U: float = 0.0
+    kappa: float = 0.0
+    infinite_depth: bool = False
+    use_expansions: bool = False
+    expansion_order: int = 1
+
+    def to_c(self) -> _lib.SfdProblem:
+        return _lib.SfdProblem(self.physics, 1 if self.infinite_depth else 0, self.rho, self.depth,
+                               self.A3 if self.A3 is not None else 0.0, self.gravity, self.U, self.kappa,
+                               1 if self.use_expansions else 0, self.expansion_order)
+
+
+@dataclass
+class Options:
+    precision: int = PRECISION_MIXED
+    refine_iters: int = 3
+    refactor_every: int = 1
+    use_graphs: bool = True
+    device: int = 0
+
+    def to_c(self) -> _lib.SfdOptions:
+        return _lib.SfdOptions(self.precision, self.refine_iters, self.refactor_every,
+                               1 if self.use_graphs else 0, self.device)
+
+
+class Engine:
+    """A batch of surfaces (possibly of different N) resident in device memory."""
+
+    def __init__(self, n, physics: Physics | list[Physics] | None = None, options: Options | None = None):
+        L = _lib.load()
+        ns = [int(n)] if np.isscalar(n) else [int(v) for v in n]
+        if physics is None:
+            physics = Physics()
+        shared = not isinstance(physics, (list, tuple))
+        probs = [physics] if shared else list(physics)
+        if not shared and len(probs) != len(ns):
+            raise ValueError("one Physics per surface required")
+        carr = (_lib.SfdProblem * len(probs))(*[p.to_c() for p in probs])
+        narr = (ctypes.c_int * len(ns))(*ns)
+        opt = (options or Options()).to_c()
+        h = ctypes.c_void_p()
+        check(L.sfd_create(narr, len(ns), carr, 1 if shared else 0, ctypes.byref(opt), ctypes.byref(h)))
+        self._h = h
+        self._L = L
+        self.sizes = ns
+        self.ntot = int(sum(ns))
+        self.nsurf = len(ns)
+        self.offsets = np.concatenate([[0], np.cumsum(ns)]).astype(np.int64)
+        self.options = options or Options()
+
+    # -- lifetime
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._L.sfd_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- state
+    def set_state(self, x, y, phi) -> None:
+        x, y, phi = _f64(x), _f64(y), _f64(phi)
+        if x.size != self.ntot or y.size != self.ntot or phi.size != self.ntot:
+            raise ValueError(f"state arrays must hold {self.ntot} nodes")
+        check(self._L.sfd_set_state_host(self._h, _dp(x), _dp(y), _dp(phi)))
+
+    def get_state(self):
+        x, y, phi = (np.empty(self.ntot) for _ in range(3))
+        check(self._L.sfd_get_state_host(self._h, _dp(x), _dp(y), _dp(phi)))
+        return x, y, phi
+
+    def set_state_device(self, x_ptr: int, y_ptr: int, phi_ptr: int) -> None:
+        check(self._L.sfd_set_state_device(self._h, x_ptr, y_ptr, phi_ptr))
+
+    def get_state_device(self, x_ptr: int, y_ptr: int, phi_ptr: int) -> None:
+        check(self._L.sfd_get_state_device(self._h, x_ptr, y_ptr, phi_ptr))
+
+    def state_device_ptr(self) -> int:
+        p = ctypes.c_void_p()
+        check(self._L.sfd_state_device_ptr(self._h, ctypes.byref(p)))
+        return int(p.value)
+
+    # -- evaluation
+    def rhs(self, diagnostics: bool = False):
+        """RHS of the resident state: (dx, dy, dphi)[, a, zp, zpp]."""
+        dx, dy, dphi, a = (np.empty(self.ntot) for _ in range(4))
+        zp = np.empty(self.ntot, np.complex128)
+        zpp = np.empty(self.ntot, np.complex128)
+        check(self._L.sfd_rhs_host(self._h, _dp(dx), _dp(dy), _dp(dphi), _dp(a),
+                                   zp.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                   zpp.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        if diagnostics:
+            return dx, dy, dphi, a, zp, zpp
+        return dx, dy, dphi
+
+    def rhs_device(self, state_ptr: int, out_ptr: int) -> None:
+        check(self._L.sfd_rhs_device(self._h, state_ptr, out_ptr))
+
+    def step(self, dt: float, steps: int = 1, sync: bool = True) -> None:
+        fn = self._L.sfd_rk4_steps if sync else self._L.sfd_rk4_steps_async
+        check(fn(self._h, float(dt), int(steps)))
+
+    def synchronize(self) -> None:
+        check(self._L.sfd_synchronize(self._h))
+
+    def invariants(self, kappa: float = 0.0) -> np.ndarray:
+        out = np.empty(5 * self.nsurf)
+        check(self._L.sfd_invariants(self._h, float(kappa), _dp(out)))
+        return out.reshape(self.nsurf, 5)
+
+    def status(self):
+        st = (ctypes.c_uint * self.nsurf)()
+        lm = np.empty(self.nsurf)
+        rn = np.empty(self.nsurf)
+        check(self._L.sfd_get_status(self._h, st, _dp(lm), _dp(rn)))
+        return np.array(list(st), dtype=np.uint32), lm, rn
+
+    def clear_status(self) -> None:
+        check(self._L.sfd_clear_status(self._h))
+
+    def set_stream(self, stream_ptr: int) -> None:
+        check(self._L.sfd_set_stream(self._h, stream_ptr))
+
+    def profile(self, enable: bool = True) -> None:
+        """Per-kernel-class CUDA-event timing (steps run without graphs meanwhile)."""
+        check(self._L.sfd_profile(self._h, 1 if enable else 0))
+
+    def profile_read(self) -> dict:
+        n = _lib.PROFILE_CLASSES
+        ms = np.zeros(n)
+        cnt = (ctypes.c_longlong * n)()
+        check(self._L.sfd_profile_read(self._h, _dp(ms), cnt, n))
+        return {self._L.sfd_profile_class_name(i).decode(): (float(ms[i]), int(cnt[i])) for i in range(n)}
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(self._L.sfd_kernel_launches(self._h))
+
+    def split(self, arr: np.ndarray) -> list[np.ndarray]:
+        return [arr[self.offsets[i]:self.offsets[i + 1]] for i in range(self.nsurf)]
+
+
+# ------------------------------------------------------------------ reference-shaped classes
+class WaterBoundaryProblem(Physics):
+    """Gravity water waves (WaterBoundaryProblem.cuh:7-40); rho is the density ratio."""
+
+    def __init__(self, rho: float = 0.0, gravity: float = 1.0):
+        super().__init__(physics=WATER, rho=rho, gravity=gravity)
+
+
+class HeliumBoundaryProblem(Physics):
+    """Finite-depth helium film (HeliumBoundaryProblem.cuh:6-47); A3 None = h^4/3."""
+
+    def __init__(self, depth: float, A3: float | None = None, infinite_depth: bool = False, kappa: float = 0.0,
+                 use_expansions: bool = False, expansion_order: int = 1):
+        super().__init__(physics=HELIUM, depth=depth, A3=A3, infinite_depth=infinite_depth, kappa=kappa,
+                         use_expansions=use_expansions, expansion_order=expansion_order)
+
+
+class BoundaryIntegralCalculator:
+    """run(state) -> rhs, with state / rhs laid out as the reference's real
+    adapter does (RealBoundaryIntegralCalculator.cuh:4-23): [x | y | phi]."""
+
+    def __init__(self, N: int, problem: Physics, options: Options | None = None, batch: int = 1):
+        self.N = N
+        self.batch = batch
+        self.engine = Engine([N] * batch, problem, options)
+
+    def run(self, state: np.ndarray) -> np.ndarray:
+        n = self.N * self.batch
+        state = _f64(state)
+        self.engine.set_state(state[:n], state[n:2 * n], state[2 * n:3 * n])
+        dx, dy, dphi = self.engine.rhs()
+        return np.concatenate([dx, dy, dphi])
+
+    def calculateVorticities(self, state: np.ndarray) -> np.ndarray:
+        n = self.N * self.batch
+        state = _f64(state)
+        self.engine.set_state(state[:n], state[n:2 * n], state[2 * n:3 * n])
+        return self.engine.rhs(diagnostics=True)[3]
+
+
+class AutonomousRungeKuttaStepper:
+    """Classic RK4 over a BoundaryIntegralCalculator (AutonomousRungeKuttaStepper.cuh:24-437)."""
+
+    def __init__(self, calculator: BoundaryIntegralCalculator, tstep: float = 1e-2):
+        self.calc = calculator
+        self.timeStep = tstep
+        self.currentTime = 0.0
+
+    def setTimeStep(self, tstep: float) -> None:
+        self.timeStep = tstep
+
+    def initialize(self, state: np.ndarray) -> None:
+        n = self.calc.N * self.calc.batch
+        state = _f64(state)
+        self.calc.engine.set_state(state[:n], state[n:2 * n], state[2 * n:3 * n])
+
+    def runStep(self) -> None:
+        self.calc.engine.step(self.timeStep, 1)
+        self.currentTime += self.timeStep
+
+    def runEvolution(self, startTime: float, endTime: float, log=None) -> None:
+        self.currentTime = startTime
+        steps = int((endTime - startTime) / self.timeStep)
+        for _ in range(steps):
+            self.calc.engine.step(self.timeStep, 1)
+            self.currentTime += self.timeStep
+            if log is not None:
+                log(self.currentTime, self.state())
+
+    def state(self) -> np.ndarray:
+        return np.concatenate(self.calc.engine.get_state())
+
+
+class SimulationManager:
+    """The reference's ctypes front end (Python/integration/rhs.py:68-365) over
+    the same exported symbols, for Linux / this library."""
+
+    def __init__(self, dll_path: str | None = None):
+        self.lib = _lib.load() if dll_path is None else ctypes.CDLL(dll_path)
+
+    def _rhs(self, fn, x, y, phi, *args):
+        x, y, phi = _f64(x), _f64(y), _f64(phi)
+        if y.shape[0] != x.shape[0] or phi.shape[0] != x.shape[0]:
+            raise ValueError("Input arrays must have the same length")
+        vx, vy, dphi = np.empty_like(x), np.empty_like(x), np.empty_like(x)
+        rc = fn(_dp(x), _dp(y), _dp(phi), _dp(vx), _dp(vy), _dp(dphi), *args)
+        return rc, vx, vy, dphi
+
+    def calculate_rhs_from_vectors(self, x, y, phi, L, rho, kappa, depth):
+        return self._rhs(self.lib.calculateRHSFromVectors, x, y, phi, L, rho, kappa, depth, len(x))
+
+    def calculate_rhs256_from_vectors(self, x, y, phi, L, rho, kappa, depth):
+        return self._rhs(self.lib.calculateRHS256FromVectors, x, y, phi, L, rho, kappa, depth)
+
+    def calculate_rhs2048_from_vectors(self, x, y, phi, L, rho, kappa, depth):
+        return self._rhs(self.lib.calculateRHS2048FromVectors, x, y, phi, L, rho, kappa, depth)
+
+    def calculate_rhs256_from_vectors_batched(self, x, y, phi, L, rho, kappa, depth, batch_size):
+        return self._rhs(self.lib.calculateRHS256FromVectorsBatched, x, y, phi, L, rho, kappa, depth, batch_size)
+
+    def calculate_vorticities256_from_vectors(self, Z, phi, L, rho, kappa, depth):
+        Z = np.ascontiguousarray(Z, dtype=np.complex128)
+        phi = np.ascontiguousarray(phi, dtype=np.complex128)
+        a = np.empty(Z.shape[0])
+        Zp = np.empty(Z.shape[0], np.complex128)
+        Zpp = np.empty(Z.shape[0], np.complex128)
+        cp = lambda v: v.ctypes.data_as(ctypes.POINTER(ctypes.c_double))  # noqa: E731
+        rc = self.lib.calculateVorticities256FromVectors(cp(Z), cp(phi), _dp(a), cp(Zp), cp(Zpp), L, rho, kappa, depth)
+        return rc, a, Zp, Zpp
+
+    def calculate_derivativeFFT256(self, inp):
+        inp = np.ascontiguousarray(inp, dtype=np.complex128)
+        out = np.empty(inp.shape[0], np.complex128)
+        cp = lambda v: v.ctypes.data_as(ctypes.POINTER(ctypes.c_double))  # noqa: E731
+        return self.lib.calculateDerivativeFFT256(cp(inp), cp(out)), out
+
+    def integrate_simulation_rk4(self, x, y, phi, L, rho, kappa, depth, t0, t1, dt, return_trajectory=True):
+        N = len(x)
+        state = np.concatenate([_f64(x), _f64(y), _f64(phi)])
+        sp = _lib.SimProperties(L, rho, kappa, depth, False, 1, False)
+        ro = _lib.RK4SolverOptions(dt, t0, t1, return_trajectory)
+        states = ctypes.POINTER(ctypes.c_double)()
+        times = ctypes.POINTER(ctypes.c_double)()
+        ns, nt = ctypes.c_size_t(), ctypes.c_size_t()
+        rc = self.lib.integrateSimulationRK4(_dp(state), ctypes.byref(states), ctypes.byref(ns), ctypes.byref(times),
+                                             ctypes.byref(nt), ctypes.byref(sp), ctypes.byref(ro), N)
+        if rc != 0:
+            raise SfdError(self.lib.sfd_last_error().decode())
+        S = np.ctypeslib.as_array(states, shape=(ns.value, 3 * N)).copy()
+        T = np.ctypeslib.as_array(times, shape=(nt.value,)).copy() if nt.value else np.empty(0)
+        self.lib.integrateSimulationRK4_freeMemory(states, times)
+        return S, T

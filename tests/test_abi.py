@@ -1,0 +1,50 @@
+"""CPU tests of the boundary: the C-ABI library builds for sm_103a, loads and
+exports every function include/sfd.h declares; calls that need no GPU behave."""
+import ctypes
+
+import pytest
+
+from superfluid_dynamics_gb300 import _lib, build
+
+
+def test_library_builds_and_exports_every_header_symbol():
+    path = build.build()
+    lib = ctypes.CDLL(path)
+    names = _lib.header_symbols()
+    assert "sfd_create" in names and "calculateRHSFromVectors" in names and "integrateSimulationRK4" in names
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, f"missing exports: {missing}"
+    # every bound signature is a header symbol
+    assert set(_lib._SIGS) <= set(names)
+
+
+def test_version_and_defaults_without_gpu():
+    L = _lib.load()
+    assert b"sm_103a" in L.sfd_version()
+    o = _lib.SfdOptions()
+    L.sfd_default_options(ctypes.byref(o))
+    assert o.precision == _lib.PRECISION_MIXED and o.refine_iters >= 1
+    p = _lib.SfdProblem()
+    L.sfd_default_problem(ctypes.byref(p))
+    assert p.physics == _lib.WATER and p.gravity == 1.0
+    assert L.sfd_set_default_precision(7) == -1
+    assert b"precision" in L.sfd_last_error()
+
+
+def test_struct_layouts_match_reference_exports():
+    # ExportTypes.cuh:8-40 field order / sizes as bound by the reference's rhs.py
+    assert ctypes.sizeof(_lib.SimProperties) == 48
+    assert ctypes.sizeof(_lib.RK4SolverOptions) == 32
+
+
+def test_create_without_device_fails_cleanly():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    L = _lib.load()
+    n = (ctypes.c_int * 1)(64)
+    p = _lib.SfdProblem()
+    L.sfd_default_problem(ctypes.byref(p))
+    h = ctypes.c_void_p()
+    rc = L.sfd_create(n, 1, ctypes.byref(p), 1, None, ctypes.byref(h))
+    assert rc == -4 and not h.value

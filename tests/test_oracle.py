@@ -1,0 +1,158 @@
+"""CPU tests: pin the FP64 oracle against the reference's own NumPy calculator
+(golden fixtures made by tests/golden/make_golden.py) and against the
+known-answer tests of the reference's gtest suite, re-derived here:
+  MatrixMTests.cuh:69-87,160-223   closed-form 2x2 M
+  MatrixMTests.cuh:89-115,225-282  M at N=4 vs a host restatement
+  MatrixMTests.cuh:117-151,396-468 V1, V2 at N=8
+  MatrixMTests.cuh:51-67,477-607   spectral derivatives of a Lagrangian Stokes wave, N=1024
+  MatrixMTests.cuh:735-820         water Bernoulli, N=32
+  ComplexFunctionsTests.cuh:169-244 cot Green's function vs a 50-digit value
+"""
+import cmath
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def rel(a, b):
+    return np.abs(np.asarray(a) - np.asarray(b)).max() / max(np.abs(b).max(), 1e-300)
+
+
+# --- Lagrangian Stokes wave of MatrixMTests.cuh:19-67 (per-index derivatives)
+def stokes(N, h, omega, t, rho=0.0):
+    j = 2 * np.pi * np.arange(N) / N
+    X = j - h * np.sin(j - omega * t)
+    Y = h * np.cos(j - omega * t)
+    Phi = h * (1 + rho) * omega * np.sin(j - omega * t)
+    s1, s2 = 2 * np.pi / N, 4 * np.pi ** 2 / N ** 2
+    Zp = s1 * ((1 - h * np.cos(j - omega * t)) + 1j * (-h * np.sin(j - omega * t)))
+    Zpp = s2 * ((h * np.sin(j - omega * t)) + 1j * (-h * np.cos(j - omega * t)))
+    PhiP = s1 * h * (1 + rho) * omega * np.cos(j - omega * t)
+    return X + 1j * Y, Phi, Zp, Zpp, PhiP
+
+
+@pytest.mark.parametrize("name", ["o1_linear_wave_n128_rhs", "o1_modes_seed2_n64_rhs",
+                                  "o1_modes_seed2_n256_rhs", "o1_steep_n64_rhs"])
+def test_oracle_rhs_matches_reference_numpy(name):
+    d = np.load(os.path.join(GOLD, name + ".npz"))
+    (dx, dy, dphi, a, zp, zpp), info = O.rhs(O.Problem(), d["x"], d["y"], d["phi"], diagnostics=True)
+    assert info == 0
+    # the reference NumPy code treats the Nyquist mode differently from the CUDA
+    # path (Derivatives.py:13-17 vs utilities.cuh:126-141): agreement ~1e-14
+    vel = dx + 1j * dy
+    for got, ref in [(vel, d["vx"] + 1j * d["vy"]), (dphi, d["dphi"]), (a, d["a"]),
+                     (zp, d["xp"] + 1j * d["yp"]), (zpp, d["xpp"] + 1j * d["ypp"])]:
+        assert rel(got, ref) < 1e-11
+
+
+def test_oracle_rk4_matches_reference_numpy():
+    d = np.load(os.path.join(GOLD, "o1_linear_wave_n128_rk4.npz"))
+    for steps in (1, 10, 100):
+        (x, y, phi), info = O.rk4_steps(O.Problem(), d["x"], d["y"], d["phi"], float(d["dt"]), steps)
+        assert info == 0
+        assert np.abs(x - d[f"x_{steps}"]).max() < 1e-13
+        assert np.abs(y - d[f"y_{steps}"]).max() < 1e-13
+        assert np.abs(phi - d[f"phi_{steps}"]).max() < 1e-13
+
+
+def test_two_by_two_M_closed_form():
+    h = 0.5
+    Z, _, Zp, Zpp, _ = stokes(2, h, 10.0, 0.0)
+    M = O.create_M(O.Problem(), Z, Zp, Zpp)
+    expect = np.array([[0.5 - 0.25 * h / (1 - h), (h - 1) / 4 * math.sinh(2 * h) / (math.cosh(2 * h) + 1)],
+                       [(h + 1) / 4 * math.sinh(2 * h) / (math.cosh(2 * h) + 1), 0.5 + 0.25 * h / (1 + h)]])
+    assert np.abs(M - expect).max() < 1e-14
+
+
+def test_M_n4_host_restatement():
+    N, h, om, t = 4, 0.5, 10.0, 0.1
+    Z, _, Zp, Zpp, _ = stokes(N, h, om, t)
+    M = O.create_M(O.Problem(), Z, Zp, Zpp)
+    for k in range(N):
+        for j in range(N):
+            if k == j:
+                e = 0.5 + 0.25 / math.pi * (Zpp[k] / Zp[k]).imag
+            else:
+                e = 0.25 / math.pi * (Zp[k] / cmath.tan(0.5 * (Z[k] - Z[j]))).imag
+            assert abs(M[k, j] - e) < 1e-14
+
+
+def test_velocity_n8_host_restatement():
+    N, h, om, t = 8, 0.5, 10.0, 0.1
+    Z, _, Zp, Zpp, _ = stokes(N, h, om, t)
+    rng = np.random.default_rng(8)
+    a = rng.standard_normal(N)
+    ap = rng.standard_normal(N) + 1j * rng.standard_normal(N)
+    V1 = np.empty((N, N), complex)
+    V2 = np.empty(N, complex)
+    for k in range(N):
+        for j in range(N):
+            if k == j:
+                V1[k, j] = -0.25j / math.pi * Zpp[k] / Zp[k] ** 2 + 0.5 / Zp[k]
+                V2[k] = 0.5j / (math.pi * Zp[k])
+            else:
+                V1[k, j] = -0.25j / math.pi / cmath.tan(0.5 * (Z[k] - Z[j]))
+    expect = np.conj(V1 @ a + V2 * ap)
+    vel = O.velocities(O.Problem(), Z, Zp, Zpp, a, ap)
+    assert rel(vel, expect) < 1e-13
+
+
+def test_stokes_derivatives_n1024():
+    N = 1024
+    Z, Phi, Zp, Zpp, PhiP = stokes(N, 0.5, 10.0, 0.0)
+    zp, php, zpp = O.zphi_derivative(Z, Phi.astype(complex))
+    assert np.abs(zp - Zp).max() < 1e-14
+    assert np.abs(zpp - Zpp).max() < 1e-14
+    assert np.abs(php.real - PhiP).max() < 1e-14
+
+
+def test_water_bernoulli_n32():
+    N, h, om, t = 32, 0.5, 10.0, 0.1
+    rng = np.random.default_rng(32)
+    Z = rng.standard_normal(N) + 1j * rng.standard_normal(N)
+    v = rng.standard_normal(N) + 1j * rng.standard_normal(N)
+    out = O.rhs_phi_water(Z, v, np.zeros(N, complex), 0.0, 1.0)
+    assert np.abs(out - (-Z.imag + 0.5 * np.abs(v) ** 2)).max() < 1e-14
+
+
+def test_cot_green_50_digits():
+    d = json.load(open(os.path.join(GOLD, "cot_50digit.json")))
+    zk = complex(math.pi, math.pi)
+    zj = complex(math.pi + 0.1, math.pi + 0.1)
+    v = O.cot_green(zk, zj)
+    assert abs(v.real - float(d["cot_re"])) < 1e-13
+    assert abs(v.imag - float(d["cot_im"])) < 1e-13
+
+
+@pytest.mark.parametrize("n", [8, 96, 128, 160, 32 * 61, 1024])
+def test_fft_matches_numpy(n):
+    rng = np.random.default_rng(n)
+    x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    assert rel(O.fft(x), np.fft.fft(x)) < 1e-14
+    assert rel(O.fft(x, inverse=True), np.fft.ifft(x) * n) < 1e-14
+
+
+def test_lu_solve_matches_numpy():
+    rng = np.random.default_rng(1)
+    A = rng.standard_normal((200, 200)) + 10 * np.eye(200)
+    b = rng.standard_normal(200)
+    x, info = O.lu_solve(A, b)
+    assert info == 0
+    assert rel(x, np.linalg.solve(A, b)) < 1e-12
+
+
+def test_helium_flat_film_is_stationary():
+    # flat film, phi = 0: the van der Waals offset makes dphi/dt = 0 and v = 0
+    N = 64
+    xi = 2 * np.pi * np.arange(N) / N
+    for A3 in (None, 1e3):
+        (dx, dy, dphi), info = O.rhs(O.Problem(physics=O.HELIUM, depth=10.0, A3=A3), xi, 0 * xi, 0 * xi)
+        assert info == 0
+        assert np.abs(dphi).max() < 1e-12 and np.abs(dy).max() < 1e-12
