@@ -142,6 +142,21 @@ const char* sfd_profile_class_name(int cls);
 const char* sfd_last_error(void);
 const char* sfd_version(void);
 
+/* One FP64 RHS evaluation of a single surface that allocates no device memory.
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc:
+ * code that runs inside another framework's memory pool, real-time loops that
+ * must not allocate after start-up, hosts that forbid runtime allocation.
+ * state_in = [x | y | phi] and rhs_out = [dx | dy | dphi] are device arrays of
+ * 3n doubles (same results as sfd_rhs_device on an FP64 engine).  Scratch is
+ * one static device array of about 8.7 MB, held by every GPU that loads the
+ * library until exit; n is limited to 1..1024 (larger n returns
+ * SFD_ERR_INVALID).  The call is asynchronous on `stream` (NULL = legacy
+ * default stream).  Its first call on a device resolves the array's device
+ * address, so make that first call before any stream capture.  All calls share
+ * the array, so calls that overlap on the GPU (different streams or threads)
+ * race; serialise them. */
+int sfd_rhs_device_noalloc(const sfd_problem* problem, int n, const void* state_in, void* rhs_out, void* stream);
+
 /* Precision used by the reference-compatible exports below (default FP64). */
 int sfd_set_default_precision(int precision);
 

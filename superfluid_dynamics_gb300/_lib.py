@@ -74,6 +74,7 @@ _SIGS = {
     "sfd_last_error": (c_char_p, []),
     "sfd_version": (c_char_p, []),
     "sfd_set_default_precision": (c_int, [c_int]),
+    "sfd_rhs_device_noalloc": (c_int, [POINTER(SfdProblem), c_int, c_void_p, c_void_p, c_void_p]),
     "calculateRHSFromVectors": (c_int, [_dp] * 6 + [c_double] * 4 + [c_size_t]),
     "calculateRHS256FromVectors": (c_int, [_dp] * 6 + [c_double] * 4),
     "calculateRHS2048FromVectors": (c_int, [_dp] * 6 + [c_double] * 4),

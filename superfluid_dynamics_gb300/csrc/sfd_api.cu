@@ -1038,3 +1038,185 @@ int integrateSimulationRK4_freeMemory(double* statesOut, double* timesOut) {
 }
 
 }  // extern "C"
+
+// ====================================================================== no-allocation RHS
+// sfd_rhs_device_noalloc: one FP64 RHS evaluation of a single surface for
+// callers that cannot call cudaMalloc (code running where the device memory
+// is owned by someone else: inside another framework's allocator, a real-time
+// loop that must not allocate after start-up, or a host that forbids runtime
+// allocation).  All scratch lives in the file-scope array below; the caller
+// passes only the state and the output.
+namespace noalloc {
+constexpr int kMaxN = 1024;  // stated maximum surface size
+constexpr size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+constexpr int kMaxChunks = (kMaxN + kSumChunk - 1) / kSumChunk;
+constexpr int kMaxItems = ((kMaxN + kSumTargets - 1) / kSumTargets) * kMaxChunks;
+constexpr int kMaxTiles = (kMaxN / 64) * (kMaxN / 64);
+constexpr size_t kBytes = align256(8ull * kMaxN * kMaxN)            // FP64 matrix (kMaxN is a multiple of 128)
+                          + 11 * align256(16ull * kMaxN)            // complex node arrays + twiddles
+                          + 2 * align256(16ull * kMaxChunks * kMaxN)  // sum partials
+                          + 5 * align256(8ull * kMaxN)              // real node arrays
+                          + align256(4ull * kMaxN)                  // node -> surface map
+                          + align256(sizeof(SurfaceDesc)) + 2 * align256(4 * sizeof(int2)) +
+                          align256(kMaxItems * sizeof(int4)) + align256(kMaxTiles * sizeof(int4)) +
+                          align256(8ull * kMaxChunks) + align256(16) + align256(4) + 2 * align256(8);
+constexpr int kMaxDevices = 64;
+}  // namespace noalloc
+
+// About 8.7 MB; every GPU that loads the library keeps it until the process exits.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[noalloc::kBytes];
+
+namespace {
+
+struct Bump {
+  unsigned char* p;
+  template <typename T>
+  T* take(size_t count) {
+    T* r = reinterpret_cast<T*>(p);
+    p += noalloc::align256(count * sizeof(T));
+    return r;
+  }
+};
+
+// Device address of g_noalloc_scratch for the current device (resolved once
+// per device, with that device current).
+int noalloc_base(unsigned char** out) {
+  static void* addr[noalloc::kMaxDevices] = {};
+  static std::mutex mu;
+  int dev = 0;
+  cudaError_t err = cudaGetDevice(&dev);
+  if (err != cudaSuccess) return sfd_fail(err);
+  if (dev < 0 || dev >= noalloc::kMaxDevices) return set_error(SFD_ERR_INVALID, "device %d out of range", dev);
+  std::lock_guard<std::mutex> lock(mu);
+  if (!addr[dev]) {
+    void* a = nullptr;
+    err = cudaGetSymbolAddress(&a, g_noalloc_scratch);
+    if (err != cudaSuccess) return set_error(SFD_ERR_CUDA, "cudaGetSymbolAddress(scratch) failed: %s", cudaGetErrorString(err));
+    addr[dev] = a;
+  }
+  *out = static_cast<unsigned char*>(addr[dev]);
+  return 0;
+}
+
+}  // namespace
+
+extern "C" int sfd_rhs_device_noalloc(const sfd_problem* problem, int n, const void* state_in, void* rhs_out,
+                                      void* stream) {
+  if (!problem || !state_in || !rhs_out) return set_error(SFD_ERR_INVALID, "sfd_rhs_device_noalloc: null argument");
+  if (n < 1 || n > noalloc::kMaxN)
+    return set_error(SFD_ERR_INVALID,
+                     "sfd_rhs_device_noalloc: n = %d is outside 1..%d, the size of its static scratch; use an engine "
+                     "(sfd_create) for larger surfaces",
+                     n, noalloc::kMaxN);
+  unsigned char* base = nullptr;
+  int rc = noalloc_base(&base);
+  if (rc) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int np = pad_n(n);
+  const int nchunk = (n + kSumChunk - 1) / kSumChunk;
+
+  // host-side descriptors, all on the stack
+  SurfaceDesc S;
+  std::memset(&S, 0, sizeof(S));
+  rc = fill_surface(S, *problem);
+  if (rc) return rc;
+  S.n = n;
+  S.off = 0;
+  S.moff = 0;
+  {
+    int m = n, k = 0;
+    while (m % 4 == 0 && k < SFD_MAX_RADICES) { S.rad[k++] = 4; m /= 4; }
+    while (m % 2 == 0 && k < SFD_MAX_RADICES) { S.rad[k++] = 2; m /= 2; }
+    for (int q = 3; m > 1 && k < SFD_MAX_RADICES; q += 2)
+      while (m % q == 0 && k < SFD_MAX_RADICES) { S.rad[k++] = q; m /= q; }
+    if (m != 1) return set_error(SFD_ERR_INVALID, "sfd_rhs_device_noalloc: n = %d has too many factors", n);
+    S.nrad = k;
+  }
+  cd tw[noalloc::kMaxN];
+  {
+    const long double two_pi = 6.283185307179586476925286766559005768L;
+    for (int e = 0; e < n; ++e) {
+      long double ang = two_pi * (long double)e / (long double)n;
+      tw[e] = cd{(double)cosl(ang), (double)(-sinl(ang))};
+    }
+    tw[0] = {1.0, 0.0};
+    if (n % 2 == 0) tw[n / 2] = {-1.0, 0.0};
+    if (n % 4 == 0) { tw[n / 4] = {0.0, -1.0}; tw[3 * n / 4] = {0.0, 1.0}; }
+  }
+  int2 jf[3] = {{0, SFD_JOB_ZP}, {0, SFD_JOB_ZPP}, {0, SFD_JOB_PHIP}};
+  int2 ja[1] = {{0, SFD_JOB_AP}};
+  int4 items[noalloc::kMaxItems];
+  int nitems = 0;
+  for (int t0 = 0; t0 < n; t0 += kSumTargets)
+    for (int c = 0; c < nchunk; ++c) items[nitems++] = {0, t0, c * kSumChunk, c};
+  int4 tiles[noalloc::kMaxTiles];
+  int ntiles = 0;
+  for (int r0 = 0; r0 < np; r0 += 64)
+    for (int c0 = 0; c0 < np; c0 += 64) tiles[ntiles++] = {0, r0, c0, 0};
+
+  // carve the static scratch (same order as its size computation)
+  Bump b{base};
+  sfd_engine e;  // on the stack; owns nothing (its containers stay empty)
+  e.m64 = b.take<double>((size_t)noalloc::kMaxN * noalloc::kMaxN);
+  e.zp = b.take<cd>(noalloc::kMaxN);
+  e.zpp = b.take<cd>(noalloc::kMaxN);
+  e.ap = b.take<cd>(noalloc::kMaxN);
+  e.nd.w = b.take<cd>(noalloc::kMaxN);
+  e.nd.p = b.take<cd>(noalloc::kMaxN);
+  e.nd.v1low = b.take<cd>(noalloc::kMaxN);
+  e.nd.v1up = b.take<cd>(noalloc::kMaxN);
+  e.nd.v2 = b.take<cd>(noalloc::kMaxN);
+  e.cacc = b.take<cd>(noalloc::kMaxN);
+  e.dacc = b.take<cd>(noalloc::kMaxN);
+  cd* d_tw = b.take<cd>(noalloc::kMaxN);
+  e.part_s = b.take<cd>((size_t)noalloc::kMaxChunks * noalloc::kMaxN);
+  e.part_t = b.take<cd>((size_t)noalloc::kMaxChunks * noalloc::kMaxN);
+  e.phip = b.take<double>(noalloc::kMaxN);
+  e.a = b.take<double>(noalloc::kMaxN);
+  e.r = b.take<double>(noalloc::kMaxN);
+  e.delta = b.take<double>(noalloc::kMaxN);
+  e.nd.mdiag = b.take<double>(noalloc::kMaxN);
+  e.d_node_surf = b.take<int>(noalloc::kMaxN);
+  e.d_surf = b.take<SurfaceDesc>(1);
+  e.d_jobs_first = b.take<int2>(4);
+  e.d_jobs_ap = b.take<int2>(4);
+  e.d_sum_items = b.take<int4>(noalloc::kMaxItems);
+  e.d_asm_tiles = b.take<int4>(noalloc::kMaxTiles);
+  e.part_a = b.take<double>(noalloc::kMaxChunks);
+  e.vel_low1 = b.take<cd>(1);
+  e.status = b.take<unsigned int>(1);
+  e.lmax = b.take<double>(1);
+  e.rnorm = b.take<double>(1);
+  if ((size_t)(b.p - base) > noalloc::kBytes) return set_error(SFD_ERR_INVALID, "scratch layout overflow");
+  S.tw = d_tw;
+
+  // upload descriptors; zero what the kernels accumulate into
+  CK(cudaMemcpyAsync(d_tw, tw, n * sizeof(cd), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(e.d_surf, &S, sizeof(S), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(e.d_jobs_first, jf, sizeof(jf), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(e.d_jobs_ap, ja, sizeof(ja), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(e.d_sum_items, items, nitems * sizeof(int4), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(e.d_asm_tiles, tiles, ntiles * sizeof(int4), cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(e.d_node_surf, 0, n * sizeof(int), st));
+  CK(cudaMemsetAsync(e.status, 0, sizeof(unsigned int), st));
+  CK(cudaMemsetAsync(e.lmax, 0, sizeof(double), st));
+  CK(cudaMemsetAsync(e.rnorm, 0, sizeof(double), st));
+
+  CK(cudaGetDevice(&e.device));
+  e.stream = st;
+  sfd_default_options(&e.opt);
+  e.opt.precision = SFD_PRECISION_FP64;
+  e.opt.use_graphs = 0;
+  e.opt.refine_iters = 0;
+  e.nsurf = 1;
+  e.ntot = n;
+  e.max_n = n;
+  e.max_np = np;
+  e.max_chunks = nchunk;
+  e.njobs_first = 3;
+  e.njobs_ap = 1;
+  e.nsum = nitems;
+  e.nasm = ntiles;
+  e.any_rho = (S.physics == 0 && S.rho != 0.0);
+  return enqueue_rhs(&e, static_cast<const double*>(state_in), static_cast<double*>(rhs_out), true);
+}
