@@ -145,7 +145,7 @@ def run_ours(args, rank, world, local_rank):
     s = workloads.random_modes(args.n, seed=2)
     prec = sfd.PRECISION_MIXED if args.precision == "mixed" else sfd.PRECISION_FP64
     opts = sfd.Options(precision=prec, refine_iters=args.refine_iters, refactor_every=args.refactor_every,
-                       device=local_rank)
+                       pre_iters=args.pre_iters, device=local_rank)
     eng = sfd.Engine(args.n, sfd.WaterBoundaryProblem(), opts)
     stream = torch.cuda.Stream(device=dev)
     eng.set_stream(stream.cuda_stream)
@@ -246,7 +246,7 @@ def run_ours(args, rank, world, local_rank):
             "vs_baseline": None, "dtype": "f64+df32 (mixed)" if args.precision == "mixed" else "f64",
             "data": "synthetic (seeded 8-mode gravity wave)",
             "config": {"workload": f"gravity wave N={n}, 8 modes seed 2, RK4 dt={DT}", "N": n,
-                       "precision": args.precision, "refine_iters": args.refine_iters,
+                       "precision": args.precision, "refine_iters": args.refine_iters, "pre_iters": args.pre_iters,
                        "refactor_every": args.refactor_every, "l2": "flushed (256 MB write) before every timed step",
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
             "roofline": roof, "cpu_baseline": cpu,
@@ -264,7 +264,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N_NODES)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
-    ap.add_argument("--refine-iters", type=int, default=3)
+    ap.add_argument("--refine-iters", type=int, default=2)
+    ap.add_argument("--pre-iters", type=int, default=1)
     ap.add_argument("--refactor-every", type=int, default=1)
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()

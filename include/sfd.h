@@ -48,6 +48,7 @@ extern "C" {
 #define SFD_STATUS_PIVOT_SWAP 0x2u      /* |l_ij| > 1: partial pivoting would have exchanged rows */
 #define SFD_STATUS_ZERO_PIVOT 0x4u
 #define SFD_STATUS_REFINE_STALL 0x8u
+#define SFD_STATUS_TIMEOUT 0x20u        /* a bounded in-kernel wait ran out; that work was skipped */
 
 /* Nondimensional physics of one surface; mirrors the fields of
  * ProblemProperties (CuSuperHelium/CuSuperHelium/ProblemProperties.hpp:5-32)
@@ -67,10 +68,12 @@ typedef struct sfd_problem {
 
 typedef struct sfd_options {
     int precision;        /* SFD_PRECISION_FP64 or SFD_PRECISION_MIXED                   */
-    int refine_iters;     /* mixed: correction iterations per RK stage (default 3)       */
+    int refine_iters;     /* mixed: FP32 corrections after the accurate pass (default 2) */
     int refactor_every;   /* mixed: rebuild the preconditioner every k RK4 steps (1)     */
     int use_graphs;       /* capture one RK4 step in a CUDA graph (1)                    */
     int device;           /* CUDA device ordinal (0)                                     */
+    int tensor_cores;     /* mixed: preconditioner update on tcgen05 tensor cores (1)    */
+    int pre_iters;        /* mixed: FP32 full-residual iterations before it (default 1)  */
 } sfd_options;
 
 typedef struct sfd_engine sfd_engine;
@@ -133,8 +136,8 @@ long long sfd_kernel_launches(const sfd_engine* e);
 /* Per-kernel-class device time: while enabled, RK4 steps run eagerly (no
  * graph) and every kernel launch is bracketed by CUDA events on the engine
  * stream; sfd_profile_read returns accumulated milliseconds and launch counts
- * per class (names from sfd_profile_class_name; 15 classes). */
-#define SFD_PROFILE_CLASSES 15
+ * per class (names from sfd_profile_class_name; 16 classes). */
+#define SFD_PROFILE_CLASSES 16
 int sfd_profile(sfd_engine* e, int enable);
 int sfd_profile_read(sfd_engine* e, double* ms, long long* counts, int nclass);
 const char* sfd_profile_class_name(int cls);
@@ -148,7 +151,7 @@ const char* sfd_version(void);
  * must not allocate after start-up, hosts that forbid runtime allocation.
  * state_in = [x | y | phi] and rhs_out = [dx | dy | dphi] are device arrays of
  * 3n doubles (same results as sfd_rhs_device on an FP64 engine).  Scratch is
- * one static device array of about 8.7 MB, held by every GPU that loads the
+ * one static device array of about 8.9 MB, held by every GPU that loads the
  * library until exit; n is limited to 1..1024 (larger n returns
  * SFD_ERR_INVALID).  The call is asynchronous on `stream` (NULL = legacy
  * default stream).  Its first call on a device resolves the array's device

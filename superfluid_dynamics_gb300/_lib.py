@@ -21,7 +21,8 @@ STATUS_NONFINITE = 0x1
 STATUS_PIVOT_SWAP = 0x2
 STATUS_ZERO_PIVOT = 0x4
 STATUS_REFINE_STALL = 0x8
-PROFILE_CLASSES = 15
+STATUS_TIMEOUT = 0x20
+PROFILE_CLASSES = 16
 
 
 class SfdProblem(ctypes.Structure):
@@ -32,7 +33,7 @@ class SfdProblem(ctypes.Structure):
 
 class SfdOptions(ctypes.Structure):
     _fields_ = [("precision", c_int), ("refine_iters", c_int), ("refactor_every", c_int),
-                ("use_graphs", c_int), ("device", c_int)]
+                ("use_graphs", c_int), ("device", c_int), ("tensor_cores", c_int), ("pre_iters", c_int)]
 
 
 class SimProperties(ctypes.Structure):

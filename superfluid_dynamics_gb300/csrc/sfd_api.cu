@@ -7,6 +7,7 @@
 // all enqueued on the engine stream with no host synchronisation; one RK4
 // step (4 evaluations + stage combines) is captured once into a CUDA graph and
 // replayed.  Host code never touches the per-stage data.
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -32,7 +33,7 @@ enum {
   SFD_K_SUMS64,
   SFD_K_SUMSDF,
   SFD_K_SUMS32,
-  SFD_K_EPILOGUE,
+  SFD_K_EPILOGUE,  // no launches: the sum epilogue runs inside the boundary-sum kernels
   SFD_K_ASSEMBLE,
   SFD_K_DIAG,
   SFD_K_PANEL,
@@ -41,6 +42,7 @@ enum {
   SFD_K_GEMV,
   SFD_K_VELOCITY,
   SFD_K_RK4,
+  SFD_K_UPDATE_TC,
   SFD_NCLASS
 };
 
@@ -128,6 +130,9 @@ struct sfd_engine {
   // work lists
   int2* d_jobs_first = nullptr; int njobs_first = 0;
   int2* d_jobs_ap = nullptr; int njobs_ap = 0;
+  int2* d_cjobs_first = nullptr; int ncjobs_first = 0;  // cluster-distributed transforms
+  int2* d_cjobs_ap = nullptr; int ncjobs_ap = 0;
+  int max_n_single = 0, max_n_cluster = 0;
   int4* d_sum_items = nullptr; int nsum = 0;
   int4* d_asm_tiles = nullptr; int nasm = 0;
   int2* d_gemv_rows = nullptr; int ngemv = 0;
@@ -138,15 +143,19 @@ struct sfd_engine {
   // stage data
   cd *zp = nullptr, *zpp = nullptr, *ap = nullptr;
   double *phip = nullptr, *a = nullptr, *r = nullptr, *delta = nullptr, *phi_im = nullptr;
+  float2 *adf = nullptr, *ddf = nullptr;  // double-float copies of a and delta
   NodeData nd{};
   cd *part_s = nullptr, *part_t = nullptr, *cacc = nullptr, *dacc = nullptr, *vel_low1 = nullptr;
-  double* part_a = nullptr;
+  double* part_a = nullptr;        // [target tile][chunk] weight sums
+  int* tile_count = nullptr;       // arrivals per target tile (boundary sums)
+  int ntiles_sum = 0;              // target tiles over all surfaces
   unsigned int* status = nullptr;
   double *lmax = nullptr, *rnorm = nullptr, *inv_out = nullptr;
   // matrices
   double* m64 = nullptr;
   float* m32 = nullptr;
   float *pbuf = nullptr, *rbuf = nullptr, *cbuf = nullptr;
+  __nv_bfloat16 *cparts = nullptr, *rparts = nullptr;  // tensor-core operands: 3 bf16 parts, panel_elems apart
   // graphs
   cudaGraphExec_t g_step[2] = {nullptr, nullptr};
   double g_dt = 0.0;
@@ -223,17 +232,16 @@ void drain_profile(sfd_engine* e) {
 
 inline int blocks_for(long long n, int t) { return (int)((n + t - 1) / t); }
 
-int enqueue_sums(sfd_engine* e, int prec, const double* weights) {
-  SumArgs A{e->d_surf, e->d_sum_items, e->nsurf, e->ntot, e->nd.w, e->nd.p, weights, e->part_s, e->part_t, e->part_a};
+// One boundary-sum pass over every surface with weights `weights`
+// (`weights_df` its double-float copy for the DF / FP32 passes); the fused
+// epilogue writes C, D and the residual (mode 0: r = phi' - M a, C/D
+// overwritten; mode 1: r -= M a, C/D accumulated).
+int enqueue_sums(sfd_engine* e, int prec, const double* weights, const float2* weights_df, int mode, bool track_norm) {
+  SumArgs A{e->d_surf, e->d_sum_items, e->nsurf, e->ntot, e->max_chunks, e->nd.w, e->nd.p, weights, e->nd.wdf,
+            e->nd.pdf, weights_df, e->part_s, e->part_t, e->part_a, e->tile_count, e->nd.mdiag, e->zp, e->phip,
+            e->cacc, e->dacc, e->r, track_norm ? e->rnorm : nullptr, mode};
   int cls = prec == SFD_PREC_F64 ? SFD_K_SUMS64 : prec == SFD_PREC_DF ? SFD_K_SUMSDF : SFD_K_SUMS32;
   LAUNCHC(e, cls, sfd_launch_sums(prec, A, e->nsum, e->stream));
-  return 0;
-}
-
-int enqueue_epilogue(sfd_engine* e, const double* weights, int mode, bool track_norm) {
-  EpiArgs E{e->d_surf, e->d_node_surf, e->nsurf, e->ntot, e->part_s, e->part_t, e->part_a, weights, e->nd.w,
-            e->zp, e->nd.mdiag, e->phip, e->cacc, e->dacc, e->r, track_norm ? e->rnorm : nullptr};
-  LAUNCHC(e, SFD_K_EPILOGUE, k_sum_epilogue<<<blocks_for(e->ntot, 256), 256, 0, e->stream>>>(E, mode));
   return 0;
 }
 
@@ -243,12 +251,25 @@ int enqueue_precond(sfd_engine* e) {
                                   e->stream));
   const int tiles = e->max_np / 64;
   for (int kb = 0; kb < nb; ++kb) {
-    LAUNCHC(e, SFD_K_DIAG, k_gj_diag<<<e->nsurf, 512, 128 * 129 * sizeof(float), e->stream>>>(e->d_surf, e->nsurf, kb, e->m32,
+    LAUNCHC(e, SFD_K_DIAG, k_gj_diag<<<e->nsurf, 512, kGjDiagSmem, e->stream>>>(e->d_surf, e->nsurf, kb, e->m32,
                                                                                   e->pbuf, e->status));
-    LAUNCHC(e, SFD_K_PANEL, k_gj_panel<<<dim3(tiles, 1, e->nsurf), 256, 0, e->stream>>>(e->d_surf, e->nsurf, kb, e->m32, e->pbuf,
-                                                                          e->rbuf, e->cbuf, e->d_poff));
-    LAUNCHC(e, SFD_K_UPDATE, k_gj_update<<<dim3(tiles, tiles, e->nsurf), 256, 0, e->stream>>>(e->d_surf, e->nsurf, kb, e->m32,
-                                                                               e->pbuf, e->rbuf, e->cbuf, e->d_poff));
+    const bool tc = e->opt.tensor_cores != 0;
+    LAUNCHC(e, SFD_K_PANEL,
+            k_gj_panel<<<dim3(tiles, 1, e->nsurf), 256, 0, e->stream>>>(
+                e->d_surf, e->nsurf, kb, e->m32, e->pbuf, e->rbuf, e->cbuf, e->d_poff, tc ? e->cparts : nullptr,
+                tc ? e->rparts : nullptr, e->panel_elems));
+    if (tc) {
+      LAUNCHC(e, SFD_K_UPDATE,
+              k_gj_update<<<dim3(4 * tiles - 4, 1, e->nsurf), 256, 0, e->stream>>>(
+                  e->d_surf, e->nsurf, kb, e->m32, e->pbuf, e->rbuf, e->cbuf, e->d_poff, 1));
+      LAUNCHC(e, SFD_K_UPDATE_TC,
+              sfd_launch_gj_update_tc(e->d_surf, e->nsurf, kb, e->max_np, e->m32, e->cparts, e->rparts,
+                                      e->panel_elems, e->d_poff, e->status, e->stream));
+    } else {
+      LAUNCHC(e, SFD_K_UPDATE,
+              k_gj_update<<<dim3(tiles, tiles, e->nsurf), 256, 0, e->stream>>>(
+                  e->d_surf, e->nsurf, kb, e->m32, e->pbuf, e->rbuf, e->cbuf, e->d_poff, 0));
+    }
   }
   return 0;
 }
@@ -260,8 +281,12 @@ int enqueue_solve(sfd_engine* e, const double* st, const double* phi_im, bool re
   const int nt = e->ntot;
   const double *x = st, *y = st + nt, *phi = st + 2 * nt;
   DerivArgs D{e->d_surf, e->nsurf, x, y, phi, phi_im, e->a, e->zp, e->zpp, e->phip, e->ap};
-  LAUNCHC(e, SFD_K_SPECTRAL, sfd_launch_spectral(D, e->d_jobs_first, e->njobs_first, e->max_n, e->stream));
-  LAUNCHC(e, SFD_K_NODE, k_node_prep<<<blocks_for(nt, 256), 256, 0, e->stream>>>(e->d_surf, e->d_node_surf, nt, x, y, e->zp,
+  if (e->njobs_first)
+    LAUNCHC(e, SFD_K_SPECTRAL, sfd_launch_spectral(D, e->d_jobs_first, e->njobs_first, e->max_n_single, e->stream));
+  if (e->ncjobs_first)
+    LAUNCHC(e, SFD_K_SPECTRAL,
+            sfd_launch_spectral_cluster(D, e->d_cjobs_first, e->ncjobs_first, e->max_n_cluster, e->stream));
+  LAUNCHC(e, SFD_K_NODE, k_node_prep<<<blocks_for(nt, 32), 32, 0, e->stream>>>(e->d_surf, e->d_node_surf, nt, x, y, e->zp,
                                                                      e->zpp, e->nd));
   if (e->opt.precision == SFD_PRECISION_FP64) {
     LAUNCHC(e, SFD_K_ASSEMBLE, sfd_launch_assemble64(e->d_surf, e->d_asm_tiles, e->nasm, e->nd.w, e->nd.p, e->zp, e->nd.mdiag,
@@ -277,9 +302,7 @@ int enqueue_solve(sfd_engine* e, const double* st, const double* phi_im, bool re
     }
     LAUNCHC(e, SFD_K_TRSV, k_lu64_solve<<<e->nsurf, 256, e->max_np * sizeof(double), e->stream>>>(e->d_surf, e->m64, e->phip,
                                                                                        e->a));
-    int rc = enqueue_sums(e, SFD_PREC_F64, e->a);
-    if (rc) return rc;
-    rc = enqueue_epilogue(e, e->a, 0, true);
+    int rc = enqueue_sums(e, SFD_PREC_F64, e->a, nullptr, 0, true);
     if (rc) return rc;
   } else {
     if (refactor || !e->have_precond) {
@@ -287,18 +310,26 @@ int enqueue_solve(sfd_engine* e, const double* st, const double* phi_im, bool re
       if (rc) return rc;
       e->have_precond = true;
     }
-    // a0 = X phi'; accurate residual; FP32 corrections
-    LAUNCHC(e, SFD_K_GEMV, k_gemv<<<e->ngemv, 256, 0, e->stream>>>(e->d_surf, e->d_gemv_rows, e->m32, e->phip, e->a));
-    int rc = enqueue_sums(e, SFD_PREC_DF, e->a);
-    if (rc) return rc;
-    rc = enqueue_epilogue(e, e->a, 0, e->opt.refine_iters == 0);
+    // a0 = X phi'; FP32 pre-iterations (full residual in FP32) bring a within
+    // ~1e-7 of the solution; one double-float pass then gives the accurate
+    // residual and C(a); FP32 post-iterations correct the small remainder.
+    LAUNCHC(e, SFD_K_GEMV, k_gemv<<<e->ngemv, 256, e->max_np * sizeof(float), e->stream>>>(
+                               e->d_surf, e->d_gemv_rows, e->m32, e->phip, e->a, e->adf));
+    int rc = 0;
+    for (int it = 0; it < e->opt.pre_iters; ++it) {
+      rc = enqueue_sums(e, SFD_PREC_F32, e->a, e->adf, 0, false);
+      if (rc) return rc;
+      LAUNCHC(e, SFD_K_GEMV, k_gemv<<<e->ngemv, 256, e->max_np * sizeof(float), e->stream>>>(
+                                 e->d_surf, e->d_gemv_rows, e->m32, e->r, e->delta, nullptr));
+      LAUNCH(e, k_axpy_inplace<<<blocks_for(nt, 256), 256, 0, e->stream>>>(nt, e->a, e->delta, e->adf));
+    }
+    rc = enqueue_sums(e, SFD_PREC_DF, e->a, e->adf, 0, e->opt.refine_iters == 0);
     if (rc) return rc;
     for (int it = 0; it < e->opt.refine_iters; ++it) {
-      LAUNCHC(e, SFD_K_GEMV, k_gemv<<<e->ngemv, 256, 0, e->stream>>>(e->d_surf, e->d_gemv_rows, e->m32, e->r, e->delta));
-      LAUNCH(e, k_axpy_inplace<<<blocks_for(nt, 256), 256, 0, e->stream>>>(nt, e->a, e->delta));
-      rc = enqueue_sums(e, SFD_PREC_F32, e->delta);
-      if (rc) return rc;
-      rc = enqueue_epilogue(e, e->delta, 1, it == e->opt.refine_iters - 1);
+      LAUNCHC(e, SFD_K_GEMV, k_gemv<<<e->ngemv, 256, e->max_np * sizeof(float), e->stream>>>(
+                                 e->d_surf, e->d_gemv_rows, e->m32, e->r, e->delta, e->ddf));
+      LAUNCH(e, k_axpy_inplace<<<blocks_for(nt, 256), 256, 0, e->stream>>>(nt, e->a, e->delta, nullptr));
+      rc = enqueue_sums(e, SFD_PREC_F32, e->delta, e->ddf, 1, it == e->opt.refine_iters - 1);
       if (rc) return rc;
     }
   }
@@ -313,11 +344,15 @@ int enqueue_rhs(sfd_engine* e, const double* st, double* out, bool refactor) {
   const double* y = st + nt;
   DerivArgs D{e->d_surf, e->nsurf, st, y, st + 2 * nt, nullptr, e->a, e->zp, e->zpp, e->phip, e->ap};
   // a' and the velocity / Bernoulli epilogue
-  LAUNCHC(e, SFD_K_SPECTRAL, sfd_launch_spectral(D, e->d_jobs_ap, e->njobs_ap, e->max_n, e->stream));
+  if (e->njobs_ap)
+    LAUNCHC(e, SFD_K_SPECTRAL, sfd_launch_spectral(D, e->d_jobs_ap, e->njobs_ap, e->max_n_single, e->stream));
+  if (e->ncjobs_ap)
+    LAUNCHC(e, SFD_K_SPECTRAL,
+            sfd_launch_spectral_cluster(D, e->d_cjobs_ap, e->ncjobs_ap, e->max_n_cluster, e->stream));
   VelArgs V{e->d_surf, e->d_node_surf, e->nsurf, nt, e->cacc, e->dacc, e->a, e->ap, e->nd.v1low, e->nd.v1up,
             e->nd.v2, y, e->zp, e->zpp, e->vel_low1, out, out + nt, out + 2 * nt, e->status};
   if (e->any_rho) LAUNCHC(e, SFD_K_VELOCITY, k_velocity_node1<<<1, 32, 0, e->stream>>>(V));
-  LAUNCHC(e, SFD_K_VELOCITY, k_velocity_bernoulli<<<blocks_for(nt, 256), 256, 0, e->stream>>>(V));
+  LAUNCHC(e, SFD_K_VELOCITY, k_velocity_bernoulli<<<blocks_for(nt, 32), 32, 0, e->stream>>>(V));
   return 0;
 }
 
@@ -407,11 +442,11 @@ void free_engine(sfd_engine* e) {
   cudaSetDevice(e->device);
   if (e->stream) cudaStreamSynchronize(e->stream);
   destroy_graphs(e);
-  void* ptrs[] = {e->d_surf, e->d_node_surf, e->d_jobs_first, e->d_jobs_ap, e->d_sum_items, e->d_asm_tiles,
+  void* ptrs[] = {e->d_surf, e->d_node_surf, e->d_jobs_first, e->d_jobs_ap, e->d_cjobs_first, e->d_cjobs_ap, e->d_sum_items, e->d_asm_tiles,
                   e->d_gemv_rows, e->d_poff, e->y0, e->ys, e->kacc, e->kcur, e->zp, e->zpp, e->ap, e->phip, e->a,
-                  e->r, e->delta, e->phi_im, e->nd.w, e->nd.p, e->nd.mdiag, e->nd.v1low, e->nd.v1up, e->nd.v2,
-                  e->part_s, e->part_t, e->cacc, e->dacc, e->vel_low1, e->part_a, e->status, e->lmax, e->rnorm,
-                  e->inv_out, e->m64, e->m32, e->pbuf, e->rbuf, e->cbuf};
+                  e->r, e->delta, e->phi_im, e->nd.w, e->nd.p, e->nd.wdf, e->nd.pdf, e->adf, e->ddf, e->nd.mdiag, e->nd.v1low, e->nd.v1up, e->nd.v2,
+                  e->part_s, e->part_t, e->cacc, e->dacc, e->vel_low1, e->part_a, e->tile_count, e->status, e->lmax, e->rnorm,
+                  e->inv_out, e->m64, e->m32, e->pbuf, e->rbuf, e->cbuf, e->cparts, e->rparts};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   drain_profile(e);
@@ -451,10 +486,12 @@ extern "C" {
 void sfd_default_options(sfd_options* o) {
   if (!o) return;
   o->precision = SFD_PRECISION_MIXED;
-  o->refine_iters = 3;
+  o->refine_iters = 2;
   o->refactor_every = 1;
   o->use_graphs = 1;
   o->device = 0;
+  o->tensor_cores = 1;
+  o->pre_iters = 1;
 }
 
 void sfd_default_problem(sfd_problem* p) {
@@ -490,6 +527,7 @@ int sfd_create(const int* n, int nsurf, const sfd_problem* problems, int shared_
     return set_error(SFD_ERR_INVALID, "unknown precision %d", e->opt.precision);
   }
   if (e->opt.refine_iters < 0) e->opt.refine_iters = 0;
+  if (e->opt.pre_iters < 0) e->opt.pre_iters = 0;
   e->device = e->opt.device;
   if (e->device < 0 || e->device >= ndev) {
     delete e;
@@ -535,6 +573,14 @@ int sfd_create(const int* n, int nsurf, const sfd_problem* problems, int shared_
     }
     S.nrad = (int)rad.size();
     for (size_t i = 0; i < rad.size(); ++i) S.rad[i] = rad[i];
+    S.nrad_m = 0;
+    if (ns % (SFD_FFT_CLUSTER * SFD_FFT_CLUSTER) == 0 && ns >= SFD_FFT_CLUSTER_MIN_N) {
+      std::vector<int> radm;
+      if (factorize(ns / SFD_FFT_CLUSTER, radm)) {
+        S.nrad_m = (int)radm.size();
+        for (size_t i = 0; i < radm.size(); ++i) S.rad_m[i] = radm[i];
+      }
+    }
     if (!e->d_tw.count(ns)) {
       std::vector<cd> t = twiddles(ns);
       cd* d = nullptr;
@@ -563,26 +609,39 @@ int sfd_create(const int* n, int nsurf, const sfd_problem* problems, int shared_
   const int nt = e->ntot;
   // work lists
   std::vector<int> node_surf(nt);
-  std::vector<int2> jf, ja;
+  std::vector<int2> jf, ja, cjf, cja;
   std::vector<int4> items, tiles;
   std::vector<int2> rows;
   for (int s = 0; s < nsurf; ++s) {
     const SurfaceDesc& S = e->hs[s];
     for (int k = 0; k < S.n; ++k) node_surf[S.off + k] = s;
-    jf.push_back({s, SFD_JOB_ZP});
-    jf.push_back({s, SFD_JOB_ZPP});
-    jf.push_back({s, SFD_JOB_PHIP});
-    ja.push_back({s, SFD_JOB_AP});
+    if (S.nrad_m > 0) {
+      cjf.push_back({s, SFD_JOB_ZP});  // the cluster Z job writes z' and z''
+      cjf.push_back({s, SFD_JOB_PHIP});
+      cja.push_back({s, SFD_JOB_AP});
+      e->max_n_cluster = std::max(e->max_n_cluster, S.n);
+    } else {
+      jf.push_back({s, SFD_JOB_ZP});
+      jf.push_back({s, SFD_JOB_ZPP});
+      jf.push_back({s, SFD_JOB_PHIP});
+      ja.push_back({s, SFD_JOB_AP});
+      e->max_n_single = std::max(e->max_n_single, S.n);
+    }
     int nch = (S.n + kSumChunk - 1) / kSumChunk;
-    for (int t0 = 0; t0 < S.n; t0 += kSumTargets)
+    e->hs[s].tile_base = e->ntiles_sum;
+    for (int t0 = 0; t0 < S.n; t0 += kSumTargets) {
       for (int c = 0; c < nch; ++c) items.push_back({s, t0, c * kSumChunk, c});
+      ++e->ntiles_sum;
+    }
     int np = pad_n(S.n);
     for (int r0 = 0; r0 < np; r0 += 64)
       for (int c0 = 0; c0 < np; c0 += 64) tiles.push_back({s, r0, c0, 0});
-    for (int r0 = 0; r0 < S.n; r0 += 8) rows.push_back({s, r0});
+    for (int r0 = 0; r0 < S.n; r0 += kGemvRows) rows.push_back({s, r0});
   }
   e->njobs_first = (int)jf.size();
   e->njobs_ap = (int)ja.size();
+  e->ncjobs_first = (int)cjf.size();
+  e->ncjobs_ap = (int)cja.size();
   e->nsum = (int)items.size();
   e->nasm = (int)tiles.size();
   e->ngemv = (int)rows.size();
@@ -594,6 +653,10 @@ int sfd_create(const int* n, int nsurf, const sfd_problem* problems, int shared_
   CKE(cudaMemcpy(e->d_jobs_first, jf.data(), jf.size() * sizeof(int2), cudaMemcpyHostToDevice));
   CKE(dalloc(&e->d_jobs_ap, ja.size()));
   CKE(cudaMemcpy(e->d_jobs_ap, ja.data(), ja.size() * sizeof(int2), cudaMemcpyHostToDevice));
+  CKE(dalloc(&e->d_cjobs_first, cjf.size()));
+  CKE(cudaMemcpy(e->d_cjobs_first, cjf.data(), cjf.size() * sizeof(int2), cudaMemcpyHostToDevice));
+  CKE(dalloc(&e->d_cjobs_ap, cja.size()));
+  CKE(cudaMemcpy(e->d_cjobs_ap, cja.data(), cja.size() * sizeof(int2), cudaMemcpyHostToDevice));
   CKE(dalloc(&e->d_sum_items, items.size()));
   CKE(cudaMemcpy(e->d_sum_items, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice));
   CKE(dalloc(&e->d_asm_tiles, tiles.size()));
@@ -616,13 +679,19 @@ int sfd_create(const int* n, int nsurf, const sfd_problem* problems, int shared_
   CKE(dalloc(&e->delta, nt));
   CKE(dalloc(&e->nd.w, nt));
   CKE(dalloc(&e->nd.p, nt));
+  CKE(dalloc(&e->nd.wdf, nt));
+  CKE(dalloc(&e->nd.pdf, nt));
+  CKE(dalloc(&e->adf, nt));
+  CKE(dalloc(&e->ddf, nt));
   CKE(dalloc(&e->nd.mdiag, nt));
   CKE(dalloc(&e->nd.v1low, nt));
   CKE(dalloc(&e->nd.v1up, nt));
   CKE(dalloc(&e->nd.v2, nt));
   CKE(dalloc(&e->part_s, (long long)e->max_chunks * nt));
   CKE(dalloc(&e->part_t, (long long)e->max_chunks * nt));
-  CKE(dalloc(&e->part_a, (long long)e->max_chunks * nsurf));
+  CKE(dalloc(&e->part_a, (long long)e->max_chunks * e->ntiles_sum));
+  CKE(dalloc(&e->tile_count, e->ntiles_sum));
+  CKE(cudaMemset(e->tile_count, 0, e->ntiles_sum * sizeof(int)));
   CKE(dalloc(&e->cacc, nt));
   CKE(dalloc(&e->dacc, nt));
   CKE(dalloc(&e->vel_low1, 1));
@@ -635,6 +704,7 @@ int sfd_create(const int* n, int nsurf, const sfd_problem* problems, int shared_
   CKE(cudaMemset(e->rnorm, 0, nsurf * sizeof(double)));
   CKE(cudaMemset(e->y0, 0, 3LL * nt * sizeof(double)));
   CKE(cudaMemset(e->nd.p, 0, nt * sizeof(cd)));
+  CKE(cudaMemset(e->nd.pdf, 0, nt * sizeof(float4)));
   CKE(cudaMemset(e->dacc, 0, nt * sizeof(cd)));
   CKE(cudaMemset(e->part_t, 0, (long long)e->max_chunks * nt * sizeof(cd)));
   if (e->opt.precision == SFD_PRECISION_FP64) {
@@ -644,9 +714,14 @@ int sfd_create(const int* n, int nsurf, const sfd_problem* problems, int shared_
     CKE(dalloc(&e->pbuf, (long long)nsurf * 128 * 128));
     CKE(dalloc(&e->rbuf, e->panel_elems));
     CKE(dalloc(&e->cbuf, e->panel_elems));
+    if (e->opt.tensor_cores) {
+      CKE(dalloc(&e->cparts, 3 * e->panel_elems));
+      CKE(dalloc(&e->rparts, 3 * e->panel_elems));
+      CKE(sfd_tc_configure());
+    }
   }
   CKE(sfd_fft_configure());
-  CKE(cudaFuncSetAttribute(k_gj_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, 128 * 129 * (int)sizeof(float)));
+  CKE(cudaFuncSetAttribute(k_gj_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, kGjDiagSmem));
   CKE(cudaFuncSetAttribute(k_lu64_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, 8320 * (int)sizeof(double)));
 #undef CKE
   *out = e;
@@ -779,7 +854,7 @@ const char* sfd_profile_class_name(int cls) {
   static const char* names[SFD_NCLASS] = {"other", "spectral_deriv", "node_prep", "boundary_sums_fp64",
                                           "boundary_sums_df", "boundary_sums_fp32", "sum_epilogue", "assemble",
                                           "factor_diag", "factor_panel", "factor_update", "lu_trsv", "gemv",
-                                          "velocity_bernoulli", "rk4_combine"};
+                                          "velocity_bernoulli", "rk4_combine", "factor_update_tcgen05"};
   return (cls >= 0 && cls < SFD_NCLASS) ? names[cls] : "";
 }
 
@@ -966,7 +1041,7 @@ int calculateDerivativeFFT256(const double* input, double* output) {
     if (!rc) cudaMemcpy(dj, &job, sizeof(int2), cudaMemcpyHostToDevice);
     const int nt = e->ntot;
     DerivArgs D{e->d_surf, e->nsurf, e->y0, e->y0 + nt, e->y0 + 2 * nt, nullptr, e->a, e->zp, e->zpp, e->phip, e->ap};
-    if (!rc && sfd_launch_spectral(D, dj, 1, n, e->stream) != cudaSuccess) rc = SFD_ERR_CUDA;
+    if (!rc && sfd_launch_spectral(D, dj, 1, n, e->stream) != cudaSuccess) rc = SFD_ERR_CUDA;  // single-CTA job
     if (!rc) {
       cudaStreamSynchronize(e->stream);
       if (cudaMemcpy(output, e->ap, n * sizeof(cd), cudaMemcpyDeviceToHost) != cudaSuccess) rc = SFD_ERR_CUDA;
@@ -1050,20 +1125,22 @@ namespace noalloc {
 constexpr int kMaxN = 1024;  // stated maximum surface size
 constexpr size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 constexpr int kMaxChunks = (kMaxN + kSumChunk - 1) / kSumChunk;
-constexpr int kMaxItems = ((kMaxN + kSumTargets - 1) / kSumTargets) * kMaxChunks;
+constexpr int kMaxTgtTiles = (kMaxN + kSumTargets - 1) / kSumTargets;
+constexpr int kMaxItems = kMaxTgtTiles * kMaxChunks;
 constexpr int kMaxTiles = (kMaxN / 64) * (kMaxN / 64);
 constexpr size_t kBytes = align256(8ull * kMaxN * kMaxN)            // FP64 matrix (kMaxN is a multiple of 128)
-                          + 11 * align256(16ull * kMaxN)            // complex node arrays + twiddles
+                          + 13 * align256(16ull * kMaxN)            // complex node arrays, twiddles, df copies
                           + 2 * align256(16ull * kMaxChunks * kMaxN)  // sum partials
                           + 5 * align256(8ull * kMaxN)              // real node arrays
                           + align256(4ull * kMaxN)                  // node -> surface map
                           + align256(sizeof(SurfaceDesc)) + 2 * align256(4 * sizeof(int2)) +
                           align256(kMaxItems * sizeof(int4)) + align256(kMaxTiles * sizeof(int4)) +
-                          align256(8ull * kMaxChunks) + align256(16) + align256(4) + 2 * align256(8);
+                          align256(8ull * kMaxChunks * kMaxTgtTiles) + align256(4ull * kMaxTgtTiles) + align256(16) +
+                          align256(4) + 2 * align256(8);
 constexpr int kMaxDevices = 64;
 }  // namespace noalloc
 
-// About 8.7 MB; every GPU that loads the library keeps it until the process exits.
+// About 8.9 MB; every GPU that loads the library keeps it until the process exits.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[noalloc::kBytes];
 
 namespace {
@@ -1163,6 +1240,8 @@ extern "C" int sfd_rhs_device_noalloc(const sfd_problem* problem, int n, const v
   e.ap = b.take<cd>(noalloc::kMaxN);
   e.nd.w = b.take<cd>(noalloc::kMaxN);
   e.nd.p = b.take<cd>(noalloc::kMaxN);
+  e.nd.wdf = b.take<float4>(noalloc::kMaxN);
+  e.nd.pdf = b.take<float4>(noalloc::kMaxN);
   e.nd.v1low = b.take<cd>(noalloc::kMaxN);
   e.nd.v1up = b.take<cd>(noalloc::kMaxN);
   e.nd.v2 = b.take<cd>(noalloc::kMaxN);
@@ -1182,7 +1261,8 @@ extern "C" int sfd_rhs_device_noalloc(const sfd_problem* problem, int n, const v
   e.d_jobs_ap = b.take<int2>(4);
   e.d_sum_items = b.take<int4>(noalloc::kMaxItems);
   e.d_asm_tiles = b.take<int4>(noalloc::kMaxTiles);
-  e.part_a = b.take<double>(noalloc::kMaxChunks);
+  e.part_a = b.take<double>((size_t)noalloc::kMaxChunks * noalloc::kMaxTgtTiles);
+  e.tile_count = b.take<int>(noalloc::kMaxTgtTiles);
   e.vel_low1 = b.take<cd>(1);
   e.status = b.take<unsigned int>(1);
   e.lmax = b.take<double>(1);
@@ -1198,6 +1278,7 @@ extern "C" int sfd_rhs_device_noalloc(const sfd_problem* problem, int n, const v
   CK(cudaMemcpyAsync(e.d_sum_items, items, nitems * sizeof(int4), cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(e.d_asm_tiles, tiles, ntiles * sizeof(int4), cudaMemcpyHostToDevice, st));
   CK(cudaMemsetAsync(e.d_node_surf, 0, n * sizeof(int), st));
+  CK(cudaMemsetAsync(e.tile_count, 0, noalloc::kMaxTgtTiles * sizeof(int), st));
   CK(cudaMemsetAsync(e.status, 0, sizeof(unsigned int), st));
   CK(cudaMemsetAsync(e.lmax, 0, sizeof(double), st));
   CK(cudaMemsetAsync(e.rnorm, 0, sizeof(double), st));
@@ -1208,14 +1289,17 @@ extern "C" int sfd_rhs_device_noalloc(const sfd_problem* problem, int n, const v
   e.opt.precision = SFD_PRECISION_FP64;
   e.opt.use_graphs = 0;
   e.opt.refine_iters = 0;
+  e.opt.pre_iters = 0;
   e.nsurf = 1;
   e.ntot = n;
   e.max_n = n;
+  e.max_n_single = n;
   e.max_np = np;
   e.max_chunks = nchunk;
   e.njobs_first = 3;
   e.njobs_ap = 1;
   e.nsum = nitems;
+  e.ntiles_sum = noalloc::kMaxTgtTiles;
   e.nasm = ntiles;
   e.any_rho = (S.physics == 0 && S.rho != 0.0);
   return enqueue_rhs(&e, static_cast<const double*>(state_in), static_cast<double*>(rhs_out), true);

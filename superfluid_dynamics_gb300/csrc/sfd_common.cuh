@@ -91,6 +91,31 @@ __device__ __forceinline__ df df_rcp(df a) {
   return quick_two_sum(r0, __fmul_rn(r0, e));
 }
 
+// a - b: hi parts differenced exactly (two-sum), lo parts in FP32, then
+// renormalised.  When a and b are close the exact hi difference is small and
+// the lo difference is not, so the renormalisation is required: df_mul and
+// df_sqsum drop lo * lo products, which is only safe for |lo| <= ulp(hi).
+__device__ __forceinline__ df df_diff(df a, df b) {
+  df s = two_sum(a.hi, -b.hi);
+  float lo = __fadd_rn(s.lo, __fsub_rn(a.lo, b.lo));
+  return two_sum(s.hi, lo);
+}
+// x^2 + y^2 for double-float x, y (normalised result).
+__device__ __forceinline__ df df_sqsum(df x, df y) {
+  df px = two_prod(x.hi, x.hi);
+  float ex = __fmaf_rn(2.0f * x.hi, x.lo, px.lo);
+  df py = two_prod(y.hi, y.hi);
+  float ey = __fmaf_rn(2.0f * y.hi, y.lo, py.lo);
+  df s = two_sum(px.hi, py.hi);
+  return quick_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(ex, ey)));
+}
+// FP32 reciprocal estimate (about 1 ulp), for the FP32 correction passes.
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
 // Double-float complex.
 struct dfc {
   df re, im;
@@ -105,6 +130,7 @@ enum : uint32_t {
   SFD_ST_ZERO_PIVOT = 1u << 2,       // a pivot was zero / below the breakdown threshold
   SFD_ST_REFINE_STALL = 1u << 3,     // iterative refinement did not reach its tolerance
   SFD_ST_REFACTORED = 1u << 4,       // informational: the preconditioner was rebuilt
+  SFD_ST_TIMEOUT = 1u << 5,          // a bounded wait in a kernel ran out (kernel skipped its work)
 };
 
 #define SFD_CUDA_OK(expr)                       \

@@ -10,6 +10,8 @@
 // factors) is supported (the batched helium case uses n = 32 m, m up to 64),
 // so the transform is a mixed-radix Stockham FFT: radix-4/2 butterflies plus an
 // output-parallel DFT stage for each odd prime factor.
+#include <cooperative_groups.h>
+
 #include "sfd_engine.cuh"
 #include "sfd_kernels.cuh"
 
@@ -19,23 +21,25 @@ constexpr int kFftThreads = 1024;
 constexpr int kMaxPerThread = 8;  // n <= 8192 = 8 * 1024
 
 __device__ __forceinline__ cd twid(const cd* tw, int e, int sign) {
-  double2 t = __ldg(reinterpret_cast<const double2*>(tw) + e);
-  return sign < 0 ? cd{t.x, t.y} : cd{t.x, -t.y};
+  cd t = tw[e];  // shared-memory table in the cluster kernel, global (L1/L2) otherwise
+  return sign < 0 ? t : cd{t.re, -t.im};
 }
 
 // multiply by -i (forward) or +i (inverse): the radix-4 rotation
 __device__ __forceinline__ cd rot(cd a, int sign) { return sign < 0 ? cd{a.im, -a.re} : cd{-a.im, a.re}; }
 
-// One Stockham pass with radix 2 or 4; p = product of the radices already done.
-template <int R>
-__device__ __forceinline__ void stockham_pass(cd* buf, int n, int p, const cd* tw, int sign) {
+// One Stockham pass with radix 2 or 4 over buf[0..n) by NT threads holding up
+// to MPT values each; p = product of the radices already done.  Twiddles come
+// from a table of a multiple of n: W_n^e = tw[e * ts].
+template <int R, int NT, int MPT>
+__device__ __forceinline__ void stockham_pass(cd* buf, int n, int p, const cd* tw, int ts, int sign) {
   const int T = n / R;
-  const int stw = n / (p * R);
-  constexpr int C = kMaxPerThread / R;
+  const int stw = n / (p * R) * ts;
+  constexpr int C = (MPT + R - 1) / R;  // butterflies per thread (T = n / R <= C * NT)
   cd u[C][R];
 #pragma unroll
   for (int c = 0; c < C; ++c) {
-    int i = threadIdx.x + c * kFftThreads;
+    int i = threadIdx.x + c * NT;
     if (i < T) {
       int k = i % p;
 #pragma unroll
@@ -49,7 +53,7 @@ __device__ __forceinline__ void stockham_pass(cd* buf, int n, int p, const cd* t
   __syncthreads();
 #pragma unroll
   for (int c = 0; c < C; ++c) {
-    int i = threadIdx.x + c * kFftThreads;
+    int i = threadIdx.x + c * NT;
     if (i < T) {
       int k = i % p;
       int j = (i - k) * R + k;
@@ -71,13 +75,14 @@ __device__ __forceinline__ void stockham_pass(cd* buf, int n, int p, const cd* t
 
 // Odd-radix pass: every output y[j + q p] = sum_r x[i + r T] W_n^{r (k + q p) n/(pR)}
 // is computed by one thread (R complex MACs), staged in registers, then stored.
-__device__ __forceinline__ void odd_pass(cd* buf, int n, int p, int R, const cd* tw, int sign) {
+template <int NT, int MPT>
+__device__ __forceinline__ void odd_pass(cd* buf, int n, int p, int R, const cd* tw, int ts, int sign) {
   const int T = n / R;
   const int stw = n / (p * R);
-  cd out[kMaxPerThread];
+  cd out[MPT];
 #pragma unroll
-  for (int c = 0; c < kMaxPerThread; ++c) {
-    int o = threadIdx.x + c * kFftThreads;
+  for (int c = 0; c < MPT; ++c) {
+    int o = threadIdx.x + c * NT;
     if (o < n) {
       int blk = o / (p * R), rem = o - blk * (p * R);
       int q = rem / p, k = rem - q * p;
@@ -86,33 +91,36 @@ __device__ __forceinline__ void odd_pass(cd* buf, int n, int p, int R, const cd*
       cd acc = buf[i];
       for (int r = 1; r < R; ++r) {
         int e = (int)(((long long)r * m * stw) % n);
-        acc = acc + buf[i + r * T] * twid(tw, e, sign);
+        acc = acc + buf[i + r * T] * twid(tw, e * ts, sign);
       }
       out[c] = acc;
     }
   }
   __syncthreads();
 #pragma unroll
-  for (int c = 0; c < kMaxPerThread; ++c) {
-    int o = threadIdx.x + c * kFftThreads;
+  for (int c = 0; c < MPT; ++c) {
+    int o = threadIdx.x + c * NT;
     if (o < n) buf[o] = out[c];
   }
   __syncthreads();
 }
 
 // Unnormalised in-place FFT of buf[0..n) (sign -1 forward as CUFFT_FORWARD,
-// +1 inverse without the 1/n).
-__device__ void cta_fft(cd* buf, const SurfaceDesc& S, int sign) {
+// +1 inverse without the 1/n); radices rad[0..nrad), twiddles tw[e * ts].
+template <int NT, int MPT>
+__device__ void cta_fft_n(cd* buf, int n, const int* rad, int nrad, const cd* tw, int ts, int sign) {
   int p = 1;
-  const int n = S.n, nrad = S.nrad;
-  const cd* tw = S.tw;
   for (int s = 0; s < nrad; ++s) {
-    int R = S.rad[s];
-    if (R == 4) stockham_pass<4>(buf, n, p, tw, sign);
-    else if (R == 2) stockham_pass<2>(buf, n, p, tw, sign);
-    else odd_pass(buf, n, p, R, tw, sign);
+    int R = rad[s];
+    if (R == 4) stockham_pass<4, NT, MPT>(buf, n, p, tw, ts, sign);
+    else if (R == 2) stockham_pass<2, NT, MPT>(buf, n, p, tw, ts, sign);
+    else odd_pass<NT, MPT>(buf, n, p, R, tw, ts, sign);
     p *= R;
   }
+}
+
+__device__ __forceinline__ void cta_fft(cd* buf, const SurfaceDesc& S, int sign) {
+  cta_fft_n<kFftThreads, kMaxPerThread>(buf, S.n, S.rad, S.nrad, S.tw, 1, sign);
 }
 
 // Spectral multipliers, restated from utilities.cuh:106-148 (first) and
@@ -178,7 +186,154 @@ __global__ void __launch_bounds__(kFftThreads, 1) k_spectral_deriv(DerivArgs A, 
   }
 }
 
+// ===================================================================== cluster version
+// One thread-block cluster of C = SFD_FFT_CLUSTER CTAs per job; the transform of
+// length n = C M is split as (with k = k1 + M k2, j = C m + c):
+//   forward:  Y_c = FFT_M(x[C m + c]);  Z_c[k1] = W_n^{c k1} Y_c[k1]          (CTA c)
+//             X[k1 + M k2] = sum_c W_C^{c k2} Z_c[k1]            (CTA owning k1, via DSMEM)
+//   multiply: X <- mult(X)  (reference Nyquist rules, global index k)
+//   inverse:  V_c[k1] = W_n^{-c k1} sum_k2 W_C^{-c k2} X[k1 + M k2]   (CTA owning k1)
+//             x[C m + c] = IFFT_M(V_c)[m]                        (CTA c, via DSMEM)
+// so each SM does 1/C of the FP64 work and the exchange stays on chip.
+namespace {
+constexpr int kCT = 512;        // threads per CTA of the cluster kernel
+constexpr int kCMPT = 2;        // values per thread in the M-point FFT (M <= 1024)
+
+// 8-point DFT of u (in place), sign -1 forward / +1 inverse, radix-2 DIT.
+__device__ __forceinline__ void dft8(cd* u, int sign) {
+  const double h = 0.70710678118654752440;
+  // bit-reversed order
+  cd a0 = u[0], a1 = u[4], a2 = u[2], a3 = u[6], a4 = u[1], a5 = u[5], a6 = u[3], a7 = u[7];
+  // stage 1 (length 2)
+  cd b0 = a0 + a1, b1 = a0 - a1, b2 = a2 + a3, b3 = a2 - a3;
+  cd b4 = a4 + a5, b5 = a4 - a5, b6 = a6 + a7, b7 = a6 - a7;
+  // stage 2 (length 4): twiddle W4^1 = -i (forward) on the odd element
+  cd t3 = rot(b3, sign), t7 = rot(b7, sign);
+  cd c0 = b0 + b2, c2 = b0 - b2, c1 = b1 + t3, c3 = b1 - t3;
+  cd c4 = b4 + b6, c6 = b4 - b6, c5 = b5 + t7, c7 = b5 - t7;
+  // stage 3 (length 8): W8^1 = h(1 - i s), W8^2 = rot, W8^3 = h(-1 - i s) with s = +-1 by sign
+  double sg = sign < 0 ? 1.0 : -1.0;
+  cd w1 = {h, -sg * h}, w3 = {-h, -sg * h};
+  cd d5 = c5 * w1, d6 = rot(c6, sign), d7 = c7 * w3;
+  u[0] = c0 + c4; u[4] = c0 - c4;
+  u[1] = c1 + d5; u[5] = c1 - d5;
+  u[2] = c2 + d6; u[6] = c2 - d6;
+  u[3] = c3 + d7; u[7] = c3 - d7;
+}
+}  // namespace
+
+__global__ void __cluster_dims__(SFD_FFT_CLUSTER, 1, 1) __launch_bounds__(kCT)
+    k_spectral_cluster(DerivArgs A, const int2* jobs) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  constexpr int C = SFD_FFT_CLUSTER;
+  extern __shared__ double2 csmem_raw[];
+  const int2 job = jobs[blockIdx.y];
+  const SurfaceDesc& S = A.surf[job.x];
+  const int n = S.n, off = S.off, kind = job.y;
+  const int M = n / C, R = M / C;
+  const int c = (int)cluster.block_rank();
+  const int nv = kind == SFD_JOB_ZP ? 2 : 1;  // the Z job yields z' and z''
+  cd* buf = reinterpret_cast<cd*>(csmem_raw);  // M values
+  cd* vbuf = buf + M;                          // 2 x (C x R) values (second half used by the Z job)
+  cd* twm = vbuf + 2 * M;                      // W_M^e = W_n^{C e}, e < M
+  cd* twc = twm + M;                           // W_n^{c k1}, k1 < M (this CTA's c)
+  cd* twq = twc + M;                           // W_n^{q k1}, q < C, k1 in this CTA's range: [q R + t]
+  const double rho = S.physics == 0 ? S.rho : 0.0;
+  for (int e = threadIdx.x; e < M; e += kCT) {
+    double2 a = __ldg(reinterpret_cast<const double2*>(S.tw) + C * e);
+    double2 b = __ldg(reinterpret_cast<const double2*>(S.tw) + c * e);
+    int q = e / R, t = e - q * R;
+    double2 d = __ldg(reinterpret_cast<const double2*>(S.tw) + q * (c * R + t));
+    twm[e] = {a.x, a.y};
+    twc[e] = {b.x, b.y};
+    twq[e] = {d.x, d.y};
+  }
+  // 1. decimated load x[C m + c]
+  for (int m = threadIdx.x; m < M; m += kCT) {
+    const int j = C * m + c;
+    cd v;
+    if (kind == SFD_JOB_ZP) v = {A.x[off + j] - 2 * SFD_PI * (double)j / n, A.y[off + j]};
+    else if (kind == SFD_JOB_PHIP)
+      v = {A.phi[off + j] - (-(1 + rho) * SFD_PI * S.U / n * (double)j), A.phi_im ? A.phi_im[off + j] : 0.0};
+    else if (kind == SFD_JOB_RAW) v = {A.x[off + j], A.y[off + j]};
+    else v = {A.a[off + j], 0.0};
+    buf[m] = v;
+  }
+  __syncthreads();
+  cta_fft_n<kCT, kCMPT>(buf, M, S.rad_m, S.nrad_m, twm, 1, -1);
+  // 2. Z_c[k1] = W_n^{c k1} Y_c[k1]
+  for (int k1 = threadIdx.x; k1 < M; k1 += kCT)
+    if (c && k1) buf[k1] = buf[k1] * twc[k1];
+  cluster.sync();
+  // 3. exchange across the cluster for this CTA's k1 range
+  for (int t = threadIdx.x; t < R; t += kCT) {
+    const int k1 = c * R + t;
+    cd u[C];
+#pragma unroll
+    for (int q = 0; q < C; ++q) u[q] = cluster.map_shared_rank(buf, q)[k1];
+    dft8(u, -1);
+    for (int v = 0; v < nv; ++v) {
+      const bool second = (kind == SFD_JOB_ZP && v == 1);
+      cd y[C];
+#pragma unroll
+      for (int k2 = 0; k2 < C; ++k2) {
+        int k = k1 + M * k2;
+        y[k2] = second ? second_mult(u[k2], k, n) : first_mult(u[k2], k, n);
+      }
+      dft8(y, +1);
+#pragma unroll
+      for (int q = 0; q < C; ++q) {
+        cd w = (q && k1) ? y[q] * cconj(twq[q * R + t]) : y[q];
+        vbuf[v * M + q * R + t] = w;
+      }
+    }
+  }
+  cluster.sync();
+  // 4. gather V_c[k1] for all k1, inverse M-point FFT, write x[C m + c]
+  const double s1 = 2.0 * SFD_PI / n;
+  const double s2 = 4.0 * SFD_PI * SFD_PI / (n * n);
+  for (int v = 0; v < nv; ++v) {
+    for (int k1 = threadIdx.x; k1 < M; k1 += kCT) {
+      int owner = k1 / R, t = k1 - owner * R;
+      buf[k1] = cluster.map_shared_rank(vbuf, owner)[v * M + c * R + t];
+    }
+    __syncthreads();
+    cta_fft_n<kCT, kCMPT>(buf, M, S.rad_m, S.nrad_m, twm, 1, +1);
+    const bool second = (kind == SFD_JOB_ZP && v == 1);
+    for (int m = threadIdx.x; m < M; m += kCT) {
+      const int j = off + C * m + c;
+      cd x = buf[m];
+      if (kind == SFD_JOB_ZP) {
+        if (second) A.zpp[j] = {x.re * s2, x.im * s2};   // Derivatives.cuh:321
+        else A.zp[j] = {x.re * s1 + s1, x.im * s1};      // :323,374
+      } else if (kind == SFD_JOB_PHIP) {
+        double r = x.re * s1;                           // :324, complex_to_real
+        if (S.U != 0) r += -(1 + rho) * SFD_PI * S.U / n;
+        A.phip[j] = r;
+      } else if (kind == SFD_JOB_RAW) {
+        A.ap[j] = x;
+      } else {
+        A.ap[j] = {x.re * s1, x.im * s1};
+      }
+    }
+    __syncthreads();
+  }
+  cluster.sync();  // keep this CTA's shared memory alive until every peer has read it
+}
+
+cudaError_t sfd_launch_spectral_cluster(const DerivArgs& A, const int2* jobs, int njobs, int max_n, cudaStream_t st) {
+  if (njobs == 0) return cudaSuccess;
+  const int M = max_n / SFD_FFT_CLUSTER;
+  size_t smem = (size_t)6 * M * sizeof(cd);
+  k_spectral_cluster<<<dim3(SFD_FFT_CLUSTER, njobs), kCT, smem, st>>>(A, jobs);
+  return cudaGetLastError();
+}
+
 cudaError_t sfd_fft_configure() {
+  cudaError_t e = cudaFuncSetAttribute(k_spectral_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       6 * (8192 / SFD_FFT_CLUSTER) * (int)sizeof(cd));
+  if (e != cudaSuccess) return e;
   return cudaFuncSetAttribute(k_spectral_deriv, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               8192 * (int)sizeof(cd));
 }

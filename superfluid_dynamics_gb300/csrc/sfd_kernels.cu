@@ -23,6 +23,8 @@
 #include "sfd_engine.cuh"
 #include "sfd_kernels.cuh"
 
+#include <type_traits>
+
 // ----------------------------------------------------------------- node prep
 // w = exp(i z) = e^{-y} (cos x + i sin x); p = w e^{-h} (helium);
 // per-node diagonal data of M and of the velocity matrices.
@@ -36,9 +38,16 @@ __global__ void k_node_prep(const SurfaceDesc* surf, const int* node_surf, int n
   double e = exp(-y[g]);
   cd w = {e * c, e * s};
   nd.w[g] = w;
+  {
+    df wr = df_from_double(w.re), wi = df_from_double(w.im);
+    nd.wdf[g] = make_float4(wr.hi, wr.lo, wi.hi, wi.lo);
+  }
   if (S.physics == 1 && !S.infinite_depth) {
     double eh = exp(-S.depth);
-    nd.p[g] = {w.re * eh, w.im * eh};
+    cd p = {w.re * eh, w.im * eh};
+    nd.p[g] = p;
+    df pr = df_from_double(p.re), pi = df_from_double(p.im);
+    nd.pdf[g] = make_float4(pr.hi, pr.lo, pi.hi, pi.lo);
   }
   cd z1 = zp[g], z2 = zpp[g];
   cd r = cdiv(z2, z1);
@@ -59,8 +68,10 @@ __global__ void k_node_prep(const SurfaceDesc* surf, const int* node_surf, int n
 // ----------------------------------------------------------------- sums
 // Work item = (surface, first target, first source, chunk index).  Each CTA
 // stages one chunk of sources in shared memory and accumulates S (and T) for
-// kTargets targets (two per thread), writing FP64 partials per chunk; the
-// epilogue reduces the chunks in a fixed order (bitwise reproducible).
+// kSumTargets targets (two per thread), writing partials per chunk.  The last
+// CTA to finish a target tile (arrival counter per tile) reduces that tile's
+// chunks in a fixed order (bitwise reproducible) and applies the epilogue, so
+// one launch does the whole pass.
 
 namespace {
 
@@ -70,10 +81,9 @@ struct SrcDF {
   float a_hi, a_lo;
 };
 
+// (sr, si) += a / (nr + i ni) = a (nr - i ni) / (nr^2 + ni^2), all double-float.
 __device__ __forceinline__ void df_div_acc(df nr, df ni, df a, df& sr, df& si) {
-  // (sr, si) += a / (nr + i ni) = a (nr - i ni) / (nr^2 + ni^2)
-  df den = df_add(df_mul(nr, nr), df_mul(ni, ni));
-  df t = df_mul(a, df_rcp(den));
+  df t = df_mul(a, df_rcp(df_sqsum(nr, ni)));
   sr = df_add(sr, df_mul(t, nr));
   si = df_sub(si, df_mul(t, ni));
 }
@@ -84,140 +94,321 @@ struct Src64 {
   double wr, wi, pr, pi, a;
 };
 
+// Accumulators of one target.
+template <int PREC>
+struct Acc;
+template <>
+struct Acc<SFD_PREC_F64> {
+  double sr = 0, si = 0, tr = 0, ti = 0;
+};
+template <>
+struct Acc<SFD_PREC_DF> {
+  df sr{0.f, 0.f}, si{0.f, 0.f}, tr{0.f, 0.f}, ti{0.f, 0.f};
+};
+template <>
+struct Acc<SFD_PREC_F32> {
+  float sr = 0.f, si = 0.f, tr = 0.f, ti = 0.f;
+};
+
+// Target data of one target.
+template <int PREC>
+struct Tgt;
+template <>
+struct Tgt<SFD_PREC_F64> {
+  cd w, p;
+  __device__ void load(cd w_, cd p_) { w = w_; p = p_; }
+};
+template <>
+struct Tgt<SFD_PREC_DF> {
+  df wr, wi, pr, pi;
+  __device__ void load(float4 w_, float4 p_) {
+    wr = {w_.x, w_.y}; wi = {w_.z, w_.w};
+    pr = {p_.x, p_.y}; pi = {p_.z, p_.w};
+  }
+};
+template <>
+struct Tgt<SFD_PREC_F32> {
+  float wr_hi, wr_lo, wi_hi, wi_lo, pr, pi;
+  __device__ void load(float4 w_, float4 p_) {
+    wr_hi = w_.x; wr_lo = w_.y; wi_hi = w_.z; wi_lo = w_.w;
+    pr = p_.x; pi = p_.z;
+  }
+};
+
+// One (target, source) pair.
+__device__ __forceinline__ void pair_acc(const Tgt<SFD_PREC_F64>& t, const Src64& s, bool self, bool image,
+                                         Acc<SFD_PREC_F64>& A) {
+  if (!self) {
+    double dr = t.w.re - s.wr, di = t.w.im - s.wi;
+    double inv = s.a / (dr * dr + di * di);
+    A.sr += inv * dr;
+    A.si -= inv * di;
+  }
+  if (image) {  // 1 - pk conj(pj)
+    double qr = t.p.re * s.pr + t.p.im * s.pi, qi = t.p.im * s.pr - t.p.re * s.pi;
+    double dr = 1.0 - qr, di = -qi;
+    double inv = s.a / (dr * dr + di * di);
+    A.tr += inv * dr;
+    A.ti -= inv * di;
+  }
+}
+__device__ __forceinline__ void pair_acc(const Tgt<SFD_PREC_DF>& t, const SrcDF& s, bool self, bool image,
+                                         Acc<SFD_PREC_DF>& A) {
+  df aj{s.a_hi, s.a_lo};
+  if (!self) {
+    df dr = df_diff(t.wr, df{s.wr_hi, s.wr_lo});
+    df di = df_diff(t.wi, df{s.wi_hi, s.wi_lo});
+    df_div_acc(dr, di, aj, A.sr, A.si);
+  }
+  if (image) {
+    df prj{s.pr_hi, s.pr_lo}, pij{s.pi_hi, s.pi_lo};
+    df qr = df_add(df_mul(t.pr, prj), df_mul(t.pi, pij));
+    df qi = df_sub(df_mul(t.pi, prj), df_mul(t.pr, pij));
+    df_div_acc(df_sub(df{1.f, 0.f}, qr), df_neg(qi), aj, A.tr, A.ti);
+  }
+}
+__device__ __forceinline__ void pair_acc(const Tgt<SFD_PREC_F32>& t, const SrcDF& s, bool self, bool image,
+                                         Acc<SFD_PREC_F32>& A) {
+  if (!self) {
+    float dr = (t.wr_hi - s.wr_hi) + (t.wr_lo - s.wr_lo);
+    float di = (t.wi_hi - s.wi_hi) + (t.wi_lo - s.wi_lo);
+    float inv = s.a_hi * rcp_approx(fmaf(dr, dr, di * di));
+    A.sr = fmaf(inv, dr, A.sr);
+    A.si = fmaf(-inv, di, A.si);
+  }
+  if (image) {
+    float qr = t.pr * s.pr_hi + t.pi * s.pi_hi, qi = t.pi * s.pr_hi - t.pr * s.pi_hi;
+    float dr = 1.f - qr, di = -qi;
+    float inv = s.a_hi * rcp_approx(fmaf(dr, dr, di * di));
+    A.tr = fmaf(inv, dr, A.tr);
+    A.ti = fmaf(-inv, di, A.ti);
+  }
+}
+__device__ __forceinline__ cd acc_s(const Acc<SFD_PREC_F64>& A) { return {A.sr, A.si}; }
+__device__ __forceinline__ cd acc_t(const Acc<SFD_PREC_F64>& A) { return {A.tr, A.ti}; }
+__device__ __forceinline__ float4 acc_s(const Acc<SFD_PREC_DF>& A) { return make_float4(A.sr.hi, A.sr.lo, A.si.hi, A.si.lo); }
+__device__ __forceinline__ float4 acc_t(const Acc<SFD_PREC_DF>& A) { return make_float4(A.tr.hi, A.tr.lo, A.ti.hi, A.ti.lo); }
+__device__ __forceinline__ float4 acc_s(const Acc<SFD_PREC_F32>& A) { return make_float4(A.sr, 0.f, A.si, 0.f); }
+__device__ __forceinline__ float4 acc_t(const Acc<SFD_PREC_F32>& A) { return make_float4(A.tr, 0.f, A.ti, 0.f); }
+
+__device__ __forceinline__ df df_warp_sum(df v) {
+  for (int o = 16; o > 0; o >>= 1) {
+    df u = {__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+    v = df_add(v, u);
+  }
+  return v;
+}
+
+template <int PREC>
+using SrcT = typename std::conditional<PREC == SFD_PREC_F64, Src64, SrcDF>::type;
+
+// Epilogue of one target tile (run by the last CTA to finish it): reduce the
+// chunk partials in fixed order (bitwise reproducible) and form, per node,
+//   C_k = i (2 w_k S_k - (A - a_k)),   D_k = -i (2 T_k - A)
+//   (M a)_k = Mdiag_k a_k + c1 Im(z'_k C_k) - [image] (1/4pi) Im D_k
+// mode 0: C/D overwritten, r = phi' - M a; mode 1: C/D accumulated, r -= M a.
+template <int PREC>
+__device__ void sums_epilogue(const SumArgs& A, const SurfaceDesc& S, int sidx, int tile, int t0, bool image) {
+  const int n = S.n, off = S.off;
+  const int nchunk = (n + kSumChunk - 1) / kSumChunk;
+  __shared__ double asum_sh;
+  if (threadIdx.x == 0) {
+    const long long ia = (long long)tile * A.max_chunks;
+    if constexpr (PREC == SFD_PREC_F64) {
+      double s = 0.0;
+      for (int c = 0; c < nchunk; ++c) s += __ldcg(A.part_a + ia + c);
+      asum_sh = s;
+    } else {
+      df s = {0.f, 0.f};
+      const float2* pa = reinterpret_cast<const float2*>(A.part_a) + ia;
+      for (int c = 0; c < nchunk; ++c) {
+        float2 v = __ldcg(pa + c);
+        s = df_add(s, df{v.x, v.y});
+      }
+      asum_sh = df_to_double(s);
+    }
+  }
+  __syncthreads();
+  const double asum = asum_sh;
+  const double c1 = S.physics == 0 ? 0.25 * (1 - S.rho) / SFD_PI : 0.25 / SFD_PI;
+  double rmax = 0.0;
+  for (int q = 0; q < kSumTargets / kSumThreads; ++q) {
+    const int tk = t0 + q * kSumThreads + threadIdx.x;
+    if (tk >= n) continue;
+    const int g = off + tk;
+    cd sum_s, sum_t = {0, 0};
+    if constexpr (PREC == SFD_PREC_F64) {
+      double sr = 0, si = 0, tr = 0, ti = 0;
+      for (int c = 0; c < nchunk; ++c) {
+        const long long o = (long long)c * A.ntot + g;
+        double2 v = __ldcg(reinterpret_cast<const double2*>(A.part_s) + o);
+        sr += v.x;
+        si += v.y;
+        if (image) {
+          double2 u = __ldcg(reinterpret_cast<const double2*>(A.part_t) + o);
+          tr += u.x;
+          ti += u.y;
+        }
+      }
+      sum_s = {sr, si};
+      sum_t = {tr, ti};
+    } else {
+      df sr = {0.f, 0.f}, si = {0.f, 0.f}, tr = {0.f, 0.f}, ti = {0.f, 0.f};
+      for (int c = 0; c < nchunk; ++c) {
+        const long long o = (long long)c * A.ntot + g;
+        float4 v = __ldcg(reinterpret_cast<const float4*>(A.part_s) + o);
+        sr = df_add(sr, df{v.x, v.y});
+        si = df_add(si, df{v.z, v.w});
+        if (image) {
+          float4 u = __ldcg(reinterpret_cast<const float4*>(A.part_t) + o);
+          tr = df_add(tr, df{u.x, u.y});
+          ti = df_add(ti, df{u.z, u.w});
+        }
+      }
+      sum_s = {df_to_double(sr), df_to_double(si)};
+      sum_t = {df_to_double(tr), df_to_double(ti)};
+    }
+    const double ak = A.a[g];
+    const cd wk = A.w[g];
+    const cd C = cmul_i(2.0 * (wk * sum_s) - cd{asum - ak, 0.0});
+    const cd D = image ? cmul_i(cd{-(2.0 * sum_t.re - asum), -(2.0 * sum_t.im)}) : cd{0, 0};
+    double ma = A.mdiag[g] * ak + c1 * (A.zp[g] * C).im;
+    if (image) ma -= 0.25 / SFD_PI * D.im;
+    double rnew;
+    if (A.mode == 0) {
+      A.cacc[g] = C;
+      if (image) A.dacc[g] = D;
+      rnew = A.phip[g] - ma;
+    } else {
+      A.cacc[g] = A.cacc[g] + C;
+      if (image) A.dacc[g] = A.dacc[g] + D;
+      rnew = A.r[g] - ma;
+    }
+    A.r[g] = rnew;
+    double rv = fabs(rnew);
+    if (!(rv == rv)) rv = 1e300;
+    rmax = fmax(rmax, rv);
+  }
+  if (A.rnorm) {
+    // |r| max per surface: non-negative doubles order like their bit patterns
+    unsigned long long m = (unsigned long long)__double_as_longlong(rmax);
+    for (int o = 16; o > 0; o >>= 1) {
+      unsigned long long v = __shfl_xor_sync(0xffffffffu, m, o);
+      m = v > m ? v : m;
+    }
+    if ((threadIdx.x & 31) == 0) atomicMax(reinterpret_cast<unsigned long long*>(A.rnorm) + sidx, m);
+  }
+}
+
 template <int PREC>
 __global__ void __launch_bounds__(kSumThreads) k_boundary_sums(SumArgs A) {
   const int4 item = A.items[blockIdx.x];
-  const SurfaceDesc S = A.surf[item.x];
+  const SurfaceDesc& S = A.surf[item.x];
   const int n = S.n, off = S.off;
   const int t0 = item.y, j0 = item.z, chunk = item.w;
   const int jn = min(kSumChunk, n - j0);
   const bool image = (S.physics == 1 && !S.infinite_depth);
-  // FP64 sources need exact doubles; the other precisions stage float pairs.
-  __shared__ __align__(16) unsigned char src_raw[kSumChunk * (PREC == SFD_PREC_F64 ? sizeof(Src64) : sizeof(SrcDF))];
-  Src64* src64 = reinterpret_cast<Src64*>(src_raw);
-  SrcDF* src = reinterpret_cast<SrcDF*>(src_raw);
+  __shared__ SrcT<PREC> src[kSumChunk];
   __shared__ double asum_warp[kSumThreads / 32];
+  __shared__ float2 asum_warp_df[kSumThreads / 32];
+  // stage the chunk's sources (and their weight sum, kept by the first target tile)
   double apart = 0.0;
+  df apart_df = {0.f, 0.f};
   for (int jj = threadIdx.x; jj < jn; jj += kSumThreads) {
     int g = off + j0 + jj;
-    cd w = A.w[g];
-    double aj = A.a[g];
-    apart += aj;
-    cd p = image ? A.p[g] : cd{0.0, 0.0};
-    if (PREC == SFD_PREC_F64) {
-      src64[jj] = Src64{w.re, w.im, p.re, p.im, aj};
+    if constexpr (PREC == SFD_PREC_F64) {
+      cd w = A.w[g];
+      double aj = A.a[g];
+      apart += aj;
+      cd p = image ? A.p[g] : cd{0.0, 0.0};
+      src[jj] = Src64{w.re, w.im, p.re, p.im, aj};
     } else {
-      SrcDF s;
-      if (PREC == SFD_PREC_F32) {
-        // w split in hi/lo so that w_k - w_j keeps FP32 relative accuracy
-        s.wr_hi = __double2float_rn(w.re); s.wr_lo = __double2float_rn(w.re - (double)s.wr_hi);
-        s.wi_hi = __double2float_rn(w.im); s.wi_lo = __double2float_rn(w.im - (double)s.wi_hi);
-        s.a_hi = __double2float_rn(aj); s.a_lo = 0.f;
-      } else {
-        df wr = df_from_double(w.re), wi = df_from_double(w.im), ad = df_from_double(aj);
-        s.wr_hi = wr.hi; s.wr_lo = wr.lo; s.wi_hi = wi.hi; s.wi_lo = wi.lo; s.a_hi = ad.hi; s.a_lo = ad.lo;
-      }
-      df pr = df_from_double(p.re), pi = df_from_double(p.im);
-      s.pr_hi = pr.hi; s.pr_lo = pr.lo; s.pi_hi = pi.hi; s.pi_lo = pi.lo;
-      src[jj] = s;
+      float4 w = A.wdf[g];
+      float2 ad = A.adf[g];
+      float4 p = image ? A.pdf[g] : make_float4(0.f, 0.f, 0.f, 0.f);
+      apart_df = df_add(apart_df, df{ad.x, ad.y});
+      src[jj] = SrcDF{w.x, w.y, w.z, w.w, p.x, p.y, p.z, p.w, ad.x, PREC == SFD_PREC_DF ? ad.y : 0.f};
     }
   }
-  // per-chunk partial of A = sum a_j (written by the first target tile only)
-  if (t0 == 0) {
-    for (int o = 16; o > 0; o >>= 1) apart += __shfl_xor_sync(0xffffffffu, apart, o);
-    if ((threadIdx.x & 31) == 0) asum_warp[threadIdx.x >> 5] = apart;
+  {
+    if constexpr (PREC == SFD_PREC_F64) {
+      for (int o = 16; o > 0; o >>= 1) apart += __shfl_xor_sync(0xffffffffu, apart, o);
+      if ((threadIdx.x & 31) == 0) asum_warp[threadIdx.x >> 5] = apart;
+    } else {
+      apart_df = df_warp_sum(apart_df);
+      if ((threadIdx.x & 31) == 0) asum_warp_df[threadIdx.x >> 5] = make_float2(apart_df.hi, apart_df.lo);
+    }
   }
   __syncthreads();
-  if (t0 == 0 && threadIdx.x == 0) {
-    double s = 0.0;
-    for (int i = 0; i < kSumThreads / 32; ++i) s += asum_warp[i];
-    A.part_a[(long long)chunk * A.nsurf + item.x] = s;
-  }
-
-  for (int rep = 0; rep < kSumTargets / kSumThreads; ++rep) {
-    const int tk = t0 + rep * kSumThreads + threadIdx.x;
-    const bool active = tk < n;
-    const int gk = off + (active ? tk : 0);
-    const int self = active ? tk - j0 : -1;  // index of j == k inside this chunk (if any)
-    cd wk = A.w[gk];
-    cd pk = image ? A.p[gk] : cd{0, 0};
-    cd outs = {0, 0}, outt = {0, 0};
-    if (PREC == SFD_PREC_F64) {
-      double sr = 0, si = 0, tr = 0, ti = 0;
-      for (int jj = 0; jj < jn; ++jj) {
-        const Src64 s = src64[jj];
-        if (jj != self) {
-          double dr = wk.re - s.wr, di = wk.im - s.wi;
-          double inv = s.a / (dr * dr + di * di);
-          sr += inv * dr;
-          si -= inv * di;
-        }
-        if (image) {
-          // 1 - pk conj(pj)
-          double qr = pk.re * s.pr + pk.im * s.pi, qi = pk.im * s.pr - pk.re * s.pi;
-          double dr = 1.0 - qr, di = -qi;
-          double inv = s.a / (dr * dr + di * di);
-          tr += inv * dr;
-          ti -= inv * di;
-        }
-      }
-      outs = {sr, si};
-      outt = {tr, ti};
-    } else if (PREC == SFD_PREC_DF) {
-      df wkr = df_from_double(wk.re), wki = df_from_double(wk.im);
-      df sr = {0.f, 0.f}, si = {0.f, 0.f}, tr = {0.f, 0.f}, ti = {0.f, 0.f};
-      df pkr = df_from_double(pk.re), pki = df_from_double(pk.im);
-      for (int jj = 0; jj < jn; ++jj) {
-        const SrcDF s = src[jj];
-        df aj = {s.a_hi, s.a_lo};
-        if (jj != self) {
-          df dr = df_sub(wkr, df{s.wr_hi, s.wr_lo});
-          df di = df_sub(wki, df{s.wi_hi, s.wi_lo});
-          df_div_acc(dr, di, aj, sr, si);
-        }
-        if (image) {
-          df prj = {s.pr_hi, s.pr_lo}, pij = {s.pi_hi, s.pi_lo};
-          df qr = df_add(df_mul(pkr, prj), df_mul(pki, pij));
-          df qi = df_sub(df_mul(pki, prj), df_mul(pkr, pij));
-          df dr = df_sub(df{1.f, 0.f}, qr);
-          df di = df_neg(qi);
-          df_div_acc(dr, di, aj, tr, ti);
-        }
-      }
-      outs = {df_to_double(sr), df_to_double(si)};
-      outt = {df_to_double(tr), df_to_double(ti)};
-    } else {  // FP32: only for small corrections
-      float wkr_hi = __double2float_rn(wk.re), wkr_lo = __double2float_rn(wk.re - (double)wkr_hi);
-      float wki_hi = __double2float_rn(wk.im), wki_lo = __double2float_rn(wk.im - (double)wki_hi);
-      float pkr = (float)pk.re, pki = (float)pk.im;
-      float sr = 0.f, si = 0.f, tr = 0.f, ti = 0.f;
-      for (int jj = 0; jj < jn; ++jj) {
-        const SrcDF s = src[jj];
-        if (jj != self) {
-          float dr = (wkr_hi - s.wr_hi) + (wkr_lo - s.wr_lo);
-          float di = (wki_hi - s.wi_hi) + (wki_lo - s.wi_lo);
-          float inv = s.a_hi / (dr * dr + di * di);
-          sr = fmaf(inv, dr, sr);
-          si = fmaf(-inv, di, si);
-        }
-        if (image) {
-          float prj = s.pr_hi, pij = s.pi_hi;
-          float qr = pkr * prj + pki * pij, qi = pki * prj - pkr * pij;
-          float dr = 1.f - qr, di = -qi;
-          float inv = s.a_hi / (dr * dr + di * di);
-          tr = fmaf(inv, dr, tr);
-          ti = fmaf(-inv, di, ti);
-        }
-      }
-      outs = {(double)sr, (double)si};
-      outt = {(double)tr, (double)ti};
-    }
-    if (active) {
-      long long o = (long long)chunk * A.ntot + gk;
-      A.part_s[o] = outs;
-      if (image) A.part_t[o] = outt;
+  if (threadIdx.x == 0) {  // this chunk's weight sum, kept per (target tile, chunk)
+    const long long ia = (long long)(S.tile_base + t0 / kSumTargets) * A.max_chunks + chunk;
+    if constexpr (PREC == SFD_PREC_F64) {
+      double s = 0.0;
+      for (int i = 0; i < kSumThreads / 32; ++i) s += asum_warp[i];
+      A.part_a[ia] = s;
+    } else {
+      df s = {0.f, 0.f};
+      for (int i = 0; i < kSumThreads / 32; ++i) s = df_add(s, df{asum_warp_df[i].x, asum_warp_df[i].y});
+      reinterpret_cast<float2*>(A.part_a)[ia] = make_float2(s.hi, s.lo);
     }
   }
+  // two targets per thread: tk0 and tk0 + kSumThreads
+  const int tk0 = t0 + threadIdx.x, tk1 = tk0 + kSumThreads;
+  const bool a0 = tk0 < n, a1 = tk1 < n;
+  const int g0 = off + (a0 ? tk0 : 0), g1 = off + (a1 ? tk1 : 0);
+  Tgt<PREC> T0, T1;
+  if constexpr (PREC == SFD_PREC_F64) {
+    T0.load(A.w[g0], image ? A.p[g0] : cd{0, 0});
+    T1.load(A.w[g1], image ? A.p[g1] : cd{0, 0});
+  } else {
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    T0.load(A.wdf[g0], image ? A.pdf[g0] : z4);
+    T1.load(A.wdf[g1], image ? A.pdf[g1] : z4);
+  }
+  const int self0 = a0 ? tk0 - j0 : -1, self1 = a1 ? tk1 - j0 : -1;
+  Acc<PREC> R0, R1;
+#pragma unroll 2
+  for (int jj = 0; jj < jn; ++jj) {
+    const SrcT<PREC> s = src[jj];
+    pair_acc(T0, s, jj == self0, image, R0);
+    pair_acc(T1, s, jj == self1, image, R1);
+  }
+  long long o = (long long)chunk * A.ntot + off;
+  const int tile = S.tile_base + t0 / kSumTargets;
+  if constexpr (PREC == SFD_PREC_F64) {
+    if (a0) {
+      A.part_s[o + tk0] = acc_s(R0);
+      if (image) A.part_t[o + tk0] = acc_t(R0);
+    }
+    if (a1) {
+      A.part_s[o + tk1] = acc_s(R1);
+      if (image) A.part_t[o + tk1] = acc_t(R1);
+    }
+  } else {
+    float4* ps = reinterpret_cast<float4*>(A.part_s);
+    float4* pt = reinterpret_cast<float4*>(A.part_t);
+    if (a0) {
+      ps[o + tk0] = acc_s(R0);
+      if (image) pt[o + tk0] = acc_t(R0);
+    }
+    if (a1) {
+      ps[o + tk1] = acc_s(R1);
+      if (image) pt[o + tk1] = acc_t(R1);
+    }
+  }
+  // ---- arrival count: the last CTA of this target tile finishes it
+  __shared__ int last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int nchunk = (n + kSumChunk - 1) / kSumChunk;
+    last = (atomicAdd(A.tile_count + tile, 1) == nchunk - 1);
+    if (last) A.tile_count[tile] = 0;  // ready for the next pass
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  sums_epilogue<PREC>(A, S, item.x, tile, t0, image);
 }
 
 cudaError_t sfd_launch_sums(int prec, const SumArgs& A, int nitems, cudaStream_t st) {
@@ -226,51 +417,6 @@ cudaError_t sfd_launch_sums(int prec, const SumArgs& A, int nitems, cudaStream_t
   else if (prec == SFD_PREC_DF) k_boundary_sums<SFD_PREC_DF><<<nitems, kSumThreads, 0, st>>>(A);
   else k_boundary_sums<SFD_PREC_F32><<<nitems, kSumThreads, 0, st>>>(A);
   return cudaGetLastError();
-}
-
-// Reduce the chunk partials and form C, D, M a for every node:
-//   C_k = i (2 w_k S_k - (A - a_k)),   D_k = -i (2 T_k - A)
-//   (M a)_k = Mdiag_k a_k + c1 Im(z'_k C_k) - [image] (1/4pi) Im D_k
-// mode 0: overwrite C/D accumulators and set r = phi' - M a
-// mode 1: add to the accumulators and set r = r - M a  (correction pass)
-__global__ void k_sum_epilogue(EpiArgs E, int mode) {
-  int g = blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= E.ntot) return;
-  const int s = E.node_surf[g];
-  const SurfaceDesc& S = E.surf[s];
-  const int nchunk = (S.n + kSumChunk - 1) / kSumChunk;
-  cd sum_s = {0, 0}, sum_t = {0, 0};
-  double asum = 0.0;
-  const bool image = (S.physics == 1 && !S.infinite_depth);
-  for (int c = 0; c < nchunk; ++c) {
-    long long o = (long long)c * E.ntot + g;
-    sum_s = sum_s + E.part_s[o];
-    if (image) sum_t = sum_t + E.part_t[o];
-    asum += E.part_a[(long long)c * E.nsurf + s];
-  }
-  double ak = E.a[g];
-  cd wk = E.w[g];
-  cd C = cmul_i(2.0 * (wk * sum_s) - cd{asum - ak, 0.0});
-  cd D = image ? cmul_i(cd{-(2.0 * sum_t.re - asum), -(2.0 * sum_t.im)}) : cd{0, 0};
-  double c1 = S.physics == 0 ? 0.25 * (1 - S.rho) / SFD_PI : 0.25 / SFD_PI;
-  double ma = E.mdiag[g] * ak + c1 * (E.zp[g] * C).im;
-  if (image) ma -= 0.25 / SFD_PI * D.im;
-  if (mode == 0) {
-    E.cacc[g] = C;
-    if (image) E.dacc[g] = D;
-    E.r[g] = E.phip[g] - ma;
-  } else {
-    E.cacc[g] = E.cacc[g] + C;
-    if (image) E.dacc[g] = E.dacc[g] + D;
-    E.r[g] = E.r[g] - ma;
-  }
-  if (E.rnorm) {
-    // |r| max per surface (for the refinement status); non-negative doubles
-    // order like their bit patterns, so an integer atomicMax works.
-    double rv = fabs(E.r[g]);
-    if (!(rv == rv)) rv = 1e300;
-    atomicMax(reinterpret_cast<unsigned long long*>(E.rnorm) + s, __double_as_longlong(rv));
-  }
 }
 
 // Velocities and Bernoulli:

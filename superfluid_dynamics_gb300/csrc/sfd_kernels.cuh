@@ -4,49 +4,49 @@
 
 enum : int { SFD_PREC_F64 = 0, SFD_PREC_DF = 1, SFD_PREC_F32 = 2 };
 
-constexpr int kSumThreads = 256;  // threads per CTA of the boundary sums
-constexpr int kSumTargets = 256;  // targets per CTA
-constexpr int kSumChunk = 512;    // sources per CTA (shared-memory chunk)
+constexpr int kSumThreads = 128;  // threads per CTA of the boundary sums
+constexpr int kSumTargets = 256;  // targets per CTA (two per thread, for ILP)
+constexpr int kSumChunk = 128;    // sources per CTA (shared-memory chunk)
 
 struct NodeData {
   cd* w;        // exp(i z)
   cd* p;        // exp(i z) e^{-h} (helium image kernel)
+  float4* wdf;  // w as double-float pairs (re.hi, re.lo, im.hi, im.lo)
+  float4* pdf;  // p likewise
   double* mdiag;
   cd* v1low;    // V1_kk lower fluid (no image term)
   cd* v1up;     // V1_kk upper fluid
   cd* v2;       // V2_k
 };
 
+// One boundary-sum pass: partial sums per (target tile, source chunk), then
+// the last CTA of each target tile reduces them in fixed chunk order and
+// applies the epilogue (C, D, M a, residual) to its targets.
 struct SumArgs {
   const SurfaceDesc* surf;
-  const int4* items;
+  const int4* items;    // (surface, first target, first source, chunk)
   int nsurf;
   int ntot;
+  int max_chunks;
   const cd* w;
   const cd* p;
-  const double* a;
-  cd* part_s;
+  const double* a;      // weights (FP64; every pass)
+  const float4* wdf;    // double-float copies (DF / FP32 passes)
+  const float4* pdf;
+  const float2* adf;
+  cd* part_s;           // [chunk][node]; FP64 pass: complex doubles; DF / FP32: float4 (re.hi, re.lo, im.hi, im.lo)
   cd* part_t;
-  double* part_a;
-};
-
-struct EpiArgs {
-  const SurfaceDesc* surf;
-  const int* node_surf;
-  int nsurf;
-  int ntot;
-  const cd* part_s;
-  const cd* part_t;
-  const double* part_a;
-  const double* a;
-  const cd* w;
-  const cd* zp;
+  double* part_a;       // [tile][chunk]; FP64 pass: doubles; DF / FP32: float2 (hi, lo)
+  int* tile_count;      // arrivals per target tile (returns to 0 after each pass)
+  // epilogue
   const double* mdiag;
+  const cd* zp;
   const double* phip;
   cd* cacc;
   cd* dacc;
   double* r;
-  double* rnorm;  // per-surface max |r| (nullable)
+  double* rnorm;        // per-surface max |r| (nullable)
+  int mode;             // 0: overwrite C/D and r = phi' - M a; 1: accumulate, r -= M a
 };
 
 struct VelArgs {
@@ -74,7 +74,6 @@ struct VelArgs {
 __global__ void k_node_prep(const SurfaceDesc* surf, const int* node_surf, int ntot, const double* x,
                             const double* y, const cd* zp, const cd* zpp, NodeData nd);
 cudaError_t sfd_launch_sums(int prec, const SumArgs& A, int nitems, cudaStream_t st);
-__global__ void k_sum_epilogue(EpiArgs E, int mode);
 __global__ void k_velocity_bernoulli(VelArgs V);
 __global__ void k_velocity_node1(VelArgs V);
 __global__ void k_rk4_stage(int n3, const double* y0, const double* k, double* kacc, double* ystage, double wk,
@@ -84,4 +83,5 @@ __global__ void k_invariants(const SurfaceDesc* surf, const double* x, const dou
                              const cd* zp, const double* u, const double* v, double kappa, double* out);
 
 cudaError_t sfd_launch_spectral(const DerivArgs& A, const int2* jobs, int njobs, int max_n, cudaStream_t st);
+cudaError_t sfd_launch_spectral_cluster(const DerivArgs& A, const int2* jobs, int njobs, int max_n, cudaStream_t st);
 cudaError_t sfd_fft_configure();

@@ -22,6 +22,8 @@
 #include "sfd_engine.cuh"
 #include "sfd_solve.cuh"
 
+#include <cuda_bf16.h>
+
 // =============================================================== assembly
 // M_kj = c1 Im(z'_k cot((z_k - z_j)/2)) - [image] (1/4pi) Im cot((z_k - conj z_j)/2 + ih)
 // M_kk = mdiag_k - [image] (1/4pi) Im cot(i (y_k + h))          (createM.cuh:43-92)
@@ -280,43 +282,134 @@ __global__ void __launch_bounds__(256) k_lu64_solve(const SurfaceDesc* surf, con
 //   P = inv(A_KK)                        k_gj_diag   (one CTA per surface)
 //   R = P A_K,:  and  C = A_:,K  (copies) k_gj_panel
 //   A_ij -= C_i R_j (i,j not in K); A_Kj = R_j; A_iK = -C_i P; A_KK = P   k_gj_update
+// In-register Gauss-Jordan inverse of a 32 x 32 block held by one warp
+// (lane l holds row l); the pivot row is broadcast with shuffles, so no block
+// barrier is needed.  Returns false on a zero pivot.
+__device__ __forceinline__ bool warp_gj32(float (&r)[32]) {
+  const int lane = threadIdx.x & 31;
+  bool ok = true;
+#pragma unroll
+  for (int c = 0; c < 32; ++c) {
+    const float piv = __shfl_sync(0xffffffffu, r[c], c);
+    ok &= fabsf(piv) > 1e-30f;
+    const float pinv = 1.0f / piv;
+    const float colc = r[c];
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+      const float rj = __shfl_sync(0xffffffffu, r[j], c) * pinv;
+      if (lane == c) r[j] = (j == c) ? pinv : rj;
+      else r[j] = (j == c) ? -colc * pinv : fmaf(-colc, rj, r[j]);
+    }
+  }
+  return ok;
+}
+
+// P = inv(A_KK) for the 128 x 128 diagonal block, blocked Gauss-Jordan with
+// 32-wide panels: warp 0 inverts the 32 x 32 pivot block in registers, then all
+// threads apply the rank-32 update to the block in shared memory.
 __global__ void __launch_bounds__(512) k_gj_diag(const SurfaceDesc* surf, int nsurf, int kb, float* mat, float* pbuf,
                                                  unsigned int* status) {
   const int s = blockIdx.x;
   const SurfaceDesc& S = surf[s];
   const int np = pad_n(S.n), k0 = kb * 128;
   if (k0 >= np) return;
-  float* A = mat + S.moff;
-  extern __shared__ float D[];  // 128 x 129
-  const int ld = 129;
-  for (int e = threadIdx.x; e < 128 * 128; e += 512) D[(e >> 7) * ld + (e & 127)] = A[(long long)(k0 + (e >> 7)) * np + k0 + (e & 127)];
+  const float* A = mat + S.moff;
+  extern __shared__ float dsm[];
+  float* D = dsm;                // 128 x 129
+  float* Cq = D + 128 * 129;     // 128 x 33: column panel (before the update)
+  float* Rq = Cq + 128 * 33;     // 32 x 128: P * row panel (P itself inside the panel)
+  float* Pq = Rq + 32 * 128;     // 32 x 33
+  for (int e = threadIdx.x; e < 128 * 128; e += 512) D[(e >> 7) * 129 + (e & 127)] = A[(long long)(k0 + (e >> 7)) * np + k0 + (e & 127)];
   __syncthreads();
-  __shared__ float colc[128], rowc[128];
-  for (int c = 0; c < 128; ++c) {
-    float piv = D[c * ld + c];
-    if (threadIdx.x == 0 && !(fabsf(piv) > 1e-30f)) atomicOr(status + s, SFD_ST_ZERO_PIVOT);
-    float pinv = 1.0f / piv;
-    if (threadIdx.x < 128) colc[threadIdx.x] = D[threadIdx.x * ld + c];
-    else if (threadIdx.x < 256) rowc[threadIdx.x - 128] = D[c * ld + threadIdx.x - 128];
+  bool ok = true;
+  for (int q = 0; q < 4; ++q) {
+    const int q0 = 32 * q;
+    if (threadIdx.x < 32) {
+      float r[32];
+#pragma unroll
+      for (int j = 0; j < 32; ++j) r[j] = D[(q0 + threadIdx.x) * 129 + q0 + j];
+      ok &= warp_gj32(r);
+#pragma unroll
+      for (int j = 0; j < 32; ++j) Pq[threadIdx.x * 33 + j] = r[j];
+    }
+    for (int e = threadIdx.x; e < 128 * 32; e += 512) Cq[(e >> 5) * 33 + (e & 31)] = D[(e >> 5) * 129 + q0 + (e & 31)];
     __syncthreads();
-    // row c scaled, column c replaced, the rest updated with the staged row/column
-    for (int e = threadIdx.x; e < 128 * 128; e += 512) {
-      int i = e >> 7, j = e & 127;
-      float v;
-      if (i == c) v = (j == c) ? pinv : rowc[j] * pinv;
-      else if (j == c) v = -colc[i] * pinv;
-      else v = D[i * ld + j] - colc[i] * (rowc[j] * pinv);
-      D[i * ld + j] = v;
+    // R = P * D[panel rows, :] (inside the panel: P itself); thread -> row i, 8 columns
+    {
+      const int i = threadIdx.x >> 4, jb = (threadIdx.x & 15) * 8;
+      const bool jk = (jb >= q0 && jb < q0 + 32);
+      float v[8];
+#pragma unroll
+      for (int jj = 0; jj < 8; ++jj) v[jj] = jk ? Pq[i * 33 + jb + jj - q0] : 0.f;
+      if (!jk) {
+        for (int k = 0; k < 32; ++k) {
+          const float pk = Pq[i * 33 + k];
+          const float* drow = D + (q0 + k) * 129 + jb;
+#pragma unroll
+          for (int jj = 0; jj < 8; ++jj) v[jj] = fmaf(pk, drow[jj], v[jj]);
+        }
+      }
+#pragma unroll
+      for (int jj = 0; jj < 8; ++jj) Rq[i * 128 + jb + jj] = v[jj];
+    }
+    __syncthreads();
+    // D update; thread -> 4 rows x 8 columns (panel membership uniform per tile)
+    {
+      const int ib = (threadIdx.x >> 4) * 4, jb = (threadIdx.x & 15) * 8;
+      const bool ik = (ib >= q0 && ib < q0 + 32), jk = (jb >= q0 && jb < q0 + 32);
+      float v[4][8];
+      if (ik) {
+#pragma unroll
+        for (int ii = 0; ii < 4; ++ii)
+#pragma unroll
+          for (int jj = 0; jj < 8; ++jj) v[ii][jj] = Rq[(ib + ii - q0) * 128 + jb + jj];
+      } else {
+        const float* bsrc = jk ? Pq : Rq;
+        const int bld = jk ? 33 : 128, boff = jk ? jb - q0 : jb;
+#pragma unroll
+        for (int ii = 0; ii < 4; ++ii)
+#pragma unroll
+          for (int jj = 0; jj < 8; ++jj) v[ii][jj] = jk ? 0.f : D[(ib + ii) * 129 + jb + jj];
+        for (int k = 0; k < 32; ++k) {
+          float c[4], b[8];
+#pragma unroll
+          for (int ii = 0; ii < 4; ++ii) c[ii] = Cq[(ib + ii) * 33 + k];
+#pragma unroll
+          for (int jj = 0; jj < 8; ++jj) b[jj] = bsrc[k * bld + boff + jj];
+#pragma unroll
+          for (int ii = 0; ii < 4; ++ii)
+#pragma unroll
+            for (int jj = 0; jj < 8; ++jj) v[ii][jj] = fmaf(-c[ii], b[jj], v[ii][jj]);
+        }
+      }
+      __syncthreads();  // every thread has read D / Cq / Rq / Pq before D is rewritten
+#pragma unroll
+      for (int ii = 0; ii < 4; ++ii)
+#pragma unroll
+        for (int jj = 0; jj < 8; ++jj) D[(ib + ii) * 129 + jb + jj] = v[ii][jj];
     }
     __syncthreads();
   }
+  if (!ok && threadIdx.x == 0) atomicOr(status + s, SFD_ST_ZERO_PIVOT);
   float* P = pbuf + (long long)s * 128 * 128;
-  for (int e = threadIdx.x; e < 128 * 128; e += 512) P[e] = D[(e >> 7) * ld + (e & 127)];
+  for (int e = threadIdx.x; e < 128 * 128; e += 512) P[e] = D[(e >> 7) * 129 + (e & 127)];
 }
 
-// R_j = P A_Kj (128 x 64 tiles over j not in K); C = A_iK copy (64-row tiles).
+// x = hi + mid + lo in bf16 (24 significant bits: exact for an FP32 value up to
+// the last rounding); parts are `stride` elements apart.
+__device__ __forceinline__ void split_bf16x3(float x, __nv_bfloat16* dst, long long stride) {
+  __nv_bfloat16 hi = __float2bfloat16_rn(x);
+  float r1 = x - __bfloat162float(hi);
+  __nv_bfloat16 mid = __float2bfloat16_rn(r1);
+  float r2 = r1 - __bfloat162float(mid);
+  dst[0] = hi;
+  dst[stride] = mid;
+  dst[2 * stride] = __float2bfloat16_rn(r2);
+}
+
 __global__ void __launch_bounds__(256) k_gj_panel(const SurfaceDesc* surf, int nsurf, int kb, const float* mat,
-                                                  const float* pbuf, float* rbuf, float* cbuf, const long long* poff) {
+                                                  const float* pbuf, float* rbuf, float* cbuf, const long long* poff,
+                                                  __nv_bfloat16* cparts, __nv_bfloat16* rparts, long long pstride) {
   const int s = blockIdx.z;
   const SurfaceDesc& S = surf[s];
   const int np = pad_n(S.n), k0 = kb * 128;
@@ -330,11 +423,15 @@ __global__ void __launch_bounds__(256) k_gj_panel(const SurfaceDesc* surf, int n
   // C copy (rows t*64 .. +64, all 128 columns of K)
   for (int e = threadIdx.x; e < 64 * 128; e += 256) {
     int r = t * 64 + (e >> 7), c = e & 127;
-    C[(long long)r * 128 + c] = A[(long long)r * np + k0 + c];
+    float v = A[(long long)r * np + k0 + c];
+    C[(long long)r * 128 + c] = v;
+    if (cparts) split_bf16x3(v, cparts + poff[s] + (long long)r * 128 + c, pstride);
   }
   if (t * 64 >= k0 && t * 64 < k0 + 128) return;  // columns inside K: R not needed
-  __shared__ float Pt[128][33];
-  __shared__ float Bt[32][65];
+  // shared memory: the GEMM operands, then (reused) the transposed tile
+  __shared__ float sm[64 * 129];
+  float (*Pt)[33] = reinterpret_cast<float (*)[33]>(sm);            // 128 x 33
+  float (*Bt)[65] = reinterpret_cast<float (*)[65]>(sm + 128 * 33);  // 32 x 65
   const int tr = (threadIdx.x >> 4) * 8, tc = (threadIdx.x & 15) * 4;  // 16 x 16 threads -> 128 x 64
   float acc[8][4] = {};
   for (int q0 = 0; q0 < 128; q0 += 32) {
@@ -358,17 +455,47 @@ __global__ void __launch_bounds__(256) k_gj_panel(const SurfaceDesc* surf, int n
   for (int i = 0; i < 8; ++i)
 #pragma unroll
     for (int j = 0; j < 4; ++j) R[(long long)(tr + i) * np + t * 64 + tc + j] = acc[i][j];
+  if (rparts) {
+    // R^T (K-major) for the tensor-core update: transpose through shared memory,
+    // then write each R^T row (128 values, three bf16 parts) coalesced
+    __syncthreads();
+    float (*Rs)[129] = reinterpret_cast<float (*)[129]>(sm);  // 64 x 129
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) Rs[tc + j][tr + i] = acc[i][j];
+    __syncthreads();
+    for (int e = threadIdx.x; e < 64 * 128; e += 256) {
+      int jl = e >> 7, k = e & 127;
+      split_bf16x3(Rs[jl][k], rparts + poff[s] + (long long)(t * 64 + jl) * 128 + k, pstride);
+    }
+  }
 }
 
 // Output tile 64 x 64 (ti, tj) over the whole padded matrix.
+// k_lines_only != 0: grid.x enumerates only the 64x64 tiles of block row K and
+// block column K (4 T - 4 of them, T = n_pad / 64); the tensor-core kernel
+// updates the rest.  Otherwise grid (T, T) covers every tile.
 __global__ void __launch_bounds__(256) k_gj_update(const SurfaceDesc* surf, int nsurf, int kb, float* mat,
                                                    const float* pbuf, const float* rbuf, const float* cbuf,
-                                                   const long long* poff) {
+                                                   const long long* poff, int k_lines_only) {
   const int s = blockIdx.z;
   const SurfaceDesc& S = surf[s];
   const int np = pad_n(S.n), k0 = kb * 128;
   if (k0 >= np) return;
-  const int ti = blockIdx.y, tj = blockIdx.x;
+  int ti = blockIdx.y, tj = blockIdx.x;
+  if (k_lines_only) {
+    const int T = np / 64, K64 = k0 / 64, idx = blockIdx.x;
+    if (idx >= 4 * T - 4) return;
+    if (idx < 2 * T) {
+      ti = K64 + idx / T;
+      tj = idx % T;
+    } else {
+      const int i2 = idx - 2 * T, r = i2 % (T - 2);
+      tj = K64 + i2 / (T - 2);
+      ti = r < K64 ? r : r + 2;
+    }
+  }
   if (ti * 64 >= np || tj * 64 >= np) return;
   float* A = mat + S.moff;
   const float* P = pbuf + (long long)s * 128 * 128;
@@ -425,31 +552,70 @@ __global__ void __launch_bounds__(256) k_gj_update(const SurfaceDesc* surf, int 
 }
 
 // =============================================================== GEMV
-// y[off + i] = sum_j X_ij v[off + j]  (X float, v / y double); one warp per row.
+// y[off + i] = sum_j X_ij v[off + j]  (X float, v / y double).  A CTA covers
+// kGemvRows rows: v is staged once as FP32 in shared memory, each warp walks two
+// rows with 16-byte loads (rows are 16-byte aligned: n_pad is a multiple of 128,
+// and X[i][j] = 0 for j >= n in the padded inverse).
 __global__ void __launch_bounds__(256) k_gemv(const SurfaceDesc* surf, const int2* rowblk, const float* mat,
-                                              const double* v, double* y) {
+                                              const double* v, double* y, float2* ydf) {
   const int2 rb = rowblk[blockIdx.x];  // (surface, first row)
   const SurfaceDesc& S = surf[rb.x];
   const int n = S.n, np = pad_n(n), off = S.off;
+  extern __shared__ float4 vs4[];
+  float* vs = reinterpret_cast<float*>(vs4);
+  const int n4 = (n + 3) & ~3;
+  for (int j = threadIdx.x; j < n4; j += 256) vs[j] = j < n ? (float)v[off + j] : 0.f;
+  __syncthreads();
   const float* X = mat + S.moff;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int row = rb.y + warp;
-  if (row >= n) return;
-  const float* xr = X + (long long)row * np;
-  float acc = 0.f;
-  for (int j = lane * 4; j < n; j += 128) {
-    float4 q = *reinterpret_cast<const float4*>(xr + j);
-    acc = fmaf(q.x, (float)v[off + j], acc);
-    if (j + 1 < n) acc = fmaf(q.y, (float)v[off + j + 1], acc);
-    if (j + 2 < n) acc = fmaf(q.z, (float)v[off + j + 2], acc);
-    if (j + 3 < n) acc = fmaf(q.w, (float)v[off + j + 3], acc);
+  const int r0 = rb.y + 2 * warp, r1 = r0 + 1;
+  if (r0 >= n) return;
+  const float4* x0 = reinterpret_cast<const float4*>(X + (long long)r0 * np);
+  const float4* x1 = reinterpret_cast<const float4*>(X + (long long)(r1 < n ? r1 : r0) * np);
+  float acc0 = 0.f, acc1 = 0.f;
+  const int nq = n4 / 4;
+  int q = lane;
+  for (; q + 96 < nq; q += 128) {  // four 16-byte loads per row in flight
+    float4 a0 = __ldg(x0 + q), a1 = __ldg(x0 + q + 32), a2 = __ldg(x0 + q + 64), a3 = __ldg(x0 + q + 96);
+    float4 b0 = __ldg(x1 + q), b1 = __ldg(x1 + q + 32), b2 = __ldg(x1 + q + 64), b3 = __ldg(x1 + q + 96);
+    float4 v0 = vs4[q], v1 = vs4[q + 32], v2 = vs4[q + 64], v3 = vs4[q + 96];
+    acc0 = fmaf(a0.x, v0.x, fmaf(a0.y, v0.y, fmaf(a0.z, v0.z, fmaf(a0.w, v0.w, acc0))));
+    acc1 = fmaf(b0.x, v0.x, fmaf(b0.y, v0.y, fmaf(b0.z, v0.z, fmaf(b0.w, v0.w, acc1))));
+    acc0 = fmaf(a1.x, v1.x, fmaf(a1.y, v1.y, fmaf(a1.z, v1.z, fmaf(a1.w, v1.w, acc0))));
+    acc1 = fmaf(b1.x, v1.x, fmaf(b1.y, v1.y, fmaf(b1.z, v1.z, fmaf(b1.w, v1.w, acc1))));
+    acc0 = fmaf(a2.x, v2.x, fmaf(a2.y, v2.y, fmaf(a2.z, v2.z, fmaf(a2.w, v2.w, acc0))));
+    acc1 = fmaf(b2.x, v2.x, fmaf(b2.y, v2.y, fmaf(b2.z, v2.z, fmaf(b2.w, v2.w, acc1))));
+    acc0 = fmaf(a3.x, v3.x, fmaf(a3.y, v3.y, fmaf(a3.z, v3.z, fmaf(a3.w, v3.w, acc0))));
+    acc1 = fmaf(b3.x, v3.x, fmaf(b3.y, v3.y, fmaf(b3.z, v3.z, fmaf(b3.w, v3.w, acc1))));
   }
-  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-  if (lane == 0) y[off + row] = (double)acc;
+  for (; q < nq; q += 32) {
+    float4 vv = vs4[q];
+    float4 a = __ldg(x0 + q), b = __ldg(x1 + q);
+    acc0 = fmaf(a.x, vv.x, fmaf(a.y, vv.y, fmaf(a.z, vv.z, fmaf(a.w, vv.w, acc0))));
+    acc1 = fmaf(b.x, vv.x, fmaf(b.y, vv.y, fmaf(b.z, vv.z, fmaf(b.w, vv.w, acc1))));
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    acc0 += __shfl_xor_sync(0xffffffffu, acc0, o);
+    acc1 += __shfl_xor_sync(0xffffffffu, acc1, o);
+  }
+  if (lane == 0) {
+    y[off + r0] = (double)acc0;
+    if (ydf) ydf[off + r0] = make_float2(acc0, 0.f);
+    if (r1 < n) {
+      y[off + r1] = (double)acc1;
+      if (ydf) ydf[off + r1] = make_float2(acc1, 0.f);
+    }
+  }
 }
 
-// a += delta (and keep delta for the FP32 correction pass)
-__global__ void k_axpy_inplace(int n, double* a, const double* d) {
+// a += delta; optionally also the double-float copy of the new a
+__global__ void k_axpy_inplace(int n, double* a, const double* d, float2* adf) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) a[i] += d[i];
+  if (i >= n) return;
+  double v = a[i] + d[i];
+  a[i] = v;
+  if (adf) {
+    float hi = __double2float_rn(v);
+    adf[i] = make_float2(hi, __double2float_rn(v - (double)hi));
+  }
 }

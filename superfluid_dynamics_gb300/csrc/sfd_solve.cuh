@@ -2,8 +2,12 @@
 #pragma once
 #include "sfd_engine.cuh"
 
+#include <cuda_bf16.h>
+
 // per-surface matrices are padded to a multiple of 128 rows/columns
 __host__ __device__ __forceinline__ int pad_n(int n) { return (n + 127) / 128 * 128; }
+constexpr int kGemvRows = 16;  // rows per CTA of k_gemv
+constexpr int kGjDiagSmem = (128 * 129 + 128 * 33 + 32 * 128 + 32 * 33) * 4;  // k_gj_diag dynamic shared memory
 
 cudaError_t sfd_launch_assemble64(const SurfaceDesc* surf, const int4* tiles, int ntiles, const cd* w, const cd* p,
                                   const cd* zp, const double* mdiag, double* mat, cudaStream_t st);
@@ -16,8 +20,14 @@ __global__ void k_lu64_gemm(const SurfaceDesc* surf, int nsurf, int kb, double* 
 __global__ void k_lu64_solve(const SurfaceDesc* surf, const double* mat, const double* b, double* x);
 __global__ void k_gj_diag(const SurfaceDesc* surf, int nsurf, int kb, float* mat, float* pbuf, unsigned int* status);
 __global__ void k_gj_panel(const SurfaceDesc* surf, int nsurf, int kb, const float* mat, const float* pbuf,
-                           float* rbuf, float* cbuf, const long long* poff);
+                           float* rbuf, float* cbuf, const long long* poff, __nv_bfloat16* cparts,
+                           __nv_bfloat16* rparts, long long pstride);
 __global__ void k_gj_update(const SurfaceDesc* surf, int nsurf, int kb, float* mat, const float* pbuf,
-                            const float* rbuf, const float* cbuf, const long long* poff);
-__global__ void k_gemv(const SurfaceDesc* surf, const int2* rowblk, const float* mat, const double* v, double* y);
-__global__ void k_axpy_inplace(int n, double* a, const double* d);
+                            const float* rbuf, const float* cbuf, const long long* poff, int k_lines_only);
+cudaError_t sfd_tc_configure();
+cudaError_t sfd_launch_gj_update_tc(const SurfaceDesc* surf, int nsurf, int kb, int max_np, float* mat,
+                                    const __nv_bfloat16* cparts, const __nv_bfloat16* rparts, long long part_stride,
+                                    const long long* poff, unsigned int* status, cudaStream_t st);
+__global__ void k_gemv(const SurfaceDesc* surf, const int2* rowblk, const float* mat, const double* v, double* y,
+                       float2* ydf);
+__global__ void k_axpy_inplace(int n, double* a, const double* d, float2* adf);

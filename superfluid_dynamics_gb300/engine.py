@@ -60,14 +60,17 @@ class Physics:
 @dataclass
 class Options:
     precision: int = PRECISION_MIXED
-    refine_iters: int = 3
+    refine_iters: int = 2
     refactor_every: int = 1
     use_graphs: bool = True
     device: int = 0
+    tensor_cores: bool = True
+    pre_iters: int = 1
 
     def to_c(self) -> _lib.SfdOptions:
         return _lib.SfdOptions(self.precision, self.refine_iters, self.refactor_every,
-                               1 if self.use_graphs else 0, self.device)
+                               1 if self.use_graphs else 0, self.device, 1 if self.tensor_cores else 0,
+                               self.pre_iters)
 
 
 class Engine:

@@ -240,3 +240,41 @@ def test_nonfinite_state_sets_status():
         e.rhs()
         st, _, _ = e.status()
     assert st[0] & sfd._lib.STATUS_NONFINITE
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_batch_mixing_cluster_and_single_cta_transforms(prec):
+    # n % 64 == 0 and n >= 512 use the cluster-distributed transforms; others one CTA
+    sizes = [512, 96, 640, 1152, 160]
+    surfs = []
+    for i, n in enumerate(sizes):
+        xi = W.nodes(n)
+        surfs.append(W.Surface(xi.copy(), 0.04 * np.cos((i + 1) * xi) + 0.01 * np.sin(3 * xi),
+                               0.02 * np.sin((i + 1) * xi)))
+    with sfd.Engine(sizes, sfd.WaterBoundaryProblem(), sfd.Options(precision=PREC[prec])) as e:
+        e.set_state(np.concatenate([s.x for s in surfs]), np.concatenate([s.y for s in surfs]),
+                    np.concatenate([s.phi for s in surfs]))
+        dx, dy, dphi, a, zp, zpp = e.rhs(diagnostics=True)
+        parts = [e.split(v) for v in (dx, dy, dphi, zp, zpp)]
+    for i, s in enumerate(surfs):
+        (ox, oy, op, oa, ozp, ozpp), _ = O.rhs(O.Problem(), s.x, s.y, s.phi, diagnostics=True)
+        assert rel(parts[3][i], ozp) < 1e-13 and rel(parts[4][i], ozpp) < 1e-11
+        assert rel(parts[0][i] + 1j * parts[1][i], ox + 1j * oy) < TOL[prec]
+        assert rel(parts[2][i], op) < TOL[prec]
+
+
+@pytest.mark.parametrize("n", [256, 640, 1024])
+def test_tensor_core_preconditioner(n):
+    # The tcgen05 (3 x bf16-split) Gauss-Jordan update must give a usable inverse on
+    # its own (no refinement: a = X phi' to ~1e-4), and the refined result must match.
+    s = W.random_modes(n, seed=11)
+    (ox, oy, op, oa, _, _), _ = O.rhs(O.Problem(), s.x, s.y, s.phi, diagnostics=True)
+    for tc in (True, False):
+        out0, st0 = engine_rhs(n, sfd.WaterBoundaryProblem(), s.x, s.y, s.phi, "mixed", refine_iters=0,
+                               tensor_cores=tc)
+        assert rel(out0[3], oa) < (1e-3 if tc else 1e-5)
+        out3, st3 = engine_rhs(n, sfd.WaterBoundaryProblem(), s.x, s.y, s.phi, "mixed", refine_iters=3,
+                               tensor_cores=tc)
+        assert rel(out3[3], oa) < 1e-10
+        assert rel(out3[0] + 1j * out3[1], ox + 1j * oy) < 1e-10
+        assert (st3[0] & (sfd._lib.STATUS_TIMEOUT | sfd._lib.STATUS_NONFINITE)).max() == 0
