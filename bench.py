@@ -10,8 +10,10 @@ reference measures on no dataset.
            stream around each step; L2 flushed between steps, outside timing)
   e2e    : steps/s through the C ABI with host buffers (pinned host -> device
            copy of the state, one step, device -> host copy, every step)
-  roofline: dominant kernel class from a per-kernel CUDA-event pass over the
-           same steps (graphs off during that pass only)
+  roofline: the RK4 step against the tensor roofline of its algorithmic FLOP
+           (dense LU + matvecs, bf16 peak / 3); per-kernel-class times from a
+           CUDA-event pass over the same workload (graphs off in that pass);
+           traffic = DRAM bytes per step from the committed ncu summary
   cpu_baseline: the FP64 CPU oracle (a port of the reference path) on a bounded
            sample (one RK4 step at N = 4096) on this host's cores
 
@@ -103,6 +105,22 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(rows)}
 
 
+def step_traffic(n, args):
+    """DRAM bytes per RK4 step (read + write, all kernels of one step) from the
+    committed ncu summary of this configuration, or None when there is none."""
+    key = (f"traffic_bytes_per_step n={n} precision={args.precision} pre_iters={args.pre_iters} "
+           f"refine_iters={args.refine_iters} refactor_every={args.refactor_every}:")
+    try:
+        with open(os.path.join(ROOT, "profiles", "rk4_step_n4096_launches.md")) as f:
+            for line in f:
+                line = line.strip().strip("`")
+                if line.startswith(key):
+                    return float(line[len(key):].split()[0])
+    except OSError:
+        pass
+    return None
+
+
 def cpu_sample(steps: int = 1, n: int = N_NODES):
     """Oracle port (FP64, OpenMP over all host cores): time `steps` RK4 steps."""
     from oracle import oracle
@@ -152,8 +170,13 @@ def run_ours(args, rank, world, local_rank):
     eng.set_state(s.x, s.y, s.phi)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
-    # warm-up (also builds the CUDA graphs)
-    for _ in range(args.warmup):
+    # warm-up (also builds the CUDA graphs), then untimed steps up to the next
+    # preconditioner rebuild so that the timed window starts with one and holds
+    # ceil(steps / refactor_every) of them
+    warm = args.warmup
+    every = max(1, args.refactor_every)
+    warm += (every - warm % every) % every if args.precision == "mixed" else 0
+    for _ in range(warm):
         eng.step(DT, 1)
     if world > 1:
         torch.distributed.barrier()
@@ -181,24 +204,38 @@ def run_ours(args, rank, world, local_rank):
         ms = float(t.item())
     value = world * args.steps / (ms * 1e-3)
 
-    # ---- end to end through the C ABI with host buffers
+    done = warm + args.steps
+
+    def align():
+        # untimed steps up to the next preconditioner rebuild
+        nonlocal done
+        extra = (every - done % every) % every if args.precision == "mixed" else 0
+        if extra:
+            eng.step(DT, extra)
+            done += extra
+
+    # ---- end to end through the C ABI with host buffers: every step copies the
+    # state in from pinned host memory and the result back out
     x = torch.from_numpy(s.x).pin_memory().numpy()
     y = torch.from_numpy(s.y).pin_memory().numpy()
     p = torch.from_numpy(s.phi).pin_memory().numpy()
-    e2e_steps = max(3, min(args.steps, 20))
+    align()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(e2e_steps):
+    for _ in range(args.steps):
         eng.set_state(x, y, p)
         eng.step(DT, 1)
         x2, y2, p2 = eng.get_state()
     e2e_s = time.perf_counter() - t0
-    e2e_value = world * e2e_steps / e2e_s
+    done += args.steps
+    e2e_value = world * args.steps / e2e_s
 
-    # ---- per-kernel classes over the same steps (events per launch, graphs off)
+    # ---- per-kernel classes (events per launch, graphs off) over one
+    # preconditioner period (at most 50 steps)
     eng.set_state(s.x, s.y, s.phi)
+    align()
     eng.profile(True)
-    prof_steps = max(1, min(args.steps, 5))
+    prof_steps = min(every, 50) if args.precision == "mixed" else 2
     eng.step(DT, prof_steps)
     prof = eng.profile_read()
     eng.profile(False)
@@ -208,33 +245,25 @@ def run_ours(args, rank, world, local_rank):
         return
     hbm, bf16, bf16s, peak_kind = peaks()
     n = args.n
-    np_ = (n + 127) // 128 * 128
-    # algorithmic work per launch of each candidate class
-    per_launch = {}
-    for name, (tms, cnt) in prof.items():
-        if cnt:
-            per_launch[name] = (tms / cnt, cnt)
-    dom = max(per_launch, key=lambda k: per_launch[k][0] * per_launch[k][1])
-    avg_ms = per_launch[dom][0]
-    if dom == "factor_update":
-        # Gauss-Jordan rank-128 update: 2 n_pad^2 128 FLOP per launch (FP32-equivalent)
-        flops = 2.0 * np_ * np_ * 128
-        roof = {"bound": "tensor", "achieved": flops / (avg_ms * 1e-3) / 1e12, "peak": bf16 / 3.0, "unit": "TFLOP/s"}
-        roof["note"] = "FP32-equivalent FLOP vs bf16 peak / 3 (3-product split)"
-    elif dom in ("gemv", "assemble"):
-        byts = 4.0 * n * n + (16.0 * n if dom == "gemv" else 0)
-        roof = {"bound": "hbm", "achieved": byts / (avg_ms * 1e-3) / 1e9, "peak": hbm, "unit": "GB/s"}
-    else:
-        # boundary sums: N^2 source-target pairs; report against HBM by their inputs (not the bound)
-        byts = 40.0 * n * ((n + 511) // 512) + 32.0 * n
-        roof = {"bound": "hbm", "achieved": byts / (avg_ms * 1e-3) / 1e9, "peak": hbm, "unit": "GB/s",
-                "note": f"{dom} is FP32-pipe bound (double-float arithmetic); HBM view shown"}
+    per_launch = {name: (tms / cnt, cnt) for name, (tms, cnt) in prof.items() if cnt}
+    # Roofline of the step: the dense second-kind solve is a contraction, so the
+    # tensor pipe bounds it.  Algorithmic FLOP per RK4 step (one surface):
+    #   F(N) = 4 [ (2/3) N^3 (LU) + 2 N^2 (triangular solves) + 2 N^2 (FP64
+    #          residual matvec) + 8 N^2 (complex velocity matvec) ]
+    # against the bf16 dense peak / 3 (the FP32-equivalent rate of a 3-product
+    # bf16 split).  The mixed path replaces most of the LU by a reused FP32
+    # preconditioner plus refinement, so this is an equivalent rate.
+    flop_step = 4.0 * (2.0 / 3.0 * n ** 3 + 2.0 * n * n + 2.0 * n * n + 8.0 * n * n)
+    step_ms = ms / args.steps
+    roof = {"bound": "tensor", "kernel": "rk4_step (one CUDA graph launch per step)",
+            "achieved": flop_step / (step_ms * 1e-3) / 1e12, "peak": bf16 / 3.0, "unit": "TFLOP/s",
+            "algorithmic_flop_per_step": flop_step, "peak_source": f"{peak_kind} bf16 burst / 3"}
     roof["frac"] = roof["achieved"] / roof["peak"]
-    roof["traffic"] = None
-    roof["kernel"] = dom
-    roof["avg_launch_ms"] = avg_ms
-    roof["peak_source"] = peak_kind
+    roof["traffic"] = step_traffic(n, args)
     roof["classes_ms_per_step"] = {k: round(v[0] * v[1] / prof_steps, 4) for k, v in per_launch.items()}
+    dom = max(per_launch, key=lambda k: per_launch[k][0] * per_launch[k][1])
+    roof["dominant_class"] = {"name": dom, "avg_launch_ms": round(per_launch[dom][0], 5),
+                              "launches_per_step": per_launch[dom][1] / prof_steps}
 
     cpu = None
     if not args.no_cpu and world >= 1:
@@ -242,7 +271,7 @@ def run_ours(args, rank, world, local_rank):
         cpu = {"value": rate, "unit": "steps/s", "cores": cores, "kind": "port",
                "sample": f"1 RK4 step at N={n} (FP64 oracle, OpenMP)"}
     line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "warmup": warm, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64+df32 (mixed)" if args.precision == "mixed" else "f64",
             "data": "synthetic (seeded 8-mode gravity wave)",
             "config": {"workload": f"gravity wave N={n}, 8 modes seed 2, RK4 dt={DT}", "N": n,
@@ -259,14 +288,14 @@ def run_ours(args, rank, world, local_rank):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N_NODES)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--refine-iters", type=int, default=2)
-    ap.add_argument("--pre-iters", type=int, default=1)
-    ap.add_argument("--refactor-every", type=int, default=1)
+    ap.add_argument("--pre-iters", type=int, default=2)
+    ap.add_argument("--refactor-every", type=int, default=50)
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
