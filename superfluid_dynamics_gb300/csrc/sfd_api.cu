@@ -120,7 +120,7 @@ struct sfd_engine {
   cudaStream_t stream = nullptr;
   cudaStream_t own_stream = nullptr;
   sfd_options opt{};
-  int nsurf = 0, ntot = 0, max_n = 0, max_np = 0, max_chunks = 0;
+  int nsurf = 0, ntot = 0, max_n = 0, max_np = 0;
   long long mat_elems = 0, panel_elems = 0;
   bool any_rho = false;
   std::vector<SurfaceDesc> hs;
@@ -133,7 +133,7 @@ struct sfd_engine {
   int2* d_cjobs_first = nullptr; int ncjobs_first = 0;  // cluster-distributed transforms
   int2* d_cjobs_ap = nullptr; int ncjobs_ap = 0;
   int max_n_single = 0, max_n_cluster = 0;
-  int4* d_sum_items = nullptr; int nsum = 0;
+  int2* d_sum_items = nullptr; int nsum = 0;
   int4* d_asm_tiles = nullptr; int nasm = 0;
   int2* d_gemv_rows = nullptr; int ngemv = 0;
   long long* d_poff = nullptr;
@@ -145,10 +145,7 @@ struct sfd_engine {
   double *phip = nullptr, *a = nullptr, *r = nullptr, *delta = nullptr, *phi_im = nullptr;
   float2 *adf = nullptr, *ddf = nullptr;  // double-float copies of a and delta
   NodeData nd{};
-  cd *part_s = nullptr, *part_t = nullptr, *cacc = nullptr, *dacc = nullptr, *vel_low1 = nullptr;
-  double* part_a = nullptr;        // [target tile][chunk] weight sums
-  int* tile_count = nullptr;       // arrivals per target tile (boundary sums)
-  int ntiles_sum = 0;              // target tiles over all surfaces
+  cd *cacc = nullptr, *dacc = nullptr, *vel_low1 = nullptr;
   unsigned int* status = nullptr;
   double *lmax = nullptr, *rnorm = nullptr, *inv_out = nullptr;
   // matrices
@@ -237,11 +234,11 @@ inline int blocks_for(long long n, int t) { return (int)((n + t - 1) / t); }
 // epilogue writes C, D and the residual (mode 0: r = phi' - M a, C/D
 // overwritten; mode 1: r -= M a, C/D accumulated).
 int enqueue_sums(sfd_engine* e, int prec, const double* weights, const float2* weights_df, int mode, bool track_norm) {
-  SumArgs A{e->d_surf, e->d_sum_items, e->nsurf, e->ntot, e->max_chunks, e->nd.w, e->nd.p, weights, e->nd.wdf,
-            e->nd.pdf, weights_df, e->part_s, e->part_t, e->part_a, e->tile_count, e->nd.mdiag, e->zp, e->phip,
+  SumArgs A{e->d_surf, e->d_sum_items, e->nsurf, e->ntot, e->nd.w, e->nd.p, weights, e->nd.wdf,
+            e->nd.pdf, weights_df, e->nd.mdiag, e->zp, e->phip,
             e->cacc, e->dacc, e->r, track_norm ? e->rnorm : nullptr, mode};
   int cls = prec == SFD_PREC_F64 ? SFD_K_SUMS64 : prec == SFD_PREC_DF ? SFD_K_SUMSDF : SFD_K_SUMS32;
-  LAUNCHC(e, cls, sfd_launch_sums(prec, A, e->nsum, e->stream));
+  LAUNCHC(e, cls, sfd_launch_sums(prec, A, e->nsum, e->max_n, e->stream));
   return 0;
 }
 
@@ -445,7 +442,7 @@ void free_engine(sfd_engine* e) {
   void* ptrs[] = {e->d_surf, e->d_node_surf, e->d_jobs_first, e->d_jobs_ap, e->d_cjobs_first, e->d_cjobs_ap, e->d_sum_items, e->d_asm_tiles,
                   e->d_gemv_rows, e->d_poff, e->y0, e->ys, e->kacc, e->kcur, e->zp, e->zpp, e->ap, e->phip, e->a,
                   e->r, e->delta, e->phi_im, e->nd.w, e->nd.p, e->nd.wdf, e->nd.pdf, e->adf, e->ddf, e->nd.mdiag, e->nd.v1low, e->nd.v1up, e->nd.v2,
-                  e->part_s, e->part_t, e->cacc, e->dacc, e->vel_low1, e->part_a, e->tile_count, e->status, e->lmax, e->rnorm,
+                  e->cacc, e->dacc, e->vel_low1, e->status, e->lmax, e->rnorm,
                   e->inv_out, e->m64, e->m32, e->pbuf, e->rbuf, e->cbuf, e->cparts, e->rparts};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -597,7 +594,6 @@ int sfd_create(const int* n, int nsurf, const sfd_problem* problems, int shared_
     moff += (long long)np * np;
     e->max_n = std::max(e->max_n, ns);
     e->max_np = std::max(e->max_np, np);
-    e->max_chunks = std::max(e->max_chunks, (ns + kSumChunk - 1) / kSumChunk);
   }
   if (off > (1LL << 30)) {
     free_engine(e);
@@ -610,13 +606,15 @@ int sfd_create(const int* n, int nsurf, const sfd_problem* problems, int shared_
   // work lists
   std::vector<int> node_surf(nt);
   std::vector<int2> jf, ja, cjf, cja;
-  std::vector<int4> items, tiles;
+  std::vector<int2> items;
+  std::vector<int4> tiles;
   std::vector<int2> rows;
   for (int s = 0; s < nsurf; ++s) {
     const SurfaceDesc& S = e->hs[s];
     for (int k = 0; k < S.n; ++k) node_surf[S.off + k] = s;
     if (S.nrad_m > 0) {
-      cjf.push_back({s, SFD_JOB_ZP});  // the cluster Z job writes z' and z''
+      cjf.push_back({s, SFD_JOB_ZP});  // z', z'' and phi' on three clusters side by side
+      cjf.push_back({s, SFD_JOB_ZPP});
       cjf.push_back({s, SFD_JOB_PHIP});
       cja.push_back({s, SFD_JOB_AP});
       e->max_n_cluster = std::max(e->max_n_cluster, S.n);
@@ -627,12 +625,7 @@ int sfd_create(const int* n, int nsurf, const sfd_problem* problems, int shared_
       ja.push_back({s, SFD_JOB_AP});
       e->max_n_single = std::max(e->max_n_single, S.n);
     }
-    int nch = (S.n + kSumChunk - 1) / kSumChunk;
-    e->hs[s].tile_base = e->ntiles_sum;
-    for (int t0 = 0; t0 < S.n; t0 += kSumTargets) {
-      for (int c = 0; c < nch; ++c) items.push_back({s, t0, c * kSumChunk, c});
-      ++e->ntiles_sum;
-    }
+    for (int t0 = 0; t0 < S.n; t0 += kSumTile) items.push_back({s, t0});
     int np = pad_n(S.n);
     for (int r0 = 0; r0 < np; r0 += 64)
       for (int c0 = 0; c0 < np; c0 += 64) tiles.push_back({s, r0, c0, 0});
@@ -658,7 +651,7 @@ int sfd_create(const int* n, int nsurf, const sfd_problem* problems, int shared_
   CKE(dalloc(&e->d_cjobs_ap, cja.size()));
   CKE(cudaMemcpy(e->d_cjobs_ap, cja.data(), cja.size() * sizeof(int2), cudaMemcpyHostToDevice));
   CKE(dalloc(&e->d_sum_items, items.size()));
-  CKE(cudaMemcpy(e->d_sum_items, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice));
+  CKE(cudaMemcpy(e->d_sum_items, items.data(), items.size() * sizeof(int2), cudaMemcpyHostToDevice));
   CKE(dalloc(&e->d_asm_tiles, tiles.size()));
   CKE(cudaMemcpy(e->d_asm_tiles, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice));
   CKE(dalloc(&e->d_gemv_rows, rows.size()));
@@ -687,11 +680,6 @@ int sfd_create(const int* n, int nsurf, const sfd_problem* problems, int shared_
   CKE(dalloc(&e->nd.v1low, nt));
   CKE(dalloc(&e->nd.v1up, nt));
   CKE(dalloc(&e->nd.v2, nt));
-  CKE(dalloc(&e->part_s, (long long)e->max_chunks * nt));
-  CKE(dalloc(&e->part_t, (long long)e->max_chunks * nt));
-  CKE(dalloc(&e->part_a, (long long)e->max_chunks * e->ntiles_sum));
-  CKE(dalloc(&e->tile_count, e->ntiles_sum));
-  CKE(cudaMemset(e->tile_count, 0, e->ntiles_sum * sizeof(int)));
   CKE(dalloc(&e->cacc, nt));
   CKE(dalloc(&e->dacc, nt));
   CKE(dalloc(&e->vel_low1, 1));
@@ -706,7 +694,6 @@ int sfd_create(const int* n, int nsurf, const sfd_problem* problems, int shared_
   CKE(cudaMemset(e->nd.p, 0, nt * sizeof(cd)));
   CKE(cudaMemset(e->nd.pdf, 0, nt * sizeof(float4)));
   CKE(cudaMemset(e->dacc, 0, nt * sizeof(cd)));
-  CKE(cudaMemset(e->part_t, 0, (long long)e->max_chunks * nt * sizeof(cd)));
   if (e->opt.precision == SFD_PRECISION_FP64) {
     CKE(dalloc(&e->m64, e->mat_elems));
   } else {
@@ -721,6 +708,7 @@ int sfd_create(const int* n, int nsurf, const sfd_problem* problems, int shared_
     }
   }
   CKE(sfd_fft_configure());
+  CKE(sfd_sums_configure());
   CKE(cudaFuncSetAttribute(k_gj_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, kGjDiagSmem));
   CKE(cudaFuncSetAttribute(k_lu64_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, 8320 * (int)sizeof(double)));
 #undef CKE
@@ -1124,18 +1112,14 @@ int integrateSimulationRK4_freeMemory(double* statesOut, double* timesOut) {
 namespace noalloc {
 constexpr int kMaxN = 1024;  // stated maximum surface size
 constexpr size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
-constexpr int kMaxChunks = (kMaxN + kSumChunk - 1) / kSumChunk;
-constexpr int kMaxTgtTiles = (kMaxN + kSumTargets - 1) / kSumTargets;
-constexpr int kMaxItems = kMaxTgtTiles * kMaxChunks;
+constexpr int kMaxItems = (kMaxN + kSumTile - 1) / kSumTile;
 constexpr int kMaxTiles = (kMaxN / 64) * (kMaxN / 64);
 constexpr size_t kBytes = align256(8ull * kMaxN * kMaxN)            // FP64 matrix (kMaxN is a multiple of 128)
                           + 13 * align256(16ull * kMaxN)            // complex node arrays, twiddles, df copies
-                          + 2 * align256(16ull * kMaxChunks * kMaxN)  // sum partials
                           + 5 * align256(8ull * kMaxN)              // real node arrays
                           + align256(4ull * kMaxN)                  // node -> surface map
                           + align256(sizeof(SurfaceDesc)) + 2 * align256(4 * sizeof(int2)) +
-                          align256(kMaxItems * sizeof(int4)) + align256(kMaxTiles * sizeof(int4)) +
-                          align256(8ull * kMaxChunks * kMaxTgtTiles) + align256(4ull * kMaxTgtTiles) + align256(16) +
+                          align256(kMaxItems * sizeof(int2)) + align256(kMaxTiles * sizeof(int4)) + align256(16) +
                           align256(4) + 2 * align256(8);
 constexpr int kMaxDevices = 64;
 }  // namespace noalloc
@@ -1190,7 +1174,6 @@ extern "C" int sfd_rhs_device_noalloc(const sfd_problem* problem, int n, const v
   if (rc) return rc;
   cudaStream_t st = (cudaStream_t)stream;
   const int np = pad_n(n);
-  const int nchunk = (n + kSumChunk - 1) / kSumChunk;
 
   // host-side descriptors, all on the stack
   SurfaceDesc S;
@@ -1222,10 +1205,9 @@ extern "C" int sfd_rhs_device_noalloc(const sfd_problem* problem, int n, const v
   }
   int2 jf[3] = {{0, SFD_JOB_ZP}, {0, SFD_JOB_ZPP}, {0, SFD_JOB_PHIP}};
   int2 ja[1] = {{0, SFD_JOB_AP}};
-  int4 items[noalloc::kMaxItems];
+  int2 items[noalloc::kMaxItems];
   int nitems = 0;
-  for (int t0 = 0; t0 < n; t0 += kSumTargets)
-    for (int c = 0; c < nchunk; ++c) items[nitems++] = {0, t0, c * kSumChunk, c};
+  for (int t0 = 0; t0 < n; t0 += kSumTile) items[nitems++] = {0, t0};
   int4 tiles[noalloc::kMaxTiles];
   int ntiles = 0;
   for (int r0 = 0; r0 < np; r0 += 64)
@@ -1248,8 +1230,6 @@ extern "C" int sfd_rhs_device_noalloc(const sfd_problem* problem, int n, const v
   e.cacc = b.take<cd>(noalloc::kMaxN);
   e.dacc = b.take<cd>(noalloc::kMaxN);
   cd* d_tw = b.take<cd>(noalloc::kMaxN);
-  e.part_s = b.take<cd>((size_t)noalloc::kMaxChunks * noalloc::kMaxN);
-  e.part_t = b.take<cd>((size_t)noalloc::kMaxChunks * noalloc::kMaxN);
   e.phip = b.take<double>(noalloc::kMaxN);
   e.a = b.take<double>(noalloc::kMaxN);
   e.r = b.take<double>(noalloc::kMaxN);
@@ -1259,10 +1239,8 @@ extern "C" int sfd_rhs_device_noalloc(const sfd_problem* problem, int n, const v
   e.d_surf = b.take<SurfaceDesc>(1);
   e.d_jobs_first = b.take<int2>(4);
   e.d_jobs_ap = b.take<int2>(4);
-  e.d_sum_items = b.take<int4>(noalloc::kMaxItems);
+  e.d_sum_items = b.take<int2>(noalloc::kMaxItems);
   e.d_asm_tiles = b.take<int4>(noalloc::kMaxTiles);
-  e.part_a = b.take<double>((size_t)noalloc::kMaxChunks * noalloc::kMaxTgtTiles);
-  e.tile_count = b.take<int>(noalloc::kMaxTgtTiles);
   e.vel_low1 = b.take<cd>(1);
   e.status = b.take<unsigned int>(1);
   e.lmax = b.take<double>(1);
@@ -1275,10 +1253,9 @@ extern "C" int sfd_rhs_device_noalloc(const sfd_problem* problem, int n, const v
   CK(cudaMemcpyAsync(e.d_surf, &S, sizeof(S), cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(e.d_jobs_first, jf, sizeof(jf), cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(e.d_jobs_ap, ja, sizeof(ja), cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(e.d_sum_items, items, nitems * sizeof(int4), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(e.d_sum_items, items, nitems * sizeof(int2), cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(e.d_asm_tiles, tiles, ntiles * sizeof(int4), cudaMemcpyHostToDevice, st));
   CK(cudaMemsetAsync(e.d_node_surf, 0, n * sizeof(int), st));
-  CK(cudaMemsetAsync(e.tile_count, 0, noalloc::kMaxTgtTiles * sizeof(int), st));
   CK(cudaMemsetAsync(e.status, 0, sizeof(unsigned int), st));
   CK(cudaMemsetAsync(e.lmax, 0, sizeof(double), st));
   CK(cudaMemsetAsync(e.rnorm, 0, sizeof(double), st));
@@ -1295,11 +1272,9 @@ extern "C" int sfd_rhs_device_noalloc(const sfd_problem* problem, int n, const v
   e.max_n = n;
   e.max_n_single = n;
   e.max_np = np;
-  e.max_chunks = nchunk;
   e.njobs_first = 3;
   e.njobs_ap = 1;
   e.nsum = nitems;
-  e.ntiles_sum = noalloc::kMaxTgtTiles;
   e.nasm = ntiles;
   e.any_rho = (S.physics == 0 && S.rho != 0.0);
   return enqueue_rhs(&e, static_cast<const double*>(state_in), static_cast<double*>(rhs_out), true);

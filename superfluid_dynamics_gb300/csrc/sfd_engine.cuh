@@ -25,7 +25,6 @@ struct SurfaceDesc {
   const cd* tw;         // forward FFT twiddles exp(-2 pi i e / n), e in [0, n)
   int nrad;
   int rad[SFD_MAX_RADICES];
-  int tile_base;        // first boundary-sum target tile of this surface
   int nrad_m;           // radices of n / SFD_FFT_CLUSTER (cluster transforms; 0 = not eligible)
   int rad_m[SFD_MAX_RADICES];
 };

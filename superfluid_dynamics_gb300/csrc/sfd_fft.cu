@@ -233,10 +233,10 @@ __global__ void __cluster_dims__(SFD_FFT_CLUSTER, 1, 1) __launch_bounds__(kCT)
   const int n = S.n, off = S.off, kind = job.y;
   const int M = n / C, R = M / C;
   const int c = (int)cluster.block_rank();
-  const int nv = kind == SFD_JOB_ZP ? 2 : 1;  // the Z job yields z' and z''
+  const bool second = (kind == SFD_JOB_ZPP);
   cd* buf = reinterpret_cast<cd*>(csmem_raw);  // M values
-  cd* vbuf = buf + M;                          // 2 x (C x R) values (second half used by the Z job)
-  cd* twm = vbuf + 2 * M;                      // W_M^e = W_n^{C e}, e < M
+  cd* vbuf = buf + M;                          // C x R values
+  cd* twm = vbuf + M;                          // W_M^e = W_n^{C e}, e < M
   cd* twc = twm + M;                           // W_n^{c k1}, k1 < M (this CTA's c)
   cd* twq = twc + M;                           // W_n^{q k1}, q < C, k1 in this CTA's range: [q R + t]
   const double rho = S.physics == 0 ? S.rho : 0.0;
@@ -253,7 +253,7 @@ __global__ void __cluster_dims__(SFD_FFT_CLUSTER, 1, 1) __launch_bounds__(kCT)
   for (int m = threadIdx.x; m < M; m += kCT) {
     const int j = C * m + c;
     cd v;
-    if (kind == SFD_JOB_ZP) v = {A.x[off + j] - 2 * SFD_PI * (double)j / n, A.y[off + j]};
+    if (kind == SFD_JOB_ZP || kind == SFD_JOB_ZPP) v = {A.x[off + j] - 2 * SFD_PI * (double)j / n, A.y[off + j]};
     else if (kind == SFD_JOB_PHIP)
       v = {A.phi[off + j] - (-(1 + rho) * SFD_PI * S.U / n * (double)j), A.phi_im ? A.phi_im[off + j] : 0.0};
     else if (kind == SFD_JOB_RAW) v = {A.x[off + j], A.y[off + j]};
@@ -273,40 +273,37 @@ __global__ void __cluster_dims__(SFD_FFT_CLUSTER, 1, 1) __launch_bounds__(kCT)
 #pragma unroll
     for (int q = 0; q < C; ++q) u[q] = cluster.map_shared_rank(buf, q)[k1];
     dft8(u, -1);
-    for (int v = 0; v < nv; ++v) {
-      const bool second = (kind == SFD_JOB_ZP && v == 1);
-      cd y[C];
+    cd y[C];
 #pragma unroll
-      for (int k2 = 0; k2 < C; ++k2) {
-        int k = k1 + M * k2;
-        y[k2] = second ? second_mult(u[k2], k, n) : first_mult(u[k2], k, n);
-      }
-      dft8(y, +1);
+    for (int k2 = 0; k2 < C; ++k2) {
+      int k = k1 + M * k2;
+      y[k2] = second ? second_mult(u[k2], k, n) : first_mult(u[k2], k, n);
+    }
+    dft8(y, +1);
 #pragma unroll
-      for (int q = 0; q < C; ++q) {
-        cd w = (q && k1) ? y[q] * cconj(twq[q * R + t]) : y[q];
-        vbuf[v * M + q * R + t] = w;
-      }
+    for (int q = 0; q < C; ++q) {
+      cd w = (q && k1) ? y[q] * cconj(twq[q * R + t]) : y[q];
+      vbuf[q * R + t] = w;
     }
   }
   cluster.sync();
   // 4. gather V_c[k1] for all k1, inverse M-point FFT, write x[C m + c]
   const double s1 = 2.0 * SFD_PI / n;
   const double s2 = 4.0 * SFD_PI * SFD_PI / (n * n);
-  for (int v = 0; v < nv; ++v) {
+  {
     for (int k1 = threadIdx.x; k1 < M; k1 += kCT) {
       int owner = k1 / R, t = k1 - owner * R;
-      buf[k1] = cluster.map_shared_rank(vbuf, owner)[v * M + c * R + t];
+      buf[k1] = cluster.map_shared_rank(vbuf, owner)[c * R + t];
     }
     __syncthreads();
     cta_fft_n<kCT, kCMPT>(buf, M, S.rad_m, S.nrad_m, twm, 1, +1);
-    const bool second = (kind == SFD_JOB_ZP && v == 1);
     for (int m = threadIdx.x; m < M; m += kCT) {
       const int j = off + C * m + c;
       cd x = buf[m];
-      if (kind == SFD_JOB_ZP) {
-        if (second) A.zpp[j] = {x.re * s2, x.im * s2};   // Derivatives.cuh:321
-        else A.zp[j] = {x.re * s1 + s1, x.im * s1};      // :323,374
+      if (kind == SFD_JOB_ZPP) {
+        A.zpp[j] = {x.re * s2, x.im * s2};               // Derivatives.cuh:321
+      } else if (kind == SFD_JOB_ZP) {
+        A.zp[j] = {x.re * s1 + s1, x.im * s1};           // :323,374
       } else if (kind == SFD_JOB_PHIP) {
         double r = x.re * s1;                           // :324, complex_to_real
         if (S.U != 0) r += -(1 + rho) * SFD_PI * S.U / n;
@@ -325,14 +322,14 @@ __global__ void __cluster_dims__(SFD_FFT_CLUSTER, 1, 1) __launch_bounds__(kCT)
 cudaError_t sfd_launch_spectral_cluster(const DerivArgs& A, const int2* jobs, int njobs, int max_n, cudaStream_t st) {
   if (njobs == 0) return cudaSuccess;
   const int M = max_n / SFD_FFT_CLUSTER;
-  size_t smem = (size_t)6 * M * sizeof(cd);
+  size_t smem = (size_t)5 * M * sizeof(cd);
   k_spectral_cluster<<<dim3(SFD_FFT_CLUSTER, njobs), kCT, smem, st>>>(A, jobs);
   return cudaGetLastError();
 }
 
 cudaError_t sfd_fft_configure() {
   cudaError_t e = cudaFuncSetAttribute(k_spectral_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       6 * (8192 / SFD_FFT_CLUSTER) * (int)sizeof(cd));
+                                       5 * (8192 / SFD_FFT_CLUSTER) * (int)sizeof(cd));
   if (e != cudaSuccess) return e;
   return cudaFuncSetAttribute(k_spectral_deriv, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               8192 * (int)sizeof(cd));

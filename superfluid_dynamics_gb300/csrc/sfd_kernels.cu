@@ -23,6 +23,7 @@
 #include "sfd_engine.cuh"
 #include "sfd_kernels.cuh"
 
+#include <cooperative_groups.h>
 #include <type_traits>
 
 // ----------------------------------------------------------------- node prep
@@ -66,12 +67,14 @@ __global__ void k_node_prep(const SurfaceDesc* surf, const int* node_surf, int n
 }
 
 // ----------------------------------------------------------------- sums
-// Work item = (surface, first target, first source, chunk index).  Each CTA
-// stages one chunk of sources in shared memory and accumulates S (and T) for
-// kSumTargets targets (two per thread), writing partials per chunk.  The last
-// CTA to finish a target tile (arrival counter per tile) reduces that tile's
-// chunks in a fixed order (bitwise reproducible) and applies the epilogue, so
-// one launch does the whole pass.
+// One cluster of kSumCL CTAs per (surface, tile of kSumTile targets).  CTA r of
+// the cluster stages sources [r per, (r+1) per) (per = ceil(n / kSumCL)) in
+// shared memory; its kSumGroups groups of kSumTile threads (one target each)
+// take every kSumGroups-th of those sources.  Group partials are summed in
+// shared memory, the cluster's CTA partials over distributed shared memory, in
+// a fixed order (bitwise reproducible), and CTA r finishes targets
+// [r kSumPerRank, (r+1) kSumPerRank) of the tile with the epilogue (C, D, M a,
+// residual).  One launch per pass; no partials leave the chip.
 
 namespace {
 
@@ -184,238 +187,210 @@ __device__ __forceinline__ void pair_acc(const Tgt<SFD_PREC_F32>& t, const SrcDF
     A.ti = fmaf(-inv, di, A.ti);
   }
 }
-__device__ __forceinline__ cd acc_s(const Acc<SFD_PREC_F64>& A) { return {A.sr, A.si}; }
-__device__ __forceinline__ cd acc_t(const Acc<SFD_PREC_F64>& A) { return {A.tr, A.ti}; }
-__device__ __forceinline__ float4 acc_s(const Acc<SFD_PREC_DF>& A) { return make_float4(A.sr.hi, A.sr.lo, A.si.hi, A.si.lo); }
-__device__ __forceinline__ float4 acc_t(const Acc<SFD_PREC_DF>& A) { return make_float4(A.tr.hi, A.tr.lo, A.ti.hi, A.ti.lo); }
-__device__ __forceinline__ float4 acc_s(const Acc<SFD_PREC_F32>& A) { return make_float4(A.sr, 0.f, A.si, 0.f); }
-__device__ __forceinline__ float4 acc_t(const Acc<SFD_PREC_F32>& A) { return make_float4(A.tr, 0.f, A.ti, 0.f); }
-
-__device__ __forceinline__ df df_warp_sum(df v) {
-  for (int o = 16; o > 0; o >>= 1) {
-    df u = {__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
-    v = df_add(v, u);
-  }
-  return v;
-}
-
 template <int PREC>
 using SrcT = typename std::conditional<PREC == SFD_PREC_F64, Src64, SrcDF>::type;
 
-// Epilogue of one target tile (run by the last CTA to finish it): reduce the
-// chunk partials in fixed order (bitwise reproducible) and form, per node,
+// Fixed-order reduction values of one target: FP64 for the FP64 pass,
+// double-float for the DF and FP32 passes.
+template <int PREC>
+struct Red {
+  df sr{0.f, 0.f}, si{0.f, 0.f}, tr{0.f, 0.f}, ti{0.f, 0.f};
+};
+template <>
+struct Red<SFD_PREC_F64> {
+  double sr = 0, si = 0, tr = 0, ti = 0;
+};
+template <int PREC>
+using WSum = typename std::conditional<PREC == SFD_PREC_F64, double, df>::type;
+
+__device__ __forceinline__ Red<SFD_PREC_F64> to_red(const Acc<SFD_PREC_F64>& A) { return {A.sr, A.si, A.tr, A.ti}; }
+__device__ __forceinline__ Red<SFD_PREC_DF> to_red(const Acc<SFD_PREC_DF>& A) { return {A.sr, A.si, A.tr, A.ti}; }
+__device__ __forceinline__ Red<SFD_PREC_F32> to_red(const Acc<SFD_PREC_F32>& A) {
+  return {df{A.sr, 0.f}, df{A.si, 0.f}, df{A.tr, 0.f}, df{A.ti, 0.f}};
+}
+__device__ __forceinline__ void red_add(Red<SFD_PREC_F64>& a, const Red<SFD_PREC_F64>& b) {
+  a.sr += b.sr; a.si += b.si; a.tr += b.tr; a.ti += b.ti;
+}
+template <int PREC>
+__device__ __forceinline__ void red_add(Red<PREC>& a, const Red<PREC>& b) {
+  a.sr = df_add(a.sr, b.sr); a.si = df_add(a.si, b.si); a.tr = df_add(a.tr, b.tr); a.ti = df_add(a.ti, b.ti);
+}
+__device__ __forceinline__ double wsum_add(double a, double b) { return a + b; }
+__device__ __forceinline__ df wsum_add(df a, df b) { return df_add(a, b); }
+__device__ __forceinline__ double shfl_x(double v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+__device__ __forceinline__ df shfl_x(df v, int o) {
+  return {__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+}
+__device__ __forceinline__ Red<SFD_PREC_F64> shfl_x(const Red<SFD_PREC_F64>& v, int o) {
+  return {shfl_x(v.sr, o), shfl_x(v.si, o), shfl_x(v.tr, o), shfl_x(v.ti, o)};
+}
+template <int PREC>
+__device__ __forceinline__ Red<PREC> shfl_x(const Red<PREC>& v, int o) {
+  return {shfl_x(v.sr, o), shfl_x(v.si, o), shfl_x(v.tr, o), shfl_x(v.ti, o)};
+}
+__device__ __forceinline__ double to_d(double v) { return v; }
+__device__ __forceinline__ double to_d(df v) { return df_to_double(v); }
+
+// Epilogue of one target g (surface S) from its sums S_k, T_k and the weight
+// sum A:
 //   C_k = i (2 w_k S_k - (A - a_k)),   D_k = -i (2 T_k - A)
 //   (M a)_k = Mdiag_k a_k + c1 Im(z'_k C_k) - [image] (1/4pi) Im D_k
 // mode 0: C/D overwritten, r = phi' - M a; mode 1: C/D accumulated, r -= M a.
-template <int PREC>
-__device__ void sums_epilogue(const SumArgs& A, const SurfaceDesc& S, int sidx, int tile, int t0, bool image) {
-  const int n = S.n, off = S.off;
-  const int nchunk = (n + kSumChunk - 1) / kSumChunk;
-  __shared__ double asum_sh;
-  if (threadIdx.x == 0) {
-    const long long ia = (long long)tile * A.max_chunks;
-    if constexpr (PREC == SFD_PREC_F64) {
-      double s = 0.0;
-      for (int c = 0; c < nchunk; ++c) s += __ldcg(A.part_a + ia + c);
-      asum_sh = s;
-    } else {
-      df s = {0.f, 0.f};
-      const float2* pa = reinterpret_cast<const float2*>(A.part_a) + ia;
-      for (int c = 0; c < nchunk; ++c) {
-        float2 v = __ldcg(pa + c);
-        s = df_add(s, df{v.x, v.y});
-      }
-      asum_sh = df_to_double(s);
-    }
-  }
-  __syncthreads();
-  const double asum = asum_sh;
+// Returns |r_k| (1e300 for NaN).
+__device__ __forceinline__ double sums_finish(const SumArgs& A, const SurfaceDesc& S, int g, cd sum_s, cd sum_t,
+                                              double asum, bool image) {
   const double c1 = S.physics == 0 ? 0.25 * (1 - S.rho) / SFD_PI : 0.25 / SFD_PI;
-  double rmax = 0.0;
-  for (int q = 0; q < kSumTargets / kSumThreads; ++q) {
-    const int tk = t0 + q * kSumThreads + threadIdx.x;
-    if (tk >= n) continue;
-    const int g = off + tk;
-    cd sum_s, sum_t = {0, 0};
-    if constexpr (PREC == SFD_PREC_F64) {
-      double sr = 0, si = 0, tr = 0, ti = 0;
-      for (int c = 0; c < nchunk; ++c) {
-        const long long o = (long long)c * A.ntot + g;
-        double2 v = __ldcg(reinterpret_cast<const double2*>(A.part_s) + o);
-        sr += v.x;
-        si += v.y;
-        if (image) {
-          double2 u = __ldcg(reinterpret_cast<const double2*>(A.part_t) + o);
-          tr += u.x;
-          ti += u.y;
-        }
-      }
-      sum_s = {sr, si};
-      sum_t = {tr, ti};
-    } else {
-      df sr = {0.f, 0.f}, si = {0.f, 0.f}, tr = {0.f, 0.f}, ti = {0.f, 0.f};
-      for (int c = 0; c < nchunk; ++c) {
-        const long long o = (long long)c * A.ntot + g;
-        float4 v = __ldcg(reinterpret_cast<const float4*>(A.part_s) + o);
-        sr = df_add(sr, df{v.x, v.y});
-        si = df_add(si, df{v.z, v.w});
-        if (image) {
-          float4 u = __ldcg(reinterpret_cast<const float4*>(A.part_t) + o);
-          tr = df_add(tr, df{u.x, u.y});
-          ti = df_add(ti, df{u.z, u.w});
-        }
-      }
-      sum_s = {df_to_double(sr), df_to_double(si)};
-      sum_t = {df_to_double(tr), df_to_double(ti)};
-    }
-    const double ak = A.a[g];
-    const cd wk = A.w[g];
-    const cd C = cmul_i(2.0 * (wk * sum_s) - cd{asum - ak, 0.0});
-    const cd D = image ? cmul_i(cd{-(2.0 * sum_t.re - asum), -(2.0 * sum_t.im)}) : cd{0, 0};
-    double ma = A.mdiag[g] * ak + c1 * (A.zp[g] * C).im;
-    if (image) ma -= 0.25 / SFD_PI * D.im;
-    double rnew;
-    if (A.mode == 0) {
-      A.cacc[g] = C;
-      if (image) A.dacc[g] = D;
-      rnew = A.phip[g] - ma;
-    } else {
-      A.cacc[g] = A.cacc[g] + C;
-      if (image) A.dacc[g] = A.dacc[g] + D;
-      rnew = A.r[g] - ma;
-    }
-    A.r[g] = rnew;
-    double rv = fabs(rnew);
-    if (!(rv == rv)) rv = 1e300;
-    rmax = fmax(rmax, rv);
+  const double ak = A.a[g];
+  const cd wk = A.w[g];
+  const cd C = cmul_i(2.0 * (wk * sum_s) - cd{asum - ak, 0.0});
+  const cd D = image ? cmul_i(cd{-(2.0 * sum_t.re - asum), -(2.0 * sum_t.im)}) : cd{0, 0};
+  double ma = A.mdiag[g] * ak + c1 * (A.zp[g] * C).im;
+  if (image) ma -= 0.25 / SFD_PI * D.im;
+  double rnew;
+  if (A.mode == 0) {
+    A.cacc[g] = C;
+    if (image) A.dacc[g] = D;
+    rnew = A.phip[g] - ma;
+  } else {
+    A.cacc[g] = A.cacc[g] + C;
+    if (image) A.dacc[g] = A.dacc[g] + D;
+    rnew = A.r[g] - ma;
   }
-  if (A.rnorm) {
-    // |r| max per surface: non-negative doubles order like their bit patterns
-    unsigned long long m = (unsigned long long)__double_as_longlong(rmax);
-    for (int o = 16; o > 0; o >>= 1) {
-      unsigned long long v = __shfl_xor_sync(0xffffffffu, m, o);
-      m = v > m ? v : m;
-    }
-    if ((threadIdx.x & 31) == 0) atomicMax(reinterpret_cast<unsigned long long*>(A.rnorm) + sidx, m);
-  }
+  A.r[g] = rnew;
+  double rv = fabs(rnew);
+  return (rv == rv) ? rv : 1e300;
 }
 
 template <int PREC>
-__global__ void __launch_bounds__(kSumThreads) k_boundary_sums(SumArgs A) {
-  const int4 item = A.items[blockIdx.x];
-  const SurfaceDesc& S = A.surf[item.x];
+__global__ void __cluster_dims__(kSumCL, 1, 1) __launch_bounds__(kSumThreads, 4) k_boundary_sums(SumArgs A) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  const int2 item = A.items[blockIdx.x / kSumCL];
+  const int sidx = item.x, t0 = item.y;
+  const SurfaceDesc& S = A.surf[sidx];
   const int n = S.n, off = S.off;
-  const int t0 = item.y, j0 = item.z, chunk = item.w;
-  const int jn = min(kSumChunk, n - j0);
   const bool image = (S.physics == 1 && !S.infinite_depth);
-  __shared__ SrcT<PREC> src[kSumChunk];
-  __shared__ double asum_warp[kSumThreads / 32];
-  __shared__ float2 asum_warp_df[kSumThreads / 32];
-  // stage the chunk's sources (and their weight sum, kept by the first target tile)
-  double apart = 0.0;
-  df apart_df = {0.f, 0.f};
-  for (int jj = threadIdx.x; jj < jn; jj += kSumThreads) {
-    int g = off + j0 + jj;
+  const int per = (n + kSumCL - 1) / kSumCL;
+  const int j_lo = min(n, rank * per), j_hi = min(n, j_lo + per);
+  const int jn = j_hi - j_lo;
+  extern __shared__ __align__(16) unsigned char sums_dyn[];
+  SrcT<PREC>* src = reinterpret_cast<SrcT<PREC>*>(sums_dyn);
+  __shared__ Red<PREC> gred[kSumGroups][kSumTile];
+  __shared__ WSum<PREC> wwarp[kSumThreads / 32];
+  __shared__ WSum<PREC> wcta;
+  const int tid = threadIdx.x, lane = tid & 31;
+
+  // ---- stage this CTA's sources and their weight sum
+  WSum<PREC> wpart{};
+  for (int jj = tid; jj < jn; jj += kSumThreads) {
+    const int g = off + j_lo + jj;
     if constexpr (PREC == SFD_PREC_F64) {
       cd w = A.w[g];
       double aj = A.a[g];
-      apart += aj;
+      wpart += aj;
       cd p = image ? A.p[g] : cd{0.0, 0.0};
       src[jj] = Src64{w.re, w.im, p.re, p.im, aj};
     } else {
       float4 w = A.wdf[g];
       float2 ad = A.adf[g];
       float4 p = image ? A.pdf[g] : make_float4(0.f, 0.f, 0.f, 0.f);
-      apart_df = df_add(apart_df, df{ad.x, ad.y});
+      wpart = df_add(wpart, df{ad.x, ad.y});
       src[jj] = SrcDF{w.x, w.y, w.z, w.w, p.x, p.y, p.z, p.w, ad.x, PREC == SFD_PREC_DF ? ad.y : 0.f};
     }
   }
-  {
-    if constexpr (PREC == SFD_PREC_F64) {
-      for (int o = 16; o > 0; o >>= 1) apart += __shfl_xor_sync(0xffffffffu, apart, o);
-      if ((threadIdx.x & 31) == 0) asum_warp[threadIdx.x >> 5] = apart;
-    } else {
-      apart_df = df_warp_sum(apart_df);
-      if ((threadIdx.x & 31) == 0) asum_warp_df[threadIdx.x >> 5] = make_float2(apart_df.hi, apart_df.lo);
-    }
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {  // this chunk's weight sum, kept per (target tile, chunk)
-    const long long ia = (long long)(S.tile_base + t0 / kSumTargets) * A.max_chunks + chunk;
-    if constexpr (PREC == SFD_PREC_F64) {
-      double s = 0.0;
-      for (int i = 0; i < kSumThreads / 32; ++i) s += asum_warp[i];
-      A.part_a[ia] = s;
-    } else {
-      df s = {0.f, 0.f};
-      for (int i = 0; i < kSumThreads / 32; ++i) s = df_add(s, df{asum_warp_df[i].x, asum_warp_df[i].y});
-      reinterpret_cast<float2*>(A.part_a)[ia] = make_float2(s.hi, s.lo);
-    }
-  }
-  // two targets per thread: tk0 and tk0 + kSumThreads
-  const int tk0 = t0 + threadIdx.x, tk1 = tk0 + kSumThreads;
-  const bool a0 = tk0 < n, a1 = tk1 < n;
-  const int g0 = off + (a0 ? tk0 : 0), g1 = off + (a1 ? tk1 : 0);
-  Tgt<PREC> T0, T1;
+  for (int o = 16; o > 0; o >>= 1) wpart = wsum_add(wpart, shfl_x(wpart, o));
+  if (lane == 0) wwarp[tid >> 5] = wpart;
+
+  // ---- one target per thread of each group
+  const int grp = tid / kSumTile, l = tid % kSumTile;
+  const int tk = t0 + l;
+  const bool active = tk < n;
+  const int gt = off + (active ? tk : 0);
+  Tgt<PREC> T;
   if constexpr (PREC == SFD_PREC_F64) {
-    T0.load(A.w[g0], image ? A.p[g0] : cd{0, 0});
-    T1.load(A.w[g1], image ? A.p[g1] : cd{0, 0});
+    T.load(A.w[gt], image ? A.p[gt] : cd{0, 0});
   } else {
-    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
-    T0.load(A.wdf[g0], image ? A.pdf[g0] : z4);
-    T1.load(A.wdf[g1], image ? A.pdf[g1] : z4);
-  }
-  const int self0 = a0 ? tk0 - j0 : -1, self1 = a1 ? tk1 - j0 : -1;
-  Acc<PREC> R0, R1;
-#pragma unroll 2
-  for (int jj = 0; jj < jn; ++jj) {
-    const SrcT<PREC> s = src[jj];
-    pair_acc(T0, s, jj == self0, image, R0);
-    pair_acc(T1, s, jj == self1, image, R1);
-  }
-  long long o = (long long)chunk * A.ntot + off;
-  const int tile = S.tile_base + t0 / kSumTargets;
-  if constexpr (PREC == SFD_PREC_F64) {
-    if (a0) {
-      A.part_s[o + tk0] = acc_s(R0);
-      if (image) A.part_t[o + tk0] = acc_t(R0);
-    }
-    if (a1) {
-      A.part_s[o + tk1] = acc_s(R1);
-      if (image) A.part_t[o + tk1] = acc_t(R1);
-    }
-  } else {
-    float4* ps = reinterpret_cast<float4*>(A.part_s);
-    float4* pt = reinterpret_cast<float4*>(A.part_t);
-    if (a0) {
-      ps[o + tk0] = acc_s(R0);
-      if (image) pt[o + tk0] = acc_t(R0);
-    }
-    if (a1) {
-      ps[o + tk1] = acc_s(R1);
-      if (image) pt[o + tk1] = acc_t(R1);
-    }
-  }
-  // ---- arrival count: the last CTA of this target tile finishes it
-  __shared__ int last;
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    const int nchunk = (n + kSumChunk - 1) / kSumChunk;
-    last = (atomicAdd(A.tile_count + tile, 1) == nchunk - 1);
-    if (last) A.tile_count[tile] = 0;  // ready for the next pass
+    T.load(A.wdf[gt], image ? A.pdf[gt] : make_float4(0.f, 0.f, 0.f, 0.f));
   }
   __syncthreads();
-  if (!last) return;
-  __threadfence();
-  sums_epilogue<PREC>(A, S, item.x, tile, t0, image);
+  if (tid == 0) {
+    WSum<PREC> t = wwarp[0];
+    for (int i = 1; i < kSumThreads / 32; ++i) t = wsum_add(t, wwarp[i]);
+    wcta = t;
+  }
+  Acc<PREC> R;
+  const bool overlap = (t0 < j_hi) && (t0 + kSumTile > j_lo);
+  if (overlap) {  // this CTA holds some targets' own node: skip j == k
+    const int self = active ? tk - j_lo : -1;
+    for (int jj = grp; jj < jn; jj += kSumGroups) pair_acc(T, src[jj], jj == self, image, R);
+  } else {
+#pragma unroll 4
+    for (int jj = grp; jj < jn; jj += kSumGroups) pair_acc(T, src[jj], false, image, R);
+  }
+  gred[grp][l] = to_red(R);
+  __syncthreads();
+  if (grp == 0) {
+    Red<PREC> v = gred[0][l];
+#pragma unroll
+    for (int q = 1; q < kSumGroups; ++q) red_add(v, gred[q][l]);
+    gred[0][l] = v;
+  }
+  cluster.sync();
+
+  // ---- CTA `rank` finishes targets [rank kSumPerRank, (rank+1) kSumPerRank)
+  if (tid < kSumPerRank * kSumCL) {  // warps 0-1 entirely
+    const int lt = rank * kSumPerRank + tid / kSumCL;
+    const int q = tid % kSumCL;
+    Red<PREC> v = cluster.map_shared_rank(&gred[0][0], q)[lt];
+    WSum<PREC> aw = *cluster.map_shared_rank(&wcta, q);
+#pragma unroll
+    for (int o = 1; o < kSumCL; o <<= 1) {
+      red_add(v, shfl_x(v, o));
+      aw = wsum_add(aw, shfl_x(aw, o));
+    }
+    double rv = 0.0;
+    const int tkk = t0 + lt;
+    if (q == 0 && tkk < n) {
+      const cd sum_s = {to_d(v.sr), to_d(v.si)};
+      const cd sum_t = {to_d(v.tr), to_d(v.ti)};
+      rv = sums_finish(A, S, off + tkk, sum_s, sum_t, to_d(aw), image);
+    }
+    if (A.rnorm) {
+      // |r| max per surface: non-negative doubles order like their bit patterns
+      unsigned long long m = (unsigned long long)__double_as_longlong(rv);
+      for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long u = __shfl_xor_sync(0xffffffffu, m, o);
+        m = u > m ? u : m;
+      }
+      if (lane == 0) atomicMax(reinterpret_cast<unsigned long long*>(A.rnorm) + sidx, m);
+    }
+  }
+  cluster.sync();  // peers may still be reading this CTA's shared memory
 }
 
-cudaError_t sfd_launch_sums(int prec, const SumArgs& A, int nitems, cudaStream_t st) {
+size_t sfd_sums_smem(int prec, int max_n) {
+  const size_t per = (size_t)(max_n + kSumCL - 1) / kSumCL;
+  return per * (prec == SFD_PREC_F64 ? sizeof(Src64) : sizeof(SrcDF));
+}
+
+cudaError_t sfd_sums_configure() {
+  const int bytes = (int)sfd_sums_smem(SFD_PREC_F64, 8192);
+  cudaError_t e = cudaFuncSetAttribute(k_boundary_sums<SFD_PREC_F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_boundary_sums<SFD_PREC_DF>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_boundary_sums<SFD_PREC_F32>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  return e;
+}
+
+cudaError_t sfd_launch_sums(int prec, const SumArgs& A, int nitems, int max_n, cudaStream_t st) {
   if (nitems == 0) return cudaSuccess;
-  if (prec == SFD_PREC_F64) k_boundary_sums<SFD_PREC_F64><<<nitems, kSumThreads, 0, st>>>(A);
-  else if (prec == SFD_PREC_DF) k_boundary_sums<SFD_PREC_DF><<<nitems, kSumThreads, 0, st>>>(A);
-  else k_boundary_sums<SFD_PREC_F32><<<nitems, kSumThreads, 0, st>>>(A);
+  const dim3 grid(nitems * kSumCL);
+  const size_t smem = sfd_sums_smem(prec, max_n);
+  if (prec == SFD_PREC_F64) k_boundary_sums<SFD_PREC_F64><<<grid, kSumThreads, smem, st>>>(A);
+  else if (prec == SFD_PREC_DF) k_boundary_sums<SFD_PREC_DF><<<grid, kSumThreads, smem, st>>>(A);
+  else k_boundary_sums<SFD_PREC_F32><<<grid, kSumThreads, smem, st>>>(A);
   return cudaGetLastError();
 }
 

@@ -4,9 +4,11 @@
 
 enum : int { SFD_PREC_F64 = 0, SFD_PREC_DF = 1, SFD_PREC_F32 = 2 };
 
-constexpr int kSumThreads = 128;  // threads per CTA of the boundary sums
-constexpr int kSumTargets = 256;  // targets per CTA (two per thread, for ILP)
-constexpr int kSumChunk = 128;    // sources per CTA (shared-memory chunk)
+constexpr int kSumCL = 8;                          // CTAs per cluster (one target tile)
+constexpr int kSumGroups = 4;                      // source groups per CTA
+constexpr int kSumTile = 64;                       // targets per tile (one per thread of a group)
+constexpr int kSumThreads = kSumGroups * kSumTile; // 256
+constexpr int kSumPerRank = kSumTile / kSumCL;     // targets finished by each CTA of the cluster
 
 struct NodeData {
   cd* w;        // exp(i z)
@@ -19,26 +21,19 @@ struct NodeData {
   cd* v2;       // V2_k
 };
 
-// One boundary-sum pass: partial sums per (target tile, source chunk), then
-// the last CTA of each target tile reduces them in fixed chunk order and
-// applies the epilogue (C, D, M a, residual) to its targets.
+// One boundary-sum pass (one cluster per (surface, target tile)) with its
+// epilogue (C, D, M a, residual) fused.
 struct SumArgs {
   const SurfaceDesc* surf;
-  const int4* items;    // (surface, first target, first source, chunk)
+  const int2* items;    // (surface, first target) per cluster
   int nsurf;
   int ntot;
-  int max_chunks;
   const cd* w;
   const cd* p;
   const double* a;      // weights (FP64; every pass)
   const float4* wdf;    // double-float copies (DF / FP32 passes)
   const float4* pdf;
   const float2* adf;
-  cd* part_s;           // [chunk][node]; FP64 pass: complex doubles; DF / FP32: float4 (re.hi, re.lo, im.hi, im.lo)
-  cd* part_t;
-  double* part_a;       // [tile][chunk]; FP64 pass: doubles; DF / FP32: float2 (hi, lo)
-  int* tile_count;      // arrivals per target tile (returns to 0 after each pass)
-  // epilogue
   const double* mdiag;
   const cd* zp;
   const double* phip;
@@ -73,7 +68,8 @@ struct VelArgs {
 
 __global__ void k_node_prep(const SurfaceDesc* surf, const int* node_surf, int ntot, const double* x,
                             const double* y, const cd* zp, const cd* zpp, NodeData nd);
-cudaError_t sfd_launch_sums(int prec, const SumArgs& A, int nitems, cudaStream_t st);
+cudaError_t sfd_launch_sums(int prec, const SumArgs& A, int nitems, int max_n, cudaStream_t st);
+cudaError_t sfd_sums_configure();
 __global__ void k_velocity_bernoulli(VelArgs V);
 __global__ void k_velocity_node1(VelArgs V);
 __global__ void k_rk4_stage(int n3, const double* y0, const double* k, double* kacc, double* ystage, double wk,
