@@ -93,6 +93,11 @@ int sfd_create(const int* n, int nsurf, const sfd_problem* problems, int shared_
 int sfd_destroy(sfd_engine* e);
 /* Use a caller stream (0 = the engine's own). */
 int sfd_set_stream(sfd_engine* e, void* cuda_stream);
+/* Replace the physical parameters of one surface (A3, g, depth, ...) on an
+ * existing engine; physics, the depth mode and whether rho is zero must stay.
+ * (The reference fixes these in the BoundaryProblem constructor,
+ * BoundaryProblem.cuh:47-62; this setter serves parameter fits.) */
+int sfd_set_problem(sfd_engine* e, int surface, const sfd_problem* problem);
 int sfd_total_nodes(const sfd_engine* e);
 
 /* State = concatenated per-surface nodes, SoA: x[ntot], y[ntot], phi[ntot]. */
@@ -151,7 +156,7 @@ const char* sfd_version(void);
  * must not allocate after start-up, hosts that forbid runtime allocation.
  * state_in = [x | y | phi] and rhs_out = [dx | dy | dphi] are device arrays of
  * 3n doubles (same results as sfd_rhs_device on an FP64 engine).  Scratch is
- * one static device array of about 8.9 MB, held by every GPU that loads the
+ * one static device array of about 8.7 MB, held by every GPU that loads the
  * library until exit; n is limited to 1..1024 (larger n returns
  * SFD_ERR_INVALID).  The call is asynchronous on `stream` (NULL = legacy
  * default stream).  Its first call on a device resolves the array's device
@@ -159,6 +164,29 @@ const char* sfd_version(void);
  * the array, so calls that overlap on the GPU (different streams or threads)
  * race; serialise them. */
 int sfd_rhs_device_noalloc(const sfd_problem* problem, int n, const void* state_in, void* rhs_out, void* stream);
+
+/* ------------------------------------------------------------ reverse mode (adjoint)
+ * Hand-written adjoint of the FP64 RHS and of RK4 trajectories.  The reference
+ * has no reverse mode (it differentiates by finite differences in
+ * Python/integration/jacobian_tests.py:10-150); these entry points are new.
+ * Requirements: an engine created with SFD_PRECISION_FP64 holding one surface,
+ * water with rho = 0 or helium with the standard Bernoulli closure, U = 0.
+ * The parameter derivative is d/dA3 for helium and d/dg for water. */
+/* grad_state = J(state)^T cotangent for the RHS state -> [dx|dy|dphi]; device
+ * arrays of 3n doubles; synchronous. */
+int sfd_rhs_vjp_device(sfd_engine* e, const void* state, const void* cotangent, void* grad_state,
+                       double* grad_param);
+/* Integrate `steps` RK4 steps of size dt from state0 (host, 3n) keeping a
+ * checkpoint every `checkpoint_every` steps on the device; the final state is
+ * written to state_final (host, 3n; nullable).  Same arithmetic as
+ * sfd_rk4_steps on an FP64 engine. */
+int sfd_rk4_record(sfd_engine* e, double dt, int steps, int checkpoint_every, const double* state0,
+                   double* state_final);
+/* Reverse the recorded trajectory: grad_state0 = (d state_final / d state0)^T
+ * cot_final and *grad_param = the parameter derivative of <cot_final,
+ * state_final>.  Each checkpoint segment is recomputed once with every stage
+ * recorded (LU factors included), then reversed stage by stage. */
+int sfd_rk4_vjp(sfd_engine* e, const double* cot_final, double* grad_state0, double* grad_param);
 
 /* Precision used by the reference-compatible exports below (default FP64). */
 int sfd_set_default_precision(int precision);

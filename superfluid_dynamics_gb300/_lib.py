@@ -76,6 +76,10 @@ _SIGS = {
     "sfd_version": (c_char_p, []),
     "sfd_set_default_precision": (c_int, [c_int]),
     "sfd_rhs_device_noalloc": (c_int, [POINTER(SfdProblem), c_int, c_void_p, c_void_p, c_void_p]),
+    "sfd_set_problem": (c_int, [c_void_p, c_int, POINTER(SfdProblem)]),
+    "sfd_rhs_vjp_device": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, _dp]),
+    "sfd_rk4_record": (c_int, [c_void_p, c_double, c_int, c_int, _dp, _dp]),
+    "sfd_rk4_vjp": (c_int, [c_void_p, _dp, _dp, _dp]),
     "calculateRHSFromVectors": (c_int, [_dp] * 6 + [c_double] * 4 + [c_size_t]),
     "calculateRHS256FromVectors": (c_int, [_dp] * 6 + [c_double] * 4),
     "calculateRHS2048FromVectors": (c_int, [_dp] * 6 + [c_double] * 4),

@@ -25,26 +25,8 @@
 #include "sfd_engine.cuh"
 #include "sfd_kernels.cuh"
 #include "sfd_solve.cuh"
+#include "sfd_internal.cuh"
 
-enum {
-  SFD_K_OTHER = 0,
-  SFD_K_SPECTRAL,
-  SFD_K_NODE,
-  SFD_K_SUMS64,
-  SFD_K_SUMSDF,
-  SFD_K_SUMS32,
-  SFD_K_EPILOGUE,  // no launches: the sum epilogue runs inside the boundary-sum kernels
-  SFD_K_ASSEMBLE,
-  SFD_K_DIAG,
-  SFD_K_PANEL,
-  SFD_K_UPDATE,
-  SFD_K_TRSV,
-  SFD_K_GEMV,
-  SFD_K_VELOCITY,
-  SFD_K_RK4,
-  SFD_K_UPDATE_TC,
-  SFD_NCLASS
-};
 
 namespace {
 
@@ -115,62 +97,6 @@ bool factorize(int n, std::vector<int>& rad) {
 
 }  // namespace
 
-struct sfd_engine {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  cudaStream_t own_stream = nullptr;
-  sfd_options opt{};
-  int nsurf = 0, ntot = 0, max_n = 0, max_np = 0;
-  long long mat_elems = 0, panel_elems = 0;
-  bool any_rho = false;
-  std::vector<SurfaceDesc> hs;
-  SurfaceDesc* d_surf = nullptr;
-  int* d_node_surf = nullptr;
-  std::map<int, cd*> d_tw;
-  // work lists
-  int2* d_jobs_first = nullptr; int njobs_first = 0;
-  int2* d_jobs_ap = nullptr; int njobs_ap = 0;
-  int2* d_cjobs_first = nullptr; int ncjobs_first = 0;  // cluster-distributed transforms
-  int2* d_cjobs_ap = nullptr; int ncjobs_ap = 0;
-  int max_n_single = 0, max_n_cluster = 0;
-  int2* d_sum_items = nullptr; int nsum = 0;
-  int4* d_asm_tiles = nullptr; int nasm = 0;
-  int2* d_gemv_rows = nullptr; int ngemv = 0;
-  long long* d_poff = nullptr;
-  int max_blocks64 = 0, max_blocks128 = 0;
-  // state (each 3 * ntot): [x | y | phi]
-  double *y0 = nullptr, *ys = nullptr, *kacc = nullptr, *kcur = nullptr;
-  // stage data
-  cd *zp = nullptr, *zpp = nullptr, *ap = nullptr;
-  double *phip = nullptr, *a = nullptr, *r = nullptr, *delta = nullptr, *phi_im = nullptr;
-  float2 *adf = nullptr, *ddf = nullptr;  // double-float copies of a and delta
-  NodeData nd{};
-  cd *cacc = nullptr, *dacc = nullptr, *vel_low1 = nullptr;
-  unsigned int* status = nullptr;
-  double *lmax = nullptr, *rnorm = nullptr, *inv_out = nullptr;
-  // matrices
-  double* m64 = nullptr;
-  float* m32 = nullptr;
-  float *pbuf = nullptr, *rbuf = nullptr, *cbuf = nullptr;
-  __nv_bfloat16 *cparts = nullptr, *rparts = nullptr;  // tensor-core operands: 3 bf16 parts, panel_elems apart
-  // graphs
-  cudaGraphExec_t g_step[2] = {nullptr, nullptr};
-  double g_dt = 0.0;
-  int g_kernels[2] = {0, 0};
-  long long step_count = 0;
-  long long launches = 0;
-  bool have_precond = false;
-  // per-kernel-class timing (eager launches only)
-  bool profile = false;
-  struct Pending {
-    int cls;
-    cudaEvent_t a, b;
-  };
-  std::vector<Pending> pending;
-  std::vector<cudaEvent_t> event_pool;
-  double class_ms[SFD_NCLASS] = {};
-  long long class_count[SFD_NCLASS] = {};
-};
 
 namespace {
 
@@ -446,6 +372,7 @@ void free_engine(sfd_engine* e) {
                   e->inv_out, e->m64, e->m32, e->pbuf, e->rbuf, e->cbuf, e->cparts, e->rparts};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  sfd_adjoint_free(e);
   drain_profile(e);
   for (cudaEvent_t ev : e->event_pool) cudaEventDestroy(ev);
   for (auto& kv : e->d_tw) cudaFree(kv.second);
@@ -476,6 +403,12 @@ int fill_surface(SurfaceDesc& S, const sfd_problem& p) {
 }
 
 }  // namespace
+
+int sfd_internal_error(int code, const char* msg) { return set_error(code, "%s", msg); }
+int sfd_internal_cuda(cudaError_t err, const char* what) {
+  return set_error(SFD_ERR_CUDA, "%s: %s", what, cudaGetErrorString(err));
+}
+int sfd_internal_rhs(sfd_engine* e, const double* st, double* out) { return enqueue_rhs(e, st, out, true); }
 
 // ====================================================================== C ABI
 extern "C" {
@@ -718,6 +651,21 @@ int sfd_create(const int* n, int nsurf, const sfd_problem* problems, int shared_
 
 int sfd_destroy(sfd_engine* e) {
   free_engine(e);
+  return 0;
+}
+
+int sfd_set_problem(sfd_engine* e, int surface, const sfd_problem* problem) {
+  if (!e || !problem || surface < 0 || surface >= e->nsurf) return set_error(SFD_ERR_INVALID, "invalid argument");
+  SurfaceDesc S = e->hs[surface];
+  int rc = fill_surface(S, *problem);
+  if (rc) return rc;
+  const SurfaceDesc& O = e->hs[surface];
+  if (S.physics != O.physics || S.infinite_depth != O.infinite_depth || (S.physics == 0 && (S.rho != 0.0) != (O.rho != 0.0)))
+    return set_error(SFD_ERR_INVALID, "sfd_set_problem: physics, depth mode and rho != 0 must not change");
+  CK(cudaSetDevice(e->device));
+  CK(cudaStreamSynchronize(e->stream));
+  e->hs[surface] = S;
+  CK(cudaMemcpy(e->d_surf + surface, &S, sizeof(SurfaceDesc), cudaMemcpyHostToDevice));
   return 0;
 }
 
@@ -1124,7 +1072,7 @@ constexpr size_t kBytes = align256(8ull * kMaxN * kMaxN)            // FP64 matr
 constexpr int kMaxDevices = 64;
 }  // namespace noalloc
 
-// About 8.9 MB; every GPU that loads the library keeps it until the process exits.
+// About 8.7 MB; every GPU that loads the library keeps it until the process exits.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[noalloc::kBytes];
 
 namespace {

@@ -41,6 +41,7 @@ enum : int {
   SFD_JOB_PHIP = 2, // phi' (real part kept)
   SFD_JOB_AP = 3,   // a' (complex kept)
   SFD_JOB_RAW = 4,  // d/dj of (x + i y) with no linear part and no 2 pi/N scale -> ap
+  SFD_JOB_RAW2 = 5, // d^2/dj^2 of (x + i y), likewise unscaled -> ap (reverse mode)
 };
 
 struct DerivArgs {

@@ -154,8 +154,8 @@ __global__ void __launch_bounds__(kFftThreads, 1) k_spectral_deriv(DerivArgs A, 
     } else if (kind == SFD_JOB_PHIP) {
       v = {A.phi[off + j] - (-(1 + rho) * SFD_PI * S.U / n * (double)j),      // Derivatives.cuh:286,318
            A.phi_im ? A.phi_im[off + j] : 0.0};
-    } else if (kind == SFD_JOB_RAW) {
-      v = {A.x[off + j], A.y[off + j]};
+    } else if (kind == SFD_JOB_RAW || kind == SFD_JOB_RAW2) {
+      v = {A.x[off + j], A.y ? A.y[off + j] : 0.0};
     } else {
       v = {A.a[off + j], 0.0};                                                 // real_to_complex(a)
     }
@@ -164,7 +164,7 @@ __global__ void __launch_bounds__(kFftThreads, 1) k_spectral_deriv(DerivArgs A, 
   __syncthreads();
   cta_fft(buf, S, -1);
   for (int i = threadIdx.x; i < n; i += kFftThreads)
-    buf[i] = kind == SFD_JOB_ZPP ? second_mult(buf[i], i, n) : first_mult(buf[i], i, n);
+    buf[i] = (kind == SFD_JOB_ZPP || kind == SFD_JOB_RAW2) ? second_mult(buf[i], i, n) : first_mult(buf[i], i, n);
   __syncthreads();
   cta_fft(buf, S, +1);
   const double s1 = 2.0 * SFD_PI / n;
@@ -180,7 +180,8 @@ __global__ void __launch_bounds__(kFftThreads, 1) k_spectral_deriv(DerivArgs A, 
         A.phip[off + j] = r;
         break;
       }
-      case SFD_JOB_RAW: A.ap[off + j] = v; break;                             // FftDerivative::exec, scale 1
+      case SFD_JOB_RAW:                                                       // FftDerivative::exec, scale 1
+      case SFD_JOB_RAW2: A.ap[off + j] = v; break;
       default: A.ap[off + j] = {v.re * s1, v.im * s1}; break;                 // BaseBoundaryIntegrator.cuh:203
     }
   }

@@ -1,0 +1,104 @@
+// sfd_internal.cuh -- the engine object shared by the orchestration files
+// (sfd_api.cu: forward path and C ABI; sfd_adjoint.cu: reverse mode).
+#pragma once
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <map>
+#include <vector>
+
+#include "../../include/sfd.h"
+#include "sfd_engine.cuh"
+#include "sfd_kernels.cuh"
+
+// kernel classes of the per-launch profile
+enum {
+  SFD_K_OTHER = 0,
+  SFD_K_SPECTRAL,
+  SFD_K_NODE,
+  SFD_K_SUMS64,
+  SFD_K_SUMSDF,
+  SFD_K_SUMS32,
+  SFD_K_EPILOGUE,  // no launches: the sum epilogue runs inside the boundary-sum kernels
+  SFD_K_ASSEMBLE,
+  SFD_K_DIAG,
+  SFD_K_PANEL,
+  SFD_K_UPDATE,
+  SFD_K_TRSV,
+  SFD_K_GEMV,
+  SFD_K_VELOCITY,
+  SFD_K_RK4,
+  SFD_K_UPDATE_TC,
+  SFD_NCLASS
+};
+
+struct AdjWork;
+
+struct sfd_engine {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaStream_t own_stream = nullptr;
+  sfd_options opt{};
+  int nsurf = 0, ntot = 0, max_n = 0, max_np = 0;
+  long long mat_elems = 0, panel_elems = 0;
+  bool any_rho = false;
+  std::vector<SurfaceDesc> hs;
+  SurfaceDesc* d_surf = nullptr;
+  int* d_node_surf = nullptr;
+  std::map<int, cd*> d_tw;
+  // work lists
+  int2* d_jobs_first = nullptr; int njobs_first = 0;
+  int2* d_jobs_ap = nullptr; int njobs_ap = 0;
+  int2* d_cjobs_first = nullptr; int ncjobs_first = 0;  // cluster-distributed transforms
+  int2* d_cjobs_ap = nullptr; int ncjobs_ap = 0;
+  int max_n_single = 0, max_n_cluster = 0;
+  int2* d_sum_items = nullptr; int nsum = 0;
+  int4* d_asm_tiles = nullptr; int nasm = 0;
+  int2* d_gemv_rows = nullptr; int ngemv = 0;
+  long long* d_poff = nullptr;
+  int max_blocks64 = 0, max_blocks128 = 0;
+  // state (each 3 * ntot): [x | y | phi]
+  double *y0 = nullptr, *ys = nullptr, *kacc = nullptr, *kcur = nullptr;
+  // stage data
+  cd *zp = nullptr, *zpp = nullptr, *ap = nullptr;
+  double *phip = nullptr, *a = nullptr, *r = nullptr, *delta = nullptr, *phi_im = nullptr;
+  float2 *adf = nullptr, *ddf = nullptr;  // double-float copies of a and delta
+  NodeData nd{};
+  cd *cacc = nullptr, *dacc = nullptr, *vel_low1 = nullptr;
+  unsigned int* status = nullptr;
+  double *lmax = nullptr, *rnorm = nullptr, *inv_out = nullptr;
+  // matrices
+  double* m64 = nullptr;
+  float* m32 = nullptr;
+  float *pbuf = nullptr, *rbuf = nullptr, *cbuf = nullptr;
+  __nv_bfloat16 *cparts = nullptr, *rparts = nullptr;  // tensor-core operands: 3 bf16 parts, panel_elems apart
+  // graphs
+  cudaGraphExec_t g_step[2] = {nullptr, nullptr};
+  double g_dt = 0.0;
+  int g_kernels[2] = {0, 0};
+  long long step_count = 0;
+  long long launches = 0;
+  bool have_precond = false;
+  // per-kernel-class timing (eager launches only)
+  bool profile = false;
+  struct Pending {
+    int cls;
+    cudaEvent_t a, b;
+  };
+  std::vector<Pending> pending;
+  std::vector<cudaEvent_t> event_pool;
+  double class_ms[SFD_NCLASS] = {};
+  long long class_count[SFD_NCLASS] = {};
+  // reverse-mode workspace (checkpoints and per-stage records), allocated on first use
+  AdjWork* adj = nullptr;
+};
+
+// Entry points of sfd_api.cu used by the reverse mode.
+int sfd_internal_error(int code, const char* msg);
+int sfd_internal_cuda(cudaError_t err, const char* what);
+// One FP64 RHS evaluation (state [x|y|phi] -> [dx|dy|dphi]) on the engine
+// stream; leaves z', z'', a, a', C, D, w, p and the LU factors of M in the
+// engine's buffers.
+int sfd_internal_rhs(sfd_engine* e, const double* st, double* out);
+// reverse-mode workspace release (sfd_adjoint.cu)
+void sfd_adjoint_free(sfd_engine* e);

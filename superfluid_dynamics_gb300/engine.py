@@ -195,6 +195,44 @@ class Engine:
     def kernel_launches(self) -> int:
         return int(self._L.sfd_kernel_launches(self._h))
 
+    def set_problem(self, physics: Physics, surface: int = 0) -> None:
+        """Replace one surface's parameters (A3, g, ...) in place."""
+        check(self._L.sfd_set_problem(self._h, int(surface), ctypes.byref(physics.to_c())))
+
+    # -------------------------------------------------------------- reverse mode
+    # FP64 engines with one surface (water rho = 0 or helium, standard closure).
+    def rhs_vjp_device(self, state_ptr: int, cot_ptr: int, grad_ptr: int) -> float:
+        """grad = J(state)^T cot on device arrays of 3n doubles; returns the
+        parameter derivative (d/dA3 helium, d/dg water)."""
+        gp = np.zeros(1)
+        check(self._L.sfd_rhs_vjp_device(self._h, state_ptr, cot_ptr, grad_ptr, _dp(gp)))
+        return float(gp[0])
+
+    def rhs_vjp(self, state: np.ndarray, cot: np.ndarray):
+        """Host convenience over rhs_vjp_device (device buffers from torch)."""
+        import torch
+        dev = torch.device("cuda", self.options.device)
+        s = torch.as_tensor(_f64(state), device=dev)
+        c = torch.as_tensor(_f64(cot), device=dev)
+        g = torch.empty_like(s)
+        gp = self.rhs_vjp_device(s.data_ptr(), c.data_ptr(), g.data_ptr())
+        return g.cpu().numpy(), gp
+
+    def rk4_record(self, dt: float, steps: int, checkpoint_every: int, state0: np.ndarray) -> np.ndarray:
+        """Integrate from state0 = [x|y|phi] keeping checkpoints; returns the final state."""
+        s0 = _f64(state0)
+        out = np.empty_like(s0)
+        check(self._L.sfd_rk4_record(self._h, float(dt), int(steps), int(checkpoint_every), _dp(s0), _dp(out)))
+        return out
+
+    def rk4_vjp(self, cot_final: np.ndarray):
+        """(d final / d state0)^T cot_final and the parameter derivative of <cot_final, final>."""
+        c = _f64(cot_final)
+        g = np.empty_like(c)
+        gp = np.zeros(1)
+        check(self._L.sfd_rk4_vjp(self._h, _dp(c), _dp(g), _dp(gp)))
+        return g, float(gp[0])
+
     def split(self, arr: np.ndarray) -> list[np.ndarray]:
         return [arr[self.offsets[i]:self.offsets[i + 1]] for i in range(self.nsurf)]
 
