@@ -121,6 +121,36 @@ def step_traffic(n, args):
     return None
 
 
+def adjoint_ratio(device: int):
+    """Cost of the hand-written adjoint against the forward pass on the fit
+    workload: helium film N=512, h0=10, A3=1e3, 500 RK4 steps at dt=1e-3,
+    initial y from 64 seeded Fourier coefficients, checkpoints every 50 steps,
+    loss = 0.5 |y_final - y_target|^2.  Forward = the recorded FP64 trajectory
+    (sfd_rk4_record); adjoint = sfd_rk4_vjp (segment recomputation with every
+    stage recorded, then the reverse sweep).  Wall-clock, synchronous."""
+    import superfluid_dynamics_gb300 as sfd
+    from superfluid_dynamics_gb300 import workloads
+    n, steps, dt, every = 512, 500, 1e-3, 50
+    s, c0, target = workloads.helium_fit(n)
+    state0 = np.concatenate([s.x, s.y, s.phi])
+    eng = sfd.Engine(n, sfd.HeliumBoundaryProblem(depth=10.0, A3=1e3),
+                     sfd.Options(precision=sfd.PRECISION_FP64, use_graphs=False, device=device))
+    eng.rk4_record(dt, 5, every, state0)          # warm-up (workspace, first launches)
+    eng.rk4_vjp(np.zeros(3 * n))
+    t0 = time.perf_counter()
+    final = eng.rk4_record(dt, steps, every, state0)
+    t_fwd = time.perf_counter() - t0
+    cot = np.zeros(3 * n)
+    cot[n:2 * n] = final[n:2 * n] - target
+    t0 = time.perf_counter()
+    g, gp = eng.rk4_vjp(cot)
+    t_adj = time.perf_counter() - t0
+    eng.close()
+    return {"workload": "helium film N=512, h0=10, A3=1e3, 500 RK4 steps dt=1e-3, 64 Fourier coefficients, "
+                        "checkpoints every 50", "forward_s": t_fwd, "adjoint_s": t_adj, "ratio": t_adj / t_fwd,
+            "loss": 0.5 * float(cot[n:2 * n] @ cot[n:2 * n]), "grad_A3": gp}
+
+
 def cpu_sample(steps: int = 1, n: int = N_NODES):
     """Oracle port (FP64, OpenMP over all host cores): time `steps` RK4 steps."""
     from oracle import oracle
@@ -265,6 +295,7 @@ def run_ours(args, rank, world, local_rank):
     roof["dominant_class"] = {"name": dom, "avg_launch_ms": round(per_launch[dom][0], 5),
                               "launches_per_step": per_launch[dom][1] / prof_steps}
 
+    adj = None if args.no_adjoint else adjoint_ratio(local_rank)
     cpu = None
     if not args.no_cpu and world >= 1:
         rate, cores = cpu_sample(1, n)
@@ -281,7 +312,7 @@ def run_ours(args, rank, world, local_rank):
             "roofline": roof, "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": 3 * n * 8,
                     "d2h_bytes_per_step": 3 * n * 8},
-            "gpu_launches": gpu_launches, "clocks": clk.summary()}
+            "gpu_launches": gpu_launches, "clocks": clk.summary(), "adjoint": adj}
     print(json.dumps(line), flush=True)
 
 
@@ -297,6 +328,7 @@ def main():
     ap.add_argument("--pre-iters", type=int, default=2)
     ap.add_argument("--refactor-every", type=int, default=50)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -195,3 +195,40 @@ def test_autograd_fourier_fit():
         fd = (float(loss_of(c0, a3 + h)) - float(loss_of(c0, a3 - h))) / (2 * h)
         assert abs(fd - ga) <= 1e-5 * max(abs(fd), 1e-14), (fd, ga)
     traj.close()
+
+
+def test_fit_workload_full_size_gradient():
+    """The fit workload at full size (N=512, h0=10, A3=1e3, 500 steps at
+    dt=1e-3, checkpoints every 50): adjoint gradient of the loss
+    0.5 |y_final - y_target|^2 against central differences (h = 1e-6) for
+    three Fourier coefficients and A3."""
+    n, steps, dt, every = 512, 500, 1e-3, 50
+    s, c0, target = W.helium_fit(n)
+    phys = sfd.HeliumBoundaryProblem(depth=10.0, A3=1e3)
+    M = c0.size // 2
+    m = np.arange(1, M + 1)
+    xi = W.nodes(n)
+    basis = np.concatenate([np.cos(m[:, None] * xi), np.sin(m[:, None] * xi)])
+
+    def state_of(c):
+        return np.concatenate([xi, c @ basis, np.zeros(n)])
+
+    with fp64_engine(n, phys) as e:
+        def loss(c, a3=1e3):
+            e.set_problem(with_param(phys, a3))
+            f = e.rk4_record(dt, steps, every, state_of(c))
+            return 0.5 * float(((f[n:2 * n] - target) ** 2).sum()), f
+
+        L0, f0 = loss(c0)
+        cot = np.zeros(3 * n)
+        cot[n:2 * n] = f0[n:2 * n] - target
+        g, ga = e.rk4_vjp(cot)
+        gc = basis @ g[n:2 * n]
+        for i in (0, 20, 45):
+            d = np.zeros_like(c0)
+            d[i] = FD_H
+            fd = (loss(c0 + d)[0] - loss(c0 - d)[0]) / (2 * FD_H)
+            assert abs(fd - gc[i]) <= 1e-5 * max(abs(fd), 1e-10), (i, fd, gc[i])
+        h = 1e-6 * 1e3
+        fd = (loss(c0, 1e3 + h)[0] - loss(c0, 1e3 - h)[0]) / (2 * h)
+        assert abs(fd - ga) <= 1e-5 * max(abs(fd), 1e-16), (fd, ga)
