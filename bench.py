@@ -316,6 +316,144 @@ def run_ours(args, rank, world, local_rank):
     print(json.dumps(line), flush=True)
 
 
+def _rel(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def _state_err(sa, sb, n):
+    """max |z_a - z_b| / max |z_b| and the same for phi, from [x|y|phi] arrays."""
+    za, zb = sa[:n] + 1j * sa[n:2 * n], sb[:n] + 1j * sb[n:2 * n]
+    return [_rel(za, zb), _rel(sa[2 * n:], sb[2 * n:])]
+
+
+def _timed_steps(eng, dt, steps, stream):
+    import torch
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        eng.step(dt, steps, sync=False)
+        e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) * 1e-3
+
+
+def run_workload(args, local_rank):
+    """Secondary workloads (parity and scale cases, one JSON line each):
+      modes1024   : gravity wave N=1024, 8 seeded modes (seed 2), dt=0.005,
+                    1000 steps mixed; state error vs the FP64 engine every 100
+                    steps beside the FP64-vs-perturbed-FP64 envelope (1e-15
+                    relative perturbation of x)
+      helium-batch: 512 helium films of uneven N (32 * U{4..64}, seed 3),
+                    dt=1e-3, 200 steps mixed in one engine (every kernel spans
+                    the batch, one CUDA graph per step); error vs the FP64
+                    engine after 5 steps; per-surface status
+      steep8192   : gravity wave y = 0.3 cos xi, phi = 0.3 sin xi, N=8192,
+                    dt=5e-4, 2000 steps mixed; error vs the FP64 engine after
+                    10 steps"""
+    import torch
+    import superfluid_dynamics_gb300 as sfd
+    from superfluid_dynamics_gb300 import workloads
+    torch.cuda.set_device(local_rank)
+    stream = torch.cuda.Stream()
+    mixed = sfd.Options(precision=sfd.PRECISION_MIXED, refine_iters=args.refine_iters, pre_iters=args.pre_iters,
+                        refactor_every=args.refactor_every, device=local_rank)
+    fp64 = sfd.Options(precision=sfd.PRECISION_FP64, device=local_rank)
+    line = {"workload": args.workload, "unit": "steps/s", "higher_is_better": True,
+            "config": {"precision": "mixed", "pre_iters": args.pre_iters, "refine_iters": args.refine_iters,
+                       "refactor_every": args.refactor_every}}
+    if args.workload == "modes1024":
+        n, dt, steps = 1024, 0.005, 1000
+        s = workloads.random_modes(n, seed=2)
+        s0 = np.concatenate([s.x, s.y, s.phi])
+        chk = list(range(100, steps + 1, 100))
+        res = {}
+        for name, opt, eps in (("mixed", mixed, 0.0), ("fp64", fp64, 0.0), ("fp64_perturbed", fp64, 1e-15)):
+            eng = sfd.Engine(n, sfd.WaterBoundaryProblem(), opt)
+            eng.set_stream(stream.cuda_stream)
+            x = s.x * (1 + eps * np.random.default_rng(7).standard_normal(n))
+            eng.set_state(x, s.y, s.phi)
+            traj, t = [], 0.0
+            done = 0
+            for c in chk:
+                t += _timed_steps(eng, dt, c - done, stream)
+                done = c
+                traj.append(np.concatenate(eng.get_state()))
+            res[name] = (traj, steps / t, eng.status())
+            eng.close()
+        line["value"] = res["mixed"][1]
+        line["fp64_steps_per_s"] = res["fp64"][1]
+        line["accuracy"] = {"steps": chk,
+                            "mixed_vs_fp64": [_state_err(a, b, n) for a, b in zip(res["mixed"][0], res["fp64"][0])],
+                            "fp64_perturbed_vs_fp64": [_state_err(a, b, n) for a, b in
+                                                       zip(res["fp64_perturbed"][0], res["fp64"][0])]}
+        line["status_or"] = int(np.bitwise_or.reduce(res["mixed"][2][0]))
+    elif args.workload == "helium-batch":
+        surfs = workloads.helium_batch(512, seed=3)
+        ns = [sf.n for sf in surfs]
+        phys = [sfd.HeliumBoundaryProblem(depth=sf.depth, A3=sf.A3) for sf in surfs]
+        dt, steps = 1e-3, 200
+        x = np.concatenate([sf.x for sf in surfs])
+        y = np.concatenate([sf.y for sf in surfs])
+        ph = np.concatenate([sf.phi for sf in surfs])
+        eng = sfd.Engine(ns, phys, mixed)
+        eng.set_stream(stream.cuda_stream)
+        eng.set_state(x, y, ph)
+        _timed_steps(eng, dt, 5, stream)
+        m5 = np.concatenate(eng.get_state())
+        t = _timed_steps(eng, dt, steps - 5, stream)
+        st = eng.status()
+        eng.close()
+        ref = sfd.Engine(ns, phys, fp64)
+        ref.set_state(x, y, ph)
+        ref.step(dt, 5)
+        f5 = np.concatenate(ref.get_state())
+        ref.close()
+        nt = sum(ns)
+        off = np.concatenate([[0], np.cumsum(ns)])
+        errs = [_state_err(np.concatenate([m5[off[i]:off[i + 1]], m5[nt + off[i]:nt + off[i + 1]],
+                                           m5[2 * nt + off[i]:2 * nt + off[i + 1]]]),
+                           np.concatenate([f5[off[i]:off[i + 1]], f5[nt + off[i]:nt + off[i + 1]],
+                                           f5[2 * nt + off[i]:2 * nt + off[i + 1]]]), ns[i]) for i in range(len(ns))]
+        line["value"] = (steps - 5) / t
+        line["config"].update({"surfaces": len(ns), "total_nodes": nt, "sum_n2": int(sum(v * v for v in ns)),
+                               "dt": dt, "timed_steps": steps - 5})
+        line["accuracy"] = {"after_steps": 5, "max_surface_err_z": max(e[0] for e in errs),
+                            "max_surface_err_phi": max(e[1] for e in errs)}
+        flags = st[0]
+        line["status"] = {"surfaces_nonfinite": int(((flags & sfd._lib.STATUS_NONFINITE) != 0).sum()),
+                          "surfaces_pivot_swap": int(((flags & 2) != 0).sum()),
+                          "surfaces_refine_stall": int(((flags & 8) != 0).sum())}
+    elif args.workload == "steep8192":
+        n, dt, steps = 8192, 5e-4, 2000
+        s = workloads.linear_wave(n, 0.3)
+        eng = sfd.Engine(n, sfd.WaterBoundaryProblem(), mixed)
+        eng.set_stream(stream.cuda_stream)
+        eng.set_state(s.x, s.y, s.phi)
+        _timed_steps(eng, dt, 10, stream)
+        m10 = np.concatenate(eng.get_state())
+        t = _timed_steps(eng, dt, steps - 10, stream)
+        st = eng.status()
+        eng.close()
+        ref = sfd.Engine(n, sfd.WaterBoundaryProblem(), fp64)
+        ref.set_state(s.x, s.y, s.phi)
+        t0 = time.perf_counter()
+        ref.step(dt, 10)
+        t64 = time.perf_counter() - t0
+        f10 = np.concatenate(ref.get_state())
+        ref.close()
+        line["value"] = (steps - 10) / t
+        line["fp64_steps_per_s"] = 10 / t64
+        line["config"].update({"N": n, "dt": dt, "timed_steps": steps - 10})
+        line["accuracy"] = {"after_steps": 10, "mixed_vs_fp64": _state_err(m10, f10, n)}
+        line["status_or"] = int(np.bitwise_or.reduce(st[0]))
+    else:
+        raise SystemExit(f"unknown workload {args.workload}")
+    line["metric"] = "RK4 steps/s"
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -329,12 +467,18 @@ def main():
     ap.add_argument("--refactor-every", type=int, default=50)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--workload", default="headline", choices=["headline", "modes1024", "helium-batch", "steep8192"],
+                    help="headline = the metric's configuration; the others print their own line")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.workload != "headline":
+        if rank == 0:
+            run_workload(args, local_rank)
         return
     if world > 1:
         import torch
