@@ -245,7 +245,7 @@ def test_nonfinite_state_sets_status():
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
 def test_batch_mixing_cluster_and_single_cta_transforms(prec):
     # n % 64 == 0 and n >= 512 use the cluster-distributed transforms; others one CTA
-    sizes = [512, 96, 640, 1152, 160]
+    sizes = [512, 96, 640, 1152, 160, 1024, 2048]
     surfs = []
     for i, n in enumerate(sizes):
         xi = W.nodes(n)
