@@ -193,7 +193,7 @@ def run_ours(args, rank, world, local_rank):
     s = workloads.random_modes(args.n, seed=2)
     prec = sfd.PRECISION_MIXED if args.precision == "mixed" else sfd.PRECISION_FP64
     opts = sfd.Options(precision=prec, refine_iters=args.refine_iters, refactor_every=args.refactor_every,
-                       pre_iters=args.pre_iters, device=local_rank)
+                       pre_iters=args.pre_iters, device=local_rank, precond_half=not args.precond_fp32)
     eng = sfd.Engine(args.n, sfd.WaterBoundaryProblem(), opts)
     stream = torch.cuda.Stream(device=dev)
     eng.set_stream(stream.cuda_stream)
@@ -307,7 +307,8 @@ def run_ours(args, rank, world, local_rank):
             "data": "synthetic (seeded 8-mode gravity wave)",
             "config": {"workload": f"gravity wave N={n}, 8 modes seed 2, RK4 dt={DT}", "N": n,
                        "precision": args.precision, "refine_iters": args.refine_iters, "pre_iters": args.pre_iters,
-                       "refactor_every": args.refactor_every, "l2": "flushed (256 MB write) before every timed step",
+                       "refactor_every": args.refactor_every, "precond_storage": "fp32" if args.precond_fp32 else "fp16",
+                       "l2": "flushed (256 MB write) before every timed step",
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
             "roofline": roof, "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": 3 * n * 8,
@@ -467,6 +468,7 @@ def main():
     ap.add_argument("--refactor-every", type=int, default=50)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--precond-fp32", action="store_true", help="apply the preconditioner from FP32 (default FP16 copy)")
     ap.add_argument("--workload", default="headline", choices=["headline", "modes1024", "helium-batch", "steep8192"],
                     help="headline = the metric's configuration; the others print their own line")
     args = ap.parse_args()

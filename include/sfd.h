@@ -74,6 +74,7 @@ typedef struct sfd_options {
     int device;           /* CUDA device ordinal (0)                                     */
     int tensor_cores;     /* mixed: preconditioner update on tcgen05 tensor cores (1)    */
     int pre_iters;        /* mixed: FP32 full-residual iterations before it (default 1)  */
+    int precond_half;     /* mixed: apply the preconditioner from an FP16 copy (1)       */
 } sfd_options;
 
 typedef struct sfd_engine sfd_engine;

@@ -33,7 +33,8 @@ class SfdProblem(ctypes.Structure):
 
 class SfdOptions(ctypes.Structure):
     _fields_ = [("precision", c_int), ("refine_iters", c_int), ("refactor_every", c_int),
-                ("use_graphs", c_int), ("device", c_int), ("tensor_cores", c_int), ("pre_iters", c_int)]
+                ("use_graphs", c_int), ("device", c_int), ("tensor_cores", c_int), ("pre_iters", c_int),
+                ("precond_half", c_int)]
 
 
 class SimProperties(ctypes.Structure):

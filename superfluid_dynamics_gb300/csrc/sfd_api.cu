@@ -168,6 +168,18 @@ int enqueue_sums(sfd_engine* e, int prec, const double* weights, const float2* w
   return 0;
 }
 
+// y = X v with the current preconditioner (FP16 copy or FP32); ydf: optional
+// double-float copy of y.
+int enqueue_gemv(sfd_engine* e, const double* v, double* y, float2* ydf) {
+  if (e->m16)
+    LAUNCHC(e, SFD_K_GEMV, k_gemv_h<<<e->ngemv, 512, e->max_np * sizeof(float), e->stream>>>(
+                               e->d_surf, e->d_gemv_rows, e->m16, e->rscale, v, y, ydf));
+  else
+    LAUNCHC(e, SFD_K_GEMV, k_gemv<<<e->ngemv, 256, e->max_np * sizeof(float), e->stream>>>(
+                               e->d_surf, e->d_gemv_rows, e->m32, v, y, ydf));
+  return 0;
+}
+
 int enqueue_precond(sfd_engine* e) {
   const int nb = e->max_np / 128;
   LAUNCHC(e, SFD_K_ASSEMBLE, sfd_launch_assemble32(e->d_surf, e->d_asm_tiles, e->nasm, e->nd.w, e->nd.p, e->zp, e->nd.mdiag, e->m32,
@@ -194,6 +206,9 @@ int enqueue_precond(sfd_engine* e) {
                   e->d_surf, e->nsurf, kb, e->m32, e->pbuf, e->rbuf, e->cbuf, e->d_poff, 0));
     }
   }
+  if (e->m16)
+    LAUNCHC(e, SFD_K_GEMV, k_precond_to_half<<<e->ngemv, 256, 0, e->stream>>>(e->d_surf, e->d_gemv_rows, e->m32,
+                                                                              e->m16, e->rscale));
   return 0;
 }
 
@@ -236,21 +251,20 @@ int enqueue_solve(sfd_engine* e, const double* st, const double* phi_im, bool re
     // a0 = X phi'; FP32 pre-iterations (full residual in FP32) bring a within
     // ~1e-7 of the solution; one double-float pass then gives the accurate
     // residual and C(a); FP32 post-iterations correct the small remainder.
-    LAUNCHC(e, SFD_K_GEMV, k_gemv<<<e->ngemv, 256, e->max_np * sizeof(float), e->stream>>>(
-                               e->d_surf, e->d_gemv_rows, e->m32, e->phip, e->a, e->adf));
-    int rc = 0;
+    int rc = enqueue_gemv(e, e->phip, e->a, e->adf);
+    if (rc) return rc;
     for (int it = 0; it < e->opt.pre_iters; ++it) {
       rc = enqueue_sums(e, SFD_PREC_F32, e->a, e->adf, 0, false);
       if (rc) return rc;
-      LAUNCHC(e, SFD_K_GEMV, k_gemv<<<e->ngemv, 256, e->max_np * sizeof(float), e->stream>>>(
-                                 e->d_surf, e->d_gemv_rows, e->m32, e->r, e->delta, nullptr));
+      rc = enqueue_gemv(e, e->r, e->delta, nullptr);
+      if (rc) return rc;
       LAUNCH(e, k_axpy_inplace<<<blocks_for(nt, 256), 256, 0, e->stream>>>(nt, e->a, e->delta, e->adf));
     }
     rc = enqueue_sums(e, SFD_PREC_DF, e->a, e->adf, 0, e->opt.refine_iters == 0);
     if (rc) return rc;
     for (int it = 0; it < e->opt.refine_iters; ++it) {
-      LAUNCHC(e, SFD_K_GEMV, k_gemv<<<e->ngemv, 256, e->max_np * sizeof(float), e->stream>>>(
-                                 e->d_surf, e->d_gemv_rows, e->m32, e->r, e->delta, e->ddf));
+      rc = enqueue_gemv(e, e->r, e->delta, e->ddf);
+      if (rc) return rc;
       LAUNCH(e, k_axpy_inplace<<<blocks_for(nt, 256), 256, 0, e->stream>>>(nt, e->a, e->delta, nullptr));
       rc = enqueue_sums(e, SFD_PREC_F32, e->delta, e->ddf, 1, it == e->opt.refine_iters - 1);
       if (rc) return rc;
@@ -369,7 +383,7 @@ void free_engine(sfd_engine* e) {
                   e->d_gemv_rows, e->d_poff, e->y0, e->ys, e->kacc, e->kcur, e->zp, e->zpp, e->ap, e->phip, e->a,
                   e->r, e->delta, e->phi_im, e->nd.w, e->nd.p, e->nd.wdf, e->nd.pdf, e->adf, e->ddf, e->nd.mdiag, e->nd.v1low, e->nd.v1up, e->nd.v2,
                   e->cacc, e->dacc, e->vel_low1, e->status, e->lmax, e->rnorm,
-                  e->inv_out, e->m64, e->m32, e->pbuf, e->rbuf, e->cbuf, e->cparts, e->rparts};
+                  e->inv_out, e->m64, e->m32, e->m16, e->rscale, e->pbuf, e->rbuf, e->cbuf, e->cparts, e->rparts};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   sfd_adjoint_free(e);
@@ -422,6 +436,7 @@ void sfd_default_options(sfd_options* o) {
   o->device = 0;
   o->tensor_cores = 1;
   o->pre_iters = 1;
+  o->precond_half = 1;
 }
 
 void sfd_default_problem(sfd_problem* p) {
@@ -631,6 +646,10 @@ int sfd_create(const int* n, int nsurf, const sfd_problem* problems, int shared_
     CKE(dalloc(&e->m64, e->mat_elems));
   } else {
     CKE(dalloc(&e->m32, e->mat_elems));
+    if (e->opt.precond_half) {
+      CKE(dalloc(&e->m16, e->mat_elems));
+      CKE(dalloc(&e->rscale, nt));
+    }
     CKE(dalloc(&e->pbuf, (long long)nsurf * 128 * 128));
     CKE(dalloc(&e->rbuf, e->panel_elems));
     CKE(dalloc(&e->cbuf, e->panel_elems));

@@ -2,6 +2,7 @@
 // (sfd_api.cu: forward path and C ABI; sfd_adjoint.cu: reverse mode).
 #pragma once
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <map>
@@ -70,6 +71,8 @@ struct sfd_engine {
   // matrices
   double* m64 = nullptr;
   float* m32 = nullptr;
+  __half* m16 = nullptr;     // FP16 copy of the preconditioner (rows scaled by powers of two)
+  float* rscale = nullptr;   // per-row inverse scales of m16
   float *pbuf = nullptr, *rbuf = nullptr, *cbuf = nullptr;
   __nv_bfloat16 *cparts = nullptr, *rparts = nullptr;  // tensor-core operands: 3 bf16 parts, panel_elems apart
   // graphs

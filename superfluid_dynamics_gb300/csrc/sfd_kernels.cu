@@ -320,14 +320,23 @@ __global__ void __cluster_dims__(kSumCL, 1, 1) __launch_bounds__(kSumThreads, 4)
     wcta = t;
   }
   Acc<PREC> R;
-  const bool overlap = (t0 < j_hi) && (t0 + kSumTile > j_lo);
-  if (overlap) {  // this CTA holds some targets' own node: skip j == k
-    const int self = active ? tk - j_lo : -1;
-    for (int jj = grp; jj < jn; jj += kSumGroups) pair_acc(T, src[jj], jj == self, image, R);
-  } else {
-#pragma unroll 4
-    for (int jj = grp; jj < jn; jj += kSumGroups) pair_acc(T, src[jj], false, image, R);
+  // Sources jj = grp, grp + G, ... in ascending order.  Only the block of
+  // sources [lo, hi) that holds the tile's own nodes needs the j == k test;
+  // the rest runs unchecked and unrolled, so the CTA holding the diagonal is
+  // not the cluster's straggler.
+  int lo = jn, hi = jn;
+  if ((t0 < j_hi) && (t0 + kSumTile > j_lo)) {
+    lo = max(0, t0 - j_lo);
+    hi = min(jn, t0 + kSumTile - j_lo);
   }
+  const int self = active ? tk - j_lo : -1;
+  auto first = [&](int a) { return a + ((grp - a) % kSumGroups + kSumGroups) % kSumGroups; };
+  int jj = grp;
+#pragma unroll 4
+  for (; jj < lo; jj += kSumGroups) pair_acc(T, src[jj], false, image, R);
+  for (jj = first(lo); jj < hi; jj += kSumGroups) pair_acc(T, src[jj], jj == self, image, R);
+#pragma unroll 4
+  for (jj = first(hi); jj < jn; jj += kSumGroups) pair_acc(T, src[jj], false, image, R);
   gred[grp][l] = to_red(R);
   __syncthreads();
   if (grp == 0) {

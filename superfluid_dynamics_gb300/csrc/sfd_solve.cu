@@ -22,6 +22,8 @@
 #include "sfd_engine.cuh"
 #include "sfd_solve.cuh"
 
+#include <cuda_fp16.h>
+
 #include <cuda_bf16.h>
 
 // =============================================================== assembly
@@ -556,6 +558,25 @@ __global__ void __launch_bounds__(256) k_gj_update(const SurfaceDesc* surf, int 
 // kGemvRows rows: v is staged once as FP32 in shared memory, each warp walks two
 // rows with 16-byte loads (rows are 16-byte aligned: n_pad is a multiple of 128,
 // and X[i][j] = 0 for j >= n in the padded inverse).
+// Stage v[0..n) (FP64) as floats in shared memory, zero-padded to n_stage:
+// all of a thread's loads are issued before its stores, so the staging costs
+// one L2 round trip instead of one per element.
+template <int NT>
+__device__ __forceinline__ void stage_vector(float* vs, const double* v, int n, int n_stage) {
+  constexpr int kPer = (8192 + NT - 1) / NT;
+  double t[kPer];
+#pragma unroll
+  for (int i = 0; i < kPer; ++i) {
+    const int j = threadIdx.x + i * NT;
+    t[i] = j < n ? v[j] : 0.0;
+  }
+#pragma unroll
+  for (int i = 0; i < kPer; ++i) {
+    const int j = threadIdx.x + i * NT;
+    if (j < n_stage) vs[j] = (float)t[i];
+  }
+}
+
 __global__ void __launch_bounds__(256) k_gemv(const SurfaceDesc* surf, const int2* rowblk, const float* mat,
                                               const double* v, double* y, float2* ydf) {
   const int2 rb = rowblk[blockIdx.x];  // (surface, first row)
@@ -564,7 +585,7 @@ __global__ void __launch_bounds__(256) k_gemv(const SurfaceDesc* surf, const int
   extern __shared__ float4 vs4[];
   float* vs = reinterpret_cast<float*>(vs4);
   const int n4 = (n + 3) & ~3;
-  for (int j = threadIdx.x; j < n4; j += 256) vs[j] = j < n ? (float)v[off + j] : 0.f;
+  stage_vector<256>(vs, v + off, n, n4);
   __syncthreads();
   const float* X = mat + S.moff;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -605,6 +626,77 @@ __global__ void __launch_bounds__(256) k_gemv(const SurfaceDesc* surf, const int
       y[off + r1] = (double)acc1;
       if (ydf) ydf[off + r1] = make_float2(acc1, 0.f);
     }
+  }
+}
+
+// FP16 copy of the preconditioner for the GEMVs: row r is scaled by a power of
+// two 2^s_r so that its largest entry lies in [2^13, 2^14) (exact scaling, no
+// subnormals for entries down to 2^-10 of the row maximum); rscale[row] =
+// 2^-s_r undoes it.  Same CTA / warp layout as k_gemv: 16 rows per CTA.
+__global__ void __launch_bounds__(256) k_precond_to_half(const SurfaceDesc* surf, const int2* rowblk,
+                                                         const float* mat, __half* mat16, float* rscale) {
+  const int2 rb = rowblk[blockIdx.x];
+  const SurfaceDesc& S = surf[rb.x];
+  const int n = S.n, np = pad_n(n), off = S.off;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int rr = 0; rr < 2; ++rr) {
+    const int r = rb.y + 2 * warp + rr;
+    if (r >= n) break;
+    const float* X = mat + S.moff + (long long)r * np;
+    __half* H = mat16 + S.moff + (long long)r * np;
+    float m = 0.f;
+    for (int j = lane; j < np; j += 32) m = fmaxf(m, fabsf(X[j]));
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    int ex = 0;
+    frexpf(m > 0.f ? m : 1.f, &ex);  // m < 2^ex
+    const float sc = ldexpf(1.f, 14 - ex);
+    for (int j = lane; j < np; j += 32) H[j] = __float2half_rn(X[j] * sc);
+    if (lane == 0) rscale[off + r] = ldexpf(1.f, ex - 14);
+  }
+}
+
+// y = X v with the FP16 copy (FP32 accumulation), y scaled back per row.
+// 16 warps per CTA, one row per warp, four 16-byte loads (32 entries) per lane
+// in flight: enough bytes in flight per SM to stream at HBM / L2 rate.
+__global__ void __launch_bounds__(512) k_gemv_h(const SurfaceDesc* surf, const int2* rowblk, const __half* mat16,
+                                                const float* rscale, const double* v, double* y, float2* ydf) {
+  const int2 rb = rowblk[blockIdx.x];
+  const SurfaceDesc& S = surf[rb.x];
+  const int n = S.n, np = pad_n(n), off = S.off;
+  extern __shared__ float4 vsh[];
+  float* vs = reinterpret_cast<float*>(vsh);
+  const int n8 = (n + 7) & ~7;
+  stage_vector<512>(vs, v + off, n, n8);
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int r = rb.y + warp;
+  if (r >= n) return;
+  const uint4* xr = reinterpret_cast<const uint4*>(mat16 + S.moff + (long long)r * np);
+  const int nq = n8 / 8;
+  auto dot8 = [&](uint4 h, int q, float acc) {
+    const __half2* hp = reinterpret_cast<const __half2*>(&h);
+    const float4 va = vsh[2 * q], vb = vsh[2 * q + 1];
+    float2 f0 = __half22float2(hp[0]), f1 = __half22float2(hp[1]), f2 = __half22float2(hp[2]),
+           f3 = __half22float2(hp[3]);
+    acc = fmaf(f0.x, va.x, fmaf(f0.y, va.y, fmaf(f1.x, va.z, fmaf(f1.y, va.w, acc))));
+    return fmaf(f2.x, vb.x, fmaf(f2.y, vb.y, fmaf(f3.x, vb.z, fmaf(f3.y, vb.w, acc))));
+  };
+  float acc0 = 0.f, acc1 = 0.f;
+  int q = lane;
+  for (; q + 96 < nq; q += 128) {
+    const uint4 a0 = __ldg(xr + q), a1 = __ldg(xr + q + 32), a2 = __ldg(xr + q + 64), a3 = __ldg(xr + q + 96);
+    acc0 = dot8(a0, q, acc0);
+    acc1 = dot8(a1, q + 32, acc1);
+    acc0 = dot8(a2, q + 64, acc0);
+    acc1 = dot8(a3, q + 96, acc1);
+  }
+  for (; q < nq; q += 32) acc0 = dot8(__ldg(xr + q), q, acc0);
+  float acc = acc0 + acc1;
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) {
+    const float yr = acc * rscale[off + r];
+    y[off + r] = (double)yr;
+    if (ydf) ydf[off + r] = make_float2(yr, 0.f);
   }
 }
 

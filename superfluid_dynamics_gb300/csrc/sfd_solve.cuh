@@ -3,6 +3,7 @@
 #include "sfd_engine.cuh"
 
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 // per-surface matrices are padded to a multiple of 128 rows/columns
 __host__ __device__ __forceinline__ int pad_n(int n) { return (n + 127) / 128 * 128; }
@@ -24,6 +25,10 @@ __global__ void k_gj_panel(const SurfaceDesc* surf, int nsurf, int kb, const flo
                            __nv_bfloat16* rparts, long long pstride);
 __global__ void k_gj_update(const SurfaceDesc* surf, int nsurf, int kb, float* mat, const float* pbuf,
                             const float* rbuf, const float* cbuf, const long long* poff, int k_lines_only);
+__global__ void k_precond_to_half(const SurfaceDesc* surf, const int2* rowblk, const float* mat, __half* mat16,
+                                  float* rscale);
+__global__ void k_gemv_h(const SurfaceDesc* surf, const int2* rowblk, const __half* mat16, const float* rscale,
+                         const double* v, double* y, float2* ydf);
 cudaError_t sfd_tc_configure();
 cudaError_t sfd_launch_gj_update_tc(const SurfaceDesc* surf, int nsurf, int kb, int max_np, float* mat,
                                     const __nv_bfloat16* cparts, const __nv_bfloat16* rparts, long long part_stride,

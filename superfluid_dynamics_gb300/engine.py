@@ -66,11 +66,12 @@ class Options:
     device: int = 0
     tensor_cores: bool = True
     pre_iters: int = 1
+    precond_half: bool = True
 
     def to_c(self) -> _lib.SfdOptions:
         return _lib.SfdOptions(self.precision, self.refine_iters, self.refactor_every,
                                1 if self.use_graphs else 0, self.device, 1 if self.tensor_cores else 0,
-                               self.pre_iters)
+                               self.pre_iters, 1 if self.precond_half else 0)
 
 
 class Engine:
