@@ -656,23 +656,29 @@ __global__ void __launch_bounds__(256) k_precond_to_half(const SurfaceDesc* surf
 }
 
 // y = X v with the FP16 copy (FP32 accumulation), y scaled back per row.
-// 16 warps per CTA, one row per warp, four 16-byte loads (32 entries) per lane
-// in flight: enough bytes in flight per SM to stream at HBM / L2 rate.
+// 16 warps per CTA, one row per warp.  Each lane streams its 16-byte chunks
+// (8 entries) of the row in batches of four, software-pipelined one batch
+// ahead; the first batch is issued before v is staged, so the staging
+// latency overlaps the first matrix loads.
 __global__ void __launch_bounds__(512) k_gemv_h(const SurfaceDesc* surf, const int2* rowblk, const __half* mat16,
                                                 const float* rscale, const double* v, double* y, float2* ydf) {
   const int2 rb = rowblk[blockIdx.x];
   const SurfaceDesc& S = surf[rb.x];
   const int n = S.n, np = pad_n(n), off = S.off;
   extern __shared__ float4 vsh[];
-  float* vs = reinterpret_cast<float*>(vsh);
-  const int n8 = (n + 7) & ~7;
-  stage_vector<512>(vs, v + off, n, n8);
-  __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int r = rb.y + warp;
-  if (r >= n) return;
-  const uint4* xr = reinterpret_cast<const uint4*>(mat16 + S.moff + (long long)r * np);
+  const bool live = r < n;
+  const int n8 = (n + 7) & ~7;
   const int nq = n8 / 8;
+  const int per_lane = lane < nq ? (nq - lane + 31) / 32 : 0;  // chunks q = lane + 32 i, i < per_lane
+  const uint4* xr = reinterpret_cast<const uint4*>(mat16 + S.moff + (long long)(live ? r : rb.y) * np) + lane;
+  uint4 cur[4], nxt[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) cur[i] = (live && i < per_lane) ? __ldg(xr + 32 * i) : make_uint4(0, 0, 0, 0);
+  stage_vector<512>(reinterpret_cast<float*>(vsh), v + off, n, n8);
+  __syncthreads();
+  if (!live) return;
   auto dot8 = [&](uint4 h, int q, float acc) {
     const __half2* hp = reinterpret_cast<const __half2*>(&h);
     const float4 va = vsh[2 * q], vb = vsh[2 * q + 1];
@@ -682,15 +688,23 @@ __global__ void __launch_bounds__(512) k_gemv_h(const SurfaceDesc* surf, const i
     return fmaf(f2.x, vb.x, fmaf(f2.y, vb.y, fmaf(f3.x, vb.z, fmaf(f3.y, vb.w, acc))));
   };
   float acc0 = 0.f, acc1 = 0.f;
-  int q = lane;
-  for (; q + 96 < nq; q += 128) {
-    const uint4 a0 = __ldg(xr + q), a1 = __ldg(xr + q + 32), a2 = __ldg(xr + q + 64), a3 = __ldg(xr + q + 96);
-    acc0 = dot8(a0, q, acc0);
-    acc1 = dot8(a1, q + 32, acc1);
-    acc0 = dot8(a2, q + 64, acc0);
-    acc1 = dot8(a3, q + 96, acc1);
+  for (int b = 0; 4 * b < per_lane; ++b) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int idx = 4 * (b + 1) + i;
+      nxt[i] = idx < per_lane ? __ldg(xr + 32 * idx) : make_uint4(0, 0, 0, 0);
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int idx = 4 * b + i;
+      if (idx < per_lane) {
+        if (i & 1) acc1 = dot8(cur[i], lane + 32 * idx, acc1);
+        else acc0 = dot8(cur[i], lane + 32 * idx, acc0);
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) cur[i] = nxt[i];
   }
-  for (; q < nq; q += 32) acc0 = dot8(__ldg(xr + q), q, acc0);
   float acc = acc0 + acc1;
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
   if (lane == 0) {
