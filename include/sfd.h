@@ -77,6 +77,21 @@ typedef struct sfd_options {
     int precond_half;     /* mixed: apply the preconditioner from an FP16 copy (1)       */
 } sfd_options;
 
+/* Optomechanical drive of a helium film, nondimensional (the reference's
+ * OptomechanicalVariables after adimensionalizeOptomechanicalVariables,
+ * Export.cu:1248-1270).  Per node, with the intensity
+ *   I(y, x) = gamma^2 max_intensity / 4 / ((detuning - G y)^2 + (gamma/2)^2)
+ *             * exp(-(x - x0)^2 / (2 sigma^2))      (LightIntensity.cuh:25-31)
+ * the helium Bernoulli gains damping * v + strength * I
+ * (HeliumDrivenAutonomousProblem.cuh:20-26, createM.cuh:141-158), and with
+ * augmented != 0 the state carries the delayed intensity D as a fourth block:
+ * dphi += D, dD/dt = beta I - D / tau (DelayedIntensityIntegrator.cuh:22-36). */
+typedef struct sfd_drive {
+    double detuning, gamma, G, tau, max_intensity, x0, sigma, beta, damping;
+    double strength;      /* prefactor of I in dphi/dt (LightIntensity.cuh:34-37)     */
+    int augmented;        /* 1: state [x | y | phi | D], RHS [dx | dy | dphi | dD]    */
+} sfd_drive;
+
 typedef struct sfd_engine sfd_engine;
 
 /* ------------------------------------------------------------ engine API */
@@ -91,6 +106,13 @@ void sfd_default_problem(sfd_problem* prob);   /* water, rho = 0, g = 1 */
  * (BaseBoundaryIntegrator.cuh:88-108, AutonomousRungeKuttaStepper.cuh:91-105). */
 int sfd_create(const int* n, int nsurf, const sfd_problem* problems, int shared_problem,
                const sfd_options* opts, sfd_engine** out);
+/* As sfd_create, with an optomechanical drive per surface (`drives` follows
+ * `shared_problem` like `problems`; NULL = no drive).  Drives need helium
+ * surfaces with the standard Bernoulli closure.  If any drive is augmented
+ * the engine state gains the delayed-intensity block D (zero for undriven
+ * surfaces), set and read with sfd_set_aux_host / sfd_get_aux_host. */
+int sfd_create_driven(const int* n, int nsurf, const sfd_problem* problems, const sfd_drive* drives,
+                      int shared_problem, const sfd_options* opts, sfd_engine** out);
 int sfd_destroy(sfd_engine* e);
 /* Use a caller stream (0 = the engine's own). */
 int sfd_set_stream(sfd_engine* e, void* cuda_stream);
@@ -104,6 +126,9 @@ int sfd_total_nodes(const sfd_engine* e);
 /* State = concatenated per-surface nodes, SoA: x[ntot], y[ntot], phi[ntot]. */
 int sfd_set_state_host(sfd_engine* e, const double* x, const double* y, const double* phi);
 int sfd_get_state_host(sfd_engine* e, double* x, double* y, double* phi);
+/* Delayed-intensity block D[ntot] of an augmented engine. */
+int sfd_set_aux_host(sfd_engine* e, const double* D);
+int sfd_get_aux_host(sfd_engine* e, double* D);
 /* Same with device pointers (each ntot doubles). */
 int sfd_set_state_device(sfd_engine* e, const void* x, const void* y, const void* phi);
 int sfd_get_state_device(sfd_engine* e, void* x, void* y, void* phi);
@@ -239,6 +264,32 @@ int integrateSimulationRK4(double* initialState, double** statesOut, size_t* sta
                            size_t* timesCount, SimProperties* simProperties, RK4SolverOptions* rkOptions, size_t N);
 /* Export.cuh:70 */
 int integrateSimulationRK4_freeMemory(double* statesOut, double* timesOut);
+
+/* COptomechanicalVariables (ExportTypes.cuh:41-63), SI units. */
+typedef struct COptomechanicalVariables {
+    double detuning;
+    double gamma;
+    double G;
+    double tau;
+    double max_intensity;
+    double initial_time;
+    double location_x0_mode;
+    double sigma_optical_mode;
+    double beta;
+    double damping_strength;
+} COptomechanicalVariables;
+/* Export.cuh:79 (Export.cu:1108-1181): RHS of the augmented driven helium
+ * problem; state = [x | y | phi | D] (4N), rhs likewise. */
+int calculateRhsAugmentedOptomechanical(double* state, double* rhs, SimProperties* simProperties,
+                                        COptomechanicalVariables* optomechanicalVariables, size_t N);
+/* Export.cuh:75 (Export.cu:980-1092): RK4 of the augmented driven helium
+ * problem from t0 to t1; initialState and every returned state = [x | y | phi | D]. */
+int integrateAugmentedOptomechanicalSimulationRK4(double* initialState, double** statesOut, size_t* statesCount,
+                                                  double** timesOut, size_t* timesCount,
+                                                  SimProperties* simProperties, RK4SolverOptions* rkOptions,
+                                                  COptomechanicalVariables* optomechanicalVariables, size_t N);
+/* Export.cuh:76 */
+int integrateAugmentedOptomechanicalSimulationRK4_freeMemory(double* statesOut, double* timesOut);
 
 #ifdef __cplusplus
 }

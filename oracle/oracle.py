@@ -65,6 +65,32 @@ class Problem:
                          1 if self.infinite_depth else 0)
 
 
+class _CDrive(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_double) for k in ("detuning", "gamma", "G", "tau", "max_intensity", "x0", "sigma",
+                                                 "beta", "damping", "strength")] + [("augmented", ctypes.c_int)]
+
+
+@dataclass
+class Drive:
+    """Optomechanical drive (nondimensional), see orc_drive in sfd_oracle.c."""
+
+    detuning: float = 0.0
+    gamma: float = 1.0
+    G: float = 1.0
+    tau: float = 1.0
+    max_intensity: float = 0.0
+    x0: float = 0.0
+    sigma: float = 1.0
+    beta: float = 0.0
+    damping: float = 0.0
+    strength: float = 0.0
+    augmented: bool = True
+
+    def to_c(self) -> _CDrive:
+        return _CDrive(self.detuning, self.gamma, self.G, self.tau, self.max_intensity, self.x0, self.sigma,
+                       self.beta, self.damping, self.strength, 1 if self.augmented else 0)
+
+
 def build(force: bool = False) -> str:
     """Compile the oracle into oracle/_build (gcc, OpenMP, no -march flags)."""
     os.makedirs(_BUILD, exist_ok=True)
@@ -106,6 +132,13 @@ def lib() -> ctypes.CDLL:
         L.orc_rk4_steps.argtypes = [pp, ctypes.c_int, ctypes.c_double, ctypes.c_int, dp, dp, dp]
         L.orc_rk4_steps.restype = ctypes.c_int
         L.orc_invariants.argtypes = [pp, ctypes.c_int, dp, dp, dp, dp, dp, ctypes.c_double, dp]
+        dr = ctypes.POINTER(_CDrive)
+        L.orc_intensity.argtypes = [dr, ctypes.c_double, ctypes.c_double]
+        L.orc_intensity.restype = ctypes.c_double
+        L.orc_rhs_driven.argtypes = [pp, dr, ctypes.c_int, dp, dp, dp, dp, dp, dp, dp, dp]
+        L.orc_rhs_driven.restype = ctypes.c_int
+        L.orc_rk4_steps_driven.argtypes = [pp, dr, ctypes.c_int, ctypes.c_double, ctypes.c_int, dp, dp, dp, dp]
+        L.orc_rk4_steps_driven.restype = ctypes.c_int
         L.orc_cot_green.argtypes = [ctypes.c_double] * 4 + [dp]
         L.orc_set_threads.argtypes = [ctypes.c_int]
         L.orc_set_threads.restype = ctypes.c_int
@@ -227,6 +260,28 @@ def rk4_steps(problem: Problem, x, y, phi, dt: float, steps: int):
     cp = problem.to_c()
     info = lib().orc_rk4_steps(ctypes.byref(cp), x.size, float(dt), int(steps), _dp(x), _dp(y), _dp(phi))
     return (x, y, phi), info
+
+
+def rhs_driven(problem: Problem, drive: Drive, x, y, phi, dl=None):
+    """Driven helium RHS: (dx, dy, dphi[, dD]) and the LU info."""
+    x, y, phi = _f64(x), _f64(y), _f64(phi)
+    n = x.size
+    dl = _f64(dl if dl is not None else np.zeros(n))
+    dx, dy, dphi, ddl = (np.empty(n) for _ in range(4))
+    cp, cd = problem.to_c(), drive.to_c()
+    info = lib().orc_rhs_driven(ctypes.byref(cp), ctypes.byref(cd), n, _dp(x), _dp(y), _dp(phi), _dp(dl),
+                                _dp(dx), _dp(dy), _dp(dphi), _dp(ddl))
+    out = (dx, dy, dphi, ddl) if drive.augmented else (dx, dy, dphi)
+    return out, info
+
+
+def rk4_steps_driven(problem: Problem, drive: Drive, x, y, phi, dl, dt: float, steps: int):
+    x, y, phi = _f64(x).copy(), _f64(y).copy(), _f64(phi).copy()
+    dl = _f64(dl if dl is not None else np.zeros(x.size)).copy()
+    cp, cd = problem.to_c(), drive.to_c()
+    info = lib().orc_rk4_steps_driven(ctypes.byref(cp), ctypes.byref(cd), x.size, float(dt), int(steps),
+                                      _dp(x), _dp(y), _dp(phi), _dp(dl))
+    return (x, y, phi, dl), info
 
 
 def invariants(problem: Problem, x, y, phi, u, v, kappa: float = 0.0) -> np.ndarray:

@@ -448,6 +448,85 @@ int orc_rk4_steps(const orc_problem* P, int n, double dt, int steps, double* x, 
 }
 
 /* ------------------------------------------------------------------ */
+/* Optomechanical drive of a helium film (nondimensional parameters).   */
+/*   intensity (CSH/LightIntensity.cuh:25-31):                          */
+/*     I(y, x) = gamma^2 I_max / 4 / ((detuning - G y)^2 + (gamma/2)^2)  */
+/*               * exp(-(x - x0)^2 / (2 sigma^2))                        */
+/*   dphi += damping * v + strength * I      (CSH/createM.cuh:141-158,   */
+/*           HeliumDrivenAutonomousProblem.cuh:20-26; v = Im of the      */
+/*           lower velocity)                                            */
+/*   augmented state D (CSH/DelayedIntensityIntegrator.cuh:22-36,        */
+/*           CSH/createM.cuh:160-178): dphi += D, dD = beta I - D / tau  */
+/* ------------------------------------------------------------------ */
+typedef struct {
+    double detuning, gamma, G, tau, max_intensity, x0, sigma, beta, damping, strength;
+    int augmented;
+} orc_drive;
+
+double orc_intensity(const orc_drive* D, double y, double x) {
+    double df = D->detuning - D->G * y;
+    double prof = exp(-pow(x - D->x0, 2.0) / (2.0 * pow(D->sigma, 2.0)));
+    return 0.25 * pow(D->gamma, 2.0) * D->max_intensity / (pow(df, 2.0) + pow(D->gamma / 2.0, 2.0)) * prof;
+}
+
+/* Driven RHS on [x, y, phi (, D)] -> [dx, dy, dphi (, dD)] (dl / ddl used  */
+/* only when augmented).                                                 */
+int orc_rhs_driven(const orc_problem* P, const orc_drive* D, int n, const double* x, const double* y,
+                   const double* phi, const double* dl, double* dx, double* dy, double* dphi, double* ddl) {
+    int info = orc_rhs(P, n, x, y, phi, dx, dy, dphi, NULL, NULL, NULL);
+    for (int i = 0; i < n; ++i) {
+        double inten = orc_intensity(D, y[i], x[i]);
+        dphi[i] += D->damping * dy[i];
+        dphi[i] += D->strength * inten;
+        if (D->augmented) {
+            dphi[i] += dl[i];
+            ddl[i] = D->beta * inten - 1.0 / D->tau * dl[i];
+        }
+    }
+    return info;
+}
+
+/* Classic RK4 of the driven problem on [x, y, phi (, D)] (same stage     */
+/* formula as orc_rk4_step).                                             */
+int orc_rk4_steps_driven(const orc_problem* P, const orc_drive* D, int n, double dt, int steps, double* x,
+                         double* y, double* phi, double* dl) {
+    const int nb = D->augmented ? 4 : 3;
+    size_t sz = sizeof(double) * nb * (size_t)n;
+    double* Y0 = (double*)malloc(sz);
+    double* Y = (double*)malloc(sz);
+    double* k[4];
+    for (int s = 0; s < 4; ++s) k[s] = (double*)calloc((size_t)nb * n, sizeof(double));
+    memcpy(Y0, x, sizeof(double) * n);
+    memcpy(Y0 + n, y, sizeof(double) * n);
+    memcpy(Y0 + 2 * n, phi, sizeof(double) * n);
+    if (D->augmented) memcpy(Y0 + 3 * n, dl, sizeof(double) * n);
+    int info = 0;
+    const double half = dt * 0.5, full = dt, sixth = dt / 6.0;
+    const double coef[3] = {half, half, full};
+    for (int st = 0; st < steps; ++st) {
+        memcpy(Y, Y0, sz);
+        for (int s = 0; s < 4; ++s) {
+            int r = orc_rhs_driven(P, D, n, Y, Y + n, Y + 2 * n, Y + 3 * n, k[s], k[s] + n, k[s] + 2 * n,
+                                   D->augmented ? k[s] + 3 * n : NULL);
+            if (r && !info) info = r;
+            if (s < 3)
+                for (int i = 0; i < nb * n; ++i) Y[i] = Y0[i] + coef[s] * k[s][i];
+        }
+        for (int i = 0; i < nb * n; ++i) {
+            double kk = k[0][i] + 2.0 * k[1][i] + 2.0 * k[2][i] + k[3][i];
+            Y0[i] = Y0[i] + sixth * kk;
+        }
+    }
+    memcpy(x, Y0, sizeof(double) * n);
+    memcpy(y, Y0 + n, sizeof(double) * n);
+    memcpy(phi, Y0 + 2 * n, sizeof(double) * n);
+    if (D->augmented) memcpy(dl, Y0 + 3 * n, sizeof(double) * n);
+    free(Y0); free(Y);
+    for (int s = 0; s < 4; ++s) free(k[s]);
+    return info;
+}
+
+/* ------------------------------------------------------------------ */
 /* Invariants (CSH/Energies.cuh:136-204 and scalings :61-128), with U=0 */
 /* out[0] kinetic   = (1/4pi) sum phi (x' v - y' u)                     */
 /* out[1] potential = water (1+rho) g/(4pi) sum y^2 x'  |  helium       */

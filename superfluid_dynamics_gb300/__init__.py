@@ -3,9 +3,9 @@ CuSuperHelium RHS / RK4 path).  The compute lives in libsfd.so (CUDA, sm_103a)
 behind the C ABI of include/sfd.h; this package is the Python host side."""
 from ._lib import (HELIUM, PRECISION_FP64, PRECISION_MIXED, WATER, SfdError,  # noqa: F401
                    load as load_library)
-from .engine import (AutonomousRungeKuttaStepper, BoundaryIntegralCalculator, Engine,  # noqa: F401
+from .engine import (AutonomousRungeKuttaStepper, BoundaryIntegralCalculator, Drive, Engine,  # noqa: F401
                      HeliumBoundaryProblem, Options, Physics, SimulationManager, WaterBoundaryProblem)
 
-__all__ = ["Engine", "Options", "Physics", "WaterBoundaryProblem", "HeliumBoundaryProblem",
+__all__ = ["Engine", "Options", "Physics", "Drive", "WaterBoundaryProblem", "HeliumBoundaryProblem",
            "BoundaryIntegralCalculator", "AutonomousRungeKuttaStepper", "SimulationManager",
            "WATER", "HELIUM", "PRECISION_FP64", "PRECISION_MIXED", "SfdError", "load_library"]

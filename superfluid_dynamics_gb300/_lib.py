@@ -48,6 +48,18 @@ class RK4SolverOptions(ctypes.Structure):
     _fields_ = [("timeStep", c_double), ("t0", c_double), ("t1", c_double), ("returnTrajectory", c_bool)]
 
 
+class SfdDrive(ctypes.Structure):
+    """sfd_drive (include/sfd.h): nondimensional optomechanical drive."""
+    _fields_ = [(k, c_double) for k in ("detuning", "gamma", "G", "tau", "max_intensity", "x0", "sigma", "beta",
+                                        "damping", "strength")] + [("augmented", c_int)]
+
+
+class COptomechanicalVariables(ctypes.Structure):
+    """ExportTypes.cuh:41-63 (SI units; the field order rhs.py binds)."""
+    _fields_ = [(k, c_double) for k in ("detuning", "gamma", "G", "tau", "max_intensity", "initial_time",
+                                        "location_x0_mode", "sigma_optical_mode", "beta", "damping_strength")]
+
+
 _dp = POINTER(c_double)
 _SIGS = {
     "sfd_default_options": (None, [POINTER(SfdOptions)]),
@@ -78,6 +90,17 @@ _SIGS = {
     "sfd_set_default_precision": (c_int, [c_int]),
     "sfd_rhs_device_noalloc": (c_int, [POINTER(SfdProblem), c_int, c_void_p, c_void_p, c_void_p]),
     "sfd_set_problem": (c_int, [c_void_p, c_int, POINTER(SfdProblem)]),
+    "sfd_create_driven": (c_int, [POINTER(c_int), c_int, POINTER(SfdProblem), POINTER(SfdDrive), c_int,
+                                  POINTER(SfdOptions), POINTER(c_void_p)]),
+    "sfd_set_aux_host": (c_int, [c_void_p, _dp]),
+    "sfd_get_aux_host": (c_int, [c_void_p, _dp]),
+    "calculateRhsAugmentedOptomechanical": (c_int, [_dp, _dp, POINTER(SimProperties),
+                                                    POINTER(COptomechanicalVariables), c_size_t]),
+    "integrateAugmentedOptomechanicalSimulationRK4": (c_int, [_dp, POINTER(_dp), POINTER(c_size_t), POINTER(_dp),
+                                                              POINTER(c_size_t), POINTER(SimProperties),
+                                                              POINTER(RK4SolverOptions),
+                                                              POINTER(COptomechanicalVariables), c_size_t]),
+    "integrateAugmentedOptomechanicalSimulationRK4_freeMemory": (c_int, [_dp, _dp]),
     "sfd_rhs_vjp_device": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, _dp]),
     "sfd_rk4_record": (c_int, [c_void_p, c_double, c_int, c_int, _dp, _dp]),
     "sfd_rk4_vjp": (c_int, [c_void_p, _dp, _dp, _dp]),

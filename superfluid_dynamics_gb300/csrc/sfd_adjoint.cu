@@ -428,6 +428,7 @@ int check_engine(sfd_engine* e) {
   if (S.physics == 1 && S.bern_variant != 0)
     return sfd_internal_error(SFD_ERR_INVALID, "reverse mode supports the standard helium Bernoulli closure only");
   if (S.U != 0.0) return sfd_internal_error(SFD_ERR_INVALID, "reverse mode supports U = 0 only");
+  if (S.drive) return sfd_internal_error(SFD_ERR_INVALID, "reverse mode does not cover the optomechanical drive");
   return 0;
 }
 

@@ -287,14 +287,15 @@ int enqueue_rhs(sfd_engine* e, const double* st, double* out, bool refactor) {
     LAUNCHC(e, SFD_K_SPECTRAL,
             sfd_launch_spectral_cluster(D, e->d_cjobs_ap, e->ncjobs_ap, e->max_n_cluster, e->stream));
   VelArgs V{e->d_surf, e->d_node_surf, e->nsurf, nt, e->cacc, e->dacc, e->a, e->ap, e->nd.v1low, e->nd.v1up,
-            e->nd.v2, y, e->zp, e->zpp, e->vel_low1, out, out + nt, out + 2 * nt, e->status};
+            e->nd.v2, y, st, e->nblk == 4 ? st + 3 * nt : nullptr, e->nblk == 4 ? out + 3 * nt : nullptr,
+            e->zp, e->zpp, e->vel_low1, out, out + nt, out + 2 * nt, e->status};
   if (e->any_rho) LAUNCHC(e, SFD_K_VELOCITY, k_velocity_node1<<<1, 32, 0, e->stream>>>(V));
   LAUNCHC(e, SFD_K_VELOCITY, k_velocity_bernoulli<<<blocks_for(nt, 32), 32, 0, e->stream>>>(V));
   return 0;
 }
 
 int enqueue_step(sfd_engine* e, double dt, bool refactor) {
-  const int n3 = 3 * e->ntot;
+  const int n3 = e->nblk * e->ntot;  // [x | y | phi (| D)]
   const int nb = blocks_for(n3, 256);
   const double wk[4] = {1.0, 2.0, 2.0, 1.0};
   const double cy[4] = {dt * 0.5, dt * 0.5, dt, 0.0};
@@ -416,6 +417,26 @@ int fill_surface(SurfaceDesc& S, const sfd_problem& p) {
   return 0;
 }
 
+// Optomechanical drive of one surface (HeliumDrivenAutonomousProblem.cuh:10-28).
+int fill_drive(SurfaceDesc& S, const sfd_drive& d) {
+  S.drive = 1;
+  S.drive_aug = d.augmented ? 1 : 0;
+  if (S.physics != SFD_HELIUM) return set_error(SFD_ERR_INVALID, "a drive needs a helium surface");
+  if (!(d.sigma != 0.0) || (d.augmented && !(d.tau != 0.0)))
+    return set_error(SFD_ERR_INVALID, "drive: sigma and (augmented) tau must be nonzero");
+  S.dr_detuning = d.detuning;
+  S.dr_gamma = d.gamma;
+  S.dr_G = d.G;
+  S.dr_tau = d.tau;
+  S.dr_imax = d.max_intensity;
+  S.dr_x0 = d.x0;
+  S.dr_sigma = d.sigma;
+  S.dr_beta = d.beta;
+  S.dr_damping = d.damping;
+  S.dr_strength = d.strength;
+  return 0;
+}
+
 }  // namespace
 
 int sfd_internal_error(int code, const char* msg) { return set_error(code, "%s", msg); }
@@ -459,6 +480,11 @@ int sfd_set_default_precision(int precision) {
 
 int sfd_create(const int* n, int nsurf, const sfd_problem* problems, int shared_problem, const sfd_options* opts,
                sfd_engine** out) {
+  return sfd_create_driven(n, nsurf, problems, nullptr, shared_problem, opts, out);
+}
+
+int sfd_create_driven(const int* n, int nsurf, const sfd_problem* problems, const sfd_drive* drives,
+                      int shared_problem, const sfd_options* opts, sfd_engine** out) {
   if (!out || !n || !problems || nsurf <= 0) return set_error(SFD_ERR_INVALID, "sfd_create: bad arguments");
   *out = nullptr;
   int ndev = 0;
@@ -507,10 +533,12 @@ int sfd_create(const int* n, int nsurf, const sfd_problem* problems, int shared_
     S.off = (int)off;
     S.moff = moff;
     rc = fill_surface(S, problems[shared_problem ? 0 : s]);
+    if (!rc && drives) rc = fill_drive(S, drives[shared_problem ? 0 : s]);
     if (rc) {
       free_engine(e);
       return rc;
     }
+    if (S.drive_aug) e->nblk = 4;
     std::vector<int> rad;
     if (!factorize(ns, rad)) {
       free_engine(e);
@@ -607,10 +635,10 @@ int sfd_create(const int* n, int nsurf, const sfd_problem* problems, int shared_
   CKE(dalloc(&e->d_poff, nsurf));
   CKE(cudaMemcpy(e->d_poff, h_poff.data(), nsurf * sizeof(long long), cudaMemcpyHostToDevice));
   // buffers
-  CKE(dalloc(&e->y0, 3LL * nt));
-  CKE(dalloc(&e->ys, 3LL * nt));
-  CKE(dalloc(&e->kacc, 3LL * nt));
-  CKE(dalloc(&e->kcur, 3LL * nt));
+  CKE(dalloc(&e->y0, (long long)e->nblk * nt));
+  CKE(dalloc(&e->ys, (long long)e->nblk * nt));
+  CKE(dalloc(&e->kacc, (long long)e->nblk * nt));
+  CKE(dalloc(&e->kcur, (long long)e->nblk * nt));
   CKE(dalloc(&e->zp, nt));
   CKE(dalloc(&e->zpp, nt));
   CKE(dalloc(&e->ap, nt));
@@ -638,7 +666,7 @@ int sfd_create(const int* n, int nsurf, const sfd_problem* problems, int shared_
   CKE(cudaMemset(e->status, 0, nsurf * sizeof(unsigned int)));
   CKE(cudaMemset(e->lmax, 0, nsurf * sizeof(double)));
   CKE(cudaMemset(e->rnorm, 0, nsurf * sizeof(double)));
-  CKE(cudaMemset(e->y0, 0, 3LL * nt * sizeof(double)));
+  CKE(cudaMemset(e->y0, 0, (long long)e->nblk * nt * sizeof(double)));
   CKE(cudaMemset(e->nd.p, 0, nt * sizeof(cd)));
   CKE(cudaMemset(e->nd.pdf, 0, nt * sizeof(float4)));
   CKE(cudaMemset(e->dacc, 0, nt * sizeof(cd)));
@@ -715,6 +743,24 @@ int sfd_get_state_host(sfd_engine* e, double* x, double* y, double* phi) {
   CK(cudaMemcpyAsync(x, e->y0, b, cudaMemcpyDeviceToHost, e->stream));
   CK(cudaMemcpyAsync(y, e->y0 + e->ntot, b, cudaMemcpyDeviceToHost, e->stream));
   CK(cudaMemcpyAsync(phi, e->y0 + 2 * e->ntot, b, cudaMemcpyDeviceToHost, e->stream));
+  CK(cudaStreamSynchronize(e->stream));
+  return 0;
+}
+
+int sfd_set_aux_host(sfd_engine* e, const double* D) {
+  if (!e || !D) return set_error(SFD_ERR_INVALID, "null argument");
+  if (e->nblk != 4) return set_error(SFD_ERR_INVALID, "the engine has no delayed-intensity block (no augmented drive)");
+  CK(cudaSetDevice(e->device));
+  CK(cudaMemcpyAsync(e->y0 + 3LL * e->ntot, D, e->ntot * sizeof(double), cudaMemcpyHostToDevice, e->stream));
+  CK(cudaStreamSynchronize(e->stream));
+  return 0;
+}
+
+int sfd_get_aux_host(sfd_engine* e, double* D) {
+  if (!e || !D) return set_error(SFD_ERR_INVALID, "null argument");
+  if (e->nblk != 4) return set_error(SFD_ERR_INVALID, "the engine has no delayed-intensity block (no augmented drive)");
+  CK(cudaSetDevice(e->device));
+  CK(cudaMemcpyAsync(D, e->y0 + 3LL * e->ntot, e->ntot * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
   CK(cudaStreamSynchronize(e->stream));
   return 0;
 }
@@ -863,7 +909,7 @@ constexpr double kAlphaHamaker = 3.5e-24;  // constants.cuh:15
 constexpr double kRhoHelium = 150.0;       // Export.cuh:82 default
 
 struct NondimProps {
-  double depth, rho, kappa, base_time;
+  double depth, rho, kappa, base_time, base_length, base_energy;
 };
 
 // adimensionalizeProperties (Export.cu:1222-1246) without the console output.
@@ -872,6 +918,8 @@ NondimProps adimensionalize(double L, double rho, double kappa, double depth) {
   double base_length = L / (2.0 * kPi);
   double base_acc = 3 * kAlphaHamaker / std::pow(depth, 4);
   p.base_time = std::sqrt(base_length / base_acc);
+  p.base_length = base_length;
+  p.base_energy = 3.0 * kRhoHelium * kAlphaHamaker * std::pow(base_length, 4) / std::pow(depth, 4);
   double stf = kRhoHelium * base_length * base_length * base_length / (p.base_time * p.base_time);
   p.kappa = kappa / stf;
   p.depth = depth / base_length;
@@ -893,13 +941,36 @@ sfd_problem helium_problem(const NondimProps& np, bool use_exp = false, int orde
   return p;
 }
 
-int make_engine(int n, int batch, const sfd_problem& p, sfd_engine** e) {
+int make_engine(int n, int batch, const sfd_problem& p, sfd_engine** e, const sfd_drive* drive = nullptr) {
   sfd_options o;
   sfd_default_options(&o);
   o.precision = g_default_precision;
   o.use_graphs = 0;
   std::vector<int> ns(batch, n);
-  return sfd_create(ns.data(), batch, &p, 1, &o, e);
+  return sfd_create_driven(ns.data(), batch, &p, drive, 1, &o, e);
+}
+
+constexpr double kHbar = 1.054571817e-34;  // constants.cuh:10
+
+// adimensionalizeOptomechanicalVariables (Export.cu:1248-1270) and the
+// instantaneous-intensity prefactor get_current_intensity_drive_strength
+// (LightIntensity.cuh:34-37), for the augmented driven problem.
+sfd_drive optomech_drive(const COptomechanicalVariables& v, const NondimProps& np) {
+  sfd_drive d;
+  std::memset(&d, 0, sizeof(d));
+  d.gamma = v.gamma * np.base_time;
+  d.detuning = v.detuning * np.base_time;
+  d.G = v.G * np.base_time * np.base_length;
+  d.tau = v.tau / np.base_time;
+  d.x0 = v.location_x0_mode / np.base_length;
+  d.sigma = v.sigma_optical_mode / np.base_length;
+  const double hbar_adim = kHbar / np.base_energy / np.base_time;
+  d.beta = v.beta * hbar_adim * d.G / d.tau / (d.sigma * d.sigma * np.rho);
+  d.max_intensity = v.max_intensity;  // not rescaled by the reference either
+  d.damping = v.damping_strength;
+  d.strength = kHbar / (np.base_energy * np.base_time * np.rho) * d.G / (d.sigma * d.sigma);
+  d.augmented = 1;
+  return d;
 }
 
 int rhs_from_vectors(const double* x, const double* y, const double* phi, double* vx, double* vy, double* rhsPhi,
@@ -1062,6 +1133,94 @@ int integrateSimulationRK4(double* initialState, double** statesOut, size_t* sta
 }
 
 int integrateSimulationRK4_freeMemory(double* statesOut, double* timesOut) {
+  std::free(statesOut);
+  std::free(timesOut);
+  return 0;
+}
+
+int calculateRhsAugmentedOptomechanical(double* state, double* rhs, SimProperties* sp, COptomechanicalVariables* ov,
+                                        size_t N) {
+  if (!state || !rhs || !sp || !ov) return set_error(SFD_ERR_INVALID, "null argument");
+  if (N < 1 || N > 8192) return set_error(SFD_ERR_INVALID, "unsupported N %zu", N);
+  NondimProps np = adimensionalize(sp->L, sp->rho, sp->kappa, sp->depth);
+  sfd_drive d = optomech_drive(*ov, np);
+  sfd_engine* e = nullptr;
+  int rc = make_engine((int)N, 1, helium_problem(np, sp->use_expansions, sp->expansion_order, sp->infinite_depth),
+                       &e, &d);
+  if (rc) return rc;
+  const size_t n4 = 4 * N;
+  rc = sfd_set_state_host(e, state, state + N, state + 2 * N);
+  if (!rc) rc = sfd_set_aux_host(e, state + 3 * N);
+  if (!rc) rc = sfd_rhs_device(e, e->y0, e->kcur);
+  if (!rc) {
+    cudaError_t err = cudaMemcpyAsync(rhs, e->kcur, n4 * sizeof(double), cudaMemcpyDeviceToHost, e->stream);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(e->stream);
+    if (err != cudaSuccess) rc = sfd_fail(err);
+  }
+  sfd_destroy(e);
+  return rc;
+}
+
+int integrateAugmentedOptomechanicalSimulationRK4(double* initialState, double** statesOut, size_t* statesCount,
+                                                  double** timesOut, size_t* timesCount, SimProperties* sp,
+                                                  RK4SolverOptions* ro, COptomechanicalVariables* ov, size_t N) {
+  if (!initialState || !statesOut || !statesCount || !timesOut || !timesCount || !sp || !ro || !ov)
+    return set_error(SFD_ERR_INVALID, "null argument");
+  if (N < 1 || N > 8192) return set_error(SFD_ERR_INVALID, "unsupported N %zu", N);
+  NondimProps np = adimensionalize(sp->L, sp->rho, sp->kappa, sp->depth);
+  sfd_drive d = optomech_drive(*ov, np);
+  double dt = ro->timeStep / np.base_time, t0 = ro->t0 / np.base_time, t1 = ro->t1 / np.base_time;
+  if (!(dt > 0)) return set_error(SFD_ERR_INVALID, "timeStep must be > 0");
+  size_t steps = (size_t)((t1 - t0) / dt);  // runEvolution (AutonomousRungeKuttaStepper.cuh:421)
+  sfd_engine* e = nullptr;
+  int rc = make_engine((int)N, 1, helium_problem(np, sp->use_expansions, sp->expansion_order, sp->infinite_depth),
+                       &e, &d);
+  if (rc) return rc;
+  e->opt.use_graphs = 1;
+  const size_t n4 = 4 * N;
+  size_t nstates = ro->returnTrajectory ? steps + 1 : 1;
+  double* states = (double*)std::malloc(nstates * n4 * sizeof(double));
+  double* times = ro->returnTrajectory ? (double*)std::malloc(nstates * sizeof(double)) : nullptr;
+  if (!states || (ro->returnTrajectory && !times)) {
+    std::free(states);
+    std::free(times);
+    sfd_destroy(e);
+    return set_error(SFD_ERR_INVALID, "host allocation failed");
+  }
+  rc = sfd_set_state_host(e, initialState, initialState + N, initialState + 2 * N);
+  if (!rc) rc = sfd_set_aux_host(e, initialState + 3 * N);
+  double t = t0;
+  if (!rc && ro->returnTrajectory) {
+    std::memcpy(states, initialState, n4 * sizeof(double));
+    times[0] = t;
+  }
+  auto fetch = [&](double* dst) {
+    int r = sfd_get_state_host(e, dst, dst + N, dst + 2 * N);
+    return r ? r : sfd_get_aux_host(e, dst + 3 * N);
+  };
+  for (size_t s = 0; s < steps && !rc; ++s) {
+    rc = sfd_rk4_steps_async(e, dt, 1);
+    t += dt;
+    if (!rc && ro->returnTrajectory) {
+      rc = fetch(states + (s + 1) * n4);
+      times[s + 1] = t;
+    }
+  }
+  if (!rc && !ro->returnTrajectory) rc = fetch(states);
+  sfd_destroy(e);
+  if (rc) {
+    std::free(states);
+    std::free(times);
+    return rc;
+  }
+  *statesOut = states;
+  *statesCount = nstates;
+  *timesOut = times;
+  *timesCount = ro->returnTrajectory ? nstates : 0;
+  return 0;
+}
+
+int integrateAugmentedOptomechanicalSimulationRK4_freeMemory(double* statesOut, double* timesOut) {
   std::free(statesOut);
   std::free(timesOut);
   return 0;

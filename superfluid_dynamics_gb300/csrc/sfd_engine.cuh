@@ -27,6 +27,10 @@ struct SurfaceDesc {
   int rad[SFD_MAX_RADICES];
   int nrad_m;           // radices of n / SFD_FFT_CLUSTER (cluster transforms; 0 = not eligible)
   int rad_m[SFD_MAX_RADICES];
+  // optomechanical drive (helium; LightIntensity.cuh:19-37, DelayedIntensityIntegrator.cuh:22-36)
+  int drive;            // 0 none, 1 drive terms in dphi/dt
+  int drive_aug;        // delayed intensity D carried in the state
+  double dr_detuning, dr_gamma, dr_G, dr_tau, dr_imax, dr_x0, dr_sigma, dr_beta, dr_damping, dr_strength;
 };
 
 // Cluster size of the distributed spectral-derivative kernel; surfaces with

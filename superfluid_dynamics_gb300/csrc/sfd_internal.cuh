@@ -41,6 +41,7 @@ struct sfd_engine {
   cudaStream_t own_stream = nullptr;
   sfd_options opt{};
   int nsurf = 0, ntot = 0, max_n = 0, max_np = 0;
+  int nblk = 3;  // state blocks: [x | y | phi] or, with an augmented drive, [x | y | phi | D]
   long long mat_elems = 0, panel_elems = 0;
   bool any_rho = false;
   std::vector<SurfaceDesc> hs;

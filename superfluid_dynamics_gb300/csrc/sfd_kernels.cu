@@ -407,7 +407,8 @@ cudaError_t sfd_launch_sums(int prec, const SumArgs& A, int nitems, int max_n, c
 //   vel_k = conj(-(i/4pi) C_k + [image] (i/4pi) D_k + V1_kk a_k + V2_k a'_k)   (lower)
 //   water:  dphi = -(1+rho) g y + |v|^2/2 + rho |v_up|^2/2 - rho (u_low[1] u_up + v_low v_up)
 //   helium: dphi = vdw (1 + y/h)^-3 - vdw + |v|^2/2
-// Output goes to the RHS slot (dx, dy, dphi).  Status bit on non-finite values.
+//   driven helium adds damping * v + strength * I(y, x) [+ D, dD = beta I - D / tau]
+// Output goes to the RHS slot (dx, dy, dphi [, dD]).  Status bit on non-finite values.
 __global__ void k_velocity_bernoulli(VelArgs V) {
   int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= V.ntot) return;
@@ -456,7 +457,24 @@ __global__ void k_velocity_bernoulli(VelArgs V) {
     double q = 1.0 + yk / S.depth;
     out = S.vdw * pow(q, -3.0) - S.vdw + 0.5 * low.re * low.re + 0.5 * low.im * low.im;
   }
+  if (S.drive) {
+    // optomechanical drive (helium): damping of the vertical velocity, the
+    // instantaneous intensity and, augmented, the delayed intensity D
+    const double df = S.dr_detuning - S.dr_G * yk;
+    const double dxk = V.x[g] - S.dr_x0;
+    const double prof = exp(-(dxk * dxk) / (2.0 * S.dr_sigma * S.dr_sigma));
+    const double inten =
+        0.25 * S.dr_gamma * S.dr_gamma * S.dr_imax / (df * df + 0.25 * S.dr_gamma * S.dr_gamma) * prof;
+    out += S.dr_damping * low.im;
+    out += S.dr_strength * inten;
+    if (S.drive_aug) {
+      const double Dk = V.aux[g];
+      out += Dk;
+      V.daux[g] = S.dr_beta * inten - 1.0 / S.dr_tau * Dk;
+    }
+  }
   V.dphi[g] = out;
+  if (V.daux && !S.drive_aug) V.daux[g] = 0.0;
   if (!isfinite(out) || !isfinite(low.re) || !isfinite(low.im)) atomicOr(V.status + s, SFD_ST_NONFINITE);
 }
 

@@ -57,6 +57,9 @@ struct VelArgs {
   const cd* v1up;
   const cd* v2;
   const double* y;
+  const double* x;      // drive profile
+  const double* aux;    // delayed intensity D (augmented drive; state block 4)
+  double* daux;         // dD/dt (RHS block 4)
   const cd* zp;
   const cd* zpp;
   cd* vel_low1;

@@ -58,6 +58,32 @@ class Physics:
 
 
 @dataclass
+class Drive:
+    """Optomechanical drive of a helium film, nondimensional (sfd_drive).
+
+    I(y, x) = gamma^2 max_intensity / 4 / ((detuning - G y)^2 + (gamma/2)^2) exp(-(x - x0)^2 / (2 sigma^2));
+    dphi/dt += damping * v + strength * I, and with `augmented` the state gains
+    the delayed intensity D: dphi/dt += D, dD/dt = beta I - D / tau
+    (HeliumDrivenAutonomousProblem.cuh, DelayedIntensityIntegrator.cuh)."""
+
+    detuning: float = 0.0
+    gamma: float = 1.0
+    G: float = 1.0
+    tau: float = 1.0
+    max_intensity: float = 0.0
+    x0: float = 0.0
+    sigma: float = 1.0
+    beta: float = 0.0
+    damping: float = 0.0
+    strength: float = 0.0
+    augmented: bool = True
+
+    def to_c(self) -> _lib.SfdDrive:
+        return _lib.SfdDrive(self.detuning, self.gamma, self.G, self.tau, self.max_intensity, self.x0, self.sigma,
+                             self.beta, self.damping, self.strength, 1 if self.augmented else 0)
+
+
+@dataclass
 class Options:
     precision: int = PRECISION_MIXED
     refine_iters: int = 2
@@ -77,7 +103,8 @@ class Options:
 class Engine:
     """A batch of surfaces (possibly of different N) resident in device memory."""
 
-    def __init__(self, n, physics: Physics | list[Physics] | None = None, options: Options | None = None):
+    def __init__(self, n, physics: Physics | list[Physics] | None = None, options: Options | None = None,
+                 drive: Drive | list[Drive] | None = None):
         L = _lib.load()
         ns = [int(n)] if np.isscalar(n) else [int(v) for v in n]
         if physics is None:
@@ -90,7 +117,15 @@ class Engine:
         narr = (ctypes.c_int * len(ns))(*ns)
         opt = (options or Options()).to_c()
         h = ctypes.c_void_p()
-        check(L.sfd_create(narr, len(ns), carr, 1 if shared else 0, ctypes.byref(opt), ctypes.byref(h)))
+        if drive is None:
+            check(L.sfd_create(narr, len(ns), carr, 1 if shared else 0, ctypes.byref(opt), ctypes.byref(h)))
+        else:
+            drs = [drive] if shared else (list(drive) if isinstance(drive, (list, tuple)) else [drive] * len(ns))
+            darr = (_lib.SfdDrive * len(drs))(*[d.to_c() for d in drs])
+            check(L.sfd_create_driven(narr, len(ns), carr, darr, 1 if shared else 0, ctypes.byref(opt),
+                                      ctypes.byref(h)))
+        self.augmented = drive is not None and any(
+            d.augmented for d in ([drive] if isinstance(drive, Drive) else drive))
         self._h = h
         self._L = L
         self.sizes = ns
@@ -128,6 +163,16 @@ class Engine:
         x, y, phi = (np.empty(self.ntot) for _ in range(3))
         check(self._L.sfd_get_state_host(self._h, _dp(x), _dp(y), _dp(phi)))
         return x, y, phi
+
+    def set_aux(self, D) -> None:
+        """Delayed-intensity block of an augmented driven engine."""
+        D = _f64(D)
+        check(self._L.sfd_set_aux_host(self._h, _dp(D)))
+
+    def get_aux(self) -> np.ndarray:
+        D = np.empty(self.ntot)
+        check(self._L.sfd_get_aux_host(self._h, _dp(D)))
+        return D
 
     def set_state_device(self, x_ptr: int, y_ptr: int, phi_ptr: int) -> None:
         check(self._L.sfd_set_state_device(self._h, x_ptr, y_ptr, phi_ptr))
@@ -370,3 +415,31 @@ class SimulationManager:
         T = np.ctypeslib.as_array(times, shape=(nt.value,)).copy() if nt.value else np.empty(0)
         self.lib.integrateSimulationRK4_freeMemory(states, times)
         return S, T
+
+    def calculate_augmented_rhs(self, y0, sim_props: _lib.SimProperties, opt_props: _lib.COptomechanicalVariables):
+        """rhs.py:348-358: RHS of [x | y | phi | D] for the augmented driven film (SI inputs)."""
+        y0 = _f64(y0)
+        rhs = np.empty_like(y0)
+        rc = self.lib.calculateRhsAugmentedOptomechanical(_dp(y0), _dp(rhs), ctypes.byref(sim_props),
+                                                          ctypes.byref(opt_props), y0.size // 4)
+        if rc != 0:
+            raise SfdError(self.lib.sfd_last_error().decode())
+        return rhs
+
+    def integrate_augmented_optomechanical_problem(self, y0, sim_props: _lib.SimProperties,
+                                                   opt_props: _lib.COptomechanicalVariables,
+                                                   rk4_props: _lib.RK4SolverOptions):
+        """rhs.py:306-346: returns (rc, times, states) with states [steps + 1, 4N]."""
+        y0 = _f64(y0)
+        states = ctypes.POINTER(ctypes.c_double)()
+        times = ctypes.POINTER(ctypes.c_double)()
+        ns, nt = ctypes.c_size_t(), ctypes.c_size_t()
+        rc = self.lib.integrateAugmentedOptomechanicalSimulationRK4(
+            _dp(y0), ctypes.byref(states), ctypes.byref(ns), ctypes.byref(times), ctypes.byref(nt),
+            ctypes.byref(sim_props), ctypes.byref(rk4_props), ctypes.byref(opt_props), y0.size // 4)
+        if rc != 0:
+            return rc, None, None
+        S = np.ctypeslib.as_array(states, shape=(ns.value, y0.size)).copy()
+        T = np.ctypeslib.as_array(times, shape=(nt.value,)).copy() if nt.value else np.empty(0)
+        self.lib.integrateAugmentedOptomechanicalSimulationRK4_freeMemory(states, times)
+        return rc, T, S

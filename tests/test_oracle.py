@@ -156,3 +156,27 @@ def test_helium_flat_film_is_stationary():
         (dx, dy, dphi), info = O.rhs(O.Problem(physics=O.HELIUM, depth=10.0, A3=A3), xi, 0 * xi, 0 * xi)
         assert info == 0
         assert np.abs(dphi).max() < 1e-12 and np.abs(dy).max() < 1e-12
+
+
+def test_oracle_drive_terms_known_answers():
+    """Driven film (CSH/createM.cuh:141-178, LightIntensity.cuh:25-37): on a
+    flat film at rest the base RHS vanishes, so dphi is exactly
+    strength * I + D and dD = beta * I - D / tau; I at the mode centre with
+    G y = 0 is gamma^2 I_max / 4 / (detuning^2 + gamma^2 / 4)."""
+    n = 32
+    xi = 2 * np.pi * np.arange(n) / n
+    P = O.Problem(physics=O.HELIUM, depth=3.0)
+    d = O.Drive(detuning=0.4, gamma=1.2, G=2.0, tau=3.0, max_intensity=0.5, x0=xi[7], sigma=0.3, beta=0.7,
+                damping=0.2, strength=1.5, augmented=True)
+    D = 0.1 * np.cos(xi)
+    (dx, dy, dphi, dD), info = O.rhs_driven(P, d, xi, np.zeros(n), np.zeros(n), D)
+    inten = 0.25 * d.gamma ** 2 * d.max_intensity / (d.detuning ** 2 + (d.gamma / 2) ** 2) * \
+        np.exp(-(xi - d.x0) ** 2 / (2 * d.sigma ** 2))
+    assert info == 0
+    assert np.abs(dx).max() < 1e-14 and np.abs(dy).max() < 1e-14
+    assert np.allclose(dphi, d.strength * inten + D, rtol=0, atol=1e-14)
+    assert np.allclose(dD, d.beta * inten - D / d.tau, rtol=0, atol=1e-14)
+    # without augmentation D is neither read nor produced
+    (dx2, dy2, dphi2), _ = O.rhs_driven(P, O.Drive(**{**d.__dict__, "augmented": False}), xi, np.zeros(n),
+                                        np.zeros(n), D)
+    assert np.allclose(dphi2, d.strength * inten, rtol=0, atol=1e-14)
