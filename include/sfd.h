@@ -213,6 +213,10 @@ int sfd_rk4_record(sfd_engine* e, double dt, int steps, int checkpoint_every, co
  * state_final>.  Each checkpoint segment is recomputed once with every stage
  * recorded (LU factors included), then reversed stage by stage. */
 int sfd_rk4_vjp(sfd_engine* e, const double* cot_final, double* grad_state0, double* grad_param);
+/* Exact Jacobian of the RHS at `state` (device, 3n) from 3n reverse sweeps
+ * over one recorded forward evaluation: jac (device, 9 n^2 doubles) in the
+ * column-major layout of calculateJacobian. */
+int sfd_jacobian_device(sfd_engine* e, const void* state, void* jac);
 
 /* Precision used by the reference-compatible exports below (default FP64). */
 int sfd_set_default_precision(int precision);
@@ -264,6 +268,14 @@ int integrateSimulationRK4(double* initialState, double** statesOut, size_t* sta
                            size_t* timesCount, SimProperties* simProperties, RK4SolverOptions* rkOptions, size_t N);
 /* Export.cuh:70 */
 int integrateSimulationRK4_freeMemory(double* statesOut, double* timesOut);
+
+/* Export.cuh:50 (Export.cu:393-519): central-difference Jacobian of the
+ * helium RHS (SI inputs as calculateRHSFromVectors), jac[col * 3N + row] =
+ * d rhs_row / d state_col, rows and columns ordered [x | y | phi]; jac holds
+ * 9 N^2 doubles.  All 6N perturbed states run as one batched FP64 engine
+ * (in chunks of at most 8 GB of matrices). */
+int calculateJacobian(const double* state, double* jac, double L, double rho, double kappa, double depth,
+                      double epsilon, size_t N);
 
 /* COptomechanicalVariables (ExportTypes.cuh:41-63), SI units. */
 typedef struct COptomechanicalVariables {

@@ -104,6 +104,8 @@ _SIGS = {
     "sfd_rhs_vjp_device": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, _dp]),
     "sfd_rk4_record": (c_int, [c_void_p, c_double, c_int, c_int, _dp, _dp]),
     "sfd_rk4_vjp": (c_int, [c_void_p, _dp, _dp, _dp]),
+    "sfd_jacobian_device": (c_int, [c_void_p, c_void_p, c_void_p]),
+    "calculateJacobian": (c_int, [_dp, _dp] + [c_double] * 5 + [c_size_t]),
     "calculateRHSFromVectors": (c_int, [_dp] * 6 + [c_double] * 4 + [c_size_t]),
     "calculateRHS256FromVectors": (c_int, [_dp] * 6 + [c_double] * 4),
     "calculateRHS2048FromVectors": (c_int, [_dp] * 6 + [c_double] * 4),

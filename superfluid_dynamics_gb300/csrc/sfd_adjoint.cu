@@ -630,6 +630,43 @@ extern "C" int sfd_rhs_vjp_device(sfd_engine* e, const void* state, const void* 
   return 0;
 }
 
+// Row i of J is J^T e_i: one reverse sweep per row over the recorded stage,
+// scattered into the column-major Jacobian.
+__global__ void k_jac_unit(int n3, int row, double* g) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < n3) g[c] = c == row ? 1.0 : 0.0;
+}
+__global__ void k_jac_scatter_row(int n3, int row, const double* g, double* jac) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < n3) jac[(long long)c * n3 + row] = g[c];
+}
+
+extern "C" int sfd_jacobian_device(sfd_engine* e, const void* state, void* jac) {
+  int rc = check_engine(e);
+  if (rc) return rc;
+  if (!state || !jac) return sfd_internal_error(SFD_ERR_INVALID, "null argument");
+  ACK(cudaSetDevice(e->device));
+  rc = ensure_work(e, 1);
+  if (rc) return rc;
+  AdjWork* W = e->adj;
+  const int n3 = 3 * W->n;
+  cudaStream_t s = e->stream;
+  AdjStage& st = W->slots[0];
+  ACK(cudaMemcpyAsync(st.Y, state, 8 * (size_t)n3, cudaMemcpyDeviceToDevice, s));
+  rc = record_rhs(e, W, st);
+  if (rc) return rc;
+  double* out = static_cast<double*>(jac);
+  for (int row = 0; row < n3; ++row) {
+    k_jac_unit<<<nblocks(n3, 256), 256, 0, s>>>(n3, row, W->gk);
+    rc = rhs_vjp(e, W, st, W->gk, W->gYs[0]);
+    if (rc) return rc;
+    k_jac_scatter_row<<<nblocks(n3, 256), 256, 0, s>>>(n3, row, W->gYs[0], out);
+    ACK(cudaGetLastError());
+  }
+  ACK(cudaStreamSynchronize(s));
+  return 0;
+}
+
 extern "C" int sfd_rk4_record(sfd_engine* e, double dt, int steps, int checkpoint_every, const double* state0,
                               double* state_final) {
   int rc = check_engine(e);

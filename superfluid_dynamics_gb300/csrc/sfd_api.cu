@@ -1138,6 +1138,65 @@ int integrateSimulationRK4_freeMemory(double* statesOut, double* timesOut) {
   return 0;
 }
 
+// calculateJacobian (Export.cu:393-519, JacobianCalculator.cuh:11-150):
+// central differences of the helium RHS, J[col * 3N + row] = d rhs_row /
+// d state_col (column-major, rows and columns ordered [x | y | phi]).  All
+// perturbed copies of the state are surfaces of one batched FP64 engine
+// (the reference batches them too); the batch is cut into chunks of at most
+// kJacBatchBytes of matrix storage.
+int calculateJacobian(const double* state, double* jac, double L, double rho, double kappa, double depth,
+                      double epsilon, size_t N) {
+  if (!state || !jac) return set_error(SFD_ERR_INVALID, "null argument");
+  if (N < 1 || N > 8192) return set_error(SFD_ERR_INVALID, "unsupported N %zu", N);
+  if (!(epsilon != 0.0)) return set_error(SFD_ERR_INVALID, "epsilon must be nonzero");
+  constexpr double kJacBatchBytes = 8e9;
+  const size_t n3 = 3 * N, np = (size_t)pad_n((int)N);
+  const size_t per_var = 2 * 8 * np * np;  // +eps and -eps copies, FP64 matrices
+  const size_t chunk = std::max<size_t>(1, std::min<size_t>(n3, (size_t)(kJacBatchBytes / (double)per_var)));
+  NondimProps np_ = adimensionalize(L, rho, kappa, depth);
+  sfd_problem p = helium_problem(np_);
+  sfd_options o;
+  sfd_default_options(&o);
+  o.precision = SFD_PRECISION_FP64;
+  o.use_graphs = 0;
+  std::vector<double> hx, hy, hp, dx, dy, dp;
+  for (size_t c0 = 0; c0 < n3; c0 += chunk) {
+    const size_t nc = std::min(chunk, n3 - c0), ns = 2 * nc;
+    std::vector<int> sizes(ns, (int)N);
+    sfd_engine* e = nullptr;
+    int rc = sfd_create(sizes.data(), (int)ns, &p, 1, &o, &e);
+    if (rc) return rc;
+    hx.resize(ns * N);
+    hy.resize(ns * N);
+    hp.resize(ns * N);
+    for (size_t b = 0; b < ns; ++b) {  // surface b: variable c0 + b % nc, sign + for b < nc
+      std::memcpy(&hx[b * N], state, N * sizeof(double));
+      std::memcpy(&hy[b * N], state + N, N * sizeof(double));
+      std::memcpy(&hp[b * N], state + 2 * N, N * sizeof(double));
+      const size_t var = c0 + b % nc, blk = var / N, j = var % N;
+      const double d = b < nc ? epsilon : -epsilon;
+      (blk == 0 ? hx : blk == 1 ? hy : hp)[b * N + j] += d;
+    }
+    dx.resize(ns * N);
+    dy.resize(ns * N);
+    dp.resize(ns * N);
+    rc = sfd_set_state_host(e, hx.data(), hy.data(), hp.data());
+    if (!rc) rc = sfd_rhs_host(e, dx.data(), dy.data(), dp.data(), nullptr, nullptr, nullptr);
+    sfd_destroy(e);
+    if (rc) return rc;
+    for (size_t k = 0; k < nc; ++k) {
+      double* col = jac + (c0 + k) * n3;
+      const size_t bp = k * N, bm = (nc + k) * N;
+      for (size_t r = 0; r < N; ++r) {
+        col[r] = (dx[bp + r] - dx[bm + r]) / (2.0 * epsilon);
+        col[N + r] = (dy[bp + r] - dy[bm + r]) / (2.0 * epsilon);
+        col[2 * N + r] = (dp[bp + r] - dp[bm + r]) / (2.0 * epsilon);
+      }
+    }
+  }
+  return 0;
+}
+
 int calculateRhsAugmentedOptomechanical(double* state, double* rhs, SimProperties* sp, COptomechanicalVariables* ov,
                                         size_t N) {
   if (!state || !rhs || !sp || !ov) return set_error(SFD_ERR_INVALID, "null argument");

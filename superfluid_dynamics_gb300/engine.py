@@ -264,6 +264,16 @@ class Engine:
         gp = self.rhs_vjp_device(s.data_ptr(), c.data_ptr(), g.data_ptr())
         return g.cpu().numpy(), gp
 
+    def jacobian(self, state: np.ndarray) -> np.ndarray:
+        """Exact RHS Jacobian J[row, col] at state = [x|y|phi] (reverse sweeps, FP64 engine, one surface)."""
+        import torch
+        dev = torch.device("cuda", self.options.device)
+        s = torch.as_tensor(_f64(state), device=dev)
+        j = torch.empty(s.numel() * s.numel(), dtype=torch.float64, device=dev)
+        check(self._L.sfd_jacobian_device(self._h, s.data_ptr(), j.data_ptr()))
+        n3 = s.numel()
+        return j.cpu().numpy().reshape(n3, n3).T.copy()
+
     def rk4_record(self, dt: float, steps: int, checkpoint_every: int, state0: np.ndarray) -> np.ndarray:
         """Integrate from state0 = [x|y|phi] keeping checkpoints; returns the final state."""
         s0 = _f64(state0)
@@ -415,6 +425,18 @@ class SimulationManager:
         T = np.ctypeslib.as_array(times, shape=(nt.value,)).copy() if nt.value else np.empty(0)
         self.lib.integrateSimulationRK4_freeMemory(states, times)
         return S, T
+
+    def calculate_jacobian(self, x, y, phi, L, rho, kappa, depth, epsilon=1e-6):
+        """rhs.py:213-222: (rc, J) with J[row, col] = d rhs_row / d state_col, a
+        Fortran-ordered [3N x 3N] array as the export writes it (column-major)."""
+        n = len(x)
+        if len(y) != n or len(phi) != n:
+            raise ValueError("Input arrays must have the same length")
+        state = np.concatenate([_f64(x), _f64(y), _f64(phi)])
+        J = np.empty((3 * n, 3 * n), dtype=np.float64, order="F")
+        rc = self.lib.calculateJacobian(_dp(state), J.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), L, rho, kappa,
+                                        depth, epsilon, n)
+        return rc, J
 
     def calculate_augmented_rhs(self, y0, sim_props: _lib.SimProperties, opt_props: _lib.COptomechanicalVariables):
         """rhs.py:348-358: RHS of [x | y | phi | D] for the augmented driven film (SI inputs)."""
