@@ -191,6 +191,27 @@ const char* sfd_version(void);
  * race; serialise them. */
 int sfd_rhs_device_noalloc(const sfd_problem* problem, int n, const void* state_in, void* rhs_out, void* stream);
 
+/* ------------------------------------------------------------ adaptive RKF45
+ * Runge-Kutta-Fehlberg 4(5) with the reference's error norm and step control
+ * (RK45Base, RK45.cuh:195-345; RK45_Options :21-27) on the engine's resident
+ * state, from t0 to t1.  One 8-byte device-to-host read per trial step. */
+typedef struct sfd_rkf45_options {
+    double atol, rtol;    /* 1e-6, 1e-3 */
+    double h_min, h_max;  /* 1e-16, 1e10 */
+    double h0;            /* first trial step (1e-2) */
+    long long max_rejected; /* per step, then status 1 (500) */
+} sfd_rkf45_options;
+typedef struct sfd_rkf45_result {
+    int status;           /* 0 reached t1, 1 too many rejections (stiffness) */
+    long long accepted, rejected;
+    double t;             /* time reached */
+    double h;             /* next step size */
+} sfd_rkf45_result;
+void sfd_default_rkf45_options(sfd_rkf45_options* o);
+/* times (nullable, capacity cap) receives the time after each accepted step. */
+int sfd_rkf45_evolve(sfd_engine* e, double t0, double t1, const sfd_rkf45_options* opts, sfd_rkf45_result* res,
+                     double* times, long long cap);
+
 /* ------------------------------------------------------------ reverse mode (adjoint)
  * Hand-written adjoint of the FP64 RHS and of RK4 trajectories.  The reference
  * has no reverse mode (it differentiates by finite differences in

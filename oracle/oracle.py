@@ -132,6 +132,11 @@ def lib() -> ctypes.CDLL:
         L.orc_rk4_steps.argtypes = [pp, ctypes.c_int, ctypes.c_double, ctypes.c_int, dp, dp, dp]
         L.orc_rk4_steps.restype = ctypes.c_int
         L.orc_invariants.argtypes = [pp, ctypes.c_int, dp, dp, dp, dp, dp, ctypes.c_double, dp]
+        ll = ctypes.c_longlong
+        L.orc_rkf45_evolve.argtypes = [pp, ctypes.c_int] + [ctypes.c_double] * 7 + [ll, dp, dp, dp, dp, dp,
+                                                                                      ctypes.POINTER(ll),
+                                                                                      ctypes.POINTER(ll), dp, ll]
+        L.orc_rkf45_evolve.restype = ctypes.c_int
         dr = ctypes.POINTER(_CDrive)
         L.orc_intensity.argtypes = [dr, ctypes.c_double, ctypes.c_double]
         L.orc_intensity.restype = ctypes.c_double
@@ -282,6 +287,21 @@ def rk4_steps_driven(problem: Problem, drive: Drive, x, y, phi, dl, dt: float, s
     info = lib().orc_rk4_steps_driven(ctypes.byref(cp), ctypes.byref(cd), x.size, float(dt), int(steps),
                                       _dp(x), _dp(y), _dp(phi), _dp(dl))
     return (x, y, phi, dl), info
+
+
+def rkf45_evolve(problem: Problem, x, y, phi, t0: float, t1: float, atol: float = 1e-6, rtol: float = 1e-3,
+                 h_min: float = 1e-16, h_max: float = 1e10, h0: float = 1e-2, max_rejected: int = 500,
+                 max_times: int = 100000):
+    """Adaptive RKF45 (orc_rkf45_evolve): returns ((x, y, phi), status, t, h, accepted, rejected, times)."""
+    x, y, phi = _f64(x).copy(), _f64(y).copy(), _f64(phi).copy()
+    cp = problem.to_c()
+    t, h = ctypes.c_double(), ctypes.c_double()
+    acc, rej = ctypes.c_longlong(), ctypes.c_longlong()
+    times = np.zeros(max_times)
+    st = lib().orc_rkf45_evolve(ctypes.byref(cp), x.size, t0, t1, atol, rtol, h_min, h_max, h0, max_rejected,
+                                _dp(x), _dp(y), _dp(phi), ctypes.byref(t), ctypes.byref(h), ctypes.byref(acc),
+                                ctypes.byref(rej), _dp(times), max_times)
+    return (x, y, phi), st, t.value, h.value, acc.value, rej.value, times[:min(acc.value, max_times)]
 
 
 def invariants(problem: Problem, x, y, phi, u, v, kappa: float = 0.0) -> np.ndarray:

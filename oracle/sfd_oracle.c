@@ -527,6 +527,118 @@ int orc_rk4_steps_driven(const orc_problem* P, const orc_drive* D, int n, double
 }
 
 /* ------------------------------------------------------------------ */
+/* Adaptive Runge-Kutta-Fehlberg 4(5) (CSH/RK45.cuh:195-345,             */
+/* CSH/RK45_Kernels.cuh:15-106): Fehlberg's 1969 tableau, the 5th-order  */
+/* solution is kept, error = h sum (b - b*) k.  The error norm runs over */
+/* the 2N complex state entries (z = x + i y, then phi):                 */
+/*   err = sqrt(mean(|e|^2 / (atol + rtol max(|y|, |y5|))^2))            */
+/* step factor 0.9 err^(-1/5), clamped to [0.2, 5] on acceptance and     */
+/* [0.2, 1] on rejection, then to [h_min, h_max]; err == 0 grows 5x.     */
+/* k1 is reused after a rejection.  The step is cut to the remaining     */
+/* interval.  Returns 0 at t1, 1 after more than max_rejected rejections */
+/* of one step; *accepted / *rejected count steps, times[] (if non-NULL, */
+/* capacity cap) receives the time after each accepted step.            */
+/* ------------------------------------------------------------------ */
+static const double RKF_A[6][5] = {
+    {0, 0, 0, 0, 0},
+    {1.0 / 4.0, 0, 0, 0, 0},
+    {3.0 / 32.0, 9.0 / 32.0, 0, 0, 0},
+    {1932.0 / 2197.0, -7200.0 / 2197.0, 7296.0 / 2197.0, 0, 0},
+    {439.0 / 216.0, -8.0, 3680.0 / 513.0, -845.0 / 4104.0, 0},
+    {-8.0 / 27.0, 2.0, -3544.0 / 2565.0, 1859.0 / 4104.0, -11.0 / 40.0}};
+static const double RKF_B[6] = {16.0 / 135.0, 0.0, 6656.0 / 12825.0, 28561.0 / 56430.0, -9.0 / 50.0, 2.0 / 55.0};
+static const double RKF_BS[6] = {25.0 / 216.0, 0.0, 1408.0 / 2565.0, 2197.0 / 4104.0, -1.0 / 5.0, 0.0};
+
+int orc_rkf45_evolve(const orc_problem* P, int n, double t0, double t1, double atol, double rtol, double h_min,
+                     double h_max, double h0, long long max_rejected, double* x, double* y, double* phi,
+                     double* t_out, double* h_out, long long* accepted, long long* rejected, double* times,
+                     long long cap) {
+    const size_t n3 = 3 * (size_t)n;
+    double* Y = (double*)malloc(sizeof(double) * n3);
+    double* T = (double*)malloc(sizeof(double) * n3);
+    double* Y5 = (double*)malloc(sizeof(double) * n3);
+    double* k[6];
+    for (int s = 0; s < 6; ++s) k[s] = (double*)malloc(sizeof(double) * n3);
+    memcpy(Y, x, sizeof(double) * n);
+    memcpy(Y + n, y, sizeof(double) * n);
+    memcpy(Y + 2 * n, phi, sizeof(double) * n);
+    double t = t0, h = h0;
+    int have_k1 = 0, status = 0;
+    long long acc = 0, rej = 0;
+    while (t < t1) {
+        if (t1 - t < h) h = t1 - t;
+        long long rej_here = 0;
+        for (;;) {
+            if (!have_k1) {
+                orc_rhs(P, n, Y, Y + n, Y + 2 * n, k[0], k[0] + n, k[0] + 2 * n, NULL, NULL, NULL);
+                have_k1 = 1;
+            }
+            for (int s = 1; s < 6; ++s) {
+                for (size_t i = 0; i < n3; ++i) {
+                    double v = Y[i];
+                    for (int j = 0; j < s; ++j) v += (RKF_A[s][j] * h) * k[j][i];
+                    T[i] = v;
+                }
+                orc_rhs(P, n, T, T + n, T + 2 * n, k[s], k[s] + n, k[s] + 2 * n, NULL, NULL, NULL);
+            }
+            double sumsq = 0.0;
+            for (int i = 0; i < 2 * n; ++i) {
+                double e2 = 0.0, y2 = 0.0, y52 = 0.0;
+                int comps = i < n ? 2 : 1;
+                for (int c = 0; c < comps; ++c) {
+                    size_t idx = i < n ? (size_t)i + (size_t)c * n : (size_t)(2 * n + (i - n));
+                    double y5v = Y[idx], ev = 0.0;
+                    for (int j = 0; j < 6; ++j) {
+                        y5v += (h * RKF_B[j]) * k[j][idx];
+                        ev += (h * (RKF_B[j] - RKF_BS[j])) * k[j][idx];
+                    }
+                    Y5[idx] = y5v;
+                    e2 += ev * ev;
+                    y2 += Y[idx] * Y[idx];
+                    y52 += y5v * y5v;
+                }
+                double sc = atol + rtol * fmax(sqrt(y2), sqrt(y52));
+                if (sc < 1e-300) sc = 1e-300;
+                sumsq += e2 / (sc * sc);
+            }
+            double err = sqrt(sumsq / (2.0 * n));
+            int ok = err <= 1.0;
+            double fac;
+            if (err == 0.0) fac = ok ? 5.0 : 1.0;
+            else {
+                fac = 0.9 * pow(err, -0.2);
+                fac = fmin(fmax(fac, 0.2), ok ? 5.0 : 1.0);
+            }
+            double hn = fmin(fmax(h * fac, h_min), h_max);
+            if (err == 0.0) hn = h * fac;
+            if (ok) {
+                memcpy(Y, Y5, sizeof(double) * n3);
+                have_k1 = 0;
+                t += h;
+                if (times && acc < cap) times[acc] = t;
+                ++acc;
+                h = hn;
+                break;
+            }
+            h = hn;
+            ++rej;
+            if (++rej_here > max_rejected) { status = 1; break; }
+        }
+        if (status) break;
+    }
+    memcpy(x, Y, sizeof(double) * n);
+    memcpy(y, Y + n, sizeof(double) * n);
+    memcpy(phi, Y + 2 * n, sizeof(double) * n);
+    *t_out = t;
+    *h_out = h;
+    *accepted = acc;
+    *rejected = rej;
+    free(Y); free(T); free(Y5);
+    for (int s = 0; s < 6; ++s) free(k[s]);
+    return status;
+}
+
+/* ------------------------------------------------------------------ */
 /* Invariants (CSH/Energies.cuh:136-204 and scalings :61-128), with U=0 */
 /* out[0] kinetic   = (1/4pi) sum phi (x' v - y' u)                     */
 /* out[1] potential = water (1+rho) g/(4pi) sum y^2 x'  |  helium       */

@@ -60,6 +60,16 @@ class COptomechanicalVariables(ctypes.Structure):
                                         "location_x0_mode", "sigma_optical_mode", "beta", "damping_strength")]
 
 
+class SfdRkf45Options(ctypes.Structure):
+    _fields_ = [("atol", c_double), ("rtol", c_double), ("h_min", c_double), ("h_max", c_double),
+                ("h0", c_double), ("max_rejected", c_longlong)]
+
+
+class SfdRkf45Result(ctypes.Structure):
+    _fields_ = [("status", c_int), ("accepted", c_longlong), ("rejected", c_longlong), ("t", c_double),
+                ("h", c_double)]
+
+
 _dp = POINTER(c_double)
 _SIGS = {
     "sfd_default_options": (None, [POINTER(SfdOptions)]),
@@ -105,6 +115,9 @@ _SIGS = {
     "sfd_rk4_record": (c_int, [c_void_p, c_double, c_int, c_int, _dp, _dp]),
     "sfd_rk4_vjp": (c_int, [c_void_p, _dp, _dp, _dp]),
     "sfd_jacobian_device": (c_int, [c_void_p, c_void_p, c_void_p]),
+    "sfd_default_rkf45_options": (None, [POINTER(SfdRkf45Options)]),
+    "sfd_rkf45_evolve": (c_int, [c_void_p, c_double, c_double, POINTER(SfdRkf45Options), POINTER(SfdRkf45Result),
+                                 _dp, c_longlong]),
     "calculateJacobian": (c_int, [_dp, _dp] + [c_double] * 5 + [c_size_t]),
     "calculateRHSFromVectors": (c_int, [_dp] * 6 + [c_double] * 4 + [c_size_t]),
     "calculateRHS256FromVectors": (c_int, [_dp] * 6 + [c_double] * 4),

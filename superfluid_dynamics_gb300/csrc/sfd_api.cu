@@ -388,6 +388,7 @@ void free_engine(sfd_engine* e) {
   for (void* p : ptrs)
     if (p) cudaFree(p);
   sfd_adjoint_free(e);
+  sfd_rkf45_free(e);
   drain_profile(e);
   for (cudaEvent_t ev : e->event_pool) cudaEventDestroy(ev);
   for (auto& kv : e->d_tw) cudaFree(kv.second);
@@ -444,6 +445,9 @@ int sfd_internal_cuda(cudaError_t err, const char* what) {
   return set_error(SFD_ERR_CUDA, "%s: %s", what, cudaGetErrorString(err));
 }
 int sfd_internal_rhs(sfd_engine* e, const double* st, double* out) { return enqueue_rhs(e, st, out, true); }
+int sfd_internal_rhs_ex(sfd_engine* e, const double* st, double* out, bool refactor) {
+  return enqueue_rhs(e, st, out, refactor);
+}
 
 // ====================================================================== C ABI
 extern "C" {

@@ -95,6 +95,8 @@ struct sfd_engine {
   long long class_count[SFD_NCLASS] = {};
   // reverse-mode workspace (checkpoints and per-stage records), allocated on first use
   AdjWork* adj = nullptr;
+  // adaptive RKF45 workspace, allocated on first use
+  struct RkfWork* rkf = nullptr;
 };
 
 // Entry points of sfd_api.cu used by the reverse mode.
@@ -104,5 +106,10 @@ int sfd_internal_cuda(cudaError_t err, const char* what);
 // stream; leaves z', z'', a, a', C, D, w, p and the LU factors of M in the
 // engine's buffers.
 int sfd_internal_rhs(sfd_engine* e, const double* st, double* out);
+// As sfd_internal_rhs, for either precision; refactor = rebuild the mixed
+// preconditioner at this evaluation (it is built anyway if there is none).
+int sfd_internal_rhs_ex(sfd_engine* e, const double* st, double* out, bool refactor);
 // reverse-mode workspace release (sfd_adjoint.cu)
 void sfd_adjoint_free(sfd_engine* e);
+// adaptive-integrator workspace release (sfd_rkf45.cu)
+void sfd_rkf45_free(sfd_engine* e);

@@ -205,6 +205,18 @@ class Engine:
         fn = self._L.sfd_rk4_steps if sync else self._L.sfd_rk4_steps_async
         check(fn(self._h, float(dt), int(steps)))
 
+    def evolve_rkf45(self, t0: float, t1: float, atol: float = 1e-6, rtol: float = 1e-3, h_min: float = 1e-16,
+                     h_max: float = 1e10, h0: float = 1e-2, max_rejected: int = 500, max_times: int = 1 << 20):
+        """Adaptive Runge-Kutta-Fehlberg 4(5) of the resident state from t0 to t1
+        (the reference's RK45Base).  Returns (result dict, times of the accepted steps)."""
+        o = _lib.SfdRkf45Options(atol, rtol, h_min, h_max, h0, max_rejected)
+        r = _lib.SfdRkf45Result()
+        times = np.zeros(max_times)
+        check(self._L.sfd_rkf45_evolve(self._h, float(t0), float(t1), ctypes.byref(o), ctypes.byref(r),
+                                       _dp(times), max_times))
+        res = {"status": r.status, "accepted": r.accepted, "rejected": r.rejected, "t": r.t, "h": r.h}
+        return res, times[:min(r.accepted, max_times)].copy()
+
     def synchronize(self) -> None:
         check(self._L.sfd_synchronize(self._h))
 
