@@ -227,6 +227,7 @@ def run_ours(args, rank, world, local_rank):
                 times.append((e0, e1))
             torch.cuda.synchronize()
     gpu_launches = eng.kernel_launches - launches0
+    tuning = eng.tuning()
     ms = sum(a.elapsed_time(b) for a, b in times)
     if world > 1:
         t = torch.tensor([ms], device=dev, dtype=torch.float64)
@@ -308,6 +309,7 @@ def run_ours(args, rank, world, local_rank):
             "config": {"workload": f"gravity wave N={n}, 8 modes seed 2, RK4 dt={DT}", "N": n,
                        "precision": args.precision, "refine_iters": args.refine_iters, "pre_iters": args.pre_iters,
                        "refactor_every": args.refactor_every, "precond_storage": "fp32" if args.precond_fp32 else "fp16",
+                       "sum_groups_per_cta": tuning,
                        "l2": "flushed (256 MB write) before every timed step",
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
             "roofline": roof, "cpu_baseline": cpu,
@@ -416,6 +418,7 @@ def run_workload(args, rank, world, local_rank):
             torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
             t = float(tt.item())
         st = eng.status()
+        line["config"]["sum_groups_per_cta"] = eng.tuning()
         eng.close()
         ref = sfd.Engine(ns, phys, fp64)
         ref.set_state(x, y, ph)

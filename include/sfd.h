@@ -75,6 +75,8 @@ typedef struct sfd_options {
     int tensor_cores;     /* mixed: preconditioner update on tcgen05 tensor cores (1)    */
     int pre_iters;        /* mixed: FP32 full-residual iterations before it (default 1)  */
     int precond_half;     /* mixed: apply the preconditioner from an FP16 copy (1)       */
+    int autotune;         /* time the boundary-sum CTA shapes on the first steps and keep
+                             the fastest per precision (1)                               */
 } sfd_options;
 
 /* Optomechanical drive of a helium film, nondimensional (the reference's
@@ -116,6 +118,9 @@ int sfd_create_driven(const int* n, int nsurf, const sfd_problem* problems, cons
 int sfd_destroy(sfd_engine* e);
 /* Use a caller stream (0 = the engine's own). */
 int sfd_set_stream(sfd_engine* e, void* cuda_stream);
+/* Source groups per CTA of the boundary sums chosen by the autotuner (or the
+ * default 4), for the FP64, double-float and FP32 passes. */
+int sfd_get_tuning(const sfd_engine* e, int* groups_f64_df_f32);
 /* Replace the physical parameters of one surface (A3, g, depth, ...) on an
  * existing engine; physics, the depth mode and whether rho is zero must stay.
  * (The reference fixes these in the BoundaryProblem constructor,

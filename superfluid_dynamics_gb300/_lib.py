@@ -34,7 +34,7 @@ class SfdProblem(ctypes.Structure):
 class SfdOptions(ctypes.Structure):
     _fields_ = [("precision", c_int), ("refine_iters", c_int), ("refactor_every", c_int),
                 ("use_graphs", c_int), ("device", c_int), ("tensor_cores", c_int), ("pre_iters", c_int),
-                ("precond_half", c_int)]
+                ("precond_half", c_int), ("autotune", c_int)]
 
 
 class SimProperties(ctypes.Structure):
@@ -100,6 +100,7 @@ _SIGS = {
     "sfd_set_default_precision": (c_int, [c_int]),
     "sfd_rhs_device_noalloc": (c_int, [POINTER(SfdProblem), c_int, c_void_p, c_void_p, c_void_p]),
     "sfd_set_problem": (c_int, [c_void_p, c_int, POINTER(SfdProblem)]),
+    "sfd_get_tuning": (c_int, [c_void_p, POINTER(c_int)]),
     "sfd_create_driven": (c_int, [POINTER(c_int), c_int, POINTER(SfdProblem), POINTER(SfdDrive), c_int,
                                   POINTER(SfdOptions), POINTER(c_void_p)]),
     "sfd_set_aux_host": (c_int, [c_void_p, _dp]),

@@ -164,7 +164,7 @@ int enqueue_sums(sfd_engine* e, int prec, const double* weights, const float2* w
             e->nd.pdf, weights_df, e->nd.mdiag, e->zp, e->phip,
             e->cacc, e->dacc, e->r, track_norm ? e->rnorm : nullptr, mode};
   int cls = prec == SFD_PREC_F64 ? SFD_K_SUMS64 : prec == SFD_PREC_DF ? SFD_K_SUMSDF : SFD_K_SUMS32;
-  LAUNCHC(e, cls, sfd_launch_sums(prec, A, e->nsum, e->max_n, e->stream));
+  LAUNCHC(e, cls, sfd_launch_sums(prec, A, e->nsum, e->max_n, e->sum_groups[prec], e->stream));
   return 0;
 }
 
@@ -342,9 +342,72 @@ int build_graph(sfd_engine* e, double dt, int variant) {
   return 0;
 }
 
+// Autotuner of the boundary-sum CTA shape: one eager RHS evaluation on the
+// resident state (it leaves valid weights and node data behind), then each
+// candidate group count is timed over three launches of every pass precision
+// the engine uses; the fastest is kept if it beats the default 4 groups by 3 %.
+// The group count sets the per-thread summation order, so runs are bitwise
+// repeatable only with autotune off (or the same choice).  The timed launches overwrite C, D
+// and r, which the next evaluation recomputes before reading.  Skipped while
+// the stream is being captured.
+int autotune_sums(sfd_engine* e) {
+  e->tune_pending = false;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  CK(cudaStreamIsCapturing(e->stream, &cs));
+  if (cs != cudaStreamCaptureStatusNone) return 0;
+  const bool prof = e->profile;
+  e->profile = false;
+  int rc = enqueue_rhs(e, e->y0, e->kcur, true);
+  if (rc) return rc;
+  const bool mixed = e->opt.precision == SFD_PRECISION_MIXED;
+  const int precs[2] = {mixed ? SFD_PREC_F32 : SFD_PREC_F64, SFD_PREC_DF};
+  cudaEvent_t a = nullptr, b = nullptr;
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  for (int pi = 0; pi < (mixed ? 2 : 1) && !rc; ++pi) {
+    const int prec = precs[pi];
+    const float2* wdf = prec == SFD_PREC_F64 ? nullptr : e->adf;
+    float best = 0.f, t4 = 0.f;
+    int best_g = 4;
+    for (int g : kSumGroupChoices) {
+      e->sum_groups[prec] = g;
+      rc = enqueue_sums(e, prec, e->a, wdf, 0, false);  // warm-up
+      if (rc) break;
+      cudaEventRecord(a, e->stream);
+      for (int r = 0; r < 3 && !rc; ++r) rc = enqueue_sums(e, prec, e->a, wdf, 0, false);
+      cudaEventRecord(b, e->stream);
+      if (rc) break;
+      cudaError_t err = cudaEventSynchronize(b);
+      float ms = 0.f;
+      if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, a, b);
+      if (err != cudaSuccess) {
+        rc = sfd_fail(err);
+        break;
+      }
+      if (g == 4) t4 = ms;
+      if (g == kSumGroupChoices[0] || ms < best) {
+        best = ms;
+        best_g = g;
+      }
+    }
+    // keep the default unless another shape is clearly faster (timing noise
+    // would otherwise flip the choice, and with it the summation order)
+    e->sum_groups[prec] = best < 0.97f * t4 ? best_g : 4;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  e->profile = prof;
+  return rc;
+}
+
 int run_steps(sfd_engine* e, double dt, int steps) {
   if (steps < 0) return set_error(SFD_ERR_INVALID, "negative step count");
   CK(cudaSetDevice(e->device));
+  if (e->tune_pending && steps > 0) {
+    int rc = autotune_sums(e);
+    if (rc) return rc;
+    destroy_graphs(e);  // captured with the previous shapes
+  }
   const bool mixed = e->opt.precision == SFD_PRECISION_MIXED;
   const int every = std::max(1, e->opt.refactor_every);
   if (e->opt.use_graphs && !e->profile) {
@@ -462,6 +525,7 @@ void sfd_default_options(sfd_options* o) {
   o->tensor_cores = 1;
   o->pre_iters = 1;
   o->precond_half = 1;
+  o->autotune = 1;
 }
 
 void sfd_default_problem(sfd_problem* p) {
@@ -502,6 +566,7 @@ int sfd_create_driven(const int* n, int nsurf, const sfd_problem* problems, cons
     return set_error(SFD_ERR_INVALID, "unknown precision %d", e->opt.precision);
   }
   if (e->opt.refine_iters < 0) e->opt.refine_iters = 0;
+  e->tune_pending = e->opt.autotune != 0;
   if (e->opt.pre_iters < 0) e->opt.pre_iters = 0;
   e->device = e->opt.device;
   if (e->device < 0 || e->device >= ndev) {
@@ -717,6 +782,12 @@ int sfd_set_problem(sfd_engine* e, int surface, const sfd_problem* problem) {
   CK(cudaStreamSynchronize(e->stream));
   e->hs[surface] = S;
   CK(cudaMemcpy(e->d_surf + surface, &S, sizeof(SurfaceDesc), cudaMemcpyHostToDevice));
+  return 0;
+}
+
+int sfd_get_tuning(const sfd_engine* e, int* g) {
+  if (!e || !g) return set_error(SFD_ERR_INVALID, "null argument");
+  for (int i = 0; i < 3; ++i) g[i] = e->sum_groups[i];
   return 0;
 }
 

@@ -42,6 +42,8 @@ struct sfd_engine {
   sfd_options opt{};
   int nsurf = 0, ntot = 0, max_n = 0, max_np = 0;
   int nblk = 3;  // state blocks: [x | y | phi] or, with an augmented drive, [x | y | phi | D]
+  int sum_groups[3] = {4, 4, 4};  // boundary-sum source groups per CTA, by pass precision
+  bool tune_pending = false;
   long long mat_elems = 0, panel_elems = 0;
   bool any_rho = false;
   std::vector<SurfaceDesc> hs;

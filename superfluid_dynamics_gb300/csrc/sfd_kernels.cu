@@ -261,8 +261,11 @@ __device__ __forceinline__ double sums_finish(const SumArgs& A, const SurfaceDes
   return (rv == rv) ? rv : 1e300;
 }
 
-template <int PREC>
-__global__ void __cluster_dims__(kSumCL, 1, 1) __launch_bounds__(kSumThreads, 4) k_boundary_sums(SumArgs A) {
+template <int PREC, int G>
+__global__ void __cluster_dims__(kSumCL, 1, 1) __launch_bounds__(G * kSumTile, 1024 / (G * kSumTile))
+    k_boundary_sums(SumArgs A) {
+  constexpr int kSumGroups = G;                  // source groups per CTA (tuned per engine)
+  constexpr int kSumThreads = G * kSumTile;
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = (int)cluster.block_rank();
@@ -383,23 +386,39 @@ size_t sfd_sums_smem(int prec, int max_n) {
   return per * (prec == SFD_PREC_F64 ? sizeof(Src64) : sizeof(SrcDF));
 }
 
+namespace {
+template <int PREC>
+cudaError_t configure_prec(int bytes) {
+  cudaError_t e = cudaFuncSetAttribute(k_boundary_sums<PREC, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_boundary_sums<PREC, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_boundary_sums<PREC, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  return e;
+}
+template <int PREC>
+void launch_prec(const SumArgs& A, dim3 grid, int groups, size_t smem, cudaStream_t st) {
+  if (groups == 2) k_boundary_sums<PREC, 2><<<grid, 2 * kSumTile, smem, st>>>(A);
+  else if (groups == 8) k_boundary_sums<PREC, 8><<<grid, 8 * kSumTile, smem, st>>>(A);
+  else k_boundary_sums<PREC, 4><<<grid, 4 * kSumTile, smem, st>>>(A);
+}
+}  // namespace
+
 cudaError_t sfd_sums_configure() {
   const int bytes = (int)sfd_sums_smem(SFD_PREC_F64, 8192);
-  cudaError_t e = cudaFuncSetAttribute(k_boundary_sums<SFD_PREC_F64>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_boundary_sums<SFD_PREC_DF>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_boundary_sums<SFD_PREC_F32>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  cudaError_t e = configure_prec<SFD_PREC_F64>(bytes);
+  if (e == cudaSuccess) e = configure_prec<SFD_PREC_DF>(bytes);
+  if (e == cudaSuccess) e = configure_prec<SFD_PREC_F32>(bytes);
   return e;
 }
 
-cudaError_t sfd_launch_sums(int prec, const SumArgs& A, int nitems, int max_n, cudaStream_t st) {
+cudaError_t sfd_launch_sums(int prec, const SumArgs& A, int nitems, int max_n, int groups, cudaStream_t st) {
   if (nitems == 0) return cudaSuccess;
   const dim3 grid(nitems * kSumCL);
   const size_t smem = sfd_sums_smem(prec, max_n);
-  if (prec == SFD_PREC_F64) k_boundary_sums<SFD_PREC_F64><<<grid, kSumThreads, smem, st>>>(A);
-  else if (prec == SFD_PREC_DF) k_boundary_sums<SFD_PREC_DF><<<grid, kSumThreads, smem, st>>>(A);
-  else k_boundary_sums<SFD_PREC_F32><<<grid, kSumThreads, smem, st>>>(A);
+  if (prec == SFD_PREC_F64) launch_prec<SFD_PREC_F64>(A, grid, groups, smem, st);
+  else if (prec == SFD_PREC_DF) launch_prec<SFD_PREC_DF>(A, grid, groups, smem, st);
+  else launch_prec<SFD_PREC_F32>(A, grid, groups, smem, st);
   return cudaGetLastError();
 }
 

@@ -5,10 +5,11 @@
 enum : int { SFD_PREC_F64 = 0, SFD_PREC_DF = 1, SFD_PREC_F32 = 2 };
 
 constexpr int kSumCL = 8;                          // CTAs per cluster (one target tile)
-constexpr int kSumGroups = 4;                      // source groups per CTA
 constexpr int kSumTile = 64;                       // targets per tile (one per thread of a group)
-constexpr int kSumThreads = kSumGroups * kSumTile; // 256
 constexpr int kSumPerRank = kSumTile / kSumCL;     // targets finished by each CTA of the cluster
+// Source groups per CTA (the CTA has groups * kSumTile threads): 2, 4 or 8,
+// picked per engine and precision by timing (sfd_options.autotune); 4 otherwise.
+constexpr int kSumGroupChoices[3] = {2, 4, 8};
 
 struct NodeData {
   cd* w;        // exp(i z)
@@ -71,7 +72,7 @@ struct VelArgs {
 
 __global__ void k_node_prep(const SurfaceDesc* surf, const int* node_surf, int ntot, const double* x,
                             const double* y, const cd* zp, const cd* zpp, NodeData nd);
-cudaError_t sfd_launch_sums(int prec, const SumArgs& A, int nitems, int max_n, cudaStream_t st);
+cudaError_t sfd_launch_sums(int prec, const SumArgs& A, int nitems, int max_n, int groups, cudaStream_t st);
 cudaError_t sfd_sums_configure();
 __global__ void k_velocity_bernoulli(VelArgs V);
 __global__ void k_velocity_node1(VelArgs V);

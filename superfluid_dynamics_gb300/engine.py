@@ -93,11 +93,12 @@ class Options:
     tensor_cores: bool = True
     pre_iters: int = 1
     precond_half: bool = True
+    autotune: bool = True
 
     def to_c(self) -> _lib.SfdOptions:
         return _lib.SfdOptions(self.precision, self.refine_iters, self.refactor_every,
                                1 if self.use_graphs else 0, self.device, 1 if self.tensor_cores else 0,
-                               self.pre_iters, 1 if self.precond_half else 0)
+                               self.pre_iters, 1 if self.precond_half else 0, 1 if self.autotune else 0)
 
 
 class Engine:
@@ -252,6 +253,12 @@ class Engine:
     @property
     def kernel_launches(self) -> int:
         return int(self._L.sfd_kernel_launches(self._h))
+
+    def tuning(self) -> dict:
+        """Boundary-sum source groups per CTA in use, by pass precision."""
+        g = (ctypes.c_int * 3)()
+        check(self._L.sfd_get_tuning(self._h, g))
+        return {"fp64": g[0], "df": g[1], "fp32": g[2]}
 
     def set_problem(self, physics: Physics, surface: int = 0) -> None:
         """Replace one surface's parameters (A3, g, ...) in place."""

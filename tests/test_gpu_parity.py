@@ -278,3 +278,18 @@ def test_tensor_core_preconditioner(n):
         assert rel(out3[3], oa) < 1e-10
         assert rel(out3[0] + 1j * out3[1], ox + 1j * oy) < 1e-10
         assert (st3[0] & (sfd._lib.STATUS_TIMEOUT | sfd._lib.STATUS_NONFINITE)).max() == 0
+
+
+def test_autotuned_sum_shape_is_valid_and_parity_holds():
+    """The boundary-sum autotuner (first step of an engine) picks 2, 4 or 8
+    source groups per CTA; the stepped result still matches the oracle."""
+    n, dt, steps = 256, 0.005, 3
+    s = W.random_modes(n, seed=2)
+    with sfd.Engine(n, sfd.WaterBoundaryProblem(), sfd.Options(precision=sfd.PRECISION_MIXED)) as e:
+        e.set_state(s.x, s.y, s.phi)
+        e.step(dt, steps)
+        t = e.tuning()
+        gx, gy, gp = e.get_state()
+    assert t["fp32"] in (2, 4, 8) and t["df"] in (2, 4, 8)
+    (ox, oy, op), _ = O.rk4_steps(O.Problem(), s.x, s.y, s.phi, dt, steps)
+    assert rel(gx + 1j * gy, ox + 1j * oy) < 1e-9 and rel(gp, op) < 1e-9
