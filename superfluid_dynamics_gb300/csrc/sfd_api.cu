@@ -234,8 +234,8 @@ int enqueue_solve(sfd_engine* e, const double* st, const double* phi_im, bool re
       LAUNCHC(e, SFD_K_DIAG, k_lu64_diag<<<e->nsurf, 256, 0, e->stream>>>(e->d_surf, e->nsurf, kb, e->m64, e->status, e->lmax));
       int rem = nb - kb - 1;
       if (rem > 0) {
-        LAUNCHC(e, SFD_K_PANEL, k_lu64_trsm<<<dim3(rem, 2, e->nsurf), 64, 0, e->stream>>>(e->d_surf, e->nsurf, kb, e->m64, e->lmax));
-        LAUNCHC(e, SFD_K_UPDATE, k_lu64_gemm<<<dim3(rem, rem, e->nsurf), 256, 0, e->stream>>>(e->d_surf, e->nsurf, kb, e->m64));
+        LAUNCHC(e, SFD_K_PANEL, k_lu64_trsm<<<dim3(rem, 2, e->nsurf), 64, kTrsmSmem, e->stream>>>(e->d_surf, e->nsurf, kb, e->m64, e->lmax));
+        LAUNCHC(e, SFD_K_UPDATE, k_lu64_gemm<<<dim3(2 * rem, 2 * rem, e->nsurf), 256, 0, e->stream>>>(e->d_surf, e->nsurf, kb, e->m64));
       }
     }
     LAUNCHC(e, SFD_K_TRSV, k_lu64_solve<<<e->nsurf, 256, e->max_np * sizeof(double), e->stream>>>(e->d_surf, e->m64, e->phip,
@@ -503,6 +503,15 @@ int fill_drive(SurfaceDesc& S, const sfd_drive& d) {
 
 }  // namespace
 
+// Dynamic shared-memory limits of the solver kernels (per device context).
+cudaError_t sfd_solve_configure() {
+  cudaError_t e = cudaFuncSetAttribute(k_gj_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, kGjDiagSmem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_lu64_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, 8320 * (int)sizeof(double));
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_lu64_trsm, cudaFuncAttributeMaxDynamicSharedMemorySize, kTrsmSmem);
+  return e;
+}
+
 int sfd_internal_error(int code, const char* msg) { return set_error(code, "%s", msg); }
 int sfd_internal_cuda(cudaError_t err, const char* what) {
   return set_error(SFD_ERR_CUDA, "%s: %s", what, cudaGetErrorString(err));
@@ -758,8 +767,7 @@ int sfd_create_driven(const int* n, int nsurf, const sfd_problem* problems, cons
   }
   CKE(sfd_fft_configure());
   CKE(sfd_sums_configure());
-  CKE(cudaFuncSetAttribute(k_gj_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, kGjDiagSmem));
-  CKE(cudaFuncSetAttribute(k_lu64_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, 8320 * (int)sizeof(double)));
+  CKE(sfd_solve_configure());
 #undef CKE
   *out = e;
   return 0;
@@ -1413,6 +1421,8 @@ int noalloc_base(unsigned char** out) {
     void* a = nullptr;
     err = cudaGetSymbolAddress(&a, g_noalloc_scratch);
     if (err != cudaSuccess) return set_error(SFD_ERR_CUDA, "cudaGetSymbolAddress(scratch) failed: %s", cudaGetErrorString(err));
+    err = sfd_solve_configure();  // dynamic shared-memory limits of the FP64 LU kernels
+    if (err != cudaSuccess) return sfd_fail(err);
     addr[dev] = a;
   }
   *out = static_cast<unsigned char*>(addr[dev]);

@@ -112,6 +112,31 @@ cudaError_t sfd_launch_assemble32(const SurfaceDesc* surf, const int4* tiles, in
 // Step kb (block column k0 = 64 kb) of the right-looking LU without row
 // exchanges.  One CTA per surface factors the 64x64 diagonal block in shared
 // memory.
+// Copy a rows x cols FP64 tile (row stride lds in the source) into shared
+// memory with row stride ldd, NT threads, B loads in flight per thread before
+// the stores (a dependent load-store loop would pay one memory latency per
+// element).  With transpose, dst[c * ldd + r] = src[r * lds + c].
+template <int NT, int B, bool TRANSPOSE = false>
+__device__ __forceinline__ void load_tile(double* dst, int ldd, const double* src, long long lds, int rows, int cols) {
+  const int total = rows * cols;
+  for (int e0 = 0; e0 < total; e0 += NT * B) {
+    double t[B];
+#pragma unroll
+    for (int b = 0; b < B; ++b) {
+      const int e = e0 + b * NT + threadIdx.x;
+      t[b] = e < total ? src[(long long)(e / cols) * lds + (e % cols)] : 0.0;
+    }
+#pragma unroll
+    for (int b = 0; b < B; ++b) {
+      const int e = e0 + b * NT + threadIdx.x;
+      if (e < total) {
+        if (TRANSPOSE) dst[(e % cols) * ldd + e / cols] = t[b];
+        else dst[(e / cols) * ldd + (e % cols)] = t[b];
+      }
+    }
+  }
+}
+
 __global__ void __launch_bounds__(256) k_lu64_diag(const SurfaceDesc* surf, int nsurf, int kb, double* mat,
                                                    unsigned int* status, double* lmax) {
   const int s = blockIdx.x;
@@ -121,7 +146,7 @@ __global__ void __launch_bounds__(256) k_lu64_diag(const SurfaceDesc* surf, int 
   if (k0 >= np) return;
   double* A = mat + S.moff;
   __shared__ double D[64][65];
-  for (int e = threadIdx.x; e < 64 * 64; e += 256) D[e >> 6][e & 63] = A[(long long)(k0 + (e >> 6)) * np + k0 + (e & 63)];
+  load_tile<256, 16>(&D[0][0], 65, A + (long long)k0 * np + k0, np, 64, 64);
   __syncthreads();
   double lm = 0.0;
   for (int c = 0; c < 64; ++c) {
@@ -156,68 +181,73 @@ __global__ void __launch_bounds__(64) k_lu64_trsm(const SurfaceDesc* surf, int n
   const int tile = kb + 1 + blockIdx.x;
   if (tile * 64 >= np) return;
   double* A = mat + S.moff;
-  __shared__ double D[64][65];
-  for (int e = threadIdx.x; e < 64 * 64; e += 64) D[e >> 6][e & 63] = A[(long long)(k0 + (e >> 6)) * np + k0 + (e & 63)];
-  __syncthreads();
-  double x[64];
+  extern __shared__ double trsm_smem[];  // 2 x 64 x 65 doubles (kTrsmSmem bytes)
+  double(*D)[65] = reinterpret_cast<double(*)[65]>(trsm_smem);
+  double(*X)[65] = reinterpret_cast<double(*)[65]>(trsm_smem + 64 * 65);  // X[t]: thread t's row / column
+  load_tile<64, 16>(&D[0][0], 65, A + (long long)k0 * np + k0, np, 64, 64);
   const int t = threadIdx.x;
+  if (blockIdx.y == 0)  // rows tile*64 + r: solve x U = a (U upper incl. diagonal)
+    load_tile<64, 16>(&X[0][0], 65, A + (long long)(tile * 64) * np + k0, np, 64, 64);
+  else  // columns tile*64 + c, stored as X[c][r]
+    load_tile<64, 16, true>(&X[0][0], 65, A + (long long)k0 * np + tile * 64, np, 64, 64);
+  __syncthreads();
   if (blockIdx.y == 0) {
-    // row r = tile*64 + t: solve x U = a (U upper incl. diagonal)
-    double* row = A + (long long)(tile * 64 + t) * np + k0;
     double lm = 0.0;
     for (int c = 0; c < 64; ++c) {
-      double v = row[c];
-      for (int q = 0; q < c; ++q) v -= x[q] * D[q][c];
-      x[c] = v / D[c][c];
+      double v = X[t][c];
+      for (int q = 0; q < c; ++q) v -= X[t][q] * D[q][c];
+      v = v / D[c][c];
+      X[t][c] = v;
+      lm = fmax(lm, fabs(v));
     }
-    for (int c = 0; c < 64; ++c) { row[c] = x[c]; lm = fmax(lm, fabs(x[c])); }
     for (int o = 16; o > 0; o >>= 1) lm = fmax(lm, __shfl_xor_sync(0xffffffffu, lm, o));
     if ((t & 31) == 0 && lm > 0) atomicMax(reinterpret_cast<unsigned long long*>(lmax) + s, __double_as_longlong(lm));
   } else {
-    // column c = tile*64 + t: solve L x = a (L unit lower)
-    double* col = A + (long long)k0 * np + tile * 64 + t;
+    // column tile*64 + t: solve L x = a (L unit lower)
     for (int r = 0; r < 64; ++r) {
-      double v = col[(long long)r * np];
-      for (int q = 0; q < r; ++q) v -= D[r][q] * x[q];
-      x[r] = v;
+      double v = X[t][r];
+      for (int q = 0; q < r; ++q) v -= D[r][q] * X[t][q];
+      X[t][r] = v;
     }
-    for (int r = 0; r < 64; ++r) col[(long long)r * np] = x[r];
+  }
+  __syncthreads();
+  if (blockIdx.y == 0) {
+    for (int e = t; e < 64 * 64; e += 64) A[(long long)(tile * 64 + (e >> 6)) * np + k0 + (e & 63)] = X[e >> 6][e & 63];
+  } else {
+    for (int e = t; e < 64 * 64; e += 64) A[(long long)(k0 + (e >> 6)) * np + tile * 64 + (e & 63)] = X[e & 63][e >> 6];
   }
 }
 
-// Trailing update A22 -= L21 U12 for step kb (64x64 output tiles, K = 64).
+// Trailing update A22 -= L21 U12 for step kb: 32x32 output tiles (four per
+// 64x64 block, so small matrices still fill the GPU), K = 64, 2x2 outputs per
+// thread.  grid = (2 rem, 2 rem, surfaces).
 __global__ void __launch_bounds__(256) k_lu64_gemm(const SurfaceDesc* surf, int nsurf, int kb, double* mat) {
   const int s = blockIdx.z;
   const SurfaceDesc& S = surf[s];
   const int np = pad_n(S.n), k0 = kb * 64;
-  const int ti = kb + 1 + blockIdx.y, tj = kb + 1 + blockIdx.x;
-  if (ti * 64 >= np || tj * 64 >= np) return;
+  const int r0 = k0 + 64 + 32 * blockIdx.y, c0 = k0 + 64 + 32 * blockIdx.x;
+  if (r0 >= np || c0 >= np) return;
   double* A = mat + S.moff;
-  __shared__ double La[64][33];
-  __shared__ double Ub[32][65];
-  const int tr = (threadIdx.x >> 4) * 4, tc = (threadIdx.x & 15) * 4;
-  double acc[4][4] = {};
-  for (int q0 = 0; q0 < 64; q0 += 32) {
-    __syncthreads();
-    for (int e = threadIdx.x; e < 64 * 32; e += 256) La[e >> 5][e & 31] = A[(long long)(ti * 64 + (e >> 5)) * np + k0 + q0 + (e & 31)];
-    for (int e = threadIdx.x; e < 32 * 64; e += 256) Ub[e >> 6][e & 63] = A[(long long)(k0 + q0 + (e >> 6)) * np + tj * 64 + (e & 63)];
-    __syncthreads();
-    for (int q = 0; q < 32; ++q) {
-      double a[4], b[4];
-#pragma unroll
-      for (int i = 0; i < 4; ++i) a[i] = La[tr + i][q];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) b[j] = Ub[q][tc + j];
-#pragma unroll
-      for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
-    }
+  __shared__ double La[32][65];
+  __shared__ double Ub[64][33];
+  load_tile<256, 8>(&La[0][0], 65, A + (long long)r0 * np + k0, np, 32, 64);
+  load_tile<256, 8>(&Ub[0][0], 33, A + (long long)k0 * np + c0, np, 64, 32);
+  __syncthreads();
+  const int tr = (threadIdx.x >> 4) * 2, tc = (threadIdx.x & 15) * 2;
+  double a00 = 0, a01 = 0, a10 = 0, a11 = 0;
+#pragma unroll 8
+  for (int q = 0; q < 64; ++q) {
+    const double x0 = La[tr][q], x1 = La[tr + 1][q], y0 = Ub[q][tc], y1 = Ub[q][tc + 1];
+    a00 = fma(x0, y0, a00);
+    a01 = fma(x0, y1, a01);
+    a10 = fma(x1, y0, a10);
+    a11 = fma(x1, y1, a11);
   }
-#pragma unroll
-  for (int i = 0; i < 4; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j) A[(long long)(ti * 64 + tr + i) * np + tj * 64 + tc + j] -= acc[i][j];
+  double* o = A + (long long)(r0 + tr) * np + c0 + tc;
+  o[0] -= a00;
+  o[1] -= a01;
+  o[np] -= a10;
+  o[np + 1] -= a11;
 }
 
 // Forward (unit L) then backward (U) substitution, one CTA per surface, in

@@ -8,6 +8,7 @@
 // per-surface matrices are padded to a multiple of 128 rows/columns
 __host__ __device__ __forceinline__ int pad_n(int n) { return (n + 127) / 128 * 128; }
 constexpr int kGemvRows = 16;  // rows per CTA of k_gemv
+constexpr int kTrsmSmem = 2 * 64 * 65 * 8;  // k_lu64_trsm dynamic shared memory
 constexpr int kGjDiagSmem = (128 * 129 + 128 * 33 + 32 * 128 + 32 * 33) * 4;  // k_gj_diag dynamic shared memory
 
 cudaError_t sfd_launch_assemble64(const SurfaceDesc* surf, const int4* tiles, int ntiles, const cd* w, const cd* p,
