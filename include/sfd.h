@@ -244,6 +244,34 @@ int sfd_rk4_vjp(sfd_engine* e, const double* cot_final, double* grad_state0, dou
  * column-major layout of calculateJacobian. */
 int sfd_jacobian_device(sfd_engine* e, const void* state, void* jac);
 
+/* ------------------------------------------------------------ C++ facade support (include/sfd.hpp)
+ * Interleaved complex state as the reference's calculators take it:
+ * state = [Z (ntot complex) | Phi (ntot complex, imaginary part ignored)],
+ * rhs = [dZ/dt | dPhi/dt (imaginary part 0)], device pointers, asynchronous on
+ * the engine stream (BaseBoundaryIntegralCalculator::run,
+ * BaseBoundaryIntegrator.cuh:137-262). */
+int sfd_rhs_device_complex(sfd_engine* e, const void* state, void* rhs);
+/* calculateVorticities (BaseBoundaryIntegrator.cuh:275-306): solves for the
+ * vortex sheet strength a of the complex state and returns device pointers
+ * to the engine's a (double[ntot]), z' and z'' (complex[ntot]); they stay
+ * valid until the next call on the engine. */
+int sfd_vorticities_device(sfd_engine* e, const void* state, double** a, void** zp, void** zpp);
+/* RK4 stage combines on n doubles (AutonomousRungeKuttaStepper.cuh:338-375):
+ * kacc = first ? k : kacc + wk k; ystage = y0 + cy k (ystage nullable);
+ * final: y0 += c kacc. */
+int sfd_rk4_stage_device(long long n, const void* y0, const void* k, void* kacc, void* ystage, double wk,
+                         double cy, int first, void* stream);
+int sfd_rk4_final_device(long long n, void* y0, const void* kacc, double c, void* stream);
+/* MatrixSolver::solve (MatrixSolver.cuh:113-172): `batch` column-major n x n
+ * systems M a = b on the device, FP64 blocked LU without row exchanges; the
+ * optional host status words get SFD_STATUS_PIVOT_SWAP where partial pivoting
+ * would have exchanged rows and SFD_STATUS_ZERO_PIVOT on a zero pivot. */
+typedef struct sfd_dense_solver sfd_dense_solver;
+int sfd_dense_solver_create(int n, int batch, sfd_dense_solver** out);
+int sfd_dense_solver_set_stream(sfd_dense_solver* d, void* stream);
+int sfd_dense_solve(sfd_dense_solver* d, const double* M, const double* b, double* x, unsigned int* status);
+int sfd_dense_solver_destroy(sfd_dense_solver* d);
+
 /* Precision used by the reference-compatible exports below (default FP64). */
 int sfd_set_default_precision(int precision);
 

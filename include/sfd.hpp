@@ -1,0 +1,256 @@
+// sfd.hpp -- C++ facade over libsfd.so with the class names and call shapes
+// of the reference's in-process interface (CuSuperHelium/CuSuperHelium):
+//
+//   AutonomousProblem<T, N>::run / setStream              (AutonomousProblem.h:9-28)
+//   BoundaryProblem<N, B>, WaterBoundaryProblem<N, B>,
+//   HeliumBoundaryProblem<N, B>                           (BoundaryProblem.cuh:47-62,
+//                                                          WaterBoundaryProblem.cuh, HeliumBoundaryProblem.cuh)
+//   BaseBoundaryIntegralCalculator<N, B>(properties, problem): run, runTimeStep,
+//     calculateVorticities, getDevA / getDevZp / getDevZpp (BaseBoundaryIntegrator.cuh:14-33)
+//   AutonomousRungeKuttaStepper<T, N>(problem, dt): setTimeStep, initialize,
+//     runStep, runEvolution, getY                         (AutonomousRungeKuttaStepper.cuh:24-44)
+//   MatrixSolver<N, B>::solve(M, b, a)                    (MatrixSolver.cuh:24-45)
+//
+// State layout is the reference's: device arrays of std_complex (two doubles,
+// real then imaginary), [Z (N B) | Phi (N B)], with Phi's imaginary part
+// ignored.  Everything runs on the GB300 engine behind the C ABI; errors throw
+// std::runtime_error with sfd_last_error().  Header-only, C++17, builds with
+// any host compiler (no CUDA code in here).
+#pragma once
+
+#include <complex>
+#include <cstddef>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "sfd.h"
+
+namespace sfd {
+
+using std_complex = std::complex<double>;  // layout of cuda::std::complex<double>
+
+inline void check(int rc) {
+  if (rc != 0) throw std::runtime_error(std::string("sfd: ") + sfd_last_error());
+}
+
+// ProblemProperties.hpp:5-32 (nondimensional), plus the explicit constants
+// the engine takes: A3 (helium; <= 0 selects h^4 / 3) and g (water).
+struct ProblemProperties {
+  double rho = 0.0;
+  double depth = 1.0;
+  double kappa = 0.0;
+  double U = 0.0;
+  bool infinite_depth = false;
+  bool use_expansions = false;
+  int expansion_order = 1;
+  double A3 = 0.0;
+  double gravity = 1.0;
+};
+
+template <typename T, int N>
+class AutonomousProblem {
+ public:
+  virtual ~AutonomousProblem() = default;
+  // rhs = f(initialState); both device pointers of N values of T
+  virtual void run(T* initialState, T* rhs) = 0;
+  virtual void setStream(cudaStream_t stream) = 0;
+};
+
+template <int N, size_t batchSize>
+class BoundaryProblem {
+ public:
+  explicit BoundaryProblem(const ProblemProperties& p) : props(p) {}
+  virtual ~BoundaryProblem() = default;
+  virtual sfd_problem problem() const = 0;
+
+ protected:
+  ProblemProperties props;
+};
+
+template <int N, size_t batchSize>
+class WaterBoundaryProblem : public BoundaryProblem<N, batchSize> {
+ public:
+  explicit WaterBoundaryProblem(const ProblemProperties& p) : BoundaryProblem<N, batchSize>(p) {}
+  sfd_problem problem() const override {
+    sfd_problem q;
+    sfd_default_problem(&q);
+    q.physics = SFD_WATER;
+    q.rho = this->props.rho;
+    q.gravity = this->props.gravity;
+    q.U = this->props.U;
+    return q;
+  }
+};
+
+template <int N, size_t batchSize>
+class HeliumBoundaryProblem : public BoundaryProblem<N, batchSize> {
+ public:
+  explicit HeliumBoundaryProblem(const ProblemProperties& p) : BoundaryProblem<N, batchSize>(p) {}
+  sfd_problem problem() const override {
+    sfd_problem q;
+    sfd_default_problem(&q);
+    q.physics = SFD_HELIUM;
+    q.depth = this->props.depth;
+    q.A3 = this->props.A3;
+    q.kappa = this->props.kappa;
+    q.U = this->props.U;
+    q.infinite_depth = this->props.infinite_depth ? 1 : 0;
+    q.use_expansions = this->props.use_expansions ? 1 : 0;
+    q.expansion_order = this->props.expansion_order;
+    return q;
+  }
+};
+
+// One engine holding batchSize surfaces of N nodes.  FP64 by default like the
+// reference; pass SFD_PRECISION_MIXED for the GB300 mixed-precision solve.
+template <int N, size_t batchSize>
+class BaseBoundaryIntegralCalculator : public AutonomousProblem<std_complex, 2 * N * (int)batchSize> {
+ public:
+  BaseBoundaryIntegralCalculator(const ProblemProperties& /*properties*/, const BoundaryProblem<N, batchSize>& bp,
+                                 int precision = SFD_PRECISION_FP64) {
+    sfd_options o;
+    sfd_default_options(&o);
+    o.precision = precision;
+    std::vector<int> ns(batchSize, N);
+    sfd_problem q = bp.problem();
+    check(sfd_create(ns.data(), (int)batchSize, &q, 1, &o, &engine_));
+  }
+  ~BaseBoundaryIntegralCalculator() override { sfd_destroy(engine_); }
+  BaseBoundaryIntegralCalculator(const BaseBoundaryIntegralCalculator&) = delete;
+  BaseBoundaryIntegralCalculator& operator=(const BaseBoundaryIntegralCalculator&) = delete;
+
+  void run(std_complex* initialState, std_complex* rhs) override { runTimeStep(initialState, rhs); }
+  void runTimeStep(const std_complex* initialState, std_complex* rhs) {
+    check(sfd_rhs_device_complex(engine_, initialState, rhs));
+  }
+  void calculateVorticities(const std_complex* initialState) {
+    void *zp = nullptr, *zpp = nullptr;
+    check(sfd_vorticities_device(engine_, initialState, &a_, &zp, &zpp));
+    zp_ = static_cast<std_complex*>(zp);
+    zpp_ = static_cast<std_complex*>(zpp);
+  }
+  double* getDevA() { return a_; }
+  std_complex* getDevZp() { return zp_; }
+  std_complex* getDevZpp() { return zpp_; }
+  void setStream(cudaStream_t stream) override { check(sfd_set_stream(engine_, stream)); }
+  sfd_engine* engine() { return engine_; }
+
+ private:
+  sfd_engine* engine_ = nullptr;
+  double* a_ = nullptr;
+  std_complex *zp_ = nullptr, *zpp_ = nullptr;
+};
+
+// Classic RK4 (AutonomousRungeKuttaStepper.cuh:123-375) on any
+// AutonomousProblem<T, N>; T is double or std_complex.  The stage combines
+// run on the device through the C ABI.
+template <typename T, int N>
+class AutonomousRungeKuttaStepper {
+ public:
+  // The stepper and the problem share one stream (created here, or the one
+  // passed to setStream), so stage combines and RHS evaluations stay ordered.
+  AutonomousRungeKuttaStepper(AutonomousProblem<T, N>& problem, double tstep = 1e-2) : problem_(problem), dt_(tstep) {
+    const size_t bytes = sizeof(T) * (size_t)N;
+    for (double** p : {&y_, &ys_, &k_, &kacc_}) {
+      if (cudaMalloc(reinterpret_cast<void**>(p), bytes) != cudaSuccess) {
+        release();
+        throw std::runtime_error("sfd: cudaMalloc failed in AutonomousRungeKuttaStepper");
+      }
+    }
+    if (cudaStreamCreateWithFlags(&own_stream_, cudaStreamNonBlocking) != cudaSuccess) {
+      release();
+      throw std::runtime_error("sfd: cudaStreamCreate failed in AutonomousRungeKuttaStepper");
+    }
+    stream_ = own_stream_;
+    problem_.setStream(stream_);
+  }
+  ~AutonomousRungeKuttaStepper() { release(); }
+  AutonomousRungeKuttaStepper(const AutonomousRungeKuttaStepper&) = delete;
+  AutonomousRungeKuttaStepper& operator=(const AutonomousRungeKuttaStepper&) = delete;
+
+  void setTimeStep(double tstep) { dt_ = tstep; }
+  void setStream(cudaStream_t s) {
+    stream_ = s;
+    problem_.setStream(s);
+  }
+  // copies the initial state (host or device pointer) into the stepper
+  void initialize(const T* y0, bool onDevice = false) {
+    if (cudaMemcpyAsync(y_, y0, sizeof(T) * (size_t)N, onDevice ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                        stream_) != cudaSuccess)
+      throw std::runtime_error("sfd: initialize copy failed");
+  }
+  void runStep(int /*step*/ = 0) {
+    const long long n = (long long)(sizeof(T) / sizeof(double)) * N;
+    const double wk[4] = {1.0, 2.0, 2.0, 1.0};
+    const double cy[4] = {0.5 * dt_, 0.5 * dt_, dt_, 0.0};
+    for (int s = 0; s < 4; ++s) {
+      problem_.run(reinterpret_cast<T*>(s == 0 ? y_ : ys_), reinterpret_cast<T*>(k_));
+      check(sfd_rk4_stage_device(n, y_, k_, kacc_, s < 3 ? ys_ : nullptr, wk[s], cy[s], s == 0, stream_));
+    }
+    check(sfd_rk4_final_device(n, y_, kacc_, dt_ / 6.0, stream_));
+    time_ += dt_;
+  }
+  // steps of dt from startTime while the time stays below endTime
+  // (runEvolution, AutonomousRungeKuttaStepper.cuh:404-437)
+  void runEvolution(double startTime, double endTime) {
+    time_ = startTime;
+    const long long steps = (long long)((endTime - startTime) / dt_);
+    for (long long i = 0; i < steps; ++i) runStep((int)i);
+    if (cudaStreamSynchronize(stream_) != cudaSuccess) throw std::runtime_error("sfd: runEvolution failed");
+  }
+  T* getY() { return reinterpret_cast<T*>(y_); }
+  double getCurrentTime() const { return time_; }
+
+ private:
+  void release() {
+    if (stream_) cudaStreamSynchronize(stream_);
+    for (double* p : {y_, ys_, k_, kacc_}) cudaFree(p);
+    y_ = ys_ = k_ = kacc_ = nullptr;
+    if (own_stream_) {
+      // the problem outlives the stepper: hand it back its default stream
+      // before the stepper's stream goes away
+      if (stream_ == own_stream_) {
+        try {
+          problem_.setStream(nullptr);
+        } catch (...) {
+        }
+      }
+      cudaStreamDestroy(own_stream_);
+    }
+    own_stream_ = nullptr;
+  }
+  AutonomousProblem<T, N>& problem_;
+  double dt_;
+  double time_ = 0.0;
+  cudaStream_t stream_ = nullptr;
+  cudaStream_t own_stream_ = nullptr;
+  double *y_ = nullptr, *ys_ = nullptr, *k_ = nullptr, *kacc_ = nullptr;
+};
+
+// Batched dense FP64 solve of column-major N x N systems (MatrixSolver.cuh).
+template <int N, size_t batchSize>
+class MatrixSolver {
+ public:
+  MatrixSolver() { check(sfd_dense_solver_create(N, (int)batchSize, &d_)); }
+  ~MatrixSolver() { sfd_dense_solver_destroy(d_); }
+  MatrixSolver(const MatrixSolver&) = delete;
+  MatrixSolver& operator=(const MatrixSolver&) = delete;
+  // devM: batchSize column-major N x N matrices; devb, deva: batchSize x N
+  void solve(double* devM, double* devb, double* deva) { check(sfd_dense_solve(d_, devM, devb, deva, nullptr)); }
+  // as solve, returning the per-system status words (SFD_STATUS_*)
+  std::vector<unsigned int> solveChecked(double* devM, double* devb, double* deva) {
+    std::vector<unsigned int> st(batchSize);
+    check(sfd_dense_solve(d_, devM, devb, deva, st.data()));
+    return st;
+  }
+  void setStream(cudaStream_t stream) { check(sfd_dense_solver_set_stream(d_, stream)); }
+
+ private:
+  sfd_dense_solver* d_ = nullptr;
+};
+
+}  // namespace sfd

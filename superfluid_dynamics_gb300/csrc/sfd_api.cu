@@ -447,7 +447,7 @@ void free_engine(sfd_engine* e) {
                   e->d_gemv_rows, e->d_poff, e->y0, e->ys, e->kacc, e->kcur, e->zp, e->zpp, e->ap, e->phip, e->a,
                   e->r, e->delta, e->phi_im, e->nd.w, e->nd.p, e->nd.wdf, e->nd.pdf, e->adf, e->ddf, e->nd.mdiag, e->nd.v1low, e->nd.v1up, e->nd.v2,
                   e->cacc, e->dacc, e->vel_low1, e->status, e->lmax, e->rnorm,
-                  e->inv_out, e->m64, e->m32, e->m16, e->rscale, e->pbuf, e->rbuf, e->cbuf, e->cparts, e->rparts};
+                  e->inv_out, e->m64, e->m32, e->m16, e->rscale, e->fc_in, e->fc_out, e->pbuf, e->rbuf, e->cbuf, e->cparts, e->rparts};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   sfd_adjoint_free(e);
@@ -517,6 +517,7 @@ int sfd_internal_cuda(cudaError_t err, const char* what) {
   return set_error(SFD_ERR_CUDA, "%s: %s", what, cudaGetErrorString(err));
 }
 int sfd_internal_rhs(sfd_engine* e, const double* st, double* out) { return enqueue_rhs(e, st, out, true); }
+int sfd_internal_solve(sfd_engine* e, const double* st) { return enqueue_solve(e, st, nullptr, true); }
 int sfd_internal_rhs_ex(sfd_engine* e, const double* st, double* out, bool refactor) {
   return enqueue_rhs(e, st, out, refactor);
 }

@@ -99,6 +99,9 @@ struct sfd_engine {
   AdjWork* adj = nullptr;
   // adaptive RKF45 workspace, allocated on first use
   struct RkfWork* rkf = nullptr;
+  // complex-layout staging of the C++ facade (sfd_facade.cu), allocated on first use
+  double* fc_in = nullptr;
+  double* fc_out = nullptr;
 };
 
 // Entry points of sfd_api.cu used by the reverse mode.
@@ -115,3 +118,8 @@ int sfd_internal_rhs_ex(sfd_engine* e, const double* st, double* out, bool refac
 void sfd_adjoint_free(sfd_engine* e);
 // adaptive-integrator workspace release (sfd_rkf45.cu)
 void sfd_rkf45_free(sfd_engine* e);
+// First half of an RHS evaluation (z', z'', phi', the solve of M a = phi',
+// C and D) on state [x|y|phi]; leaves a, z', z'' in the engine's buffers.
+int sfd_internal_solve(sfd_engine* e, const double* st);
+// Dynamic shared-memory limits of the solver kernels on the current device.
+cudaError_t sfd_solve_configure();

@@ -1,0 +1,156 @@
+// Drives the C++ facade (include/sfd.hpp) the way the reference's C++ apps
+// drive their classes, and checks it against the engine's own C ABI:
+//   BaseBoundaryIntegralCalculator::run  vs sfd_rhs_host (same state, SoA)
+//   calculateVorticities / getDevA        vs the vortex strength of sfd_rhs_host
+//   AutonomousRungeKuttaStepper, 10 steps vs sfd_rk4_steps
+//   MatrixSolver<64, 3>                   vs Gaussian elimination on the host
+// Prints the differences and exits 0 when all are within tolerance.
+#include <cmath>
+#include <cstdio>
+#include <random>
+#include <vector>
+
+#include "sfd.hpp"
+
+using sfd::std_complex;
+
+static double maxrel(const std::vector<double>& a, const std::vector<double>& b) {
+  double d = 0, m = 0;
+  for (size_t i = 0; i < a.size(); ++i) {
+    d = std::fmax(d, std::fabs(a[i] - b[i]));
+    m = std::fmax(m, std::fabs(b[i]));
+  }
+  return d / (m > 0 ? m : 1.0);
+}
+
+static void stage(const char* what) { std::fprintf(stderr, "facade_check: %s\n", what); }
+
+int main() {
+  constexpr int N = 128;
+  const double PI = 3.14159265358979323846;
+  sfd::ProblemProperties props;
+  sfd::WaterBoundaryProblem<N, 1> water(props);
+  sfd::BaseBoundaryIntegralCalculator<N, 1> calc(props, water);
+
+  std::vector<std_complex> h(2 * N);
+  std::vector<double> x(N), y(N), phi(N);
+  for (int j = 0; j < N; ++j) {
+    const double xi = 2 * PI * j / N;
+    x[j] = xi;
+    y[j] = 0.05 * std::cos(xi) + 0.01 * std::sin(3 * xi);
+    phi[j] = 0.05 * std::sin(xi);
+    h[j] = {x[j], y[j]};
+    h[N + j] = {phi[j], 0.0};
+  }
+  std_complex *dS = nullptr, *dR = nullptr;
+  cudaMalloc(&dS, sizeof(std_complex) * 2 * N);
+  cudaMalloc(&dR, sizeof(std_complex) * 2 * N);
+  cudaMemcpy(dS, h.data(), sizeof(std_complex) * 2 * N, cudaMemcpyHostToDevice);
+
+  // reference values through the plain C ABI
+  sfd_problem p;
+  sfd_default_problem(&p);
+  sfd_options o;
+  sfd_default_options(&o);
+  o.precision = SFD_PRECISION_FP64;
+  int n = N;
+  sfd_engine* e = nullptr;
+  sfd::check(sfd_create(&n, 1, &p, 1, &o, &e));
+  sfd::check(sfd_set_state_host(e, x.data(), y.data(), phi.data()));
+  std::vector<double> dx(N), dy(N), dp(N), a(N);
+  sfd::check(sfd_rhs_host(e, dx.data(), dy.data(), dp.data(), a.data(), nullptr, nullptr));
+
+  // 1. run
+  stage("run");
+  calc.run(dS, dR);
+  sfd::check(sfd_synchronize(calc.engine()));
+  std::vector<std_complex> r(2 * N);
+  cudaMemcpy(r.data(), dR, sizeof(std_complex) * 2 * N, cudaMemcpyDeviceToHost);
+  std::vector<double> fr(3 * N), er(3 * N);
+  for (int j = 0; j < N; ++j) {
+    fr[j] = r[j].real(); fr[N + j] = r[j].imag(); fr[2 * N + j] = r[N + j].real();
+    er[j] = dx[j]; er[N + j] = dy[j]; er[2 * N + j] = dp[j];
+  }
+  const double e_run = maxrel(fr, er);
+
+  // 2. vorticities
+  stage("vorticities");
+  calc.calculateVorticities(dS);
+  sfd::check(sfd_synchronize(calc.engine()));
+  std::vector<double> fa(N);
+  cudaMemcpy(fa.data(), calc.getDevA(), sizeof(double) * N, cudaMemcpyDeviceToHost);
+  const double e_a = maxrel(fa, a);
+
+  // 3. stepper
+  stage("stepper");
+  const double dt = 0.01;
+  sfd::AutonomousRungeKuttaStepper<std_complex, 2 * N> stepper(calc, dt);
+  stepper.initialize(h.data(), false);
+  stepper.runEvolution(0.0, 10 * dt + 0.5 * dt);
+  std::vector<std_complex> ys(2 * N);
+  cudaMemcpy(ys.data(), stepper.getY(), sizeof(std_complex) * 2 * N, cudaMemcpyDeviceToHost);
+  sfd::check(sfd_rk4_steps(e, dt, 10));
+  std::vector<double> ex(N), ey(N), ep(N);
+  sfd::check(sfd_get_state_host(e, ex.data(), ey.data(), ep.data()));
+  std::vector<double> fs(3 * N), es(3 * N);
+  for (int j = 0; j < N; ++j) {
+    fs[j] = ys[j].real(); fs[N + j] = ys[j].imag(); fs[2 * N + j] = ys[N + j].real();
+    es[j] = ex[j]; es[N + j] = ey[j]; es[2 * N + j] = ep[j];
+  }
+  const double e_step = maxrel(fs, es);
+
+  stage("dense solver");
+  // 4. dense solver on column-major, diagonally dominant systems
+  constexpr int M = 64, B = 3;
+  std::mt19937_64 rng(5);
+  std::uniform_real_distribution<double> U(-1.0, 1.0);
+  std::vector<double> Ah((size_t)B * M * M), bh((size_t)B * M), xh((size_t)B * M);
+  for (int s = 0; s < B; ++s)
+    for (int c = 0; c < M; ++c)
+      for (int rr = 0; rr < M; ++rr) Ah[(size_t)s * M * M + (size_t)c * M + rr] = U(rng) / M + (rr == c ? 2.0 : 0.0);
+  for (auto& v : bh) v = U(rng);
+  double *dA = nullptr, *db = nullptr, *dxs = nullptr;
+  cudaMalloc(&dA, sizeof(double) * Ah.size());
+  cudaMalloc(&db, sizeof(double) * bh.size());
+  cudaMalloc(&dxs, sizeof(double) * bh.size());
+  cudaMemcpy(dA, Ah.data(), sizeof(double) * Ah.size(), cudaMemcpyHostToDevice);
+  cudaMemcpy(db, bh.data(), sizeof(double) * bh.size(), cudaMemcpyHostToDevice);
+  sfd::MatrixSolver<M, B> solver;
+  std::vector<unsigned int> st = solver.solveChecked(dA, db, dxs);
+  cudaDeviceSynchronize();
+  cudaMemcpy(xh.data(), dxs, sizeof(double) * xh.size(), cudaMemcpyDeviceToHost);
+  double e_solve = 0;
+  for (int s = 0; s < B; ++s) {  // host Gaussian elimination with partial pivoting
+    std::vector<double> Ar((size_t)M * M), br(bh.begin() + (size_t)s * M, bh.begin() + (size_t)(s + 1) * M);
+    for (int rr = 0; rr < M; ++rr)
+      for (int c = 0; c < M; ++c) Ar[(size_t)rr * M + c] = Ah[(size_t)s * M * M + (size_t)c * M + rr];
+    for (int k = 0; k < M; ++k) {
+      int piv = k;
+      for (int rr = k + 1; rr < M; ++rr)
+        if (std::fabs(Ar[(size_t)rr * M + k]) > std::fabs(Ar[(size_t)piv * M + k])) piv = rr;
+      for (int c = 0; c < M; ++c) std::swap(Ar[(size_t)k * M + c], Ar[(size_t)piv * M + c]);
+      std::swap(br[k], br[piv]);
+      for (int rr = k + 1; rr < M; ++rr) {
+        const double l = Ar[(size_t)rr * M + k] / Ar[(size_t)k * M + k];
+        for (int c = k; c < M; ++c) Ar[(size_t)rr * M + c] -= l * Ar[(size_t)k * M + c];
+        br[rr] -= l * br[k];
+      }
+    }
+    for (int k = M - 1; k >= 0; --k) {
+      double v = br[k];
+      for (int c = k + 1; c < M; ++c) v -= Ar[(size_t)k * M + c] * br[c];
+      br[k] = v / Ar[(size_t)k * M + k];
+    }
+    std::vector<double> got(xh.begin() + (size_t)s * M, xh.begin() + (size_t)(s + 1) * M);
+    e_solve = std::fmax(e_solve, maxrel(got, br));
+  }
+  unsigned int st_or = 0;
+  for (unsigned int v : st) st_or |= v;
+
+  std::printf("run %.3e vorticity %.3e stepper %.3e solve %.3e status %u\n", e_run, e_a, e_step, e_solve, st_or);
+  std::fflush(stdout);
+  sfd_destroy(e);
+  for (void* p : {(void*)dS, (void*)dR, (void*)dA, (void*)db, (void*)dxs}) cudaFree(p);
+  const bool ok = e_run < 1e-13 && e_a < 1e-13 && e_step < 1e-13 && e_solve < 1e-12 && st_or == 0;
+  return ok ? 0 : 1;
+}

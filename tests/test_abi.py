@@ -1,6 +1,7 @@
 """CPU tests of the boundary: the C-ABI library builds for sm_103a, loads and
 exports every function include/sfd.h declares; calls that need no GPU behave."""
 import ctypes
+import os
 
 import pytest
 
@@ -48,3 +49,28 @@ def test_create_without_device_fails_cleanly():
     h = ctypes.c_void_p()
     rc = L.sfd_create(n, 1, ctypes.byref(p), 1, None, ctypes.byref(h))
     assert rc == -4 and not h.value
+
+
+def _build_facade_check(tmp_path):
+    """Compile tests/cpp/facade_check.cpp against include/sfd.hpp and libsfd.so
+    with the host C++ compiler (the facade is header-only C++17)."""
+    import shutil
+    import subprocess
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    lib = _lib.load()  # builds libsfd.so if needed
+    libdir = os.path.dirname(lib._name)
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    exe = str(tmp_path / "facade_check")
+    cmd = [cxx, "-std=c++17", "-O1", os.path.join(root, "tests", "cpp", "facade_check.cpp"),
+           "-I", os.path.join(root, "include"), "-I", os.path.join(cuda, "include"),
+           "-L", libdir, "-lsfd", f"-Wl,-rpath,{libdir}",
+           "-L", os.path.join(cuda, "lib64"), "-lcudart", f"-Wl,-rpath,{os.path.join(cuda, 'lib64')}", "-o", exe]
+    subprocess.check_call(cmd)
+    return exe
+
+
+def test_cpp_facade_compiles_and_links(tmp_path):
+    assert os.path.exists(_build_facade_check(tmp_path))
