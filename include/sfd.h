@@ -217,6 +217,43 @@ void sfd_default_rkf45_options(sfd_rkf45_options* o);
 int sfd_rkf45_evolve(sfd_engine* e, double t0, double t1, const sfd_rkf45_options* opts, sfd_rkf45_result* res,
                      double* times, long long cap);
 
+/* ------------------------------------------------------------ implicit Gauss-Legendre 2
+ * Two-stage Gauss-Legendre (order 4, A-stable) with damped Newton on the
+ * stage equations (GaussLegendre2, GaussLegendre.cuh:216-605): an FP64
+ * engine with one surface and no drive, from t0 to t1, step halving on
+ * Newton failure.  The two stage states are evaluated as one two-surface
+ * batch; the stage Jacobians come from central differences over a batched
+ * FP64 engine (JacobianCalculator.cuh:223-284) or from the exact reverse-mode
+ * Jacobian; the 6n x 6n Newton system is solved by the FP64 blocked LU. */
+#define SFD_GL2_JACOBIAN_AUTO 0   /* exact where reverse mode covers the engine and n >= 384, else FD */
+#define SFD_GL2_JACOBIAN_FD 1
+#define SFD_GL2_JACOBIAN_EXACT 2
+typedef struct sfd_gl2_options {
+    double step;            /* first (and largest) step, 0.01 */
+    double newton_tol;      /* converged when |R| <= tol (1 + |k|), 1e-10 */
+    long long max_newton;   /* Newton iterations per attempt, 20 */
+    int allow_simplified;   /* after a failed line search, continue once with J(y) frozen (0) */
+    double armijo_c;        /* 1e-4 */
+    double backtrack;       /* 0.5 */
+    double min_alpha;       /* 1e-6 */
+    long long max_halvings; /* step halvings per step, 6 */
+    double fd_eps;          /* central-difference step, 1e-6 */
+    int jacobian;           /* SFD_GL2_JACOBIAN_* */
+} sfd_gl2_options;
+typedef struct sfd_gl2_result {
+    int status;             /* 0 reached t1; 1 Newton failed at every halving (state left at t) */
+    long long steps, newton_iters, rhs_evals, jacobians, halvings;
+    double t;               /* time reached */
+    double h;               /* last accepted step */
+    double residual;        /* Newton residual norm of the last attempt */
+} sfd_gl2_result;
+void sfd_default_gl2_options(sfd_gl2_options* o);
+/* Advances the engine's resident state.  times (capacity cap, nullable)
+ * receives the time after each accepted step, states (cap x 3n, nullable)
+ * the state after it. */
+int sfd_gl2_evolve(sfd_engine* e, double t0, double t1, const sfd_gl2_options* opts, sfd_gl2_result* res,
+                   double* times, double* states, long long cap);
+
 /* ------------------------------------------------------------ reverse mode (adjoint)
  * Hand-written adjoint of the FP64 RHS and of RK4 trajectories.  The reference
  * has no reverse mode (it differentiates by finite differences in
@@ -330,6 +367,32 @@ int integrateSimulationRK4_freeMemory(double* statesOut, double* timesOut);
  * (in chunks of at most 8 GB of matrices). */
 int calculateJacobian(const double* state, double* jac, double L, double rho, double kappa, double depth,
                       double epsilon, size_t N);
+
+/* GaussLegendreOptions (ExportTypes.cuh:21-34). */
+typedef struct GaussLegendreOptions {
+    double t0;
+    double t1;
+    double stepSize;
+    double newtonTolerance;
+    size_t maxNewtonIterations;
+    SFD_BOOL allowSimplifiedFallback;
+    SFD_BOOL returnTrajectory;
+    double armijo_c;
+    double backtrack;
+    double minAlpha;
+    size_t maxStepsHalves;
+} GaussLegendreOptions;
+/* Export.cuh:66 (Export.cu:665-738): GL2 integration of the helium problem
+ * (SI properties as the other exports; initial state [x | y | phi], t0, t1
+ * and stepSize nondimensional as the reference takes them).  statesOut gets
+ * the initial state and the state after every accepted step when
+ * returnTrajectory (times likewise), else only the final state and no times.
+ * Returns -1 when a step fails to converge at every halving. */
+int integrateSimulationGL2(double* initialState, double** statesOut, size_t* statesCount, double** timesOut,
+                           size_t* timesCount, SimProperties* simProperties, GaussLegendreOptions* glCOptions,
+                           size_t N);
+/* Export.cuh:67 */
+int integrateSimulationGL2_freeMemory(double* statesOut, double* timesOut);
 
 /* COptomechanicalVariables (ExportTypes.cuh:41-63), SI units. */
 typedef struct COptomechanicalVariables {

@@ -7,8 +7,9 @@
 //                                                          WaterBoundaryProblem.cuh, HeliumBoundaryProblem.cuh)
 //   BaseBoundaryIntegralCalculator<N, B>(properties, problem): run, runTimeStep,
 //     calculateVorticities, getDevA / getDevZp / getDevZpp (BaseBoundaryIntegrator.cuh:14-33)
-//   AutonomousRungeKuttaStepper<T, N>(problem, dt): setTimeStep, initialize,
+//   AutonomousRungeKuttaStepper<T, N>(problem, dt, logger): setTimeStep, initialize,
 //     runStep, runEvolution, getY                         (AutonomousRungeKuttaStepper.cuh:24-44)
+//   TrajectoryLogger<T, N>, OdeSolverResult               (TrajectoryLogger.cuh, OdeSolver.h)
 //   MatrixSolver<N, B>::solve(M, b, a)                    (MatrixSolver.cuh:24-45)
 //
 // State layout is the reference's: device arrays of std_complex (two doubles,
@@ -18,8 +19,10 @@
 // any host compiler (no CUDA code in here).
 #pragma once
 
+#include <algorithm>
 #include <complex>
 #include <cstddef>
+#include <cstdlib>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -145,6 +148,79 @@ class BaseBoundaryIntegralCalculator : public AutonomousProblem<std_complex, 2 *
   std_complex *zp_ = nullptr, *zpp_ = nullptr;
 };
 
+// OdeSolver.h:2-5
+enum class OdeSolverResult { ReachedEndTime, StiffnessDetected };
+
+// Device-side trajectory record (TrajectoryLogger.cuh:8-79): one state of N
+// values of T per logged time, appended on the logger's stream into a device
+// buffer that doubles when full.  copyTimesToHost / copyStatesToHost return
+// std::malloc'd arrays that the caller releases with std::free.
+template <typename T, size_t N>
+class TrajectoryLogger {
+ public:
+  TrajectoryLogger() = default;
+  virtual ~TrajectoryLogger() { cudaFree(states_); }
+  TrajectoryLogger(const TrajectoryLogger&) = delete;
+  TrajectoryLogger& operator=(const TrajectoryLogger&) = delete;
+
+  void logTrajectory(double currentTime, const T* devState) {
+    if (!enabled_) return;
+    if (times_.size() == cap_) grow();
+    T* dst = states_ + times_.size() * N;
+    if (cudaMemcpyAsync(dst, devState, sizeof(T) * N, cudaMemcpyDeviceToDevice, stream_) != cudaSuccess)
+      throw std::runtime_error("sfd: TrajectoryLogger copy failed");
+    times_.push_back(currentTime);
+  }
+  virtual int copyTimesToHost(double** times, size_t* count) {
+    if (!enabled_ || !times || !count) return -1;
+    double* t = static_cast<double*>(std::malloc(times_.size() * sizeof(double) + 1));
+    if (!t) return -1;
+    std::copy(times_.begin(), times_.end(), t);
+    *times = t;
+    *count = times_.size();
+    return 0;
+  }
+  virtual int copyStatesToHost(T** hostStates, size_t* countHost) {
+    if (!enabled_ || !hostStates || !countHost) return -1;
+    const size_t bytes = times_.size() * N * sizeof(T);
+    T* h = static_cast<T*>(std::malloc(bytes + 1));
+    if (!h) return -1;
+    if (bytes && (cudaMemcpyAsync(h, states_, bytes, cudaMemcpyDeviceToHost, stream_) != cudaSuccess ||
+                  cudaStreamSynchronize(stream_) != cudaSuccess)) {
+      std::free(h);
+      return -1;
+    }
+    *hostStates = h;
+    *countHost = times_.size();
+    return 0;
+  }
+  bool isEnabled() const { return enabled_; }
+  void setEnabled(bool on) { enabled_ = on; }
+  void setStream(cudaStream_t s) { stream_ = s; }
+  size_t size() const { return times_.size(); }
+
+ private:
+  void grow() {
+    const size_t cap = cap_ ? 2 * cap_ : 64;
+    T* p = nullptr;
+    if (cudaMalloc(reinterpret_cast<void**>(&p), cap * N * sizeof(T)) != cudaSuccess)
+      throw std::runtime_error("sfd: TrajectoryLogger allocation failed");
+    if (cap_ && (cudaMemcpyAsync(p, states_, cap_ * N * sizeof(T), cudaMemcpyDeviceToDevice, stream_) != cudaSuccess ||
+                 cudaStreamSynchronize(stream_) != cudaSuccess)) {
+      cudaFree(p);
+      throw std::runtime_error("sfd: TrajectoryLogger copy failed");
+    }
+    cudaFree(states_);
+    states_ = p;
+    cap_ = cap;
+  }
+  std::vector<double> times_;
+  T* states_ = nullptr;
+  size_t cap_ = 0;
+  bool enabled_ = true;
+  cudaStream_t stream_ = nullptr;
+};
+
 // Classic RK4 (AutonomousRungeKuttaStepper.cuh:123-375) on any
 // AutonomousProblem<T, N>; T is double or std_complex.  The stage combines
 // run on the device through the C ABI.
@@ -153,9 +229,11 @@ class AutonomousRungeKuttaStepper {
  public:
   // The stepper and the problem share one stream (created here, or the one
   // passed to setStream), so stage combines and RHS evaluations stay ordered.
-  AutonomousRungeKuttaStepper(AutonomousProblem<T, N>& problem, double tstep = 1e-2) : problem_(problem), dt_(tstep) {
+  AutonomousRungeKuttaStepper(AutonomousProblem<T, N>& problem, double tstep = 1e-2,
+                              std::shared_ptr<TrajectoryLogger<T, N>> logger = nullptr)
+      : problem_(problem), dt_(tstep), logger_(std::move(logger)) {
     const size_t bytes = sizeof(T) * (size_t)N;
-    for (double** p : {&y_, &ys_, &k_, &kacc_}) {
+    for (double** p : {&own_y_, &ys_, &k_, &kacc_}) {
       if (cudaMalloc(reinterpret_cast<void**>(p), bytes) != cudaSuccess) {
         release();
         throw std::runtime_error("sfd: cudaMalloc failed in AutonomousRungeKuttaStepper");
@@ -167,6 +245,8 @@ class AutonomousRungeKuttaStepper {
     }
     stream_ = own_stream_;
     problem_.setStream(stream_);
+    if (logger_) logger_->setStream(stream_);
+    y_ = own_y_;
   }
   ~AutonomousRungeKuttaStepper() { release(); }
   AutonomousRungeKuttaStepper(const AutonomousRungeKuttaStepper&) = delete;
@@ -176,11 +256,18 @@ class AutonomousRungeKuttaStepper {
   void setStream(cudaStream_t s) {
     stream_ = s;
     problem_.setStream(s);
+    if (logger_) logger_->setStream(s);
   }
-  // copies the initial state (host or device pointer) into the stepper
-  void initialize(const T* y0, bool onDevice = false) {
-    if (cudaMemcpyAsync(y_, y0, sizeof(T) * (size_t)N, onDevice ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
-                        stream_) != cudaSuccess)
+  // onDevice: adopt the caller's device array and advance it in place
+  // (AutonomousRungeKuttaStepper.cuh:312-318); otherwise copy the host state
+  // into the stepper's own array.
+  void initialize(T* y0, bool onDevice = false) {
+    if (onDevice) {
+      y_ = reinterpret_cast<double*>(y0);
+      return;
+    }
+    y_ = own_y_;
+    if (cudaMemcpyAsync(y_, y0, sizeof(T) * (size_t)N, cudaMemcpyHostToDevice, stream_) != cudaSuccess)
       throw std::runtime_error("sfd: initialize copy failed");
   }
   void runStep(int /*step*/ = 0) {
@@ -194,13 +281,18 @@ class AutonomousRungeKuttaStepper {
     check(sfd_rk4_final_device(n, y_, kacc_, dt_ / 6.0, stream_));
     time_ += dt_;
   }
-  // steps of dt from startTime while the time stays below endTime
-  // (runEvolution, AutonomousRungeKuttaStepper.cuh:404-437)
-  void runEvolution(double startTime, double endTime) {
+  // floor((endTime - startTime) / dt) steps, logging the state after each
+  // one when a logger is attached (AutonomousRungeKuttaStepper.cuh:417-437).
+  // Returns ReachedEndTime once all steps ran.
+  OdeSolverResult runEvolution(double startTime, double endTime) {
     time_ = startTime;
     const long long steps = (long long)((endTime - startTime) / dt_);
-    for (long long i = 0; i < steps; ++i) runStep((int)i);
+    for (long long i = 0; i < steps; ++i) {
+      runStep((int)i);
+      if (logger_) logger_->logTrajectory(time_, reinterpret_cast<const T*>(y_));
+    }
     if (cudaStreamSynchronize(stream_) != cudaSuccess) throw std::runtime_error("sfd: runEvolution failed");
+    return OdeSolverResult::ReachedEndTime;
   }
   T* getY() { return reinterpret_cast<T*>(y_); }
   double getCurrentTime() const { return time_; }
@@ -208,16 +300,17 @@ class AutonomousRungeKuttaStepper {
  private:
   void release() {
     if (stream_) cudaStreamSynchronize(stream_);
-    for (double* p : {y_, ys_, k_, kacc_}) cudaFree(p);
-    y_ = ys_ = k_ = kacc_ = nullptr;
+    for (double* p : {own_y_, ys_, k_, kacc_}) cudaFree(p);
+    y_ = own_y_ = ys_ = k_ = kacc_ = nullptr;
     if (own_stream_) {
-      // the problem outlives the stepper: hand it back its default stream
-      // before the stepper's stream goes away
+      // the problem and the logger outlive the stepper: hand them back their
+      // default streams before the stepper's stream goes away
       if (stream_ == own_stream_) {
         try {
           problem_.setStream(nullptr);
         } catch (...) {
         }
+        if (logger_) logger_->setStream(nullptr);
       }
       cudaStreamDestroy(own_stream_);
     }
@@ -228,7 +321,9 @@ class AutonomousRungeKuttaStepper {
   double time_ = 0.0;
   cudaStream_t stream_ = nullptr;
   cudaStream_t own_stream_ = nullptr;
-  double *y_ = nullptr, *ys_ = nullptr, *k_ = nullptr, *kacc_ = nullptr;
+  std::shared_ptr<TrajectoryLogger<T, N>> logger_;
+  double* y_ = nullptr;  // the state advanced in place: own_y_ or an adopted caller array
+  double *own_y_ = nullptr, *ys_ = nullptr, *k_ = nullptr, *kacc_ = nullptr;
 };
 
 // Batched dense FP64 solve of column-major N x N systems (MatrixSolver.cuh).

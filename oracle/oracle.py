@@ -310,3 +310,115 @@ def invariants(problem: Problem, x, y, phi, u, v, kappa: float = 0.0) -> np.ndar
     cp = problem.to_c()
     lib().orc_invariants(ctypes.byref(cp), x.size, _dp(x), _dp(y), _dp(phi), _dp(u), _dp(v), kappa, _dp(out))
     return out
+
+
+# ------------------------------------------------------------------ implicit GL2
+# Two-stage Gauss-Legendre (order 4) with damped Newton, as GaussLegendre2
+# (GaussLegendre.cuh:216-605, GLCoefficients.hpp:5-17, JacobianCalculator.cuh:223-284).
+# Generic over the right-hand side f: R^m -> R^m.  The Newton matrix is the
+# exact one of the stage equations R_i = k_i - f(y + h sum_j A_ij k_j):
+#   dR_i/dk_j = delta_ij I - h A_ij J(y_i);
+# the residual norm runs over both stages; the Armijo target stays at the
+# iteration's base point (phi(k + a d) <= phi(k) - c a |R(k)|^2); the step is
+# halved up to max_halvings times down to hmin = |t1 - t0| / 2^20 and then kept.
+_SQ3 = 1.7320508075688772935
+GL2_A = ((0.25, 0.25 - _SQ3 / 6.0), (0.25 + _SQ3 / 6.0, 0.25))
+GL2_B = (0.5, 0.5)
+
+
+def fd_jacobian(f, y, eps: float = 1e-6) -> np.ndarray:
+    """Central differences, column j = (f(y + eps e_j) - f(y - eps e_j)) / (2 eps)."""
+    y = _f64(y)
+    m = y.size
+    J = np.empty((m, m))
+    for j in range(m):
+        yp = y.copy()
+        ym = y.copy()
+        yp[j] += eps
+        ym[j] -= eps
+        J[:, j] = (f(yp) - f(ym)) / (2.0 * eps)
+    return J
+
+
+def gl2_step(f, jac, y, h: float, tol: float = 1e-10, max_newton: int = 20, allow_simplified: bool = False,
+             armijo_c: float = 1e-4, backtrack: float = 0.5, min_alpha: float = 1e-6):
+    """One GL2 step of size h: returns (converged, y_next, iterations, residual norm)."""
+    (a11, a12), (a21, a22) = GL2_A
+    m = y.size
+    fy = f(y)
+    k = np.concatenate([fy, fy])
+
+    def residual(kk):
+        y1 = y + h * (a11 * kk[:m] + a12 * kk[m:])
+        y2 = y + h * (a21 * kk[:m] + a22 * kk[m:])
+        return np.concatenate([kk[:m] - f(y1), kk[m:] - f(y2)]), (y1, y2)
+
+    R, ys = residual(k)
+    frozen = None
+    converged = False
+    it = 0
+    for it in range(max_newton):
+        nr = float(np.linalg.norm(R))
+        if nr <= tol * (1.0 + float(np.linalg.norm(k))):
+            converged = True
+            break
+        J1, J2 = (frozen, frozen) if frozen is not None else (jac(ys[0]), jac(ys[1]))
+        eye = np.eye(m)
+        M = np.block([[eye - h * a11 * J1, -h * a12 * J1], [-h * a21 * J2, eye - h * a22 * J2]])
+        d = np.linalg.solve(M, -R)
+        phi = 0.5 * nr * nr
+        alpha = 1.0
+        while True:
+            kt = k + alpha * d
+            Rt, yst = residual(kt)
+            if 0.5 * float(Rt @ Rt) <= phi - armijo_c * alpha * nr * nr:
+                k, R, ys = kt, Rt, yst
+                break
+            alpha *= backtrack
+            if alpha < min_alpha:
+                if frozen is None and allow_simplified:
+                    frozen = jac(y)
+                    break
+                return False, None, it, float(np.linalg.norm(Rt))
+    y_next = y + h * (GL2_B[0] * k[:m] + GL2_B[1] * k[m:])
+    return converged, y_next, it, float(np.linalg.norm(R))
+
+
+def gl2_evolve(f, y0, t0: float, t1: float, step: float, jac=None, tol: float = 1e-10, max_newton: int = 20,
+               allow_simplified: bool = False, armijo_c: float = 1e-4, backtrack: float = 0.5,
+               min_alpha: float = 1e-6, max_halvings: int = 6, eps: float = 1e-6):
+    """GaussLegendre2::runEvolution (GaussLegendre.cuh:227-330): returns (times, states), the
+    initial point included; raises RuntimeError when a step fails at every halving."""
+    if jac is None:
+        jac = lambda yy: fd_jacobian(f, yy, eps)  # noqa: E731
+    y = _f64(y0).copy()
+    fwd = 1.0 if t1 >= t0 else -1.0
+    hmin = abs(t1 - t0) / 2.0 ** 20
+    t = t0
+    times, states = [t], [y.copy()]
+    while (t - t1) * fwd < 0.0:
+        htry = min(step, abs(t1 - t)) * fwd
+        ok = False
+        for _ in range(max_halvings + 1):
+            ok, yn, _, res = gl2_step(f, jac, y, htry, tol, max_newton, allow_simplified, armijo_c, backtrack,
+                                      min_alpha)
+            if ok or abs(htry) <= hmin:
+                break
+            htry *= 0.5
+        if not ok:
+            raise RuntimeError(f"GL2 failed to converge at t={t}; residual {res:.3e}; last h {htry:.3e}")
+        y = yn
+        t += htry
+        step = abs(htry)
+        times.append(t)
+        states.append(y.copy())
+    return np.array(times), np.array(states)
+
+
+def boundary_rhs(problem: Problem):
+    """The oracle RHS as f(state) on the real state [x | y | phi]."""
+    def f(s):
+        n = s.size // 3
+        (dx, dy, dp), _ = rhs(problem, s[:n], s[n:2 * n], s[2 * n:])
+        return np.concatenate([dx, dy, dp])
+    return f

@@ -70,6 +70,28 @@ class SfdRkf45Result(ctypes.Structure):
                 ("h", c_double)]
 
 
+class GaussLegendreOptions(ctypes.Structure):
+    """ExportTypes.cuh:21-34 (the field order rhs.py's CGaussLegendreProperties binds)."""
+    _fields_ = [("t0", c_double), ("t1", c_double), ("stepSize", c_double), ("newtonTolerance", c_double),
+                ("maxNewtonIterations", c_size_t), ("allowSimplifiedFallback", c_bool),
+                ("returnTrajectory", c_bool), ("armijo_c", c_double), ("backtrack", c_double),
+                ("minAlpha", c_double), ("maxStepsHalves", c_size_t)]
+
+
+class SfdGl2Options(ctypes.Structure):
+    _fields_ = [("step", c_double), ("newton_tol", c_double), ("max_newton", c_longlong),
+                ("allow_simplified", c_int), ("armijo_c", c_double), ("backtrack", c_double),
+                ("min_alpha", c_double), ("max_halvings", c_longlong), ("fd_eps", c_double), ("jacobian", c_int)]
+
+
+class SfdGl2Result(ctypes.Structure):
+    _fields_ = [("status", c_int), ("steps", c_longlong), ("newton_iters", c_longlong), ("rhs_evals", c_longlong),
+                ("jacobians", c_longlong), ("halvings", c_longlong), ("t", c_double), ("h", c_double),
+                ("residual", c_double)]
+
+
+GL2_JACOBIAN_AUTO, GL2_JACOBIAN_FD, GL2_JACOBIAN_EXACT = 0, 1, 2
+
 _dp = POINTER(c_double)
 _SIGS = {
     "sfd_default_options": (None, [POINTER(SfdOptions)]),
@@ -129,6 +151,12 @@ _SIGS = {
     "integrateSimulationRK4": (c_int, [_dp, POINTER(_dp), POINTER(c_size_t), POINTER(_dp), POINTER(c_size_t),
                                        POINTER(SimProperties), POINTER(RK4SolverOptions), c_size_t]),
     "integrateSimulationRK4_freeMemory": (c_int, [_dp, _dp]),
+    "sfd_default_gl2_options": (None, [POINTER(SfdGl2Options)]),
+    "sfd_gl2_evolve": (c_int, [c_void_p, c_double, c_double, POINTER(SfdGl2Options), POINTER(SfdGl2Result), _dp, _dp,
+                               c_longlong]),
+    "integrateSimulationGL2": (c_int, [_dp, POINTER(_dp), POINTER(c_size_t), POINTER(_dp), POINTER(c_size_t),
+                                       POINTER(SimProperties), POINTER(GaussLegendreOptions), c_size_t]),
+    "integrateSimulationGL2_freeMemory": (c_int, [_dp, _dp]),
 }
 
 _lib = None

@@ -402,6 +402,18 @@ void sfd_adjoint_free(sfd_engine* e) {
   e->adj = nullptr;
 }
 
+// Why reverse mode does not cover the engine, or null when it does.
+const char* sfd_adjoint_unsupported(const sfd_engine* e) {
+  if (e->opt.precision != SFD_PRECISION_FP64) return "reverse mode needs an engine created with SFD_PRECISION_FP64";
+  if (e->nsurf != 1) return "reverse mode supports engines with one surface";
+  const SurfaceDesc& S = e->hs[0];
+  if (S.physics == 0 && S.rho != 0.0) return "reverse mode supports water with rho = 0 only";
+  if (S.physics == 1 && S.bern_variant != 0) return "reverse mode supports the standard helium Bernoulli closure only";
+  if (S.U != 0.0) return "reverse mode supports U = 0 only";
+  if (S.drive) return "reverse mode does not cover the optomechanical drive";
+  return nullptr;
+}
+
 namespace {
 
 template <typename T>
@@ -419,17 +431,8 @@ cudaError_t adj_alloc(AdjWork* W, T** p, size_t count) {
 
 int check_engine(sfd_engine* e) {
   if (!e) return sfd_internal_error(SFD_ERR_INVALID, "null engine");
-  if (e->opt.precision != SFD_PRECISION_FP64)
-    return sfd_internal_error(SFD_ERR_INVALID, "reverse mode needs an engine created with SFD_PRECISION_FP64");
-  if (e->nsurf != 1) return sfd_internal_error(SFD_ERR_INVALID, "reverse mode supports engines with one surface");
-  const SurfaceDesc& S = e->hs[0];
-  if (S.physics == 0 && S.rho != 0.0)
-    return sfd_internal_error(SFD_ERR_INVALID, "reverse mode supports water with rho = 0 only");
-  if (S.physics == 1 && S.bern_variant != 0)
-    return sfd_internal_error(SFD_ERR_INVALID, "reverse mode supports the standard helium Bernoulli closure only");
-  if (S.U != 0.0) return sfd_internal_error(SFD_ERR_INVALID, "reverse mode supports U = 0 only");
-  if (S.drive) return sfd_internal_error(SFD_ERR_INVALID, "reverse mode does not cover the optomechanical drive");
-  return 0;
+  const char* why = sfd_adjoint_unsupported(e);
+  return why ? sfd_internal_error(SFD_ERR_INVALID, why) : 0;
 }
 
 // Workspace with room for `steps` recorded steps (4 stage slots each).

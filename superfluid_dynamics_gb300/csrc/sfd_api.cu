@@ -452,6 +452,7 @@ void free_engine(sfd_engine* e) {
     if (p) cudaFree(p);
   sfd_adjoint_free(e);
   sfd_rkf45_free(e);
+  sfd_gl2_free(e);
   drain_profile(e);
   for (cudaEvent_t ev : e->event_pool) cudaEventDestroy(ev);
   for (auto& kv : e->d_tw) cudaFree(kv.second);
@@ -598,6 +599,7 @@ int sfd_create_driven(const int* n, int nsurf, const sfd_problem* problems, cons
   e->stream = e->own_stream;
   e->nsurf = nsurf;
   e->hs.resize(nsurf);
+  for (int s = 0; s < nsurf; ++s) e->hp.push_back(problems[shared_problem ? 0 : s]);
   long long off = 0, moff = 0, poff = 0;
   std::vector<long long> h_poff(nsurf);
   for (int s = 0; s < nsurf; ++s) {
@@ -1217,6 +1219,77 @@ int integrateSimulationRK4(double* initialState, double** statesOut, size_t* sta
 }
 
 int integrateSimulationRK4_freeMemory(double* statesOut, double* timesOut) {
+  std::free(statesOut);
+  std::free(timesOut);
+  return 0;
+}
+
+// integrateSimulationGL2 (Export.cu:665-738): helium (SI properties made
+// nondimensional as the other exports), state and times nondimensional as the
+// reference takes them, FP64 engine, GL2 options mapped one to one.
+int integrateSimulationGL2(double* initialState, double** statesOut, size_t* statesCount, double** timesOut,
+                           size_t* timesCount, SimProperties* sp, GaussLegendreOptions* gl, size_t N) {
+  if (!initialState || !statesOut || !statesCount || !timesOut || !timesCount || !sp || !gl)
+    return set_error(SFD_ERR_INVALID, "null argument");
+  if (N < 1 || 6 * N > 8192) return set_error(SFD_ERR_INVALID, "unsupported N %zu (GL2 needs 6N <= 8192)", N);
+  if (!(gl->stepSize > 0)) return set_error(SFD_ERR_INVALID, "Step size must be positive.");
+  NondimProps np = adimensionalize(sp->L, sp->rho, sp->kappa, sp->depth);
+  sfd_problem p = helium_problem(np, sp->use_expansions, sp->expansion_order, sp->infinite_depth);
+  sfd_options o;
+  sfd_default_options(&o);
+  o.precision = SFD_PRECISION_FP64;
+  o.use_graphs = 0;
+  o.autotune = 0;
+  int n = (int)N;
+  sfd_engine* e = nullptr;
+  int rc = sfd_create(&n, 1, &p, 1, &o, &e);
+  if (rc) return rc;
+  sfd_gl2_options go;
+  sfd_default_gl2_options(&go);
+  go.step = gl->stepSize;
+  go.newton_tol = gl->newtonTolerance;
+  go.max_newton = (long long)gl->maxNewtonIterations;
+  go.allow_simplified = gl->allowSimplifiedFallback ? 1 : 0;
+  go.armijo_c = gl->armijo_c;
+  go.backtrack = gl->backtrack;
+  go.min_alpha = gl->minAlpha;
+  go.max_halvings = (long long)gl->maxStepsHalves;
+  const size_t n3 = 3 * N;
+  std::vector<double> T, Y;
+  const bool traj = gl->returnTrajectory;
+  if (traj) {
+    T.push_back(gl->t0);
+    Y.assign(initialState, initialState + n3);
+  }
+  rc = sfd_set_state_host(e, initialState, initialState + N, initialState + 2 * N);
+  sfd_gl2_result r;
+  if (!rc) rc = sfd_internal_gl2(e, gl->t0, gl->t1, go, r, traj ? &T : nullptr, traj ? &Y : nullptr);
+  if (!rc && r.status != 0)
+    rc = set_error(SFD_ERR_NUMERICS, "Gauss-Legendre 2nd Order method failed to converge at t=%g; residual=%.3e; last htry=%.3e",
+                   r.t, r.residual, r.h);
+  if (!rc && !traj) {
+    Y.resize(n3);
+    rc = sfd_get_state_host(e, Y.data(), Y.data() + N, Y.data() + 2 * N);
+  }
+  sfd_destroy(e);
+  if (rc) return -1;
+  double* states = (double*)std::malloc(Y.size() * sizeof(double) + 1);
+  double* times = traj ? (double*)std::malloc(T.size() * sizeof(double) + 1) : nullptr;
+  if (!states || (traj && !times)) {
+    std::free(states);
+    std::free(times);
+    return set_error(SFD_ERR_INVALID, "host allocation failed");
+  }
+  std::memcpy(states, Y.data(), Y.size() * sizeof(double));
+  if (traj) std::memcpy(times, T.data(), T.size() * sizeof(double));
+  *statesOut = states;
+  *statesCount = Y.size() / n3;
+  *timesOut = times;
+  *timesCount = traj ? T.size() : 0;
+  return 0;
+}
+
+int integrateSimulationGL2_freeMemory(double* statesOut, double* timesOut) {
   std::free(statesOut);
   std::free(timesOut);
   return 0;

@@ -117,14 +117,6 @@ extern "C" int sfd_rk4_final_device(long long n, void* y0, const void* kacc, dou
 // factored by the engine's FP64 blocked LU without row exchanges (with the
 // pivot-growth certificate: max |l_ij| <= 1 means partial pivoting would have
 // chosen the same rows; otherwise the status word gets SFD_STATUS_PIVOT_SWAP).
-struct sfd_dense_solver {
-  int n = 0, np = 0, batch = 0;
-  SurfaceDesc* d_surf = nullptr;
-  double* mat = nullptr;
-  double* lmax = nullptr;
-  unsigned int* status = nullptr;
-  cudaStream_t stream = nullptr;
-};
 
 extern "C" int sfd_dense_solver_create(int n, int batch, sfd_dense_solver** out) {
   if (!out || n < 1 || n > 8192 || batch < 1) return sfd_internal_error(SFD_ERR_INVALID, "invalid argument");
@@ -166,12 +158,16 @@ extern "C" int sfd_dense_solver_set_stream(sfd_dense_solver* d, void* stream) {
 
 extern "C" int sfd_dense_solve(sfd_dense_solver* d, const double* M, const double* b, double* x, unsigned int* status) {
   if (!d || !M || !b || !x) return sfd_internal_error(SFD_ERR_INVALID, "null argument");
+  dim3 blk(16, 16), grid(nb(d->np, 16), nb(d->np, 16), d->batch);
+  k_colmajor_to_padded<<<grid, blk, 0, d->stream>>>(d->n, d->np, M, d->mat);
+  FCK(cudaGetLastError());
+  return sfd_internal_dense_factor_solve(d, b, x, status);
+}
+
+int sfd_internal_dense_factor_solve(sfd_dense_solver* d, const double* b, double* x, unsigned int* status) {
   cudaStream_t s = d->stream;
   FCK(cudaMemsetAsync(d->status, 0, d->batch * sizeof(unsigned int), s));
   FCK(cudaMemsetAsync(d->lmax, 0, d->batch * sizeof(double), s));
-  dim3 blk(16, 16), grid(nb(d->np, 16), nb(d->np, 16), d->batch);
-  k_colmajor_to_padded<<<grid, blk, 0, s>>>(d->n, d->np, M, d->mat);
-  FCK(cudaGetLastError());
   const int nbk = d->np / 64;
   for (int kb = 0; kb < nbk; ++kb) {
     k_lu64_diag<<<d->batch, 256, 0, s>>>(d->d_surf, d->batch, kb, d->mat, d->status, d->lmax);

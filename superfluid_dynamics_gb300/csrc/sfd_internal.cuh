@@ -102,7 +102,26 @@ struct sfd_engine {
   // complex-layout staging of the C++ facade (sfd_facade.cu), allocated on first use
   double* fc_in = nullptr;
   double* fc_out = nullptr;
+  // the problem of each surface as given to sfd_create (helper engines copy it)
+  std::vector<sfd_problem> hp;
+  // implicit Gauss-Legendre workspace (sfd_gl2.cu), allocated on first use
+  struct Gl2Work* gl2 = nullptr;
 };
+
+// Batched dense FP64 solver (sfd_facade.cu): `batch` systems of order n held
+// as padded row-major matrices (np = pad_n(n), identity padding) in `mat`.
+struct sfd_dense_solver {
+  int n = 0, np = 0, batch = 0;
+  SurfaceDesc* d_surf = nullptr;
+  double* mat = nullptr;
+  double* lmax = nullptr;
+  unsigned int* status = nullptr;
+  cudaStream_t stream = nullptr;
+};
+// Factor d->mat in place (blocked LU without row exchanges) and solve for
+// each system's right-hand side b (batch x n) into x; status (host, nullable,
+// batch words) as sfd_dense_solve.  Asynchronous unless status is given.
+int sfd_internal_dense_factor_solve(sfd_dense_solver* d, const double* b, double* x, unsigned int* status);
 
 // Entry points of sfd_api.cu used by the reverse mode.
 int sfd_internal_error(int code, const char* msg);
@@ -123,3 +142,11 @@ void sfd_rkf45_free(sfd_engine* e);
 int sfd_internal_solve(sfd_engine* e, const double* st);
 // Dynamic shared-memory limits of the solver kernels on the current device.
 cudaError_t sfd_solve_configure();
+// Why reverse mode does not cover the engine, or null when it does (sfd_adjoint.cu).
+const char* sfd_adjoint_unsupported(const sfd_engine* e);
+// implicit Gauss-Legendre workspace release (sfd_gl2.cu)
+void sfd_gl2_free(sfd_engine* e);
+// GL2 from t0 to t1 on the engine state (sfd_gl2.cu); times / states (host,
+// nullable) are appended the time and the 3n state after each accepted step.
+int sfd_internal_gl2(sfd_engine* e, double t0, double t1, const sfd_gl2_options& o, sfd_gl2_result& r,
+                     std::vector<double>* times, std::vector<double>* states);

@@ -218,6 +218,27 @@ class Engine:
         res = {"status": r.status, "accepted": r.accepted, "rejected": r.rejected, "t": r.t, "h": r.h}
         return res, times[:min(r.accepted, max_times)].copy()
 
+    def evolve_gl2(self, t0: float, t1: float, step: float = 0.01, newton_tol: float = 1e-10, max_newton: int = 20,
+                   allow_simplified: bool = False, armijo_c: float = 1e-4, backtrack: float = 0.5,
+                   min_alpha: float = 1e-6, max_halvings: int = 6, fd_eps: float = 1e-6,
+                   jacobian: str = "auto", max_steps: int = 1 << 16, record_states: bool = False):
+        """Implicit two-stage Gauss-Legendre of the resident state from t0 to t1
+        (the reference's GaussLegendre2).  jacobian: "auto", "fd" or "exact".
+        Returns (result dict, times of the accepted steps[, states after them])."""
+        mode = {"auto": _lib.GL2_JACOBIAN_AUTO, "fd": _lib.GL2_JACOBIAN_FD, "exact": _lib.GL2_JACOBIAN_EXACT}[jacobian]
+        o = _lib.SfdGl2Options(step, newton_tol, max_newton, 1 if allow_simplified else 0, armijo_c, backtrack,
+                               min_alpha, max_halvings, fd_eps, mode)
+        r = _lib.SfdGl2Result()
+        times = np.zeros(max_steps)
+        states = np.zeros((max_steps, 3 * self.ntot)) if record_states else None
+        check(self._L.sfd_gl2_evolve(self._h, float(t0), float(t1), ctypes.byref(o), ctypes.byref(r), _dp(times),
+                                     _dp(states) if record_states else None, max_steps))
+        res = {k: getattr(r, k) for k, _ in _lib.SfdGl2Result._fields_}
+        k = min(r.steps, max_steps)
+        if record_states:
+            return res, times[:k].copy(), states[:k].copy()
+        return res, times[:k].copy()
+
     def synchronize(self) -> None:
         check(self._L.sfd_synchronize(self._h))
 
@@ -444,6 +465,26 @@ class SimulationManager:
         T = np.ctypeslib.as_array(times, shape=(nt.value,)).copy() if nt.value else np.empty(0)
         self.lib.integrateSimulationRK4_freeMemory(states, times)
         return S, T
+
+    def integrate(self, y0, sim_props: _lib.SimProperties, gl_props: _lib.GaussLegendreOptions):
+        """rhs.py:224-264: GL2 integration (integrateSimulationGL2); returns
+        (rc, times, states) with states[i] = [x | y | phi] after step i (the
+        initial state first), or (rc, None, None) on failure."""
+        y0 = _f64(y0)
+        n = y0.size // 3
+        states = ctypes.POINTER(ctypes.c_double)()
+        times = ctypes.POINTER(ctypes.c_double)()
+        ns, nt = ctypes.c_size_t(), ctypes.c_size_t()
+        rc = self.lib.integrateSimulationGL2(_dp(y0), ctypes.byref(states), ctypes.byref(ns), ctypes.byref(times),
+                                             ctypes.byref(nt), ctypes.byref(sim_props), ctypes.byref(gl_props), n)
+        if rc != 0:
+            return rc, None, None
+        try:
+            S = np.ctypeslib.as_array(states, shape=(ns.value, 3 * n)).copy()
+            T = np.ctypeslib.as_array(times, shape=(nt.value,)).copy() if nt.value else np.empty(0)
+        finally:
+            self.lib.integrateSimulationGL2_freeMemory(states, times)
+        return rc, T, S
 
     def calculate_jacobian(self, x, y, phi, L, rho, kappa, depth, epsilon=1e-6):
         """rhs.py:213-222: (rc, J) with J[row, col] = d rhs_row / d state_col, a
