@@ -83,6 +83,23 @@ std::vector<cd> twiddles(int n) {
   return t;
 }
 
+// Twiddles of the cluster transform of length n = C M (C CTAs, R = M / C),
+// laid out so that each CTA reads its own slice contiguously:
+// [W_n^{C e}, e < M | for c < C: W_n^{c e}, e < M; W_n^{q (c R + t)}, q < C, t < R].
+std::vector<cd> cluster_twiddles(int n, const std::vector<cd>& tw) {
+  const int C = SFD_FFT_CLUSTER, M = n / C, R = M / C;
+  std::vector<cd> t((size_t)(1 + 2 * C) * M);
+  for (int e = 0; e < M; ++e) t[e] = tw[(size_t)C * e];
+  for (int c = 0; c < C; ++c) {
+    cd* twc = t.data() + M + (size_t)c * 2 * M;
+    cd* twq = twc + M;
+    for (int e = 0; e < M; ++e) twc[e] = tw[(size_t)c * e];
+    for (int q = 0; q < C; ++q)
+      for (int r = 0; r < R; ++r) twq[q * R + r] = tw[(size_t)q * (c * R + r)];
+  }
+  return t;
+}
+
 // radices: 4s, then a 2, then odd primes ascending
 bool factorize(int n, std::vector<int>& rad) {
   rad.clear();
@@ -456,6 +473,7 @@ void free_engine(sfd_engine* e) {
   drain_profile(e);
   for (cudaEvent_t ev : e->event_pool) cudaEventDestroy(ev);
   for (auto& kv : e->d_tw) cudaFree(kv.second);
+  for (auto& kv : e->d_ctw) cudaFree(kv.second);
   if (e->own_stream) cudaStreamDestroy(e->own_stream);
   delete e;
 }
@@ -643,6 +661,16 @@ int sfd_create_driven(const int* n, int nsurf, const sfd_problem* problems, cons
       CKE(cudaMemcpy(d, t.data(), ns * sizeof(cd), cudaMemcpyHostToDevice));
     }
     S.tw = e->d_tw[ns];
+    if (S.nrad_m > 0) {
+      if (!e->d_ctw.count(ns)) {
+        std::vector<cd> t = twiddles(ns), ct = cluster_twiddles(ns, t);
+        cd* d = nullptr;
+        CKE(dalloc(&d, (long long)ct.size()));
+        e->d_ctw[ns] = d;
+        CKE(cudaMemcpy(d, ct.data(), ct.size() * sizeof(cd), cudaMemcpyHostToDevice));
+      }
+      S.ctw = e->d_ctw[ns];
+    }
     if (S.physics == 0 && S.rho != 0.0) e->any_rho = true;
     int np = pad_n(ns);
     h_poff[s] = poff;

@@ -23,6 +23,7 @@ struct SurfaceDesc {
   int bern_variant;     // 0 standard, 1 series expansion (createM.cuh:171-193), 2 surface tension (:200-211)
   int expansion_order;
   const cd* tw;         // forward FFT twiddles exp(-2 pi i e / n), e in [0, n)
+  const cd* ctw;        // cluster transforms (nrad_m > 0): [W_n^{C e} | per CTA c: W_n^{c e}, W_n^{q (c R + t)}], M = n / C, R = M / C
   int nrad;
   int rad[SFD_MAX_RADICES];
   int nrad_m;           // radices of n / SFD_FFT_CLUSTER (cluster transforms; 0 = not eligible)

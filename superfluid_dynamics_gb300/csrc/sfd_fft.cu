@@ -37,11 +37,12 @@ __device__ __forceinline__ void stockham_pass(cd* buf, int n, int p, const cd* t
   const int stw = n / (p * R) * ts;
   constexpr int C = (MPT + R - 1) / R;  // butterflies per thread (T = n / R <= C * NT)
   cd u[C][R];
+  const bool pow2 = (p & (p - 1)) == 0;
 #pragma unroll
   for (int c = 0; c < C; ++c) {
     int i = threadIdx.x + c * NT;
     if (i < T) {
-      int k = i % p;
+      int k = pow2 ? (i & (p - 1)) : i % p;
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         cd v = buf[i + r * T];
@@ -55,7 +56,7 @@ __device__ __forceinline__ void stockham_pass(cd* buf, int n, int p, const cd* t
   for (int c = 0; c < C; ++c) {
     int i = threadIdx.x + c * NT;
     if (i < T) {
-      int k = i % p;
+      int k = pow2 ? (i & (p - 1)) : i % p;
       int j = (i - k) * R + k;
       if (R == 2) {
         buf[j] = u[c][0] + u[c][1];
@@ -126,16 +127,32 @@ __device__ __forceinline__ void cta_fft(cd* buf, const SurfaceDesc& S, int sign)
 // Spectral multipliers, restated from utilities.cuh:106-148 (first) and
 // :178-200 (second), including the reference's Nyquist treatment: the first
 // derivative maps mode n/2 to i (pi/2) c and zeroes mode n/2 + 1.
-__device__ __forceinline__ cd first_mult(cd c, int i, int n) {
-  double dn = (double)n;
-  if (i < n / 2) return {(double)(-i) * c.im / dn, (double)i * c.re / dn};
-  if (i == n / 2) return {-SFD_PI * i * c.im / dn, SFD_PI * i * c.re / dn};
-  if (i == n / 2 + 1) return {0.0, 0.0};
-  return {(double)(-(i - n)) * c.im / dn, (double)(i - n) * c.re / dn};
+// inv_n = 1 / n: the multipliers scale by a reciprocal instead of dividing
+// (FP64 division is a long dependent sequence on the FP64 pipe).
+__device__ __forceinline__ cd first_mult(cd c, int i, int n, double inv_n) {
+  double f;
+  if (i < n / 2) f = (double)i * inv_n;
+  else if (i == n / 2) f = SFD_PI * i * inv_n;
+  else if (i == n / 2 + 1) return {0.0, 0.0};
+  else f = (double)(i - n) * inv_n;
+  return {-f * c.im, f * c.re};
 }
-__device__ __forceinline__ cd second_mult(cd c, int i, int n) {
-  int kk = (i <= n / 2) ? -i * i : -(i - n) * (i - n);
-  return {(double)kk * c.re / (double)n, (double)kk * c.im / (double)n};
+__device__ __forceinline__ cd second_mult(cd c, int i, int n, double inv_n) {
+  const int kk = (i <= n / 2) ? -i * i : -(i - n) * (i - n);
+  const double f = (double)kk * inv_n;
+  return {f * c.re, f * c.im};
+}
+// xi_j = 2 pi j / n rounded exactly as the division of the reference
+// (Derivatives.cuh:285) rounds it: the product 2 pi j, then its quotient by n
+// from the correctly rounded reciprocal and one correction with the exact
+// remainder (Markstein's quotient refinement), which gives the correctly
+// rounded quotient.  x - xi is a near-cancellation for Eulerian nodes, so the
+// abscissa must match the reference's bit for bit, not to within an ulp.
+__device__ __forceinline__ double xi_node(int j, double dn, double inv_n) {
+  const double a = 2.0 * SFD_PI * (double)j;
+  const double q0 = a * inv_n;
+  const double r = fma(-q0, dn, a);
+  return fma(r, inv_n, q0);
 }
 
 }  // namespace
@@ -147,12 +164,14 @@ __global__ void __launch_bounds__(kFftThreads, 1) k_spectral_deriv(DerivArgs A, 
   const SurfaceDesc& S = A.surf[job.x];  // read in place: copying would put rad[] on the stack
   const int n = S.n, off = S.off, kind = job.y;
   const double rho = S.physics == 0 ? S.rho : 0.0;
+  const double dn = (double)n, inv_n = 1.0 / dn;
+  const double uq = -(1 + rho) * SFD_PI * S.U / n;  // linear part of phi per node (same rounding as per element)
   for (int j = threadIdx.x; j < n; j += kFftThreads) {
     cd v;
     if (kind == SFD_JOB_ZP || kind == SFD_JOB_ZPP) {
-      v = {A.x[off + j] - 2 * SFD_PI * (double)j / n, A.y[off + j]};          // Derivatives.cuh:285,317
+      v = {A.x[off + j] - xi_node(j, dn, inv_n), A.y[off + j]};                // Derivatives.cuh:285,317
     } else if (kind == SFD_JOB_PHIP) {
-      v = {A.phi[off + j] - (-(1 + rho) * SFD_PI * S.U / n * (double)j),      // Derivatives.cuh:286,318
+      v = {A.phi[off + j] - uq * (double)j,                                    // Derivatives.cuh:286,318
            A.phi_im ? A.phi_im[off + j] : 0.0};
     } else if (kind == SFD_JOB_RAW || kind == SFD_JOB_RAW2) {
       v = {A.x[off + j], A.y ? A.y[off + j] : 0.0};
@@ -164,7 +183,8 @@ __global__ void __launch_bounds__(kFftThreads, 1) k_spectral_deriv(DerivArgs A, 
   __syncthreads();
   cta_fft(buf, S, -1);
   for (int i = threadIdx.x; i < n; i += kFftThreads)
-    buf[i] = (kind == SFD_JOB_ZPP || kind == SFD_JOB_RAW2) ? second_mult(buf[i], i, n) : first_mult(buf[i], i, n);
+    buf[i] = (kind == SFD_JOB_ZPP || kind == SFD_JOB_RAW2) ? second_mult(buf[i], i, n, inv_n)
+                                                           : first_mult(buf[i], i, n, inv_n);
   __syncthreads();
   cta_fft(buf, S, +1);
   const double s1 = 2.0 * SFD_PI / n;
@@ -195,31 +215,39 @@ __global__ void __launch_bounds__(kFftThreads, 1) k_spectral_deriv(DerivArgs A, 
 //   multiply: X <- mult(X)  (reference Nyquist rules, global index k)
 //   inverse:  V_c[k1] = W_n^{-c k1} sum_k2 W_C^{-c k2} X[k1 + M k2]   (CTA owning k1)
 //             x[C m + c] = IFFT_M(V_c)[m]                        (CTA c, via DSMEM)
-// so each SM does 1/C of the FP64 work and the exchange stays on chip.
+// so each SM does 1/C of the FP64 work and the exchange stays on chip.  GB300
+// runs FP64 at 2 FMA per clock per SM, so the kernel counts FP64 operations:
+// no division per element, and the exchange's 8-point transforms split over
+// two lanes (one shuffle butterfly + a 4-point DFT each), which keeps one
+// warp per SM sub-partition busy at R = 64 with close to the arithmetic of a
+// single-lane transform.
 namespace {
 constexpr int kCT = 512;        // threads per CTA of the cluster kernel
 constexpr int kCMPT = 2;        // values per thread in the M-point FFT (M <= 1024)
+constexpr double kH = 0.70710678118654752440;
 
-// 8-point DFT of u (in place), sign -1 forward / +1 inverse, radix-2 DIT.
-__device__ __forceinline__ void dft8(cd* u, int sign) {
-  const double h = 0.70710678118654752440;
-  // bit-reversed order
-  cd a0 = u[0], a1 = u[4], a2 = u[2], a3 = u[6], a4 = u[1], a5 = u[5], a6 = u[3], a7 = u[7];
-  // stage 1 (length 2)
-  cd b0 = a0 + a1, b1 = a0 - a1, b2 = a2 + a3, b3 = a2 - a3;
-  cd b4 = a4 + a5, b5 = a4 - a5, b6 = a6 + a7, b7 = a6 - a7;
-  // stage 2 (length 4): twiddle W4^1 = -i (forward) on the odd element
-  cd t3 = rot(b3, sign), t7 = rot(b7, sign);
-  cd c0 = b0 + b2, c2 = b0 - b2, c1 = b1 + t3, c3 = b1 - t3;
-  cd c4 = b4 + b6, c6 = b4 - b6, c5 = b5 + t7, c7 = b5 - t7;
-  // stage 3 (length 8): W8^1 = h(1 - i s), W8^2 = rot, W8^3 = h(-1 - i s) with s = +-1 by sign
-  double sg = sign < 0 ? 1.0 : -1.0;
-  cd w1 = {h, -sg * h}, w3 = {-h, -sg * h};
-  cd d5 = c5 * w1, d6 = rot(c6, sign), d7 = c7 * w3;
-  u[0] = c0 + c4; u[4] = c0 - c4;
-  u[1] = c1 + d5; u[5] = c1 - d5;
-  u[2] = c2 + d6; u[6] = c2 - d6;
-  u[3] = c3 + d7; u[7] = c3 - d7;
+__device__ __forceinline__ cd shfl_xor_cd(cd a, int m) {
+  return {__shfl_xor_sync(0xffffffffu, a.re, m), __shfl_xor_sync(0xffffffffu, a.im, m)};
+}
+// W_8^j for j < 4, sign -1 (forward, e^{-2 pi i j / 8}) or +1 (inverse)
+__device__ __forceinline__ cd w8(int j, int sign) {
+  const double sg = sign < 0 ? -1.0 : 1.0;
+  switch (j) {
+    case 0: return {1.0, 0.0};
+    case 1: return {kH, sg * kH};
+    case 2: return {0.0, sg};
+    default: return {-kH, sg * kH};
+  }
+}
+// 4-point DFT in registers, natural order in and out (sign -1 forward,
+// +1 inverse without scaling).
+__device__ __forceinline__ void dft4(cd* y, int sign) {
+  const cd a0 = y[0] + y[2], a1 = y[0] - y[2];
+  const cd b0 = y[1] + y[3], b1 = rot(y[1] - y[3], sign);
+  y[0] = a0 + b0;
+  y[1] = a1 + b1;
+  y[2] = a0 - b0;
+  y[3] = a1 - b1;
 }
 }  // namespace
 
@@ -228,6 +256,7 @@ __global__ void __cluster_dims__(SFD_FFT_CLUSTER, 1, 1) __launch_bounds__(kCT)
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();
   constexpr int C = SFD_FFT_CLUSTER;
+  static_assert(C == 8, "the exchange step is written for 8-CTA clusters");
   extern __shared__ double2 csmem_raw[];
   const int2 job = jobs[blockIdx.y];
   const SurfaceDesc& S = A.surf[job.x];
@@ -238,25 +267,21 @@ __global__ void __cluster_dims__(SFD_FFT_CLUSTER, 1, 1) __launch_bounds__(kCT)
   cd* buf = reinterpret_cast<cd*>(csmem_raw);  // M values
   cd* vbuf = buf + M;                          // C x R values
   cd* twm = vbuf + M;                          // W_M^e = W_n^{C e}, e < M
-  cd* twc = twm + M;                           // W_n^{c k1}, k1 < M (this CTA's c)
-  cd* twq = twc + M;                           // W_n^{q k1}, q < C, k1 in this CTA's range: [q R + t]
+  const double2* twc = reinterpret_cast<const double2*>(S.ctw) + M + (size_t)c * 2 * M;  // W_n^{c k1}
+  const double2* twq = twc + M;                                                          // W_n^{q (c R + t)}
   const double rho = S.physics == 0 ? S.rho : 0.0;
+  const double dn = (double)n, inv_n = 1.0 / dn;
+  const double uq = -(1 + rho) * SFD_PI * S.U / n;  // linear part of phi per node
   for (int e = threadIdx.x; e < M; e += kCT) {
-    double2 a = __ldg(reinterpret_cast<const double2*>(S.tw) + C * e);
-    double2 b = __ldg(reinterpret_cast<const double2*>(S.tw) + c * e);
-    int q = e / R, t = e - q * R;
-    double2 d = __ldg(reinterpret_cast<const double2*>(S.tw) + q * (c * R + t));
+    const double2 a = __ldg(reinterpret_cast<const double2*>(S.ctw) + e);
     twm[e] = {a.x, a.y};
-    twc[e] = {b.x, b.y};
-    twq[e] = {d.x, d.y};
   }
   // 1. decimated load x[C m + c]
   for (int m = threadIdx.x; m < M; m += kCT) {
     const int j = C * m + c;
     cd v;
-    if (kind == SFD_JOB_ZP || kind == SFD_JOB_ZPP) v = {A.x[off + j] - 2 * SFD_PI * (double)j / n, A.y[off + j]};
-    else if (kind == SFD_JOB_PHIP)
-      v = {A.phi[off + j] - (-(1 + rho) * SFD_PI * S.U / n * (double)j), A.phi_im ? A.phi_im[off + j] : 0.0};
+    if (kind == SFD_JOB_ZP || kind == SFD_JOB_ZPP) v = {A.x[off + j] - xi_node(j, dn, inv_n), A.y[off + j]};
+    else if (kind == SFD_JOB_PHIP) v = {A.phi[off + j] - uq * (double)j, A.phi_im ? A.phi_im[off + j] : 0.0};
     else if (kind == SFD_JOB_RAW) v = {A.x[off + j], A.y[off + j]};
     else v = {A.a[off + j], 0.0};
     buf[m] = v;
@@ -264,27 +289,65 @@ __global__ void __cluster_dims__(SFD_FFT_CLUSTER, 1, 1) __launch_bounds__(kCT)
   __syncthreads();
   cta_fft_n<kCT, kCMPT>(buf, M, S.rad_m, S.nrad_m, twm, 1, -1);
   // 2. Z_c[k1] = W_n^{c k1} Y_c[k1]
-  for (int k1 = threadIdx.x; k1 < M; k1 += kCT)
-    if (c && k1) buf[k1] = buf[k1] * twc[k1];
+  if (c) {
+    for (int k1 = threadIdx.x; k1 < M; k1 += kCT)
+      if (k1) {
+        const double2 w = __ldg(twc + k1);
+        buf[k1] = buf[k1] * cd{w.x, w.y};
+      }
+  }
   cluster.sync();
-  // 3. exchange across the cluster for this CTA's k1 range
-  for (int t = threadIdx.x; t < R; t += kCT) {
-    const int k1 = c * R + t;
-    cd u[C];
+  // 3. exchange across the cluster for this CTA's k1 range.  Two lanes per
+  //    k1: lane h holds the values of CTAs 4h..4h+3; one shuffle butterfly
+  //    (span 4) plus an in-register 4-point DFT per lane give X[k1 + M (2k + h)]
+  //    in lane h, and the inverse runs the same two steps backwards.  A warp
+  //    covers 16 k1 values and skips the loop when none of them is in range;
+  //    inside a partly filled warp every lane shuffles and the idle ones only
+  //    skip their loads and stores.
+  {
+    const int h = threadIdx.x & 1;
+    const int warp_t = (threadIdx.x >> 5) * 16;
+    for (int t0 = 0; t0 < R; t0 += kCT / 2) {
+      if (t0 + warp_t >= R) break;
+      const int t = t0 + (threadIdx.x >> 1);
+      const bool act = t < R;
+      const int k1 = c * R + t;
+      cd v[4];
 #pragma unroll
-    for (int q = 0; q < C; ++q) u[q] = cluster.map_shared_rank(buf, q)[k1];
-    dft8(u, -1);
-    cd y[C];
+      for (int q = 0; q < 4; ++q) v[q] = act ? cluster.map_shared_rank(buf, 4 * h + q)[k1] : cd{0.0, 0.0};
+      // forward, span 4: lane 0 keeps x_q + x_{q+4}, lane 1 (x_q - x_{q+4}) W_8^q
 #pragma unroll
-    for (int k2 = 0; k2 < C; ++k2) {
-      int k = k1 + M * k2;
-      y[k2] = second ? second_mult(u[k2], k, n) : first_mult(u[k2], k, n);
-    }
-    dft8(y, +1);
+      for (int q = 0; q < 4; ++q) {
+        const cd o = shfl_xor_cd(v[q], 1);
+        const cd sq = h ? o - v[q] : v[q] + o;
+        v[q] = (h && q) ? sq * w8(q, -1) : sq;
+      }
+      dft4(v, -1);  // lane h: X[k1 + M (2k + h)] in v[k]
 #pragma unroll
-    for (int q = 0; q < C; ++q) {
-      cd w = (q && k1) ? y[q] * cconj(twq[q * R + t]) : y[q];
-      vbuf[q * R + t] = w;
+      for (int k = 0; k < 4; ++k) {
+        const int kk = k1 + M * (2 * k + h);
+        v[k] = second ? second_mult(v[k], kk, n, inv_n) : first_mult(v[k], kk, n, inv_n);
+      }
+      // inverse: 4-point inverse DFT per lane, then the span-4 butterfly with W_8^{+q}
+      dft4(v, +1);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const cd wq = (h && q) ? v[q] * w8(q, +1) : v[q];
+        const cd o = shfl_xor_cd(wq, 1);
+        v[q] = h ? o - wq : wq + o;  // lane h: sum over k2 for target CTA 4h + q
+      }
+      if (act) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int qq = 4 * h + q;
+          cd u = v[q];
+          if (qq && k1) {
+            const double2 w = __ldg(twq + qq * R + t);
+            u = u * cd{w.x, -w.y};
+          }
+          vbuf[qq * R + t] = u;
+        }
+      }
     }
   }
   cluster.sync();
@@ -307,7 +370,7 @@ __global__ void __cluster_dims__(SFD_FFT_CLUSTER, 1, 1) __launch_bounds__(kCT)
         A.zp[j] = {x.re * s1 + s1, x.im * s1};           // :323,374
       } else if (kind == SFD_JOB_PHIP) {
         double r = x.re * s1;                           // :324, complex_to_real
-        if (S.U != 0) r += -(1 + rho) * SFD_PI * S.U / n;
+        if (S.U != 0) r += uq;
         A.phip[j] = r;
       } else if (kind == SFD_JOB_RAW) {
         A.ap[j] = x;
@@ -323,14 +386,14 @@ __global__ void __cluster_dims__(SFD_FFT_CLUSTER, 1, 1) __launch_bounds__(kCT)
 cudaError_t sfd_launch_spectral_cluster(const DerivArgs& A, const int2* jobs, int njobs, int max_n, cudaStream_t st) {
   if (njobs == 0) return cudaSuccess;
   const int M = max_n / SFD_FFT_CLUSTER;
-  size_t smem = (size_t)5 * M * sizeof(cd);
+  size_t smem = (size_t)3 * M * sizeof(cd);
   k_spectral_cluster<<<dim3(SFD_FFT_CLUSTER, njobs), kCT, smem, st>>>(A, jobs);
   return cudaGetLastError();
 }
 
 cudaError_t sfd_fft_configure() {
   cudaError_t e = cudaFuncSetAttribute(k_spectral_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       5 * (8192 / SFD_FFT_CLUSTER) * (int)sizeof(cd));
+                                       3 * (8192 / SFD_FFT_CLUSTER) * (int)sizeof(cd));
   if (e != cudaSuccess) return e;
   return cudaFuncSetAttribute(k_spectral_deriv, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               8192 * (int)sizeof(cd));

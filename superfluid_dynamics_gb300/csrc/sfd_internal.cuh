@@ -50,6 +50,7 @@ struct sfd_engine {
   SurfaceDesc* d_surf = nullptr;
   int* d_node_surf = nullptr;
   std::map<int, cd*> d_tw;
+  std::map<int, cd*> d_ctw;  // cluster-transform twiddle tables by n
   // work lists
   int2* d_jobs_first = nullptr; int njobs_first = 0;
   int2* d_jobs_ap = nullptr; int njobs_ap = 0;
