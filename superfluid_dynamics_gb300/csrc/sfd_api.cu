@@ -179,7 +179,7 @@ inline int blocks_for(long long n, int t) { return (int)((n + t - 1) / t); }
 int enqueue_sums(sfd_engine* e, int prec, const double* weights, const float2* weights_df, int mode, bool track_norm) {
   SumArgs A{e->d_surf, e->d_sum_items, e->nsurf, e->ntot, e->nd.w, e->nd.p, weights, e->nd.wdf,
             e->nd.pdf, weights_df, e->nd.mdiag, e->zp, e->phip,
-            e->cacc, e->dacc, e->r, track_norm ? e->rnorm : nullptr, mode};
+            e->cacc, e->dacc, e->r, track_norm ? e->rnorm : nullptr, mode, e->rf};
   int cls = prec == SFD_PREC_F64 ? SFD_K_SUMS64 : prec == SFD_PREC_DF ? SFD_K_SUMSDF : SFD_K_SUMS32;
   LAUNCHC(e, cls, sfd_launch_sums(prec, A, e->nsum, e->max_n, e->sum_groups[prec], e->stream));
   return 0;
@@ -187,13 +187,19 @@ int enqueue_sums(sfd_engine* e, int prec, const double* weights, const float2* w
 
 // y = X v with the current preconditioner (FP16 copy or FP32); ydf: optional
 // double-float copy of y.
-int enqueue_gemv(sfd_engine* e, const double* v, double* y, float2* ydf) {
-  if (e->m16)
+int enqueue_gemv(sfd_engine* e, const float* vf, double* y, float2* ydf, double* acc, float2* accdf) {
+  if (e->m16 && e->nsurf == 1 && e->nsm > 0) {
+    // one surface: a whole number of waves of two CTAs per SM, rows interleaved
+    const int wave = 2 * e->nsm, need = (e->max_n + kGemvRows - 1) / kGemvRows;
+    const int grid = (need + wave - 1) / wave * wave;
+    LAUNCHC(e, SFD_K_GEMV, k_gemv_h<<<grid, 512, e->max_np * sizeof(float), e->stream>>>(
+                               e->d_surf, nullptr, e->m16, e->rscale, vf, y, ydf, acc, accdf));
+  } else if (e->m16)
     LAUNCHC(e, SFD_K_GEMV, k_gemv_h<<<e->ngemv, 512, e->max_np * sizeof(float), e->stream>>>(
-                               e->d_surf, e->d_gemv_rows, e->m16, e->rscale, v, y, ydf));
+                               e->d_surf, e->d_gemv_rows, e->m16, e->rscale, vf, y, ydf, acc, accdf));
   else
     LAUNCHC(e, SFD_K_GEMV, k_gemv<<<e->ngemv, 256, e->max_np * sizeof(float), e->stream>>>(
-                               e->d_surf, e->d_gemv_rows, e->m32, v, y, ydf));
+                               e->d_surf, e->d_gemv_rows, e->m32, vf, y, ydf, acc, accdf));
   return 0;
 }
 
@@ -235,7 +241,7 @@ int enqueue_precond(sfd_engine* e) {
 int enqueue_solve(sfd_engine* e, const double* st, const double* phi_im, bool refactor) {
   const int nt = e->ntot;
   const double *x = st, *y = st + nt, *phi = st + 2 * nt;
-  DerivArgs D{e->d_surf, e->nsurf, x, y, phi, phi_im, e->a, e->zp, e->zpp, e->phip, e->ap};
+  DerivArgs D{e->d_surf, e->nsurf, x, y, phi, phi_im, e->a, e->zp, e->zpp, e->phip, e->ap, e->phipf};
   if (e->njobs_first)
     LAUNCHC(e, SFD_K_SPECTRAL, sfd_launch_spectral(D, e->d_jobs_first, e->njobs_first, e->max_n_single, e->stream));
   if (e->ncjobs_first)
@@ -268,21 +274,21 @@ int enqueue_solve(sfd_engine* e, const double* st, const double* phi_im, bool re
     // a0 = X phi'; FP32 pre-iterations (full residual in FP32) bring a within
     // ~1e-7 of the solution; one double-float pass then gives the accurate
     // residual and C(a); FP32 post-iterations correct the small remainder.
-    int rc = enqueue_gemv(e, e->phip, e->a, e->adf);
+    // The products read FP32 copies of phi' and r written by their producers;
+    // the updates a += delta run in the product's epilogue.
+    int rc = enqueue_gemv(e, e->phipf, e->a, e->adf, nullptr, nullptr);
     if (rc) return rc;
     for (int it = 0; it < e->opt.pre_iters; ++it) {
       rc = enqueue_sums(e, SFD_PREC_F32, e->a, e->adf, 0, false);
       if (rc) return rc;
-      rc = enqueue_gemv(e, e->r, e->delta, nullptr);
+      rc = enqueue_gemv(e, e->rf, nullptr, nullptr, e->a, e->adf);
       if (rc) return rc;
-      LAUNCH(e, k_axpy_inplace<<<blocks_for(nt, 256), 256, 0, e->stream>>>(nt, e->a, e->delta, e->adf));
     }
     rc = enqueue_sums(e, SFD_PREC_DF, e->a, e->adf, 0, e->opt.refine_iters == 0);
     if (rc) return rc;
     for (int it = 0; it < e->opt.refine_iters; ++it) {
-      rc = enqueue_gemv(e, e->r, e->delta, e->ddf);
+      rc = enqueue_gemv(e, e->rf, e->delta, e->ddf, e->a, nullptr);
       if (rc) return rc;
-      LAUNCH(e, k_axpy_inplace<<<blocks_for(nt, 256), 256, 0, e->stream>>>(nt, e->a, e->delta, nullptr));
       rc = enqueue_sums(e, SFD_PREC_F32, e->delta, e->ddf, 1, it == e->opt.refine_iters - 1);
       if (rc) return rc;
     }
@@ -464,7 +470,7 @@ void free_engine(sfd_engine* e) {
                   e->d_gemv_rows, e->d_poff, e->y0, e->ys, e->kacc, e->kcur, e->zp, e->zpp, e->ap, e->phip, e->a,
                   e->r, e->delta, e->phi_im, e->nd.w, e->nd.p, e->nd.wdf, e->nd.pdf, e->adf, e->ddf, e->nd.mdiag, e->nd.v1low, e->nd.v1up, e->nd.v2,
                   e->cacc, e->dacc, e->vel_low1, e->status, e->lmax, e->rnorm,
-                  e->inv_out, e->m64, e->m32, e->m16, e->rscale, e->fc_in, e->fc_out, e->pbuf, e->rbuf, e->cbuf, e->cparts, e->rparts};
+                  e->inv_out, e->m64, e->m32, e->m16, e->rscale, e->fc_in, e->fc_out, e->rf, e->phipf, e->pbuf, e->rbuf, e->cbuf, e->cparts, e->rparts};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   sfd_adjoint_free(e);
@@ -613,6 +619,7 @@ int sfd_create_driven(const int* n, int nsurf, const sfd_problem* problems, cons
     }                               \
   } while (0)
   CKE(cudaSetDevice(e->device));
+  CKE(cudaDeviceGetAttribute(&e->nsm, cudaDevAttrMultiProcessorCount, e->device));
   CKE(cudaStreamCreateWithFlags(&e->own_stream, cudaStreamNonBlocking));
   e->stream = e->own_stream;
   e->nsurf = nsurf;
@@ -761,6 +768,10 @@ int sfd_create_driven(const int* n, int nsurf, const sfd_problem* problems, cons
   CKE(dalloc(&e->nd.pdf, nt));
   CKE(dalloc(&e->adf, nt));
   CKE(dalloc(&e->ddf, nt));
+  if (e->opt.precision == SFD_PRECISION_MIXED) {
+    CKE(dalloc(&e->rf, nt));
+    CKE(dalloc(&e->phipf, nt));
+  }
   CKE(dalloc(&e->nd.mdiag, nt));
   CKE(dalloc(&e->nd.v1low, nt));
   CKE(dalloc(&e->nd.v1up, nt));

@@ -61,4 +61,5 @@ struct DerivArgs {
   cd* zpp;
   double* phip;
   cd* ap;
+  float* phipf;  // FP32 copy of phi' for the preconditioner product (nullable)
 };

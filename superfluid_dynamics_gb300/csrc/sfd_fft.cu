@@ -198,6 +198,7 @@ __global__ void __launch_bounds__(kFftThreads, 1) k_spectral_deriv(DerivArgs A, 
         double r = v.re * s1;                                                 // :324, complex_to_real
         if (S.U != 0) r += -(1 + rho) * SFD_PI * S.U / n;                     // :380-383
         A.phip[off + j] = r;
+        if (A.phipf) A.phipf[off + j] = (float)r;
         break;
       }
       case SFD_JOB_RAW:                                                       // FftDerivative::exec, scale 1
@@ -372,6 +373,7 @@ __global__ void __cluster_dims__(SFD_FFT_CLUSTER, 1, 1) __launch_bounds__(kCT)
         double r = x.re * s1;                           // :324, complex_to_real
         if (S.U != 0) r += uq;
         A.phip[j] = r;
+        if (A.phipf) A.phipf[j] = (float)r;
       } else if (kind == SFD_JOB_RAW) {
         A.ap[j] = x;
       } else {

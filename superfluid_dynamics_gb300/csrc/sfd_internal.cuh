@@ -37,6 +37,7 @@ struct AdjWork;
 
 struct sfd_engine {
   int device = 0;
+  int nsm = 0;  // SMs of the device
   cudaStream_t stream = nullptr;
   cudaStream_t own_stream = nullptr;
   sfd_options opt{};
@@ -68,6 +69,7 @@ struct sfd_engine {
   cd *zp = nullptr, *zpp = nullptr, *ap = nullptr;
   double *phip = nullptr, *a = nullptr, *r = nullptr, *delta = nullptr, *phi_im = nullptr;
   float2 *adf = nullptr, *ddf = nullptr;  // double-float copies of a and delta
+  float *rf = nullptr, *phipf = nullptr;   // FP32 copies of r and phi' (inputs of the preconditioner product)
   NodeData nd{};
   cd *cacc = nullptr, *dacc = nullptr, *vel_low1 = nullptr;
   unsigned int* status = nullptr;

@@ -257,6 +257,7 @@ __device__ __forceinline__ double sums_finish(const SumArgs& A, const SurfaceDes
     rnew = A.r[g] - ma;
   }
   A.r[g] = rnew;
+  if (A.rf) A.rf[g] = (float)rnew;
   double rv = fabs(rnew);
   return (rv == rv) ? rv : 1e300;
 }

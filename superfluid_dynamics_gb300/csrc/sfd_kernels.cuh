@@ -43,6 +43,7 @@ struct SumArgs {
   double* r;
   double* rnorm;        // per-surface max |r| (nullable)
   int mode;             // 0: overwrite C/D and r = phi' - M a; 1: accumulate, r -= M a
+  float* rf;            // FP32 copy of r for the preconditioner product (nullable)
 };
 
 struct VelArgs {

@@ -584,38 +584,43 @@ __global__ void __launch_bounds__(256) k_gj_update(const SurfaceDesc* surf, int 
 }
 
 // =============================================================== GEMV
-// y[off + i] = sum_j X_ij v[off + j]  (X float, v / y double).  A CTA covers
-// kGemvRows rows: v is staged once as FP32 in shared memory, each warp walks two
-// rows with 16-byte loads (rows are 16-byte aligned: n_pad is a multiple of 128,
-// and X[i][j] = 0 for j >= n in the padded inverse).
-// Stage v[0..n) (FP64) as floats in shared memory, zero-padded to n_stage:
-// all of a thread's loads are issued before its stores, so the staging costs
-// one L2 round trip instead of one per element.
+// y[off + i] = sum_j X_ij v[off + j]  (X float or half, v float, y double).  A
+// CTA covers kGemvRows rows: v (an FP32 copy written by the producer of the
+// vector, so no CTA converts from FP64) is staged in shared memory, and the
+// warps walk their rows with 16-byte loads (rows are 16-byte aligned: n_pad is
+// a multiple of 128, and X[i][j] = 0 for j >= n in the padded inverse).
+// Stage an FP32 vector (n entries, zero-padded to n_stage) in shared memory.
 template <int NT>
-__device__ __forceinline__ void stage_vector(float* vs, const double* v, int n, int n_stage) {
-  constexpr int kPer = (8192 + NT - 1) / NT;
-  double t[kPer];
-#pragma unroll
-  for (int i = 0; i < kPer; ++i) {
-    const int j = threadIdx.x + i * NT;
-    t[i] = j < n ? v[j] : 0.0;
-  }
-#pragma unroll
-  for (int i = 0; i < kPer; ++i) {
-    const int j = threadIdx.x + i * NT;
-    if (j < n_stage) vs[j] = (float)t[i];
+__device__ __forceinline__ void stage_vector_f(float* vs, const float* v, int n, int n_stage) {
+  for (int j = threadIdx.x; j < n_stage; j += NT) vs[j] = j < n ? v[j] : 0.f;
+}
+
+// Epilogue of the products: y (FP64, nullable), its double-float copy ydf
+// (nullable), and the in-place update acc += y with the double-float copy of
+// the new value (both nullable).
+__device__ __forceinline__ void gemv_store(float yr, int g, double* y, float2* ydf, double* acc, float2* accdf) {
+  const double d = (double)yr;
+  if (y) y[g] = d;
+  if (ydf) ydf[g] = make_float2(yr, 0.f);
+  if (acc) {
+    const double v = acc[g] + d;
+    acc[g] = v;
+    if (accdf) {
+      const float hi = __double2float_rn(v);
+      accdf[g] = make_float2(hi, __double2float_rn(v - (double)hi));
+    }
   }
 }
 
 __global__ void __launch_bounds__(256) k_gemv(const SurfaceDesc* surf, const int2* rowblk, const float* mat,
-                                              const double* v, double* y, float2* ydf) {
+                                              const float* v, double* y, float2* ydf, double* accv, float2* accdf) {
   const int2 rb = rowblk[blockIdx.x];  // (surface, first row)
   const SurfaceDesc& S = surf[rb.x];
   const int n = S.n, np = pad_n(n), off = S.off;
   extern __shared__ float4 vs4[];
   float* vs = reinterpret_cast<float*>(vs4);
   const int n4 = (n + 3) & ~3;
-  stage_vector<256>(vs, v + off, n, n4);
+  stage_vector_f<256>(vs, v + off, n, n4);
   __syncthreads();
   const float* X = mat + S.moff;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -650,12 +655,8 @@ __global__ void __launch_bounds__(256) k_gemv(const SurfaceDesc* surf, const int
     acc1 += __shfl_xor_sync(0xffffffffu, acc1, o);
   }
   if (lane == 0) {
-    y[off + r0] = (double)acc0;
-    if (ydf) ydf[off + r0] = make_float2(acc0, 0.f);
-    if (r1 < n) {
-      y[off + r1] = (double)acc1;
-      if (ydf) ydf[off + r1] = make_float2(acc1, 0.f);
-    }
+    gemv_store(acc0, off + r0, y, ydf, accv, accdf);
+    if (r1 < n) gemv_store(acc1, off + r1, y, ydf, accv, accdf);
   }
 }
 
@@ -691,22 +692,33 @@ __global__ void __launch_bounds__(256) k_precond_to_half(const SurfaceDesc* surf
 // ahead; the first batch is issued before v is staged, so the staging
 // latency overlaps the first matrix loads.
 __global__ void __launch_bounds__(512) k_gemv_h(const SurfaceDesc* surf, const int2* rowblk, const __half* mat16,
-                                                const float* rscale, const double* v, double* y, float2* ydf) {
-  const int2 rb = rowblk[blockIdx.x];
-  const SurfaceDesc& S = surf[rb.x];
+                                                const float* rscale, const float* v, double* y, float2* ydf,
+                                                double* accv, float2* accdf) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // row blocks from the list, or (rowblk null: one surface) rows interleaved
+  // over the grid, r = block + grid * warp, so every SM gets the same number
+  // of rows within one
+  int sidx, r;
+  if (rowblk) {
+    const int2 rb = rowblk[blockIdx.x];
+    sidx = rb.x;
+    r = rb.y + warp;
+  } else {
+    sidx = 0;
+    r = blockIdx.x + gridDim.x * warp;
+  }
+  const SurfaceDesc& S = surf[sidx];
   const int n = S.n, np = pad_n(n), off = S.off;
   extern __shared__ float4 vsh[];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int r = rb.y + warp;
   const bool live = r < n;
   const int n8 = (n + 7) & ~7;
   const int nq = n8 / 8;
   const int per_lane = lane < nq ? (nq - lane + 31) / 32 : 0;  // chunks q = lane + 32 i, i < per_lane
-  const uint4* xr = reinterpret_cast<const uint4*>(mat16 + S.moff + (long long)(live ? r : rb.y) * np) + lane;
+  const uint4* xr = reinterpret_cast<const uint4*>(mat16 + S.moff + (long long)(live ? r : 0) * np) + lane;
   uint4 cur[4], nxt[4];
 #pragma unroll
   for (int i = 0; i < 4; ++i) cur[i] = (live && i < per_lane) ? __ldg(xr + 32 * i) : make_uint4(0, 0, 0, 0);
-  stage_vector<512>(reinterpret_cast<float*>(vsh), v + off, n, n8);
+  stage_vector_f<512>(reinterpret_cast<float*>(vsh), v + off, n, n8);
   __syncthreads();
   if (!live) return;
   auto dot8 = [&](uint4 h, int q, float acc) {
@@ -737,21 +749,6 @@ __global__ void __launch_bounds__(512) k_gemv_h(const SurfaceDesc* surf, const i
   }
   float acc = acc0 + acc1;
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-  if (lane == 0) {
-    const float yr = acc * rscale[off + r];
-    y[off + r] = (double)yr;
-    if (ydf) ydf[off + r] = make_float2(yr, 0.f);
-  }
+  if (lane == 0) gemv_store(acc * rscale[off + r], off + r, y, ydf, accv, accdf);
 }
 
-// a += delta; optionally also the double-float copy of the new a
-__global__ void k_axpy_inplace(int n, double* a, const double* d, float2* adf) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  double v = a[i] + d[i];
-  a[i] = v;
-  if (adf) {
-    float hi = __double2float_rn(v);
-    adf[i] = make_float2(hi, __double2float_rn(v - (double)hi));
-  }
-}

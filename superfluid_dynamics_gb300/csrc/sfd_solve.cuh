@@ -28,12 +28,12 @@ __global__ void k_gj_update(const SurfaceDesc* surf, int nsurf, int kb, float* m
                             const float* rbuf, const float* cbuf, const long long* poff, int k_lines_only);
 __global__ void k_precond_to_half(const SurfaceDesc* surf, const int2* rowblk, const float* mat, __half* mat16,
                                   float* rscale);
+// y = X v (v FP32); optional double-float copy of y and in-place acc += y
 __global__ void k_gemv_h(const SurfaceDesc* surf, const int2* rowblk, const __half* mat16, const float* rscale,
-                         const double* v, double* y, float2* ydf);
+                         const float* v, double* y, float2* ydf, double* acc, float2* accdf);
 cudaError_t sfd_tc_configure();
 cudaError_t sfd_launch_gj_update_tc(const SurfaceDesc* surf, int nsurf, int kb, int max_np, float* mat,
                                     const __nv_bfloat16* cparts, const __nv_bfloat16* rparts, long long part_stride,
                                     const long long* poff, unsigned int* status, cudaStream_t st);
-__global__ void k_gemv(const SurfaceDesc* surf, const int2* rowblk, const float* mat, const double* v, double* y,
-                       float2* ydf);
-__global__ void k_axpy_inplace(int n, double* a, const double* d, float2* adf);
+__global__ void k_gemv(const SurfaceDesc* surf, const int2* rowblk, const float* mat, const float* v, double* y,
+                       float2* ydf, double* acc, float2* accdf);
