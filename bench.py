@@ -193,7 +193,8 @@ def run_ours(args, rank, world, local_rank):
     s = workloads.random_modes(args.n, seed=2)
     prec = sfd.PRECISION_MIXED if args.precision == "mixed" else sfd.PRECISION_FP64
     opts = sfd.Options(precision=prec, refine_iters=args.refine_iters, refactor_every=args.refactor_every,
-                       pre_iters=args.pre_iters, device=local_rank, precond_half=not args.precond_fp32)
+                       pre_iters=args.pre_iters, device=local_rank, precond_half=not args.precond_fp32,
+                       refactor_lag=args.refactor_lag)
     eng = sfd.Engine(args.n, sfd.WaterBoundaryProblem(), opts)
     stream = torch.cuda.Stream(device=dev)
     eng.set_stream(stream.cuda_stream)
@@ -212,23 +213,34 @@ def run_ours(args, rank, world, local_rank):
         torch.distributed.barrier()
     torch.cuda.synchronize()
 
-    # ---- device-resident timed region
+    # ---- device-resident timed region: one event pair around the K steps and
+    # the L2 flushes between them (any background preconditioner rebuild runs
+    # beside them and is joined before the end event), minus K isolated flushes
+    with torch.cuda.stream(stream):
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        for _ in range(3):
+            flush.fill_(1.0)
+        f0.record(stream)
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+        f1.record(stream)
+        torch.cuda.synchronize()
+    flush_ms = f0.elapsed_time(f1)
     launches0 = eng.kernel_launches
-    times = []
     with ClockSampler(local_rank) as clk:
         with torch.cuda.stream(stream):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
             for _ in range(args.steps):
                 flush.fill_(1.0)
-                e0 = torch.cuda.Event(enable_timing=True)
-                e1 = torch.cuda.Event(enable_timing=True)
-                e0.record(stream)
                 eng.step(DT, 1, sync=False)
-                e1.record(stream)
-                times.append((e0, e1))
+            eng.join_background()
+            e1.record(stream)
             torch.cuda.synchronize()
     gpu_launches = eng.kernel_launches - launches0
     tuning = eng.tuning()
-    ms = sum(a.elapsed_time(b) for a, b in times)
+    ms = e0.elapsed_time(e1) - flush_ms
     if world > 1:
         t = torch.tensor([ms], device=dev, dtype=torch.float64)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -308,9 +320,12 @@ def run_ours(args, rank, world, local_rank):
             "data": "synthetic (seeded 8-mode gravity wave)",
             "config": {"workload": f"gravity wave N={n}, 8 modes seed 2, RK4 dt={DT}", "N": n,
                        "precision": args.precision, "refine_iters": args.refine_iters, "pre_iters": args.pre_iters,
-                       "refactor_every": args.refactor_every, "precond_storage": "fp32" if args.precond_fp32 else "fp16",
+                       "refactor_every": args.refactor_every, "refactor_lag": args.refactor_lag,
+                       "precond_storage": "fp32" if args.precond_fp32 else "fp16",
                        "sum_groups_per_cta": tuning,
                        "l2": "flushed (256 MB write) before every timed step",
+                       "timing": "CUDA events around the K steps and their L2 flushes (background rebuild joined), "
+                                 "minus K flushes timed alone",
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
             "roofline": roof, "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": 3 * n * 8,
@@ -491,6 +506,8 @@ def main():
     ap.add_argument("--refine-iters", type=int, default=2)
     ap.add_argument("--pre-iters", type=int, default=2)
     ap.add_argument("--refactor-every", type=int, default=50)
+    ap.add_argument("--refactor-lag", type=int, default=8,
+                    help="rebuild the preconditioner on a side stream and switch to it this many steps later")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--precond-fp32", action="store_true", help="apply the preconditioner from FP32 (default FP16 copy)")

@@ -77,6 +77,11 @@ typedef struct sfd_options {
     int precond_half;     /* mixed: apply the preconditioner from an FP16 copy (1)       */
     int autotune;         /* time the boundary-sum CTA shapes on the first steps and keep
                              the fastest per precision (1)                               */
+    int refactor_lag;     /* mixed, sfd_rk4_steps: 0 rebuilds the preconditioner inside the
+                             step it is due (default); k > 0 rebuilds it on a low-priority
+                             side stream from the state at that step and switches to it k
+                             steps later (k < refactor_every), so the rebuild overlaps the
+                             stepping.  Deterministic: the switch step is fixed.          */
 } sfd_options;
 
 /* Optomechanical drive of a helium film, nondimensional (the reference's
@@ -154,6 +159,10 @@ int sfd_rk4_steps(sfd_engine* e, double dt, int steps);
 /* Enqueue without waiting for completion (timed loops). */
 int sfd_rk4_steps_async(sfd_engine* e, double dt, int steps);
 int sfd_synchronize(sfd_engine* e);
+/* Make the engine stream wait for the work in flight on its background
+ * rebuild stream (refactor_lag > 0), without switching to the rebuilt
+ * preconditioner and without blocking the host. */
+int sfd_join_background(sfd_engine* e);
 
 /* Invariants of the current state, 5 doubles per surface: kinetic, potential
  * (gravitational or van der Waals), surface, volume flux (Energies.cuh:136-204)

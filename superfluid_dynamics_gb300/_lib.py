@@ -34,7 +34,7 @@ class SfdProblem(ctypes.Structure):
 class SfdOptions(ctypes.Structure):
     _fields_ = [("precision", c_int), ("refine_iters", c_int), ("refactor_every", c_int),
                 ("use_graphs", c_int), ("device", c_int), ("tensor_cores", c_int), ("pre_iters", c_int),
-                ("precond_half", c_int), ("autotune", c_int)]
+                ("precond_half", c_int), ("autotune", c_int), ("refactor_lag", c_int)]
 
 
 class SimProperties(ctypes.Structure):
@@ -152,6 +152,7 @@ _SIGS = {
                                        POINTER(SimProperties), POINTER(RK4SolverOptions), c_size_t]),
     "integrateSimulationRK4_freeMemory": (c_int, [_dp, _dp]),
     "sfd_default_gl2_options": (None, [POINTER(SfdGl2Options)]),
+    "sfd_join_background": (c_int, [c_void_p]),
     "sfd_gl2_evolve": (c_int, [c_void_p, c_double, c_double, POINTER(SfdGl2Options), POINTER(SfdGl2Result), _dp, _dp,
                                c_longlong]),
     "integrateSimulationGL2": (c_int, [_dp, POINTER(_dp), POINTER(c_size_t), POINTER(_dp), POINTER(c_size_t),

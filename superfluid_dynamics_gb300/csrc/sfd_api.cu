@@ -203,7 +203,11 @@ int enqueue_gemv(sfd_engine* e, const float* vf, double* y, float2* ydf, double*
   return 0;
 }
 
+int bg_flush(sfd_engine* e);
+
 int enqueue_precond(sfd_engine* e) {
+  int rc = bg_flush(e);  // a rebuild in flight on the side stream owns the work buffers
+  if (rc) return rc;
   const int nb = e->max_np / 128;
   LAUNCHC(e, SFD_K_ASSEMBLE, sfd_launch_assemble32(e->d_surf, e->d_asm_tiles, e->nasm, e->nd.w, e->nd.p, e->zp, e->nd.mdiag, e->m32,
                                   e->stream));
@@ -423,6 +427,105 @@ int autotune_sums(sfd_engine* e) {
   return rc;
 }
 
+// ------------------------------------------------------- background rebuild
+// With refactor_lag = k > 0 the preconditioner due at step s is built on a
+// low-priority side stream: the main stream copies the state and records
+// ev_snap; the side stream waits for it, recomputes z', z'' and the node data
+// of the copy into its own buffers, assembles M, runs the Gauss-Jordan
+// inverse and writes the FP16 copy into m16_next / rscale_next, then records
+// ev_done.  Before the graph of step s + k the main stream waits for ev_done
+// and copies m16_next / rscale_next over the live preconditioner.  The switch
+// step does not depend on timing, so runs are deterministic.  The work
+// buffers of the inverse (m32, panels, parts) belong to the side stream while
+// a rebuild is in flight; any synchronous rebuild first flushes it.
+namespace {
+int bg_alloc(sfd_engine* e) {
+  auto& B = e->bg;
+  if (B.side) return 0;
+  int least = 0, greatest = 0;
+  CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+  CK(cudaStreamCreateWithPriority(&B.side, cudaStreamNonBlocking, least));
+  CK(cudaEventCreateWithFlags(&B.ev_snap, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&B.ev_done, cudaEventDisableTiming));
+  const int nt = e->ntot;
+  CK(dalloc(&B.snap, 3LL * nt));
+  CK(dalloc(&B.zp, nt));
+  CK(dalloc(&B.zpp, nt));
+  CK(dalloc(&B.phip, nt));
+  CK(dalloc(&B.nd.w, nt));
+  CK(dalloc(&B.nd.p, nt));
+  CK(dalloc(&B.nd.wdf, nt));
+  CK(dalloc(&B.nd.pdf, nt));
+  CK(dalloc(&B.nd.mdiag, nt));
+  CK(dalloc(&B.nd.v1low, nt));
+  CK(dalloc(&B.nd.v1up, nt));
+  CK(dalloc(&B.nd.v2, nt));
+  CK(dalloc(&B.m16_next, e->mat_elems));
+  CK(dalloc(&B.rscale_next, nt));
+  return 0;
+}
+
+// Enqueue the rebuild of the preconditioner from the current state.
+int bg_start(sfd_engine* e) {
+  int rc = bg_alloc(e);
+  if (rc) return rc;
+  auto& B = e->bg;
+  const int nt = e->ntot;
+  cudaStream_t side = B.side;
+  CK(cudaMemcpyAsync(B.snap, e->y0, 3LL * nt * sizeof(double), cudaMemcpyDeviceToDevice, e->stream));
+  CK(cudaEventRecord(B.ev_snap, e->stream));
+  CK(cudaStreamWaitEvent(side, B.ev_snap, 0));
+  const double *x = B.snap, *y = B.snap + nt, *phi = B.snap + 2 * nt;
+  DerivArgs D{e->d_surf, e->nsurf, x, y, phi, nullptr, nullptr, B.zp, B.zpp, B.phip, nullptr, nullptr};
+  if (e->njobs_first) CK(sfd_launch_spectral(D, e->d_jobs_first, e->njobs_first, e->max_n_single, side));
+  if (e->ncjobs_first) CK(sfd_launch_spectral_cluster(D, e->d_cjobs_first, e->ncjobs_first, e->max_n_cluster, side));
+  k_node_prep<<<blocks_for(nt, 32), 32, 0, side>>>(e->d_surf, e->d_node_surf, nt, x, y, B.zp, B.zpp, B.nd);
+  CK(cudaGetLastError());
+  CK(sfd_launch_assemble32(e->d_surf, e->d_asm_tiles, e->nasm, B.nd.w, B.nd.p, B.zp, B.nd.mdiag, e->m32, side));
+  const int nb = e->max_np / 128, tiles = e->max_np / 64;
+  for (int kb = 0; kb < nb; ++kb) {
+    k_gj_diag<<<e->nsurf, 512, kGjDiagSmem, side>>>(e->d_surf, e->nsurf, kb, e->m32, e->pbuf, e->status);
+    k_gj_panel<<<dim3(tiles, 1, e->nsurf), 256, 0, side>>>(e->d_surf, e->nsurf, kb, e->m32, e->pbuf, e->rbuf, e->cbuf,
+                                                            e->d_poff, e->cparts, e->rparts, e->panel_elems);
+    k_gj_update<<<dim3(4 * tiles - 4, 1, e->nsurf), 256, 0, side>>>(e->d_surf, e->nsurf, kb, e->m32, e->pbuf, e->rbuf,
+                                                                     e->cbuf, e->d_poff, 1);
+    CK(sfd_launch_gj_update_tc(e->d_surf, e->nsurf, kb, e->max_np, e->m32, e->cparts, e->rparts, e->panel_elems,
+                               e->d_poff, e->status, side));
+  }
+  k_precond_to_half<<<e->ngemv, 256, 0, side>>>(e->d_surf, e->d_gemv_rows, e->m32, B.m16_next, B.rscale_next);
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(B.ev_done, side));
+  e->launches += 4 + 4LL * nb;
+  B.rebuilds++;
+  return 0;
+}
+
+// Switch to the rebuilt preconditioner (main stream waits for it).
+int bg_swap(sfd_engine* e) {
+  auto& B = e->bg;
+  CK(cudaStreamWaitEvent(e->stream, B.ev_done, 0));
+  CK(cudaMemcpyAsync(e->m16, B.m16_next, (size_t)e->mat_elems * sizeof(__half), cudaMemcpyDeviceToDevice, e->stream));
+  CK(cudaMemcpyAsync(e->rscale, B.rscale_next, (size_t)e->ntot * sizeof(float), cudaMemcpyDeviceToDevice, e->stream));
+  B.swap_at = -1;
+  return 0;
+}
+
+bool bg_usable(const sfd_engine* e) {
+  return e->opt.precision == SFD_PRECISION_MIXED && e->opt.refactor_lag > 0 && e->m16 && e->opt.tensor_cores &&
+         e->opt.refactor_lag < std::max(1, e->opt.refactor_every);
+}
+}  // namespace
+
+// Apply a pending background rebuild now (before anything else uses the
+// inverse's work buffers or replaces the preconditioner).
+int bg_flush(sfd_engine* e) {
+  if (e->bg.swap_at < 0) return 0;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  CK(cudaStreamIsCapturing(e->stream, &cs));
+  if (cs != cudaStreamCaptureStatusNone) return set_error(SFD_ERR_INVALID, "background rebuild pending during capture");
+  return bg_swap(e);
+}
+
 int run_steps(sfd_engine* e, double dt, int steps) {
   if (steps < 0) return set_error(SFD_ERR_INVALID, "negative step count");
   CK(cudaSetDevice(e->device));
@@ -433,30 +536,40 @@ int run_steps(sfd_engine* e, double dt, int steps) {
   }
   const bool mixed = e->opt.precision == SFD_PRECISION_MIXED;
   const int every = std::max(1, e->opt.refactor_every);
-  if (e->opt.use_graphs && !e->profile) {
-    if (e->g_dt != dt) {
-      destroy_graphs(e);
-      e->g_dt = dt;
+  const bool graphs = e->opt.use_graphs && !e->profile;
+  if (graphs && e->g_dt != dt) {
+    destroy_graphs(e);
+    e->g_dt = dt;
+  }
+  for (int s = 0; s < steps; ++s) {
+    const bool due = (e->step_count % every) == 0;
+    bool refactor = !mixed || !e->have_precond || due;
+    if (mixed && e->have_precond && bg_usable(e)) {
+      if (e->bg.swap_at == e->step_count) {
+        int rc = bg_swap(e);
+        if (rc) return rc;
+      }
+      if (due && e->bg.swap_at < 0) {
+        int rc = bg_start(e);
+        if (rc) return rc;
+        e->bg.swap_at = e->step_count + e->opt.refactor_lag;
+      }
+      refactor = false;
     }
-    for (int s = 0; s < steps; ++s) {
-      int variant = (!mixed || (e->step_count % every) == 0 || !e->have_precond) ? 1 : 0;
-      if (!mixed) variant = 1;
+    if (graphs) {
+      const int variant = refactor ? 1 : 0;
       if (!e->g_step[variant]) {
         int rc = build_graph(e, dt, variant);
         if (rc) return rc;
       }
       CK(cudaGraphLaunch(e->g_step[variant], e->stream));
       e->launches += e->g_kernels[variant];
-      if (variant == 1 && mixed) e->have_precond = true;
-      e->step_count++;
-    }
-  } else {
-    for (int s = 0; s < steps; ++s) {
-      bool refactor = !mixed || (e->step_count % every) == 0;
+    } else {
       int rc = enqueue_step(e, dt, refactor);
       if (rc) return rc;
-      e->step_count++;
     }
+    if (refactor && mixed) e->have_precond = true;
+    e->step_count++;
   }
   return 0;
 }
@@ -465,6 +578,7 @@ void free_engine(sfd_engine* e) {
   if (!e) return;
   cudaSetDevice(e->device);
   if (e->stream) cudaStreamSynchronize(e->stream);
+  if (e->bg.side) cudaStreamSynchronize(e->bg.side);  // a background rebuild uses the inverse's buffers
   destroy_graphs(e);
   void* ptrs[] = {e->d_surf, e->d_node_surf, e->d_jobs_first, e->d_jobs_ap, e->d_cjobs_first, e->d_cjobs_ap, e->d_sum_items, e->d_asm_tiles,
                   e->d_gemv_rows, e->d_poff, e->y0, e->ys, e->kacc, e->kcur, e->zp, e->zpp, e->ap, e->phip, e->a,
@@ -473,6 +587,16 @@ void free_engine(sfd_engine* e) {
                   e->inv_out, e->m64, e->m32, e->m16, e->rscale, e->fc_in, e->fc_out, e->rf, e->phipf, e->pbuf, e->rbuf, e->cbuf, e->cparts, e->rparts};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  {
+    auto& B = e->bg;
+    void* bp[] = {B.snap, B.zp, B.zpp, B.phip, B.nd.w, B.nd.p, B.nd.wdf, B.nd.pdf, B.nd.mdiag, B.nd.v1low, B.nd.v1up,
+                  B.nd.v2, B.m16_next, B.rscale_next};
+    for (void* p : bp)
+      if (p) cudaFree(p);
+    if (B.ev_snap) cudaEventDestroy(B.ev_snap);
+    if (B.ev_done) cudaEventDestroy(B.ev_done);
+    if (B.side) cudaStreamDestroy(B.side);
+  }
   sfd_adjoint_free(e);
   sfd_rkf45_free(e);
   sfd_gl2_free(e);
@@ -561,6 +685,7 @@ void sfd_default_options(sfd_options* o) {
   o->pre_iters = 1;
   o->precond_half = 1;
   o->autotune = 1;
+  o->refactor_lag = 0;
 }
 
 void sfd_default_problem(sfd_problem* p) {
@@ -948,6 +1073,19 @@ int sfd_synchronize(sfd_engine* e) {
   CK(cudaSetDevice(e->device));
   CK(cudaStreamSynchronize(e->stream));
   if (e->profile) drain_profile(e);
+  return 0;
+}
+
+int sfd_join_background(sfd_engine* e) {
+  if (!e) return set_error(SFD_ERR_INVALID, "null engine");
+  if (!e->bg.side) return 0;
+  CK(cudaSetDevice(e->device));
+  cudaEvent_t ev = nullptr;
+  CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  cudaError_t err = cudaEventRecord(ev, e->bg.side);
+  if (err == cudaSuccess) err = cudaStreamWaitEvent(e->stream, ev, 0);
+  cudaEventDestroy(ev);
+  CK(err);
   return 0;
 }
 

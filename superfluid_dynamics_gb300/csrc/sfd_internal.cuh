@@ -8,6 +8,8 @@
 #include <map>
 #include <vector>
 
+#include "sfd_kernels.cuh"
+
 #include "../../include/sfd.h"
 #include "sfd_engine.cuh"
 #include "sfd_kernels.cuh"
@@ -105,6 +107,21 @@ struct sfd_engine {
   // complex-layout staging of the C++ facade (sfd_facade.cu), allocated on first use
   double* fc_in = nullptr;
   double* fc_out = nullptr;
+  // background preconditioner rebuild (opt.refactor_lag > 0): a low-priority
+  // side stream assembles and inverts M from a snapshot of the state into
+  // m16_next / rscale_next; the main stream switches at step bg_swap_at
+  struct Background {
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_snap = nullptr, ev_done = nullptr;
+    double* snap = nullptr;     // state copy [x | y | phi]
+    cd *zp = nullptr, *zpp = nullptr;
+    double* phip = nullptr;
+    NodeData nd{};
+    __half* m16_next = nullptr;
+    float* rscale_next = nullptr;
+    long long swap_at = -1;     // step index of the switch; -1: none pending
+    long long rebuilds = 0;
+  } bg;
   // the problem of each surface as given to sfd_create (helper engines copy it)
   std::vector<sfd_problem> hp;
   // implicit Gauss-Legendre workspace (sfd_gl2.cu), allocated on first use

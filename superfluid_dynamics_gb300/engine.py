@@ -94,11 +94,13 @@ class Options:
     pre_iters: int = 1
     precond_half: bool = True
     autotune: bool = True
+    refactor_lag: int = 0
 
     def to_c(self) -> _lib.SfdOptions:
         return _lib.SfdOptions(self.precision, self.refine_iters, self.refactor_every,
                                1 if self.use_graphs else 0, self.device, 1 if self.tensor_cores else 0,
-                               self.pre_iters, 1 if self.precond_half else 0, 1 if self.autotune else 0)
+                               self.pre_iters, 1 if self.precond_half else 0, 1 if self.autotune else 0,
+                               self.refactor_lag)
 
 
 class Engine:
@@ -241,6 +243,10 @@ class Engine:
 
     def synchronize(self) -> None:
         check(self._L.sfd_synchronize(self._h))
+
+    def join_background(self) -> None:
+        """Make the engine stream wait for an in-flight background rebuild."""
+        check(self._L.sfd_join_background(self._h))
 
     def invariants(self, kappa: float = 0.0) -> np.ndarray:
         out = np.empty(5 * self.nsurf)
