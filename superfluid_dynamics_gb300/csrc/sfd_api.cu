@@ -239,10 +239,35 @@ int enqueue_precond(sfd_engine* e) {
   return 0;
 }
 
+// a' = d a / d xi (FftDerivative on a, BaseBoundaryIntegrator.cuh:201-203):
+// on the engine stream, or forked onto the auxiliary stream so that it runs
+// beside the last boundary-sum pass (that pass reads the weights delta and
+// writes C, D and r; the transform reads a and writes a').  The fork is
+// skipped under per-kernel profiling, whose events live on the engine stream.
+int enqueue_ap(sfd_engine* e, bool fork) {
+  DerivArgs D{e->d_surf, e->nsurf, nullptr, nullptr, nullptr, nullptr, e->a, e->zp, e->zpp, e->phip, e->ap};
+  if (fork && e->aux && !e->profile) {
+    CK(cudaEventRecord(e->ev_fork, e->stream));
+    CK(cudaStreamWaitEvent(e->aux, e->ev_fork, 0));
+    if (e->njobs_ap) CK(sfd_launch_spectral(D, e->d_jobs_ap, e->njobs_ap, e->max_n_single, e->aux));
+    if (e->ncjobs_ap) CK(sfd_launch_spectral_cluster(D, e->d_cjobs_ap, e->ncjobs_ap, e->max_n_cluster, e->aux));
+    CK(cudaEventRecord(e->ev_join, e->aux));
+    e->launches += (e->njobs_ap ? 1 : 0) + (e->ncjobs_ap ? 1 : 0);
+    e->ap_forked = true;
+    return 0;
+  }
+  if (e->njobs_ap)
+    LAUNCHC(e, SFD_K_SPECTRAL, sfd_launch_spectral(D, e->d_jobs_ap, e->njobs_ap, e->max_n_single, e->stream));
+  if (e->ncjobs_ap)
+    LAUNCHC(e, SFD_K_SPECTRAL,
+            sfd_launch_spectral_cluster(D, e->d_cjobs_ap, e->ncjobs_ap, e->max_n_cluster, e->stream));
+  return 0;
+}
+
 // First half of an RHS evaluation (calculateVorticities,
 // BaseBoundaryIntegrator.cuh:275-306): z', z'', phi', M a = phi' and the
 // boundary sums C, D of the solution.
-int enqueue_solve(sfd_engine* e, const double* st, const double* phi_im, bool refactor) {
+int enqueue_solve(sfd_engine* e, const double* st, const double* phi_im, bool refactor, bool fork_ap = false) {
   const int nt = e->ntot;
   const double *x = st, *y = st + nt, *phi = st + 2 * nt;
   DerivArgs D{e->d_surf, e->nsurf, x, y, phi, phi_im, e->a, e->zp, e->zpp, e->phip, e->ap, e->phipf};
@@ -267,6 +292,10 @@ int enqueue_solve(sfd_engine* e, const double* st, const double* phi_im, bool re
     }
     LAUNCHC(e, SFD_K_TRSV, k_lu64_solve<<<e->nsurf, 256, e->max_np * sizeof(double), e->stream>>>(e->d_surf, e->m64, e->phip,
                                                                                        e->a));
+    if (fork_ap) {
+      int rc = enqueue_ap(e, true);
+      if (rc) return rc;
+    }
     int rc = enqueue_sums(e, SFD_PREC_F64, e->a, nullptr, 0, true);
     if (rc) return rc;
   } else {
@@ -280,6 +309,7 @@ int enqueue_solve(sfd_engine* e, const double* st, const double* phi_im, bool re
     // residual and C(a); FP32 post-iterations correct the small remainder.
     // The products read FP32 copies of phi' and r written by their producers;
     // the updates a += delta run in the product's epilogue.
+    // a is final after the last product: a' forks from there
     int rc = enqueue_gemv(e, e->phipf, e->a, e->adf, nullptr, nullptr);
     if (rc) return rc;
     for (int it = 0; it < e->opt.pre_iters; ++it) {
@@ -288,11 +318,19 @@ int enqueue_solve(sfd_engine* e, const double* st, const double* phi_im, bool re
       rc = enqueue_gemv(e, e->rf, nullptr, nullptr, e->a, e->adf);
       if (rc) return rc;
     }
+    if (fork_ap && e->opt.refine_iters == 0) {
+      rc = enqueue_ap(e, true);
+      if (rc) return rc;
+    }
     rc = enqueue_sums(e, SFD_PREC_DF, e->a, e->adf, 0, e->opt.refine_iters == 0);
     if (rc) return rc;
     for (int it = 0; it < e->opt.refine_iters; ++it) {
       rc = enqueue_gemv(e, e->rf, e->delta, e->ddf, e->a, nullptr);
       if (rc) return rc;
+      if (fork_ap && it == e->opt.refine_iters - 1) {
+        rc = enqueue_ap(e, true);
+        if (rc) return rc;
+      }
       rc = enqueue_sums(e, SFD_PREC_F32, e->delta, e->ddf, 1, it == e->opt.refine_iters - 1);
       if (rc) return rc;
     }
@@ -302,17 +340,19 @@ int enqueue_solve(sfd_engine* e, const double* st, const double* phi_im, bool re
 
 // One RHS evaluation: state [x|y|phi] -> out [dx|dy|dphi].
 int enqueue_rhs(sfd_engine* e, const double* st, double* out, bool refactor) {
-  int rc = enqueue_solve(e, st, nullptr, refactor);
+  e->ap_forked = false;
+  int rc = enqueue_solve(e, st, nullptr, refactor, true);
   if (rc) return rc;
   const int nt = e->ntot;
   const double* y = st + nt;
-  DerivArgs D{e->d_surf, e->nsurf, st, y, st + 2 * nt, nullptr, e->a, e->zp, e->zpp, e->phip, e->ap};
-  // a' and the velocity / Bernoulli epilogue
-  if (e->njobs_ap)
-    LAUNCHC(e, SFD_K_SPECTRAL, sfd_launch_spectral(D, e->d_jobs_ap, e->njobs_ap, e->max_n_single, e->stream));
-  if (e->ncjobs_ap)
-    LAUNCHC(e, SFD_K_SPECTRAL,
-            sfd_launch_spectral_cluster(D, e->d_cjobs_ap, e->ncjobs_ap, e->max_n_cluster, e->stream));
+  // a' (forked during the solve, or here) and the velocity / Bernoulli epilogue
+  if (e->ap_forked) {
+    CK(cudaStreamWaitEvent(e->stream, e->ev_join, 0));
+    e->ap_forked = false;
+  } else {
+    rc = enqueue_ap(e, false);
+    if (rc) return rc;
+  }
   VelArgs V{e->d_surf, e->d_node_surf, e->nsurf, nt, e->cacc, e->dacc, e->a, e->ap, e->nd.v1low, e->nd.v1up,
             e->nd.v2, y, st, e->nblk == 4 ? st + 3 * nt : nullptr, e->nblk == 4 ? out + 3 * nt : nullptr,
             e->zp, e->zpp, e->vel_low1, out, out + nt, out + 2 * nt, e->status};
@@ -604,6 +644,10 @@ void free_engine(sfd_engine* e) {
   for (cudaEvent_t ev : e->event_pool) cudaEventDestroy(ev);
   for (auto& kv : e->d_tw) cudaFree(kv.second);
   for (auto& kv : e->d_ctw) cudaFree(kv.second);
+  if (e->aux) cudaStreamSynchronize(e->aux);
+  if (e->ev_fork) cudaEventDestroy(e->ev_fork);
+  if (e->ev_join) cudaEventDestroy(e->ev_join);
+  if (e->aux) cudaStreamDestroy(e->aux);
   if (e->own_stream) cudaStreamDestroy(e->own_stream);
   delete e;
 }
@@ -747,6 +791,9 @@ int sfd_create_driven(const int* n, int nsurf, const sfd_problem* problems, cons
   CKE(cudaDeviceGetAttribute(&e->nsm, cudaDevAttrMultiProcessorCount, e->device));
   CKE(cudaStreamCreateWithFlags(&e->own_stream, cudaStreamNonBlocking));
   e->stream = e->own_stream;
+  CKE(cudaStreamCreateWithFlags(&e->aux, cudaStreamNonBlocking));
+  CKE(cudaEventCreateWithFlags(&e->ev_fork, cudaEventDisableTiming));
+  CKE(cudaEventCreateWithFlags(&e->ev_join, cudaEventDisableTiming));
   e->nsurf = nsurf;
   e->hs.resize(nsurf);
   for (int s = 0; s < nsurf; ++s) e->hp.push_back(problems[shared_problem ? 0 : s]);

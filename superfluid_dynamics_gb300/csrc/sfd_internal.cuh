@@ -42,6 +42,11 @@ struct sfd_engine {
   int nsm = 0;  // SMs of the device
   cudaStream_t stream = nullptr;
   cudaStream_t own_stream = nullptr;
+  // auxiliary stream of the a' transform, forked from `stream` once a is final
+  // and joined before the velocity epilogue (also inside captured graphs)
+  cudaStream_t aux = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  bool ap_forked = false;
   sfd_options opt{};
   int nsurf = 0, ntot = 0, max_n = 0, max_np = 0;
   int nblk = 3;  // state blocks: [x | y | phi] or, with an augmented drive, [x | y | phi | D]
