@@ -276,7 +276,7 @@ int enqueue_solve(sfd_engine* e, const double* st, const double* phi_im, bool re
   if (e->ncjobs_first)
     LAUNCHC(e, SFD_K_SPECTRAL,
             sfd_launch_spectral_cluster(D, e->d_cjobs_first, e->ncjobs_first, e->max_n_cluster, e->stream));
-  LAUNCHC(e, SFD_K_NODE, k_node_prep<<<blocks_for(nt, 32), 32, 0, e->stream>>>(e->d_surf, e->d_node_surf, nt, x, y, e->zp,
+  LAUNCHC(e, SFD_K_NODE, k_node_prep<<<blocks_for(nt, 32), 64, 0, e->stream>>>(e->d_surf, e->d_node_surf, nt, x, y, e->zp,
                                                                      e->zpp, e->nd));
   if (e->opt.precision == SFD_PRECISION_FP64) {
     LAUNCHC(e, SFD_K_ASSEMBLE, sfd_launch_assemble64(e->d_surf, e->d_asm_tiles, e->nasm, e->nd.w, e->nd.p, e->zp, e->nd.mdiag,
@@ -519,7 +519,7 @@ int bg_start(sfd_engine* e) {
   DerivArgs D{e->d_surf, e->nsurf, x, y, phi, nullptr, nullptr, B.zp, B.zpp, B.phip, nullptr, nullptr};
   if (e->njobs_first) CK(sfd_launch_spectral(D, e->d_jobs_first, e->njobs_first, e->max_n_single, side));
   if (e->ncjobs_first) CK(sfd_launch_spectral_cluster(D, e->d_cjobs_first, e->ncjobs_first, e->max_n_cluster, side));
-  k_node_prep<<<blocks_for(nt, 32), 32, 0, side>>>(e->d_surf, e->d_node_surf, nt, x, y, B.zp, B.zpp, B.nd);
+  k_node_prep<<<blocks_for(nt, 32), 64, 0, side>>>(e->d_surf, e->d_node_surf, nt, x, y, B.zp, B.zpp, B.nd);
   CK(cudaGetLastError());
   CK(sfd_launch_assemble32(e->d_surf, e->d_asm_tiles, e->nasm, B.nd.w, B.nd.p, B.zp, B.nd.mdiag, e->m32, side));
   const int nb = e->max_np / 128, tiles = e->max_np / 64;

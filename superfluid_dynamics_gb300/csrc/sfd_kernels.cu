@@ -29,41 +29,47 @@
 // ----------------------------------------------------------------- node prep
 // w = exp(i z) = e^{-y} (cos x + i sin x); p = w e^{-h} (helium);
 // per-node diagonal data of M and of the velocity matrices.
-__global__ void k_node_prep(const SurfaceDesc* surf, const int* node_surf, int ntot, const double* x,
-                            const double* y, const cd* zp, const cd* zpp, NodeData nd) {
-  int g = blockIdx.x * blockDim.x + threadIdx.x;
+// Two independent FP64 chains per node, one per warp of a 64-thread block of
+// 32 nodes (GB300's FP64 pipe is narrow, so the chains' latency is the cost):
+// warp 0 the exponentials (w, p), warp 1 the z' / z'' terms, which share one
+// reciprocal 1 / z'.
+__global__ void __launch_bounds__(64) k_node_prep(const SurfaceDesc* surf, const int* node_surf, int ntot,
+                                                  const double* x, const double* y, const cd* zp, const cd* zpp,
+                                                  NodeData nd) {
+  const int g = blockIdx.x * 32 + (threadIdx.x & 31);
   if (g >= ntot) return;
   const SurfaceDesc& S = surf[node_surf[g]];
-  double s, c;
-  sincos(x[g], &s, &c);
-  double e = exp(-y[g]);
-  cd w = {e * c, e * s};
-  nd.w[g] = w;
-  {
-    df wr = df_from_double(w.re), wi = df_from_double(w.im);
+  if (threadIdx.x < 32) {
+    double s, c;
+    sincos(x[g], &s, &c);
+    const double e = exp(-y[g]);
+    const cd w = {e * c, e * s};
+    nd.w[g] = w;
+    const df wr = df_from_double(w.re), wi = df_from_double(w.im);
     nd.wdf[g] = make_float4(wr.hi, wr.lo, wi.hi, wi.lo);
+    if (S.physics == 1 && !S.infinite_depth) {
+      const double eh = exp(-S.depth);
+      const cd p = {w.re * eh, w.im * eh};
+      nd.p[g] = p;
+      const df pr = df_from_double(p.re), pi = df_from_double(p.im);
+      nd.pdf[g] = make_float4(pr.hi, pr.lo, pi.hi, pi.lo);
+    }
+    return;
   }
-  if (S.physics == 1 && !S.infinite_depth) {
-    double eh = exp(-S.depth);
-    cd p = {w.re * eh, w.im * eh};
-    nd.p[g] = p;
-    df pr = df_from_double(p.re), pi = df_from_double(p.im);
-    nd.pdf[g] = make_float4(pr.hi, pr.lo, pi.hi, pi.lo);
-  }
-  cd z1 = zp[g], z2 = zpp[g];
-  cd r = cdiv(z2, z1);
-  const double inv4pi = 0.25 / SFD_PI;
+  const cd z1 = zp[g], z2 = zpp[g];
+  const cd iz = cdiv(cd{1.0, 0.0}, z1);  // 1 / z'
+  const cd r = z2 * iz;                  // z'' / z'
+  constexpr double inv4pi = 0.25 / SFD_PI;
   double mdiag;
-  if (S.physics == 0) mdiag = 0.5 * (1 + S.rho) + 0.25 * (1 - S.rho) / SFD_PI * r.im;  // createM.cuh:56
-  else mdiag = 0.5 + 0.25 / SFD_PI * r.im;                                               // createM.cuh:78
+  if (S.physics == 0) mdiag = 0.5 * (1 + S.rho) + inv4pi * (1 - S.rho) * r.im;  // createM.cuh:56
+  else mdiag = 0.5 + inv4pi * r.im;                                             // createM.cuh:78
   nd.mdiag[g] = mdiag;
   // V1_kk (without the image term) = -(i/4pi) z''/z'^2 +- 1/(2 z')   (WaterVelocities.cuh:54-62,87-97)
-  cd zz = z1 * z1;
-  cd t = cmul_i(-inv4pi * cdiv(z2, zz));
-  cd half_inv = cdiv(cd{1.0, 0.0}, 2.0 * z1);
+  const cd t = cmul_i(-inv4pi * (r * iz));
+  const cd half_inv = 0.5 * iz;
   nd.v1low[g] = t + half_inv;
   nd.v1up[g] = t - half_inv;
-  nd.v2[g] = cmul_i(cdiv(cd{1.0, 0.0}, 2.0 * SFD_PI * z1));  // i / (2 pi z')   (:63,98)
+  nd.v2[g] = cmul_i((0.5 / SFD_PI) * iz);  // i / (2 pi z')   (:63,98)
 }
 
 // ----------------------------------------------------------------- sums
@@ -239,7 +245,8 @@ __device__ __forceinline__ double to_d(df v) { return df_to_double(v); }
 // Returns |r_k| (1e300 for NaN).
 __device__ __forceinline__ double sums_finish(const SumArgs& A, const SurfaceDesc& S, int g, cd sum_s, cd sum_t,
                                               double asum, bool image) {
-  const double c1 = S.physics == 0 ? 0.25 * (1 - S.rho) / SFD_PI : 0.25 / SFD_PI;
+  constexpr double inv4pi = 0.25 / SFD_PI;
+  const double c1 = S.physics == 0 ? inv4pi * (1 - S.rho) : inv4pi;
   const double ak = A.a[g];
   const cd wk = A.w[g];
   const cd C = cmul_i(2.0 * (wk * sum_s) - cd{asum - ak, 0.0});
@@ -435,7 +442,7 @@ __global__ void k_velocity_bernoulli(VelArgs V) {
   const int s = V.node_surf[g];
   const SurfaceDesc& S = V.surf[s];
   const bool image = (S.physics == 1 && !S.infinite_depth);
-  const double inv4pi = 1.0 / (4.0 * SFD_PI);
+  constexpr double inv4pi = 0.25 / SFD_PI;
   cd C = V.cacc[g];
   cd base = cmul_i(-inv4pi * C);
   if (image) base = base + cmul_i(inv4pi * V.dacc[g]);
@@ -463,19 +470,21 @@ __global__ void k_velocity_bernoulli(VelArgs V) {
     double kin = 0.5 * low.re * low.re + 0.5 * low.im * low.im;
     double vdw = 0.0;
     const int o = S.expansion_order;  // switch fall-through of the reference: 3 -> 2 -> 1
-    if (o == 3) vdw += -10.0 / 3.0 * pow(yk, 3.0) / (S.depth * S.depth);
-    if (o == 3 || o == 2) vdw += 2.0 * pow(yk, 2.0) / S.depth;
+    if (o == 3) vdw += -10.0 / 3.0 * (yk * yk * yk) / (S.depth * S.depth);
+    if (o == 3 || o == 2) vdw += 2.0 * (yk * yk) / S.depth;
     if (o >= 1 && o <= 3) vdw += -yk;
     out = vdw + kin;
   } else if (S.bern_variant == 2) {
     // surface-tension variant with the reference's fixed prefactor (createM.cuh:195-211)
     cd z1 = V.zp[g], z2 = V.zpp[g];
-    double curv = (z1.re * z2.im - z1.im * z2.re) / pow(z1.re * z1.re + z1.im * z1.im, 1.5);
+    const double m2 = z1.re * z1.re + z1.im * z1.im;
+    double curv = (z1.re * z2.im - z1.im * z2.re) / (m2 * sqrt(m2));
     double v1 = low.re * low.re + low.im * low.im;
-    out = 20.447761896665416 * S.depth / 3.0 * (1.0 / pow(1.0 + yk / S.depth, 3) - 1) + 0.5 * v1 + S.kappa * curv;
+    const double iq = S.depth / (S.depth + yk);  // (1 + y/h)^-1
+    out = 20.447761896665416 * S.depth / 3.0 * (iq * iq * iq - 1) + 0.5 * v1 + S.kappa * curv;
   } else {
-    double q = 1.0 + yk / S.depth;
-    out = S.vdw * pow(q, -3.0) - S.vdw + 0.5 * low.re * low.re + 0.5 * low.im * low.im;
+    const double iq = S.depth / (S.depth + yk);  // (1 + y/h)^-1: one division instead of pow
+    out = S.vdw * (iq * iq * iq) - S.vdw + 0.5 * low.re * low.re + 0.5 * low.im * low.im;
   }
   if (S.drive) {
     // optomechanical drive (helium): damping of the vertical velocity, the
