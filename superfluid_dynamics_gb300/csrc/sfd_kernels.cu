@@ -90,11 +90,29 @@ struct SrcDF {
   float a_hi, a_lo;
 };
 
+// acc += x with the running high part tracked exactly by a two-sum and every
+// low-order bit collected in acc.lo (cascaded summation, Ogita, Rump and
+// Oishi's Sum2): as accurate as summing in twice the working precision, with
+// one renormalisation at the end (df_acc_done) instead of one per term.
+__device__ __forceinline__ void df_acc(df& acc, float xh, float xl) {
+  const df s = two_sum(acc.hi, xh);
+  acc.hi = s.hi;
+  acc.lo = __fadd_rn(acc.lo, __fadd_rn(s.lo, xl));
+}
+__device__ __forceinline__ df df_acc_done(df acc) { return two_sum(acc.hi, acc.lo); }
+// a * b as an unnormalised pair (p + e == a b to double-float accuracy); the
+// accumulator absorbs e, so the product needs no renormalisation.
+__device__ __forceinline__ df df_mul_raw(df a, df b) {
+  const df p = two_prod(a.hi, b.hi);
+  return {p.hi, __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, p.lo))};
+}
+
 // (sr, si) += a / (nr + i ni) = a (nr - i ni) / (nr^2 + ni^2), all double-float.
 __device__ __forceinline__ void df_div_acc(df nr, df ni, df a, df& sr, df& si) {
   df t = df_mul(a, df_rcp(df_sqsum(nr, ni)));
-  sr = df_add(sr, df_mul(t, nr));
-  si = df_sub(si, df_mul(t, ni));
+  const df pr = df_mul_raw(t, nr), pi = df_mul_raw(t, ni);
+  df_acc(sr, pr.hi, pr.lo);
+  df_acc(si, -pi.hi, -pi.lo);
 }
 
 }  // namespace
@@ -210,7 +228,9 @@ template <int PREC>
 using WSum = typename std::conditional<PREC == SFD_PREC_F64, double, df>::type;
 
 __device__ __forceinline__ Red<SFD_PREC_F64> to_red(const Acc<SFD_PREC_F64>& A) { return {A.sr, A.si, A.tr, A.ti}; }
-__device__ __forceinline__ Red<SFD_PREC_DF> to_red(const Acc<SFD_PREC_DF>& A) { return {A.sr, A.si, A.tr, A.ti}; }
+__device__ __forceinline__ Red<SFD_PREC_DF> to_red(const Acc<SFD_PREC_DF>& A) {
+  return {df_acc_done(A.sr), df_acc_done(A.si), df_acc_done(A.tr), df_acc_done(A.ti)};
+}
 __device__ __forceinline__ Red<SFD_PREC_F32> to_red(const Acc<SFD_PREC_F32>& A) {
   return {df{A.sr, 0.f}, df{A.si, 0.f}, df{A.tr, 0.f}, df{A.ti, 0.f}};
 }
