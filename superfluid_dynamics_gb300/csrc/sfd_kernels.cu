@@ -107,9 +107,28 @@ __device__ __forceinline__ df df_mul_raw(df a, df b) {
   return {p.hi, __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, p.lo))};
 }
 
+// x^2 + y^2 and 1 / a as unnormalised pairs (low part within a few ulp of
+// the high part), for operands that only enter df_mul_raw / df_rcp_raw.
+__device__ __forceinline__ df df_sqsum_raw(df x, df y) {
+  const df px = two_prod(x.hi, x.hi);
+  const float ex = __fmaf_rn(2.0f * x.hi, x.lo, px.lo);
+  const df py = two_prod(y.hi, y.hi);
+  const float ey = __fmaf_rn(2.0f * y.hi, y.lo, py.lo);
+  const df s = two_sum(px.hi, py.hi);
+  return {s.hi, __fadd_rn(s.lo, __fadd_rn(ex, ey))};
+}
+__device__ __forceinline__ df df_rcp_raw(df a) {
+  float r0;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r0) : "f"(a.hi));
+  const df p = two_prod(a.hi, r0);
+  float e = __fsub_rn(__fsub_rn(1.0f, p.hi), p.lo);
+  e = __fmaf_rn(-a.lo, r0, e);
+  return {r0, __fmul_rn(r0, e)};
+}
+
 // (sr, si) += a / (nr + i ni) = a (nr - i ni) / (nr^2 + ni^2), all double-float.
 __device__ __forceinline__ void df_div_acc(df nr, df ni, df a, df& sr, df& si) {
-  df t = df_mul(a, df_rcp(df_sqsum(nr, ni)));
+  const df t = df_mul_raw(a, df_rcp_raw(df_sqsum_raw(nr, ni)));
   const df pr = df_mul_raw(t, nr), pi = df_mul_raw(t, ni);
   df_acc(sr, pr.hi, pr.lo);
   df_acc(si, -pi.hi, -pi.lo);
