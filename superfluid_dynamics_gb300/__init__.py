@@ -5,7 +5,8 @@ from ._lib import (HELIUM, PRECISION_FP64, PRECISION_MIXED, WATER, SfdError,  # 
                    load as load_library)
 from .engine import (AutonomousRungeKuttaStepper, BoundaryIntegralCalculator, Drive, Engine,  # noqa: F401
                      HeliumBoundaryProblem, Options, Physics, SimulationManager, WaterBoundaryProblem)
+from . import h5io  # noqa: F401  (state / trajectory files in the reference's HDF5 layouts)
 
 __all__ = ["Engine", "Options", "Physics", "Drive", "WaterBoundaryProblem", "HeliumBoundaryProblem",
            "BoundaryIntegralCalculator", "AutonomousRungeKuttaStepper", "SimulationManager",
-           "WATER", "HELIUM", "PRECISION_FP64", "PRECISION_MIXED", "SfdError", "load_library"]
+           "WATER", "HELIUM", "PRECISION_FP64", "PRECISION_MIXED", "SfdError", "load_library", "h5io"]

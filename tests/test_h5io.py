@@ -1,0 +1,114 @@
+"""HDF5 state and trajectory files (superfluid_dynamics_gb300.h5io) in the
+reference's layouts: the reader against the two libhdf5-written trajectory
+files the reference ships (when present), the writer's dataset encoding
+against theirs, and round trips of the state-file (SimulationRunner.cuh:99-178)
+and simulation-file (Python/simulation.py:97-130) layouts."""
+import os
+import struct
+
+import numpy as np
+import pytest
+
+from superfluid_dynamics_gb300 import h5io
+
+_REF = "/root/reference/CuSuperHelium/Python"
+_FILES = [os.path.join(_REF, "integration", "simulation_15modes.h5"),
+          os.path.join(_REF, "simulation_gaussian_highampl0.1.h5")]
+
+
+def _ref_file(i):
+    if not os.path.exists(_FILES[i]):
+        pytest.skip("reference trajectory files not present")
+    return _FILES[i]
+
+
+@pytest.mark.parametrize("i", [0, 1])
+def test_reader_reads_the_reference_trajectories(i):
+    ds, attrs = h5io.read(_ref_file(i))
+    n = ds["x0"].size
+    assert ds["Y"].shape == (ds["T"].size, 3 * n)
+    assert np.all(np.diff(ds["T"]) > 0) and ds["T"][0] == 0.0
+    # the first stored state is the initial state written beside it
+    assert np.array_equal(ds["Y"][0], np.concatenate([ds["x0"], ds["y0"], ds["pot0"]]))
+
+
+def _dataset_messages(path):
+    b = open(path, "rb").read()
+    R = h5io._Reader(b)
+    bt = hp = None
+    for t, body, _ in R.messages(R.u("Q", 64)[0]):
+        if t == 0x11:
+            bt, hp = struct.unpack_from("<QQ", body)
+    hdata = R.u("Q", hp + 24)[0]
+    snod = R.u("Q", bt + 32)[0]
+    name = lambda off: b[hdata + off:b.index(b"\0", hdata + off)].decode()  # noqa: E731
+    out = {}
+    for i in range(R.u("H", snod + 6)[0]):
+        off, oh = R.u("QQ", snod + 8 + 40 * i)
+        # the layout message without its data address
+        out[name(off)] = [(t, fl, body[:2] + body[10:18] if t == 0x8 else body)
+                          for t, body, fl in R.messages(oh) if t != 0]
+    keys = [name(R.u("Q", bt + 24)[0]), name(R.u("Q", bt + 40)[0])]
+    return b[8:24], keys, list(out), out
+
+
+def test_writer_encodes_datasets_as_libhdf5_does(tmp_path):
+    ref = _ref_file(1)
+    ds, _ = h5io.read(ref)
+    mine = str(tmp_path / "t.h5")
+    h5io.write(mine, {k: ds[k] for k in ("T", "Y", "x0", "y0", "pot0")})
+    sb_a, keys_a, order_a, msgs_a = _dataset_messages(ref)
+    sb_b, keys_b, order_b, msgs_b = _dataset_messages(mine)
+    assert sb_a == sb_b and keys_a == keys_b and order_a == order_b
+    assert msgs_a == msgs_b
+
+
+def test_attribute_message_layout():
+    body = h5io._attr_msg("depth", 2.5)
+    t, size, flags = struct.unpack_from("<HHB", body)
+    assert t == 0xC and size == len(body) - 8 and size % 8 == 0
+    ver, _, nlen, dlen, slen = struct.unpack_from("<BBHHH", body, 8)
+    assert (ver, nlen, dlen, slen) == (1, 6, 20, 8)
+    assert body[16:22] == b"depth\0"
+    value = struct.unpack_from("<d", body, 8 + 8 + 8 + 24 + 8)[0]
+    assert value == 2.5
+
+
+def test_state_file_round_trip_and_checks(tmp_path):
+    n = 64
+    xi = 2 * np.pi * np.arange(n) / n
+    Z = xi + 1j * 0.05 * np.cos(xi)
+    phi = 0.01 * np.sin(xi)
+    p = str(tmp_path / "state.h5")
+    props = {"rho": 0.3, "kappa": 1e-4, "U": 0.0, "depth": 2.0, "initial_amplitude": 0.05}
+    assert h5io.save_state_file(p, Z, phi, props, rhs=True) == 0
+    ds, attrs = h5io.read(p)
+    assert ds["interface"].shape == (n, 2) and ds["potential"].shape == (n,)
+    assert attrs == {**props, "rhs": True}
+    Z2, phi2 = h5io.load_state_file(p, n, scale_y=2.0)
+    assert np.array_equal(Z2.real, Z.real) and np.array_equal(Z2.imag, 2.0 * Z.imag)
+    assert np.array_equal(phi2, phi)
+    with pytest.raises(RuntimeError, match=r"Interface must have shape \(32, 2\), instead it has \(64, 2\)"):
+        h5io.load_state_file(p, 32)
+
+
+def test_simulation_file_round_trip(tmp_path):
+    rng = np.random.default_rng(3)
+    n = 16
+    T = np.linspace(0.0, 1.0, 11)
+    Y = rng.normal(size=(11, 3 * n))
+    p = str(tmp_path / "sim.h5")
+    h5io.save_simulation_file(p, T, Y, Y[0], L=1e-3, depth=2e-8, t0=0.0, t1=1.0, initial_amplitude=1e-9, g=9.81)
+    out = h5io.load_simulation_file(p)
+    T2, Y2, Y02, L, depth, N, t0, t1, amp, g = out
+    assert np.array_equal(T2, T) and np.array_equal(Y2, Y) and np.array_equal(Y02, Y[0])
+    assert (L, depth, N, t0, t1, amp, g) == (1e-3, 2e-8, n, 0.0, 1.0, 1e-9, 9.81)
+    assert isinstance(N, int)
+    assert h5io.load_simulation_file(str(tmp_path / "missing.h5")) is None
+
+
+def test_not_hdf5_is_rejected(tmp_path):
+    p = tmp_path / "x.h5"
+    p.write_bytes(b"not an hdf5 file at all")
+    with pytest.raises(h5io.H5FormatError):
+        h5io.read(str(p))
