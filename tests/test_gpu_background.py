@@ -43,3 +43,21 @@ def test_background_rebuild_lag_must_be_below_the_interval():
     a, _, _ = run(512, 30, 0, every=10)
     b, _, _ = run(512, 30, 10, every=10)
     assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("n", [4096, 8192])
+def test_mixed_rhs_at_large_n_matches_fp64(n):
+    """The large-surface path (column-sliced preconditioner product, cluster
+    transforms) against the FP64 engine on the same state, with the bench's
+    solver settings (2 FP32 pre-iterations, 2 corrections): 1e-11 of the
+    largest entry (the project's mixed-precision bound against the oracle is
+    1e-10)."""
+    s = W.random_modes(n, seed=2)
+    out = {}
+    for prec in (sfd.PRECISION_FP64, sfd.PRECISION_MIXED):
+        opt = sfd.Options(precision=prec, use_graphs=False, pre_iters=2, refine_iters=2)
+        with sfd.Engine(n, sfd.WaterBoundaryProblem(), opt) as e:
+            e.set_state(s.x, s.y, s.phi)
+            out[prec] = np.concatenate(e.rhs()[:3])
+    ref = out[sfd.PRECISION_FP64]
+    assert np.abs(out[sfd.PRECISION_MIXED] - ref).max() <= 1e-11 * np.abs(ref).max()
