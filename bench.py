@@ -357,6 +357,32 @@ def _timed_steps(eng, dt, steps, stream):
     return e0.elapsed_time(e1) * 1e-3
 
 
+def _empty_graph_ms(kernels: int, replays: int = 50) -> float:
+    """Replay time of a CUDA graph of `kernels` dependent one-element kernels:
+    the launch-latency floor of a step graph with that many nodes."""
+    import torch
+    t = torch.zeros(1, device="cuda")
+    g = torch.cuda.CUDAGraph()
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        t.add_(1.0)  # warm the kernel before capture
+    torch.cuda.current_stream().wait_stream(side)
+    with torch.cuda.graph(g):
+        for _ in range(kernels):
+            t.add_(1.0)
+    for _ in range(3):
+        g.replay()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(replays):
+        g.replay()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / replays
+
+
 def run_workload(args, rank, world, local_rank):
     """Secondary workloads (parity and scale cases, one JSON line each):
       modes1024   : gravity wave N=1024, 8 seeded modes (seed 2), dt=0.005,
@@ -396,13 +422,19 @@ def run_workload(args, rank, world, local_rank):
             eng.set_state(x, s.y, s.phi)
             traj, t = [], 0.0
             done = 0
+            l0 = eng.kernel_launches
             for c in chk:
                 t += _timed_steps(eng, dt, c - done, stream)
                 done = c
                 traj.append(np.concatenate(eng.get_state()))
-            res[name] = (traj, steps / t, eng.status())
+            res[name] = (traj, steps / t, eng.status(), (eng.kernel_launches - l0) / steps)
             eng.close()
         line["value"] = res["mixed"][1]
+        # latency view: a step against a graph of as many empty dependent kernels
+        k = int(round(res["mixed"][3]))
+        step_ms = 1e3 / res["mixed"][1]
+        line["latency"] = {"step_ms": step_ms, "stage_ms": step_ms / 4, "kernels_per_step": k,
+                           "empty_graph_ms": _empty_graph_ms(k)}
         line["fp64_steps_per_s"] = res["fp64"][1]
         line["accuracy"] = {"steps": chk,
                             "mixed_vs_fp64": [_state_err(a, b, n) for a, b in zip(res["mixed"][0], res["fp64"][0])],
