@@ -6,8 +6,10 @@ dispersion relation, g = 1, RK4 dt = 0.005, mixed precision (FP32
 preconditioner + double-float / FP64 refinement).  Synthetic data: the
 reference measures on no dataset.
 
-  value  : steps/s with the state resident in HBM (CUDA events on the engine
-           stream around each step; L2 flushed between steps, outside timing)
+  value  : steps/s with the state resident in HBM: one CUDA event pair on the
+           engine stream around the K steps and the L2 flush (a 256 MB write)
+           before each, minus K flushes timed alone; the background
+           preconditioner rebuild (refactor_lag) is joined before the end event
   e2e    : steps/s through the C ABI with host buffers (pinned host -> device
            copy of the state, one step, device -> host copy, every step)
   roofline: the RK4 step against the tensor roofline of its algorithmic FLOP
