@@ -262,6 +262,11 @@ void sfd_default_gl2_options(sfd_gl2_options* o);
  * the state after it. */
 int sfd_gl2_evolve(sfd_engine* e, double t0, double t1, const sfd_gl2_options* opts, sfd_gl2_result* res,
                    double* times, double* states, long long cap);
+/* As sfd_gl2_evolve, calling fn(user, t, state) after each accepted step with
+ * the time reached and the state (host, 3n doubles, valid during the call). */
+typedef void (*sfd_gl2_step_fn)(void* user, double t, const double* state);
+int sfd_gl2_evolve_cb(sfd_engine* e, double t0, double t1, const sfd_gl2_options* opts, sfd_gl2_result* res,
+                      sfd_gl2_step_fn fn, void* user);
 
 /* ------------------------------------------------------------ reverse mode (adjoint)
  * Hand-written adjoint of the FP64 RHS and of RK4 trajectories.  The reference

@@ -11,6 +11,8 @@
 //     runStep, runEvolution, getY                         (AutonomousRungeKuttaStepper.cuh:24-44)
 //   TrajectoryLogger<T, N>, OdeSolverResult               (TrajectoryLogger.cuh, OdeSolver.h)
 //   MatrixSolver<N, B>::solve(M, b, a)                    (MatrixSolver.cuh:24-45)
+//   RealBoundaryItegralCalculator<N>, GaussLegendre2<N>    (RealBoundaryIntegralCalculator.cuh,
+//                                                          GaussLegendre.cuh:128-214)
 //
 // State layout is the reference's: device arrays of std_complex (two doubles,
 // real then imaginary), [Z (N B) | Phi (N B)], with Phi's imaginary part
@@ -20,6 +22,7 @@
 #pragma once
 
 #include <algorithm>
+#include <cmath>
 #include <complex>
 #include <cstddef>
 #include <cstdlib>
@@ -148,8 +151,125 @@ class BaseBoundaryIntegralCalculator : public AutonomousProblem<std_complex, 2 *
   std_complex *zp_ = nullptr, *zpp_ = nullptr;
 };
 
+// Real-state view of a one-surface calculator (RealBoundaryIntegralCalculator.cuh:34-80,
+// the reference's class name kept with its spelling): state and rhs are device
+// arrays [x (N) | y (N) | phi (N)], which is the engine's own layout, so no
+// conversion runs.
+template <int N>
+class RealBoundaryItegralCalculator : public AutonomousProblem<double, 3 * N> {
+ public:
+  explicit RealBoundaryItegralCalculator(BaseBoundaryIntegralCalculator<N, 1>& calculator) : calc_(calculator) {}
+  void run(double* initialState, double* rhs) override { check(sfd_rhs_device(calc_.engine(), initialState, rhs)); }
+  void setStream(cudaStream_t stream) override { calc_.setStream(stream); }
+
+ private:
+  BaseBoundaryIntegralCalculator<N, 1>& calc_;
+};
+
 // OdeSolver.h:2-5
 enum class OdeSolverResult { ReachedEndTime, StiffnessDetected };
+
+// GaussLegendre2Options (GaussLegendre.cuh:83-104), same fields and defaults.
+struct GaussLegendre2Options {
+  double stepSize = 0.01;
+  double newtonTolerance = 1e-10;
+  size_t maxNewtonIterations = 20;
+  bool allowSimplifiedFallback = false;
+  bool returnTrajectory = true;
+  double armijo_c = 1e-4;
+  double backtrack = 0.5;
+  double minAlpha = 1e-6;
+  size_t maxStepsHalves = 6;
+};
+
+// Implicit two-stage Gauss-Legendre (GaussLegendre.cuh:128-214) on the
+// engine of a one-surface FP64 calculator; the stage Jacobians are the
+// engine's (finite differences, or exact where reverse mode covers the
+// problem), so no JacobianCalculator is passed.  States are [x | y | phi].
+template <int N>
+class GaussLegendre2 {
+ public:
+  explicit GaussLegendre2(BaseBoundaryIntegralCalculator<N, 1>& calculator,
+                          GaussLegendre2Options options = GaussLegendre2Options())
+      : calc_(calculator), opt_(options) {}
+  // host (onDevice false) or device state [x | y | phi]
+  void initialize(const double* initialState, bool onDevice = false) {
+    if (onDevice) {
+      const size_t b = 3 * (size_t)N * sizeof(double);
+      std::vector<double> h(3 * (size_t)N);
+      if (cudaMemcpy(h.data(), initialState, b, cudaMemcpyDeviceToHost) != cudaSuccess)
+        throw std::runtime_error("sfd: initialize copy failed");
+      set_(h.data());
+    } else {
+      set_(initialState);
+    }
+  }
+  // throws std::runtime_error when a step fails to converge at every halving
+  // (the reference throws as well)
+  OdeSolverResult runEvolution(double startTime, double endTime) {
+    sfd_gl2_options o;
+    sfd_default_gl2_options(&o);
+    o.step = opt_.stepSize;
+    o.newton_tol = opt_.newtonTolerance;
+    o.max_newton = (long long)opt_.maxNewtonIterations;
+    o.allow_simplified = opt_.allowSimplifiedFallback ? 1 : 0;
+    o.armijo_c = opt_.armijo_c;
+    o.backtrack = opt_.backtrack;
+    o.min_alpha = opt_.minAlpha;
+    o.max_halvings = (long long)opt_.maxStepsHalves;
+    if (opt_.returnTrajectory && times_.empty()) {
+      times_.push_back(startTime);
+      states_.insert(states_.end(), start_.begin(), start_.end());
+    }
+    sfd_gl2_result r;
+    check(sfd_gl2_evolve_cb(calc_.engine(), startTime, endTime, &o, &r, opt_.returnTrajectory ? &record_ : nullptr,
+                            this));
+    if (r.status != 0)
+      throw std::runtime_error("sfd: Gauss-Legendre 2nd Order method failed to converge at t=" + std::to_string(r.t));
+    if (r.steps > 0) opt_.stepSize = std::fabs(r.h);  // the last accepted step carries over (GaussLegendre.cuh:318)
+    last_.resize(3 * (size_t)N);
+    check(sfd_get_state_host(calc_.engine(), last_.data(), last_.data() + N, last_.data() + 2 * N));
+    start_ = last_;
+    return OdeSolverResult::ReachedEndTime;
+  }
+  // std::malloc'd copies, released by the caller with std::free
+  // (GaussLegendre.cuh:386-436); without returnTrajectory: no times, the last state
+  int copyTimesToHost(double** hostTimes, size_t* countHost) const {
+    if (!opt_.returnTrajectory) {
+      *hostTimes = nullptr;
+      *countHost = 0;
+      return 0;
+    }
+    return copy_(times_, hostTimes, countHost, 1);
+  }
+  int copyStatesToHost(double** hostStates, size_t* countHost) const {
+    return copy_(opt_.returnTrajectory ? states_ : last_, hostStates, countHost, 3 * (size_t)N);
+  }
+  void setStream(cudaStream_t stream) { calc_.setStream(stream); }
+
+ private:
+  void set_(const double* y) {
+    check(sfd_set_state_host(calc_.engine(), y, y + N, y + 2 * N));
+    start_.assign(y, y + 3 * (size_t)N);
+    last_ = start_;
+  }
+  static void record_(void* self, double t, const double* state) {
+    auto* g = static_cast<GaussLegendre2*>(self);
+    g->times_.push_back(t);
+    g->states_.insert(g->states_.end(), state, state + 3 * (size_t)N);
+  }
+  static int copy_(const std::vector<double>& v, double** out, size_t* count, size_t per) {
+    double* p = static_cast<double*>(std::malloc(v.size() * sizeof(double) + 1));
+    if (!p) return -1;
+    std::copy(v.begin(), v.end(), p);
+    *out = p;
+    *count = v.size() / per;
+    return 0;
+  }
+  BaseBoundaryIntegralCalculator<N, 1>& calc_;
+  GaussLegendre2Options opt_;
+  std::vector<double> times_, states_, start_, last_;
+};
 
 // Device-side trajectory record (TrajectoryLogger.cuh:8-79): one state of N
 // values of T per logged time, appended on the logger's stream into a device

@@ -155,6 +155,8 @@ _SIGS = {
     "sfd_join_background": (c_int, [c_void_p]),
     "sfd_gl2_evolve": (c_int, [c_void_p, c_double, c_double, POINTER(SfdGl2Options), POINTER(SfdGl2Result), _dp, _dp,
                                c_longlong]),
+    "sfd_gl2_evolve_cb": (c_int, [c_void_p, c_double, c_double, POINTER(SfdGl2Options), POINTER(SfdGl2Result),
+                                  c_void_p, c_void_p]),
     "integrateSimulationGL2": (c_int, [_dp, POINTER(_dp), POINTER(c_size_t), POINTER(_dp), POINTER(c_size_t),
                                        POINTER(SimProperties), POINTER(GaussLegendreOptions), c_size_t]),
     "integrateSimulationGL2_freeMemory": (c_int, [_dp, _dp]),
@@ -167,6 +169,7 @@ def header_symbols() -> list[str]:
     """Function names declared in include/sfd.h."""
     txt = open(os.path.join(_build.ROOT, "include", "sfd.h")).read()
     txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    txt = re.sub(r"^\s*typedef\b.*?;", "", txt, flags=re.S | re.M)  # function-pointer and struct typedefs
     names = re.findall(r"^\s*(?:[A-Za-z_][A-Za-z0-9_]*[\s*]+)+([A-Za-z_][A-Za-z0-9_]*)\s*\(", txt, flags=re.M)
     return sorted(set(n for n in names if n not in ("if", "while", "return")))
 

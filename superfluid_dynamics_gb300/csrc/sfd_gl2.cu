@@ -410,7 +410,7 @@ int attempt(sfd_engine* e, Gl2Work* W, const sfd_gl2_options& o, bool exact, dou
 }  // namespace
 
 int sfd_internal_gl2(sfd_engine* e, double t0, double t1, const sfd_gl2_options& o, sfd_gl2_result& r,
-                     std::vector<double>* times, std::vector<double>* states) {
+                     std::vector<double>* times, std::vector<double>* states, sfd_gl2_step_fn fn, void* user) {
   std::memset(&r, 0, sizeof(r));
   if (!e) return sfd_internal_error(SFD_ERR_INVALID, "null engine");
   if (e->nsurf != 1 || e->nblk != 3)
@@ -444,6 +444,7 @@ int sfd_internal_gl2(sfd_engine* e, double t0, double t1, const sfd_gl2_options&
   Gl2Stats S;
   long long steps = 0, halvings = 0;
   double resid = 0.0, last_h = 0.0;
+  std::vector<double> step_host;
   int status = 0;
   while ((t - t1) * fwd < 0.0) {
     double htry = std::min(step, std::fabs(t1 - t)) * fwd;
@@ -469,6 +470,12 @@ int sfd_internal_gl2(sfd_engine* e, double t0, double t1, const sfd_gl2_options&
       const size_t off = states->size();
       states->resize(off + n3);
       GCK(cudaMemcpyAsync(states->data() + off, e->y0, n3 * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+    }
+    if (fn) {
+      step_host.resize(n3);
+      GCK(cudaMemcpyAsync(step_host.data(), e->y0, n3 * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+      GCK(cudaStreamSynchronize(e->stream));
+      fn(user, t, step_host.data());
     }
   }
   GCK(cudaStreamSynchronize(e->stream));
@@ -496,6 +503,12 @@ extern "C" void sfd_default_gl2_options(sfd_gl2_options* o) {
   o->max_halvings = 6;
   o->fd_eps = 1e-6;  // JacobianCalculator::eps
   o->jacobian = SFD_GL2_JACOBIAN_AUTO;
+}
+
+extern "C" int sfd_gl2_evolve_cb(sfd_engine* e, double t0, double t1, const sfd_gl2_options* opts,
+                                 sfd_gl2_result* res, sfd_gl2_step_fn fn, void* user) {
+  if (!opts || !res) return sfd_internal_error(SFD_ERR_INVALID, "null argument");
+  return sfd_internal_gl2(e, t0, t1, *opts, *res, nullptr, nullptr, fn, user);
 }
 
 extern "C" int sfd_gl2_evolve(sfd_engine* e, double t0, double t1, const sfd_gl2_options* opts, sfd_gl2_result* res,

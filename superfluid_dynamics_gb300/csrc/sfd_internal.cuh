@@ -174,4 +174,5 @@ void sfd_gl2_free(sfd_engine* e);
 // GL2 from t0 to t1 on the engine state (sfd_gl2.cu); times / states (host,
 // nullable) are appended the time and the 3n state after each accepted step.
 int sfd_internal_gl2(sfd_engine* e, double t0, double t1, const sfd_gl2_options& o, sfd_gl2_result& r,
-                     std::vector<double>* times, std::vector<double>* states);
+                     std::vector<double>* times, std::vector<double>* states, sfd_gl2_step_fn fn = nullptr,
+                     void* user = nullptr);

@@ -5,6 +5,8 @@
 //   AutonomousRungeKuttaStepper, 10 steps vs sfd_rk4_steps; its TrajectoryLogger
 //     record and initialize(devptr, true) in place vs the same steps
 //   MatrixSolver<64, 3>                   vs Gaussian elimination on the host
+//   RealBoundaryItegralCalculator and RK4 on it vs sfd_rhs_host / sfd_rk4_steps
+//   GaussLegendre2                         vs sfd_gl2_evolve
 // Prints the differences and exits 0 when all are within tolerance.
 #include <cmath>
 #include <cstdio>
@@ -182,11 +184,83 @@ int main() {
   unsigned int st_or = 0;
   for (unsigned int v : st) st_or |= v;
 
-  std::printf("run %.3e vorticity %.3e stepper %.3e logger/in-place %.3e solve %.3e status %u\n", e_run, e_a, e_step,
-              e_log, e_solve, st_or);
+  // 5. real-state calculator, RK4 on it, and GL2, each against the engine's own entry points
+  stage("real state, GL2");
+  constexpr int M2 = 32;
+  std::vector<double> s2(3 * M2);
+  for (int j = 0; j < M2; ++j) {
+    const double xi = 2 * PI * j / M2;
+    s2[j] = xi;
+    s2[M2 + j] = 0.05 * std::cos(xi);
+    s2[2 * M2 + j] = 0.015 * std::sin(xi);
+  }
+  sfd::WaterBoundaryProblem<M2, 1> water2(props);
+  sfd::BaseBoundaryIntegralCalculator<M2, 1> calc2(props, water2);
+  sfd::RealBoundaryItegralCalculator<M2> real2(calc2);
+  double *dS2 = nullptr, *dR2 = nullptr;
+  cudaMalloc(&dS2, sizeof(double) * 3 * M2);
+  cudaMalloc(&dR2, sizeof(double) * 3 * M2);
+  cudaMemcpy(dS2, s2.data(), sizeof(double) * 3 * M2, cudaMemcpyHostToDevice);
+  real2.run(dS2, dR2);
+  sfd::check(sfd_synchronize(calc2.engine()));
+  std::vector<double> r2(3 * M2), er2(3 * M2);
+  cudaMemcpy(r2.data(), dR2, sizeof(double) * 3 * M2, cudaMemcpyDeviceToHost);
+  int m2 = M2;
+  sfd_engine* e2 = nullptr;
+  sfd::check(sfd_create(&m2, 1, &p, 1, &o, &e2));
+  sfd::check(sfd_set_state_host(e2, s2.data(), s2.data() + M2, s2.data() + 2 * M2));
+  sfd::check(sfd_rhs_host(e2, er2.data(), er2.data() + M2, er2.data() + 2 * M2, nullptr, nullptr, nullptr));
+  double e_real = maxrel(r2, er2);
+  std::vector<double> y2(3 * M2), ey2(3 * M2);
+  {
+    sfd::AutonomousRungeKuttaStepper<double, 3 * M2> rk(real2, dt);
+    rk.initialize(s2.data(), false);
+    rk.runEvolution(0.0, 5 * dt + 0.5 * dt);
+    cudaMemcpy(y2.data(), rk.getY(), sizeof(double) * 3 * M2, cudaMemcpyDeviceToHost);
+  }
+  sfd::check(sfd_set_state_host(e2, s2.data(), s2.data() + M2, s2.data() + 2 * M2));
+  sfd::check(sfd_rk4_steps(e2, dt, 5));
+  sfd::check(sfd_get_state_host(e2, ey2.data(), ey2.data() + M2, ey2.data() + 2 * M2));
+  e_real = std::fmax(e_real, maxrel(y2, ey2));
+  // GL2 through the facade and through the C entry point
+  sfd::GaussLegendre2Options gopt;
+  gopt.stepSize = 0.01;
+  sfd::GaussLegendre2<M2> gl(calc2, gopt);
+  gl.initialize(s2.data(), false);
+  if (gl.runEvolution(0.0, 0.03) != sfd::OdeSolverResult::ReachedEndTime) return 5;
+  double* gtimes = nullptr;
+  double* gstates = nullptr;
+  size_t gnt = 0, gns = 0;
+  if (gl.copyTimesToHost(&gtimes, &gnt) || gl.copyStatesToHost(&gstates, &gns)) return 6;
+  sfd::check(sfd_set_state_host(e2, s2.data(), s2.data() + M2, s2.data() + 2 * M2));
+  sfd_gl2_options go;
+  sfd_default_gl2_options(&go);
+  go.step = 0.01;
+  go.max_newton = 20;
+  go.allow_simplified = 0;
+  sfd_gl2_result gr;
+  std::vector<double> ctimes(64);
+  sfd::check(sfd_gl2_evolve(e2, 0.0, 0.03, &go, &gr, ctimes.data(), nullptr, 64));
+  std::vector<double> gfin(3 * M2);
+  sfd::check(sfd_get_state_host(e2, gfin.data(), gfin.data() + M2, gfin.data() + 2 * M2));
+  double e_gl2 = (gnt == (size_t)gr.steps + 1 && gns == gnt && gtimes[0] == 0.0) ? 0.0 : 1.0;
+  for (long long i = 0; i < gr.steps && e_gl2 == 0.0; ++i) e_gl2 = std::fabs(gtimes[i + 1] - ctimes[(size_t)i]);
+  if (gns == gnt) {
+    std::vector<double> last(gstates + (gns - 1) * 3 * M2, gstates + gns * 3 * M2);
+    e_gl2 = std::fmax(e_gl2, maxrel(last, gfin));
+  }
+  std::free(gtimes);
+  std::free(gstates);
+  sfd_destroy(e2);
+  cudaFree(dS2);
+  cudaFree(dR2);
+
+  std::printf("run %.3e vorticity %.3e stepper %.3e logger/in-place %.3e solve %.3e real %.3e gl2 %.3e status %u\n",
+              e_run, e_a, e_step, e_log, e_solve, e_real, e_gl2, st_or);
   std::fflush(stdout);
   sfd_destroy(e);
   for (void* p : {(void*)dS, (void*)dR, (void*)dA, (void*)db, (void*)dxs}) cudaFree(p);
-  const bool ok = e_run < 1e-13 && e_a < 1e-13 && e_step < 1e-13 && e_log < 1e-14 && e_solve < 1e-12 && st_or == 0;
+  const bool ok = e_run < 1e-13 && e_a < 1e-13 && e_step < 1e-13 && e_log < 1e-14 && e_solve < 1e-12 &&
+                  e_real < 1e-13 && e_gl2 < 1e-12 && st_or == 0;
   return ok ? 0 : 1;
 }
