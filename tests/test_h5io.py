@@ -112,3 +112,58 @@ def test_not_hdf5_is_rejected(tmp_path):
     p.write_bytes(b"not an hdf5 file at all")
     with pytest.raises(h5io.H5FormatError):
         h5io.read(str(p))
+
+
+# ---------------------------------------------------------------- C++ side (include/sfd_h5.hpp)
+def _cxx_tool(tmp_path):
+    import shutil
+    import subprocess
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    exe = str(tmp_path / "h5_check")
+    subprocess.check_call([cxx, "-std=c++17", "-O1", os.path.join(root, "tests", "cpp", "h5_check.cpp"),
+                           "-I", os.path.join(root, "include"), "-o", exe])
+    return exe
+
+
+def test_cpp_and_python_writers_produce_the_same_bytes(tmp_path):
+    import subprocess
+    exe = _cxx_tool(tmp_path)
+    pc = str(tmp_path / "cxx.h5")
+    subprocess.check_call([exe, "write", pc])
+    n = 8
+    j = np.arange(n)
+    Z = 0.25 * j + 1j * (0.5 * j - 1.0)
+    pp = str(tmp_path / "py.h5")
+    h5io.save_state_file(pp, Z, 0.1 * j, {"rho": 0.25, "kappa": 1e-3, "U": 0.0, "depth": 2.0,
+                                          "initial_amplitude": 0.05}, rhs=True)
+    assert open(pc, "rb").read() == open(pp, "rb").read()
+    Zc, phic = h5io.load_state_file(pc, n)
+    assert np.array_equal(Zc, Z) and np.array_equal(phic, 0.1 * j)
+
+
+def test_cpp_reader_reads_python_files_and_checks_shapes(tmp_path):
+    import subprocess
+    exe = _cxx_tool(tmp_path)
+    rng = np.random.default_rng(9)
+    n = 12
+    Z = rng.normal(size=n) + 1j * rng.normal(size=n)
+    phi = rng.normal(size=n)
+    p = str(tmp_path / "s.h5")
+    h5io.save_state_file(p, Z, phi, {"depth": 3.0})
+    out = subprocess.run([exe, "read", p, str(n)], capture_output=True, text=True, check=True).stdout
+    vals = np.array([[float(v) for v in line.split()] for line in out.strip().splitlines()])
+    assert np.array_equal(vals[:, 0], Z.real) and np.array_equal(vals[:, 1], Z.imag) and np.array_equal(vals[:, 2], phi)
+    bad = subprocess.run([exe, "read", p, "5"], capture_output=True, text=True)
+    assert bad.returncode == 1 and "Interface must have shape (5, 2), instead it has (12, 2)" in bad.stderr
+
+
+@pytest.mark.parametrize("i", [0, 1])
+def test_cpp_reader_reads_the_reference_trajectories(tmp_path, i):
+    import subprocess
+    path = _ref_file(i)
+    exe = _cxx_tool(tmp_path)
+    r = subprocess.run([exe, "traj", path], capture_output=True, text=True)
+    assert r.returncode == 0 and r.stdout.startswith("ok"), r.stdout + r.stderr
