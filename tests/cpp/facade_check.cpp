@@ -7,6 +7,7 @@
 //   MatrixSolver<64, 3>                   vs Gaussian elimination on the host
 //   RealBoundaryItegralCalculator and RK4 on it vs sfd_rhs_host / sfd_rk4_steps
 //   GaussLegendre2                         vs sfd_gl2_evolve
+//   the generic stepper on 256 rotations     vs the exact solution (10^4 steps of 1e-3)
 // Prints the differences and exits 0 when all are within tolerance.
 #include <cmath>
 #include <cstdio>
@@ -255,12 +256,58 @@ int main() {
   cudaFree(dS2);
   cudaFree(dR2);
 
-  std::printf("run %.3e vorticity %.3e stepper %.3e logger/in-place %.3e solve %.3e real %.3e gl2 %.3e status %u\n",
-              e_run, e_a, e_step, e_log, e_solve, e_real, e_gl2, st_or);
+  // 6. the generic stepper on a user-defined problem: M rotations dx/dt = -y,
+  //    dy/dt = x (ODE_Solvers.RK4, ODESolverTests.cuh:73-246), against cos / sin
+  stage("rotation");
+  double e_rot = 0.0;
+  {
+    constexpr int MR = 256;
+    struct Rotation : sfd::AutonomousProblem<double, 2 * MR> {
+      double *zeros = nullptr, *scratch = nullptr;
+      cudaStream_t st = nullptr;
+      Rotation() {
+        cudaMalloc(&zeros, sizeof(double) * MR);
+        cudaMalloc(&scratch, sizeof(double) * MR);
+        cudaMemset(zeros, 0, sizeof(double) * MR);
+      }
+      ~Rotation() override {
+        cudaFree(zeros);
+        cudaFree(scratch);
+      }
+      // rhs = [-y | x]: -y as the stage combine 0 + (-1) y, x as a copy
+      void run(double* state, double* rhs) override {
+        sfd::check(sfd_rk4_stage_device(MR, zeros, state + MR, scratch, rhs, 1.0, -1.0, 1, st));
+        cudaMemcpyAsync(rhs + MR, state, sizeof(double) * MR, cudaMemcpyDeviceToDevice, st);
+      }
+      void setStream(cudaStream_t s) override { st = s; }
+    } rot;
+    std::vector<double> r0(2 * MR), rT(2 * MR);
+    for (int i = 0; i < MR; ++i) {
+      const double th = 2 * PI * i / MR;
+      r0[i] = std::cos(th);
+      r0[MR + i] = std::sin(th);
+    }
+    const double h = 1e-3;
+    const long long nsteps = 10000;
+    sfd::AutonomousRungeKuttaStepper<double, 2 * MR> rk(rot, h);
+    rk.initialize(r0.data(), false);
+    rk.runEvolution(0.0, nsteps * h + 0.5 * h);
+    cudaMemcpy(rT.data(), rk.getY(), sizeof(double) * 2 * MR, cudaMemcpyDeviceToHost);
+    const double T = rk.getCurrentTime();
+    for (int i = 0; i < MR; ++i) {
+      const double th = 2 * PI * i / MR;
+      e_rot = std::fmax(e_rot, std::fabs(rT[i] - std::cos(th + T)));
+      e_rot = std::fmax(e_rot, std::fabs(rT[MR + i] - std::sin(th + T)));
+    }
+  }
+
+  std::printf("run %.3e vorticity %.3e stepper %.3e logger/in-place %.3e solve %.3e real %.3e gl2 %.3e rotation %.3e "
+              "status %u\n",
+              e_run, e_a, e_step, e_log, e_solve, e_real, e_gl2, e_rot, st_or);
   std::fflush(stdout);
   sfd_destroy(e);
   for (void* p : {(void*)dS, (void*)dR, (void*)dA, (void*)db, (void*)dxs}) cudaFree(p);
   const bool ok = e_run < 1e-13 && e_a < 1e-13 && e_step < 1e-13 && e_log < 1e-14 && e_solve < 1e-12 &&
-                  e_real < 1e-13 && e_gl2 < 1e-12 && st_or == 0;
+                  e_real < 1e-13 && e_gl2 < 1e-12 && e_rot < 1e-9 && st_or == 0;
   return ok ? 0 : 1;
 }
