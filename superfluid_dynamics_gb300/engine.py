@@ -85,6 +85,20 @@ class Drive:
 
 @dataclass
 class Options:
+    """Engine options (sfd_options of include/sfd.h).
+
+    precision      PRECISION_MIXED (FP32 / tensor-core preconditioner with
+                   double-float refinement) or PRECISION_FP64 (blocked FP64 LU)
+    refine_iters   mixed: FP32 corrections after the double-float residual
+    refactor_every mixed: rebuild the preconditioner every k RK4 steps
+    use_graphs     capture one RK4 step in a CUDA graph
+    tensor_cores   mixed: Gauss-Jordan update on tcgen05 (else SIMT)
+    pre_iters      mixed: FP32 full-residual iterations before the accurate pass
+    precond_half   mixed: apply the preconditioner from its FP16 copy
+    autotune       time the boundary-sum CTA shapes on the first steps
+    refactor_lag   mixed, stepping: rebuild on a side stream and switch k steps
+                   later (0 < k < refactor_every; 0 rebuilds inside the step)
+    """
     precision: int = PRECISION_MIXED
     refine_iters: int = 2
     refactor_every: int = 1
