@@ -260,18 +260,17 @@ def run_ours(args, rank, world, local_rank):
             eng.step(DT, extra)
             done += extra
 
-    # ---- end to end through the C ABI with host buffers: every step copies the
-    # state in from pinned host memory and the result back out
-    x = torch.from_numpy(s.x).pin_memory().numpy()
-    y = torch.from_numpy(s.y).pin_memory().numpy()
-    p = torch.from_numpy(s.phi).pin_memory().numpy()
+    # ---- end to end through the C ABI with host buffers: every step is one
+    # sfd_rk4_steps_host call that copies the state in from pinned host memory,
+    # steps, and copies the result back into the same buffers
+    x = torch.from_numpy(s.x.copy()).pin_memory().numpy()
+    y = torch.from_numpy(s.y.copy()).pin_memory().numpy()
+    p = torch.from_numpy(s.phi.copy()).pin_memory().numpy()
     align()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        eng.set_state(x, y, p)
-        eng.step(DT, 1)
-        x2, y2, p2 = eng.get_state()
+        eng.step_host(x, y, p, DT, 1)
     e2e_s = time.perf_counter() - t0
     done += args.steps
     e2e_value = world * args.steps / e2e_s

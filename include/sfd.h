@@ -156,6 +156,10 @@ int sfd_rhs_device(sfd_engine* e, const void* state_in, void* rhs_out);
 /* `steps` classic RK4 steps of size dt on the resident state
  * (AutonomousRungeKuttaStepper<std_complex,2N>::runStep, :123-307). */
 int sfd_rk4_steps(sfd_engine* e, double dt, int steps);
+/* Host-buffer stepping in one call: copy the state [x | y | phi] (ntot each)
+ * in, run `steps` RK4 steps, copy it back out into the same arrays, with one
+ * synchronisation.  Pinned host arrays make the copies asynchronous. */
+int sfd_rk4_steps_host(sfd_engine* e, double* x, double* y, double* phi, double dt, int steps);
 /* Enqueue without waiting for completion (timed loops). */
 int sfd_rk4_steps_async(sfd_engine* e, double dt, int steps);
 int sfd_synchronize(sfd_engine* e);

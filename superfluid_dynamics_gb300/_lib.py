@@ -153,6 +153,7 @@ _SIGS = {
     "integrateSimulationRK4_freeMemory": (c_int, [_dp, _dp]),
     "sfd_default_gl2_options": (None, [POINTER(SfdGl2Options)]),
     "sfd_join_background": (c_int, [c_void_p]),
+    "sfd_rk4_steps_host": (c_int, [c_void_p, _dp, _dp, _dp, c_double, c_int]),
     "sfd_gl2_evolve": (c_int, [c_void_p, c_double, c_double, POINTER(SfdGl2Options), POINTER(SfdGl2Result), _dp, _dp,
                                c_longlong]),
     "sfd_gl2_evolve_cb": (c_int, [c_void_p, c_double, c_double, POINTER(SfdGl2Options), POINTER(SfdGl2Result),

@@ -1175,6 +1175,23 @@ int sfd_rk4_steps(sfd_engine* e, double dt, int steps) {
   return sfd_synchronize(e);
 }
 
+int sfd_rk4_steps_host(sfd_engine* e, double* x, double* y, double* phi, double dt, int steps) {
+  if (!e || !x || !y || !phi) return set_error(SFD_ERR_INVALID, "null argument");
+  if (e->nblk != 3) return set_error(SFD_ERR_INVALID, "the engine carries a fourth state block: use the aux calls");
+  CK(cudaSetDevice(e->device));
+  const size_t b = (size_t)e->ntot * sizeof(double);
+  CK(cudaMemcpyAsync(e->y0, x, b, cudaMemcpyHostToDevice, e->stream));
+  CK(cudaMemcpyAsync(e->y0 + e->ntot, y, b, cudaMemcpyHostToDevice, e->stream));
+  CK(cudaMemcpyAsync(e->y0 + 2 * e->ntot, phi, b, cudaMemcpyHostToDevice, e->stream));
+  int rc = run_steps(e, dt, steps);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(x, e->y0, b, cudaMemcpyDeviceToHost, e->stream));
+  CK(cudaMemcpyAsync(y, e->y0 + e->ntot, b, cudaMemcpyDeviceToHost, e->stream));
+  CK(cudaMemcpyAsync(phi, e->y0 + 2 * e->ntot, b, cudaMemcpyDeviceToHost, e->stream));
+  CK(cudaStreamSynchronize(e->stream));
+  return 0;
+}
+
 int sfd_invariants(sfd_engine* e, double kappa, double* out) {
   if (!e || !out) return set_error(SFD_ERR_INVALID, "null argument");
   CK(cudaSetDevice(e->device));

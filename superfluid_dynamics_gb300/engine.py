@@ -222,6 +222,14 @@ class Engine:
         fn = self._L.sfd_rk4_steps if sync else self._L.sfd_rk4_steps_async
         check(fn(self._h, float(dt), int(steps)))
 
+    def step_host(self, x: np.ndarray, y: np.ndarray, phi: np.ndarray, dt: float, steps: int = 1) -> None:
+        """Copy the host state in, run `steps` RK4 steps and copy it back into
+        the same float64 arrays (one call, one synchronisation)."""
+        for a in (x, y, phi):
+            if a.dtype != np.float64 or not a.flags.c_contiguous or a.size != self.ntot:
+                raise ValueError(f"state arrays must be contiguous float64 of {self.ntot} nodes")
+        check(self._L.sfd_rk4_steps_host(self._h, _dp(x), _dp(y), _dp(phi), float(dt), int(steps)))
+
     def evolve_rkf45(self, t0: float, t1: float, atol: float = 1e-6, rtol: float = 1e-3, h_min: float = 1e-16,
                      h_max: float = 1e10, h0: float = 1e-2, max_rejected: int = 500, max_times: int = 1 << 20):
         """Adaptive Runge-Kutta-Fehlberg 4(5) of the resident state from t0 to t1

@@ -61,3 +61,21 @@ def test_mixed_rhs_at_large_n_matches_fp64(n):
             out[prec] = np.concatenate(e.rhs()[:3])
     ref = out[sfd.PRECISION_FP64]
     assert np.abs(out[sfd.PRECISION_MIXED] - ref).max() <= 1e-11 * np.abs(ref).max()
+
+
+def test_step_host_matches_resident_stepping():
+    """sfd_rk4_steps_host (copy in, step, copy out in one call) equals setting
+    the state, stepping on the device and reading it back."""
+    n = 512
+    s = W.random_modes(n, seed=2)
+    opt = sfd.Options(autotune=False, refactor_every=10)
+    with sfd.Engine(n, sfd.WaterBoundaryProblem(), opt) as e:
+        e.set_state(s.x, s.y, s.phi)
+        e.step(0.005, 7)
+        ref = np.concatenate(e.get_state())
+    with sfd.Engine(n, sfd.WaterBoundaryProblem(), opt) as e:
+        x, y, p = s.x.copy(), s.y.copy(), s.phi.copy()
+        for _ in range(7):
+            e.step_host(x, y, p, 0.005, 1)
+        got = np.concatenate([x, y, p])
+    assert np.array_equal(got, ref)
