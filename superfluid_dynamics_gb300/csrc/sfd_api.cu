@@ -40,6 +40,10 @@ int set_error(int code, const char* fmt, ...) {
   vsnprintf(buf, sizeof(buf), fmt, ap);
   va_end(ap);
   g_last_error = buf;
+  // A CUDA failure is reported here once: consume the runtime's record of it,
+  // so that a later, unrelated launch check does not report it again (errors
+  // that leave the context unusable persist regardless).
+  if (code == SFD_ERR_CUDA) (void)cudaGetLastError();
   return code;
 }
 

@@ -390,7 +390,7 @@ cudaError_t sfd_launch_spectral_cluster(const DerivArgs& A, const int2* jobs, in
   const int M = max_n / SFD_FFT_CLUSTER;
   size_t smem = (size_t)3 * M * sizeof(cd);
   k_spectral_cluster<<<dim3(SFD_FFT_CLUSTER, njobs), kCT, smem, st>>>(A, jobs);
-  return cudaGetLastError();
+  return cudaPeekAtLastError();  // the caller's launch check reads and clears it
 }
 
 cudaError_t sfd_fft_configure() {
@@ -406,5 +406,5 @@ cudaError_t sfd_launch_spectral(const DerivArgs& A, const int2* jobs, int njobs,
   if (njobs == 0) return cudaSuccess;
   size_t smem = (size_t)max_n * sizeof(cd);
   k_spectral_deriv<<<njobs, kFftThreads, smem, st>>>(A, jobs);
-  return cudaGetLastError();
+  return cudaPeekAtLastError();
 }

@@ -466,7 +466,7 @@ cudaError_t sfd_launch_sums(int prec, const SumArgs& A, int nitems, int max_n, i
   if (prec == SFD_PREC_F64) launch_prec<SFD_PREC_F64>(A, grid, groups, smem, st);
   else if (prec == SFD_PREC_DF) launch_prec<SFD_PREC_DF>(A, grid, groups, smem, st);
   else launch_prec<SFD_PREC_F32>(A, grid, groups, smem, st);
-  return cudaGetLastError();
+  return cudaPeekAtLastError();  // the caller's launch check reads and clears it
 }
 
 // Velocities and Bernoulli:

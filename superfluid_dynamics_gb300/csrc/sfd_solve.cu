@@ -100,12 +100,12 @@ __global__ void k_assemble(const SurfaceDesc* surf, const int4* tiles, const cd*
 cudaError_t sfd_launch_assemble64(const SurfaceDesc* surf, const int4* tiles, int ntiles, const cd* w, const cd* p,
                                   const cd* zp, const double* mdiag, double* mat, cudaStream_t st) {
   k_assemble<double><<<ntiles, 256, 0, st>>>(surf, tiles, w, p, zp, mdiag, mat);
-  return cudaGetLastError();
+  return cudaPeekAtLastError();  // the caller's launch check reads and clears it
 }
 cudaError_t sfd_launch_assemble32(const SurfaceDesc* surf, const int4* tiles, int ntiles, const cd* w, const cd* p,
                                   const cd* zp, const double* mdiag, float* mat, cudaStream_t st) {
   k_assemble<float><<<ntiles, 256, 0, st>>>(surf, tiles, w, p, zp, mdiag, mat);
-  return cudaGetLastError();
+  return cudaPeekAtLastError();
 }
 
 // =============================================================== FP64 LU

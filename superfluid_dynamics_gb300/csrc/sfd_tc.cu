@@ -221,5 +221,5 @@ cudaError_t sfd_launch_gj_update_tc(const SurfaceDesc* surf, int nsurf, int kb, 
   const int t = max_np / kTile;
   k_gj_update_tc<<<dim3(t, t, nsurf), kTcThreads, 2 * kParts * kOpBytes + 1024, st>>>(surf, kb, mat, cparts, rparts,
                                                                                        part_stride, poff, status);
-  return cudaGetLastError();
+  return cudaPeekAtLastError();  // the caller's launch check reads and clears it
 }
