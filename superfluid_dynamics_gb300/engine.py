@@ -184,6 +184,8 @@ class Engine:
     def set_aux(self, D) -> None:
         """Delayed-intensity block of an augmented driven engine."""
         D = _f64(D)
+        if D.size != self.ntot:
+            raise ValueError(f"the delayed intensity must hold {self.ntot} nodes")
         check(self._L.sfd_set_aux_host(self._h, _dp(D)))
 
     def get_aux(self) -> np.ndarray:
@@ -441,10 +443,13 @@ class SimulationManager:
     def __init__(self, dll_path: str | None = None):
         self.lib = _lib.load() if dll_path is None else ctypes.CDLL(dll_path)
 
-    def _rhs(self, fn, x, y, phi, *args):
+    def _rhs(self, fn, x, y, phi, *args, nodes=None):
         x, y, phi = _f64(x), _f64(y), _f64(phi)
         if y.shape[0] != x.shape[0] or phi.shape[0] != x.shape[0]:
             raise ValueError("Input arrays must have the same length")
+        if nodes is not None and x.shape[0] != nodes:
+            # the fixed-size exports read exactly this many nodes
+            raise ValueError(f"Input arrays must hold {nodes} nodes")
         vx, vy, dphi = np.empty_like(x), np.empty_like(x), np.empty_like(x)
         rc = fn(_dp(x), _dp(y), _dp(phi), _dp(vx), _dp(vy), _dp(dphi), *args)
         return rc, vx, vy, dphi
@@ -453,17 +458,25 @@ class SimulationManager:
         return self._rhs(self.lib.calculateRHSFromVectors, x, y, phi, L, rho, kappa, depth, len(x))
 
     def calculate_rhs256_from_vectors(self, x, y, phi, L, rho, kappa, depth):
-        return self._rhs(self.lib.calculateRHS256FromVectors, x, y, phi, L, rho, kappa, depth)
+        return self._rhs(self.lib.calculateRHS256FromVectors, x, y, phi, L, rho, kappa, depth, nodes=256)
 
     def calculate_rhs2048_from_vectors(self, x, y, phi, L, rho, kappa, depth):
-        return self._rhs(self.lib.calculateRHS2048FromVectors, x, y, phi, L, rho, kappa, depth)
+        return self._rhs(self.lib.calculateRHS2048FromVectors, x, y, phi, L, rho, kappa, depth, nodes=2048)
 
     def calculate_rhs256_from_vectors_batched(self, x, y, phi, L, rho, kappa, depth, batch_size):
+        # rhs.py:187-189 checks y and phi against 256 * batch_size
+        n = len(x) // batch_size if batch_size > 0 else 0
+        if batch_size <= 0 or len(y) != n * batch_size or len(phi) != 256 * batch_size or len(x) != 256 * batch_size:
+            raise ValueError("Input arrays must have the same length equal to 256 * batch_size")
         return self._rhs(self.lib.calculateRHS256FromVectorsBatched, x, y, phi, L, rho, kappa, depth, batch_size)
 
     def calculate_vorticities256_from_vectors(self, Z, phi, L, rho, kappa, depth):
         Z = np.ascontiguousarray(Z, dtype=np.complex128)
         phi = np.ascontiguousarray(phi, dtype=np.complex128)
+        if phi.shape[0] != Z.shape[0]:
+            raise ValueError("Input arrays must have the same length")
+        if Z.shape[0] != 256:
+            raise ValueError("Input arrays must hold 256 nodes")
         a = np.empty(Z.shape[0])
         Zp = np.empty(Z.shape[0], np.complex128)
         Zpp = np.empty(Z.shape[0], np.complex128)
@@ -473,6 +486,8 @@ class SimulationManager:
 
     def calculate_derivativeFFT256(self, inp):
         inp = np.ascontiguousarray(inp, dtype=np.complex128)
+        if inp.shape[0] != 256:
+            raise ValueError("Input array must hold 256 nodes")
         out = np.empty(inp.shape[0], np.complex128)
         cp = lambda v: v.ctypes.data_as(ctypes.POINTER(ctypes.c_double))  # noqa: E731
         return self.lib.calculateDerivativeFFT256(cp(inp), cp(out)), out
@@ -489,9 +504,11 @@ class SimulationManager:
                                              ctypes.byref(nt), ctypes.byref(sp), ctypes.byref(ro), N)
         if rc != 0:
             raise SfdError(self.lib.sfd_last_error().decode())
-        S = np.ctypeslib.as_array(states, shape=(ns.value, 3 * N)).copy()
-        T = np.ctypeslib.as_array(times, shape=(nt.value,)).copy() if nt.value else np.empty(0)
-        self.lib.integrateSimulationRK4_freeMemory(states, times)
+        try:
+            S = np.ctypeslib.as_array(states, shape=(ns.value, 3 * N)).copy()
+            T = np.ctypeslib.as_array(times, shape=(nt.value,)).copy() if nt.value else np.empty(0)
+        finally:
+            self.lib.integrateSimulationRK4_freeMemory(states, times)
         return S, T
 
     def integrate(self, y0, sim_props: _lib.SimProperties, gl_props: _lib.GaussLegendreOptions):
@@ -549,7 +566,9 @@ class SimulationManager:
             ctypes.byref(sim_props), ctypes.byref(rk4_props), ctypes.byref(opt_props), y0.size // 4)
         if rc != 0:
             return rc, None, None
-        S = np.ctypeslib.as_array(states, shape=(ns.value, y0.size)).copy()
-        T = np.ctypeslib.as_array(times, shape=(nt.value,)).copy() if nt.value else np.empty(0)
-        self.lib.integrateAugmentedOptomechanicalSimulationRK4_freeMemory(states, times)
+        try:
+            S = np.ctypeslib.as_array(states, shape=(ns.value, y0.size)).copy()
+            T = np.ctypeslib.as_array(times, shape=(nt.value,)).copy() if nt.value else np.empty(0)
+        finally:
+            self.lib.integrateAugmentedOptomechanicalSimulationRK4_freeMemory(states, times)
         return rc, T, S
