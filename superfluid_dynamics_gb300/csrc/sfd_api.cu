@@ -43,7 +43,7 @@ int set_error(int code, const char* fmt, ...) {
   // A CUDA failure is reported here once: consume the runtime's record of it,
   // so that a later, unrelated launch check does not report it again (errors
   // that leave the context unusable persist regardless).
-  if (code == SFD_ERR_CUDA) (void)cudaGetLastError();
+  if (code == SFD_ERR_CUDA || code == SFD_ERR_NO_DEVICE) (void)cudaGetLastError();
   return code;
 }
 
@@ -572,6 +572,7 @@ int bg_flush(sfd_engine* e) {
 
 int run_steps(sfd_engine* e, double dt, int steps) {
   if (steps < 0) return set_error(SFD_ERR_INVALID, "negative step count");
+  if (!std::isfinite(dt)) return set_error(SFD_ERR_INVALID, "time step must be finite");
   CK(cudaSetDevice(e->device));
   if (e->tune_pending && steps > 0) {
     int rc = autotune_sums(e);
@@ -770,16 +771,18 @@ int sfd_create_driven(const int* n, int nsurf, const sfd_problem* problems, cons
   if (opts) e->opt = *opts;
   else sfd_default_options(&e->opt);
   if (e->opt.precision != SFD_PRECISION_FP64 && e->opt.precision != SFD_PRECISION_MIXED) {
+    const int precision = e->opt.precision;
     delete e;
-    return set_error(SFD_ERR_INVALID, "unknown precision %d", e->opt.precision);
+    return set_error(SFD_ERR_INVALID, "unknown precision %d", precision);
   }
   if (e->opt.refine_iters < 0) e->opt.refine_iters = 0;
   e->tune_pending = e->opt.autotune != 0;
   if (e->opt.pre_iters < 0) e->opt.pre_iters = 0;
   e->device = e->opt.device;
   if (e->device < 0 || e->device >= ndev) {
+    const int device = e->device;
     delete e;
-    return set_error(SFD_ERR_INVALID, "device %d out of range", e->opt.device);
+    return set_error(SFD_ERR_INVALID, "device %d out of range", device);
   }
   int rc = 0;
 #define CKE(expr)                   \
@@ -1179,20 +1182,35 @@ int sfd_rk4_steps(sfd_engine* e, double dt, int steps) {
   return sfd_synchronize(e);
 }
 
+// The three state blocks between host arrays and the resident state, on the
+// engine stream.
+static cudaError_t copy_state_host(sfd_engine* e, double* x, double* y, double* phi, bool to_device) {
+  const size_t b = (size_t)e->ntot * sizeof(double);
+  double* h[3] = {x, y, phi};
+  for (int k = 0; k < 3; ++k) {
+    double* d = e->y0 + (size_t)k * e->ntot;
+    const cudaError_t err = to_device ? cudaMemcpyAsync(d, h[k], b, cudaMemcpyHostToDevice, e->stream)
+                                      : cudaMemcpyAsync(h[k], d, b, cudaMemcpyDeviceToHost, e->stream);
+    if (err != cudaSuccess) return err;
+  }
+  return cudaSuccess;
+}
+
 int sfd_rk4_steps_host(sfd_engine* e, double* x, double* y, double* phi, double dt, int steps) {
   if (!e || !x || !y || !phi) return set_error(SFD_ERR_INVALID, "null argument");
   if (e->nblk != 3) return set_error(SFD_ERR_INVALID, "the engine carries a fourth state block: use the aux calls");
+  if (steps < 0) return set_error(SFD_ERR_INVALID, "negative step count");
+  if (!std::isfinite(dt)) return set_error(SFD_ERR_INVALID, "time step must be finite");
   CK(cudaSetDevice(e->device));
-  const size_t b = (size_t)e->ntot * sizeof(double);
-  CK(cudaMemcpyAsync(e->y0, x, b, cudaMemcpyHostToDevice, e->stream));
-  CK(cudaMemcpyAsync(e->y0 + e->ntot, y, b, cudaMemcpyHostToDevice, e->stream));
-  CK(cudaMemcpyAsync(e->y0 + 2 * e->ntot, phi, b, cudaMemcpyHostToDevice, e->stream));
-  int rc = run_steps(e, dt, steps);
+  // Once a copy is queued every exit waits for the stream, so that no copy
+  // still reads or writes the caller's arrays when the call returns.
+  cudaError_t err = copy_state_host(e, x, y, phi, true);
+  int rc = err == cudaSuccess ? run_steps(e, dt, steps) : 0;
+  if (err == cudaSuccess && rc == 0) err = copy_state_host(e, x, y, phi, false);
+  const cudaError_t sync = cudaStreamSynchronize(e->stream);
+  if (err != cudaSuccess) return set_error(SFD_ERR_CUDA, "sfd_rk4_steps_host: %s", cudaGetErrorString(err));
   if (rc) return rc;
-  CK(cudaMemcpyAsync(x, e->y0, b, cudaMemcpyDeviceToHost, e->stream));
-  CK(cudaMemcpyAsync(y, e->y0 + e->ntot, b, cudaMemcpyDeviceToHost, e->stream));
-  CK(cudaMemcpyAsync(phi, e->y0 + 2 * e->ntot, b, cudaMemcpyDeviceToHost, e->stream));
-  CK(cudaStreamSynchronize(e->stream));
+  if (sync != cudaSuccess) return set_error(SFD_ERR_CUDA, "sfd_rk4_steps_host: %s", cudaGetErrorString(sync));
   return 0;
 }
 

@@ -79,3 +79,4 @@ def test_step_host_matches_resident_stepping():
             e.step_host(x, y, p, 0.005, 1)
         got = np.concatenate([x, y, p])
     assert np.array_equal(got, ref)
+
