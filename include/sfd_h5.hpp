@@ -358,12 +358,15 @@ inline void read(const std::string& path, std::map<std::string, Dataset>& datase
       }
       if (!is_double) continue;  // not a double dataset: outside this reader
       uint64_t count = 1;
-      for (uint64_t s : d.shape) count *= s;
-      d.data.resize(count);
-      if (addr != kUndef && count) {
-        if (addr + count * 8 > f.b.size()) throw std::runtime_error("HDF5: dataset " + name + " past the end");
-        std::memcpy(d.data.data(), f.b.data() + addr, count * 8);
+      for (uint64_t s : d.shape) {
+        if (s != 0 && count > UINT64_MAX / s) throw std::runtime_error("HDF5: dataset " + name + ": shape overflows");
+        count *= s;
       }
+      // checked before the allocation, so a malformed shape cannot ask for more than the file holds
+      if (addr != kUndef && count && (addr > f.b.size() || count > (f.b.size() - addr) / 8))
+        throw std::runtime_error("HDF5: dataset " + name + " runs past the end of the file");
+      d.data.resize(count);
+      if (addr != kUndef && count) std::memcpy(d.data.data(), f.b.data() + addr, count * 8);
       datasets[name] = std::move(d);
     }
   }

@@ -25,6 +25,7 @@ messages, for files from other writers that keep to it.
 """
 from __future__ import annotations
 
+import math
 import os
 import struct
 
@@ -304,10 +305,12 @@ def read(path: str):
                     addr, size = struct.unpack_from("<QQ", body, 2)
             if shape is None or dt is None or addr is None:
                 continue  # not a dataset (a subgroup): outside this subset
-            count = int(np.prod(shape)) if shape else 1
+            count = math.prod(shape) if shape else 1  # Python integers: no wrap-around
             if addr == _UNDEF:
                 arr = np.zeros(count, dtype=dt)
             else:
+                if addr > len(b) or count * dt.itemsize > len(b) - addr:
+                    raise H5FormatError(f"{path}: dataset {name} runs past the end of the file")
                 arr = np.frombuffer(b, dtype=dt, count=count, offset=addr).copy()
             datasets[name] = arr.reshape(shape).astype(dt.newbyteorder("="))
     return datasets, attrs

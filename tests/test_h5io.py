@@ -107,6 +107,23 @@ def test_simulation_file_round_trip(tmp_path):
     assert h5io.load_simulation_file(str(tmp_path / "missing.h5")) is None
 
 
+def test_truncated_dataset_is_rejected(tmp_path):
+    """A dataset whose data would run past the end of the file is a format
+    error, found before the array is allocated (Python and C++ readers)."""
+    import subprocess
+    n = 16
+    p = str(tmp_path / "state.h5")
+    h5io.save_state_file(p, np.arange(n) + 0.5j, np.ones(n), {"depth": 1.0})
+    raw = open(p, "rb").read()
+    cut = str(tmp_path / "cut.h5")
+    open(cut, "wb").write(raw[:-8])  # the last dataset's data ends the file
+    with pytest.raises(h5io.H5FormatError, match="past the end"):
+        h5io.read(cut)
+    exe = _cxx_tool(tmp_path)
+    bad = subprocess.run([exe, "read", cut, str(n)], capture_output=True, text=True)
+    assert bad.returncode == 1 and "past the end" in bad.stderr
+
+
 def test_not_hdf5_is_rejected(tmp_path):
     p = tmp_path / "x.h5"
     p.write_bytes(b"not an hdf5 file at all")
