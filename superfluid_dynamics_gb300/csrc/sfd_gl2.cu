@@ -418,9 +418,16 @@ int sfd_internal_gl2(sfd_engine* e, double t0, double t1, const sfd_gl2_options&
   if (e->hs[0].drive) return sfd_internal_error(SFD_ERR_INVALID, "GL2 does not cover the optomechanical drive");
   const int n = e->hs[0].n;
   if (6 * n > 8192) return sfd_internal_error(SFD_ERR_INVALID, "GL2 supports n <= 1365 (Newton systems of order 6n)");
-  if (!(o.step > 0)) return sfd_internal_error(SFD_ERR_INVALID, "step must be > 0");
-  if (o.max_newton < 0 || o.max_halvings < 0 || !(o.backtrack > 0 && o.backtrack < 1) || !(o.fd_eps != 0))
-    return sfd_internal_error(SFD_ERR_INVALID, "invalid GL2 options");
+  if (!std::isfinite(t0) || !std::isfinite(t1)) return sfd_internal_error(SFD_ERR_INVALID, "t0 and t1 must be finite");
+  if (!(o.step > 0) || !std::isfinite(o.step)) return sfd_internal_error(SFD_ERR_INVALID, "step must be finite and > 0");
+  // The line search ends when alpha falls below min_alpha: with min_alpha <= 0
+  // (or NaN) and a non-finite trial residual it would never end.
+  if (o.max_newton < 0 || o.max_halvings < 0 || !(o.backtrack > 0 && o.backtrack < 1) ||
+      !(o.min_alpha > 0 && o.min_alpha <= 1) || !(o.armijo_c >= 0 && o.armijo_c < 1) || !(o.newton_tol >= 0) ||
+      !(std::isfinite(o.fd_eps) && o.fd_eps != 0))
+    return sfd_internal_error(SFD_ERR_INVALID,
+                              "invalid GL2 options: need max_newton, max_halvings >= 0, 0 < backtrack < 1, "
+                              "0 < min_alpha <= 1, 0 <= armijo_c < 1, newton_tol >= 0 and a finite nonzero fd_eps");
   GCK(cudaSetDevice(e->device));
   int rc = ensure_work(e);
   if (rc) return rc;

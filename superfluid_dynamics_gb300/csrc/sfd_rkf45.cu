@@ -136,7 +136,8 @@ extern "C" void sfd_default_rkf45_options(sfd_rkf45_options* o) {
 extern "C" int sfd_rkf45_evolve(sfd_engine* e, double t0, double t1, const sfd_rkf45_options* opt,
                                 sfd_rkf45_result* res, double* times, long long cap) {
   if (!e || !opt || !res) return sfd_internal_error(SFD_ERR_INVALID, "null argument");
-  if (!(opt->h0 > 0)) return sfd_internal_error(SFD_ERR_INVALID, "h0 must be > 0");
+  if (!std::isfinite(t0) || !std::isfinite(t1)) return sfd_internal_error(SFD_ERR_INVALID, "t0 and t1 must be finite");
+  if (!(opt->h0 > 0) || !std::isfinite(opt->h0)) return sfd_internal_error(SFD_ERR_INVALID, "h0 must be finite and > 0");
   RCK(cudaSetDevice(e->device));
   const long long n = (long long)e->nblk * e->ntot;
   if (!e->rkf) {

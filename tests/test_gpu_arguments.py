@@ -37,3 +37,31 @@ def test_create_rejects_bad_options(opts, msg):
         e.set_state(s.x, s.y, s.phi)
         e.step(0.005, 2)
         assert np.all(np.isfinite(np.concatenate(e.get_state())))
+
+
+@pytest.mark.parametrize("kw, msg", [({"min_alpha": 0.0}, "min_alpha"), ({"min_alpha": float("nan")}, "min_alpha"),
+                                     ({"armijo_c": 1.5}, "armijo_c"), ({"fd_eps": float("inf")}, "fd_eps"),
+                                     ({"step": float("inf")}, "step"), ({"t1": float("inf")}, "finite")])
+def test_gl2_rejects_options_that_cannot_end(kw, msg):
+    """A line search with min_alpha <= 0 never ends on a non-finite trial, and
+    an infinite end time never ends: both are refused up front."""
+    n = 64
+    s = W.random_modes(n, seed=4)
+    t1 = kw.pop("t1", 0.05)
+    with sfd.Engine(n, sfd.WaterBoundaryProblem(), sfd.Options(precision=sfd.PRECISION_FP64)) as e:
+        e.set_state(s.x, s.y, s.phi)
+        with pytest.raises(sfd.SfdError, match=msg):
+            e.evolve_gl2(0.0, t1, **kw)
+        res, times = e.evolve_gl2(0.0, 0.02, step=0.01)
+        assert res["steps"] == 2 and np.allclose(times, [0.01, 0.02])
+
+
+def test_rkf45_rejects_infinite_end_time():
+    n = 64
+    s = W.random_modes(n, seed=4)
+    with sfd.Engine(n, sfd.WaterBoundaryProblem(), sfd.Options(precision=sfd.PRECISION_FP64)) as e:
+        e.set_state(s.x, s.y, s.phi)
+        with pytest.raises(sfd.SfdError, match="finite"):
+            e.evolve_rkf45(0.0, float("inf"))
+        with pytest.raises(sfd.SfdError, match="h0"):
+            e.evolve_rkf45(0.0, 0.1, h0=float("nan"))
