@@ -29,16 +29,18 @@ class _RK4Trajectory(torch.autograd.Function):
         traj._apply_param(float(param))
         final = traj.engine.rk4_record(traj.dt, traj.steps, traj.checkpoint_every,
                                        state0.detach().cpu().numpy())
+        traj._recordings += 1
         ctx.traj = traj
+        ctx.recording = traj._recordings  # the engine keeps only the latest recording
         ctx.param_device = param.device
-        traj._recorded = True
         return torch.from_numpy(final).to(state0.device)
 
     @staticmethod
     def backward(ctx, grad_final):
         traj = ctx.traj
-        if not traj._recorded:
-            raise RuntimeError("the trajectory was re-recorded before backward")
+        if traj._recordings != ctx.recording:
+            raise RuntimeError("the trajectory was re-recorded before backward: "
+                               "call backward before the next forward of the same Trajectory")
         g0, gp = traj.engine.rk4_vjp(grad_final.detach().cpu().numpy())
         return (torch.from_numpy(g0).to(grad_final.device),
                 torch.tensor(gp, dtype=torch.float64, device=ctx.param_device), None)
@@ -47,8 +49,9 @@ class _RK4Trajectory(torch.autograd.Function):
 class Trajectory:
     """An FP64 engine for one surface plus the RK4 settings of the trajectory.
 
-    The differentiated parameter is A3 for helium films and g for water.  One
-    backward may follow each forward on the same object."""
+    The differentiated parameter is A3 for helium films and g for water.  The
+    engine holds one recording, so the backward of a forward must come before
+    the next forward on the same object (an out-of-order backward raises)."""
 
     def __init__(self, n: int, physics: Physics, dt: float, steps: int, checkpoint_every: int = 50,
                  device: int = 0):
@@ -58,7 +61,7 @@ class Trajectory:
         self.steps = int(steps)
         self.checkpoint_every = int(checkpoint_every)
         self.engine = Engine(self.n, physics, Options(precision=PRECISION_FP64, use_graphs=False, device=device))
-        self._recorded = False
+        self._recordings = 0  # forwards so far; a backward must belong to the latest
 
     def _apply_param(self, value: float) -> None:
         fields = {f.name: getattr(self.physics, f.name) for f in dataclasses.fields(Physics)}
