@@ -385,6 +385,21 @@ int integrateSimulationRK4_freeMemory(double* statesOut, double* timesOut);
  * (in chunks of at most 8 GB of matrices). */
 int calculateJacobian(const double* state, double* jac, double L, double rho, double kappa, double depth,
                       double epsilon, size_t N);
+/* Export.cuh:53 (Export.cu:601-662, JacobianCalculator.cuh:11-75): the 3N
+ * perturbed complex states [Z | Phi] of the finite-difference Jacobian at
+ * N = 256.  Zperturbed holds 6 N^2 complex values (interleaved re, im):
+ * positions of perturbation b at [b N, (b+1) N), potentials at
+ * [3 N^2 + b N, ...); b / N perturbs x, y or phi by epsilon at node b % N.
+ * Written on the host; L, rho, kappa and depth are unused, as in the reference. */
+int calculatePerturbedStates256(const double* x, const double* y, const double* phi, double* Zperturbed, double L,
+                                double rho, double kappa, double depth, double epsilon);
+/* Export.cuh:28 (Export.cu:42-113): read a state file of N = 256 nodes
+ * (`interface`, `potential`; y scaled by 2 pi / L), evaluate the helium RHS
+ * and write it to outputFile as a state file (`interface` = (dx, dy),
+ * `potential` = dphi) with attributes rho, kappa, U, depth (nondimensional),
+ * initial_amplitude = (max y - min y) / 2 and rhs = true. */
+int calculateRHS256FromFile(const char* inputFile, const char* outputFile, double L, double rho, double kappa,
+                            double depth);
 
 /* GaussLegendreOptions (ExportTypes.cuh:21-34). */
 typedef struct GaussLegendreOptions {

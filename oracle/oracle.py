@@ -340,6 +340,30 @@ def fd_jacobian(f, y, eps: float = 1e-6) -> np.ndarray:
     return J
 
 
+def perturbed_states(x, y, phi, eps: float) -> np.ndarray:
+    """The 3N perturbed complex states of the batched finite-difference
+    Jacobian (JacobianCalculator.cuh:11-75 createInitialBatchedZ, :154-161
+    createInitialState): 6 N^2 complex values.  Perturbation b (b / N picks
+    x, y or phi, b % N the node) has its positions Z = x + i y at [b N, (b+1) N)
+    and its potentials phi + 0 i at [3 N^2 + b N, ...); the perturbed entry is
+    the complex sum with (eps, 0) or (0, eps), both parts added."""
+    x, y, phi = _f64(x), _f64(y), _f64(phi)
+    n = x.size
+    re = np.empty((2, 3 * n, n))
+    im = np.empty((2, 3 * n, n))
+    re[0], im[0] = x, y
+    re[1], im[1] = phi, 0.0
+    for b in range(3 * n):
+        c, j = divmod(b, n)
+        part = 1 if c == 2 else 0
+        re[part, b, j] = re[part, b, j] + (0.0 if c == 1 else eps)
+        im[part, b, j] = im[part, b, j] + (eps if c == 1 else 0.0)
+    out = np.empty(re.size, dtype=np.complex128)  # assembled without arithmetic: signs of zeros kept
+    out.real = re.reshape(-1)
+    out.imag = im.reshape(-1)
+    return out
+
+
 def gl2_step(f, jac, y, h: float, tol: float = 1e-10, max_newton: int = 20, allow_simplified: bool = False,
              armijo_c: float = 1e-4, backtrack: float = 0.5, min_alpha: float = 1e-6):
     """One GL2 step of size h: returns (converged, y_next, iterations, residual norm)."""

@@ -148,6 +148,8 @@ _SIGS = {
     "calculateRHS256FromVectorsBatched": (c_int, [_dp] * 6 + [c_double] * 4 + [c_int]),
     "calculateVorticities256FromVectors": (c_int, [_dp] * 5 + [c_double] * 4),
     "calculateDerivativeFFT256": (c_int, [_dp, _dp]),
+    "calculatePerturbedStates256": (c_int, [_dp] * 4 + [c_double] * 5),
+    "calculateRHS256FromFile": (c_int, [ctypes.c_char_p, ctypes.c_char_p] + [c_double] * 4),
     "integrateSimulationRK4": (c_int, [_dp, POINTER(_dp), POINTER(c_size_t), POINTER(_dp), POINTER(c_size_t),
                                        POINTER(SimProperties), POINTER(RK4SolverOptions), c_size_t]),
     "integrateSimulationRK4_freeMemory": (c_int, [_dp, _dp]),

@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "../../include/sfd.h"
+#include "../../include/sfd_h5.hpp"
 #include "sfd_engine.cuh"
 #include "sfd_kernels.cuh"
 #include "sfd_solve.cuh"
@@ -1359,6 +1360,82 @@ int calculateRHS256FromVectorsBatched(const double* x, const double* y, const do
                                       int batchSize) {
   if (batchSize < 1) return set_error(SFD_ERR_INVALID, "unsupported batch size %d", batchSize);
   return rhs_from_vectors(x, y, phi, vx, vy, rhsPhi, L, rho, kappa, depth, 256, batchSize);
+}
+
+int calculateRHS256FromFile(const char* inputFile, const char* outputFile, double L, double rho, double kappa,
+                            double depth) {
+  // Export.cu:42-113: read a state file (y scaled by 2 pi / L), evaluate the
+  // helium RHS at N = 256 and write it as a state file flagged rhs, with the
+  // nondimensional properties and the amplitude (max y - min y) / 2.
+  if (!inputFile || !outputFile) return set_error(SFD_ERR_INVALID, "null argument");
+  const int n = 256;
+  std::vector<std::complex<double>> Z;
+  std::vector<double> phi;
+  try {
+    sfd::loadStateFile(inputFile, Z, phi, n, 2.0 * kPi / L);
+  } catch (const std::exception& ex) {
+    return set_error(SFD_ERR_INVALID, "calculateRHS256FromFile: %s: %s", inputFile, ex.what());
+  }
+  if (phi.size() != (size_t)n)
+    return set_error(SFD_ERR_INVALID, "calculateRHS256FromFile: %s: potential holds %zu values, not %d", inputFile,
+                     phi.size(), n);
+  std::vector<double> x(n), y(n), vx(n), vy(n), dphi(n);
+  for (int i = 0; i < n; ++i) {
+    x[i] = Z[i].real();
+    y[i] = Z[i].imag();
+  }
+  const auto mm = std::minmax_element(y.begin(), y.end());
+  const double amplitude = (*mm.second - *mm.first) / 2.0;
+  int rc = rhs_from_vectors(x.data(), y.data(), phi.data(), vx.data(), vy.data(), dphi.data(), L, rho, kappa, depth,
+                            n, 1);
+  if (rc) return rc;
+  const NondimProps np = adimensionalize(L, rho, kappa, depth);
+  std::vector<std::complex<double>> dz(n);
+  for (int i = 0; i < n; ++i) dz[i] = {vx[i], vy[i]};
+  try {
+    sfd::saveStateFile(outputFile, dz, dphi, n, np.rho, np.kappa, 0.0, np.depth, amplitude, true);
+  } catch (const std::exception& ex) {
+    return set_error(SFD_ERR_INVALID, "calculateRHS256FromFile: %s: %s", outputFile, ex.what());
+  }
+  return 0;
+}
+
+int calculatePerturbedStates256(const double* x, const double* y, const double* phi, double* Zperturbed, double L,
+                                double rho, double kappa, double depth, double epsilon) {
+  // Export.cu:601-662 with JacobianCalculator.cuh:11-75 and :154-161: the 3N
+  // states of the finite-difference Jacobian, each the complex state
+  // [Z | Phi] = [x + i y | phi + 0 i] with one coordinate raised by epsilon.
+  // Positions of perturbation b fill entries [b N, (b+1) N), potentials
+  // [3N^2 + b N, 3N^2 + (b+1) N); b / N picks x, y or phi and b % N the node.
+  // The output is a host array and the layout is a copy with one shifted
+  // entry per block, so it is written on the host: a device pass would only
+  // add the 6.3 MB copy back.  L, rho, kappa and depth are unused, as in the
+  // reference.
+  (void)L;
+  (void)rho;
+  (void)kappa;
+  (void)depth;
+  if (!x || !y || !phi || !Zperturbed) return set_error(SFD_ERR_INVALID, "null argument");
+  constexpr size_t n = 256, m = 3 * n;
+  double* pos = Zperturbed;
+  double* pot = Zperturbed + 2 * m * n;
+  for (size_t b = 0; b < m; ++b) {
+    double* zp = pos + 2 * b * n;
+    double* pp = pot + 2 * b * n;
+    for (size_t t = 0; t < n; ++t) {
+      zp[2 * t] = x[t];
+      zp[2 * t + 1] = y[t];
+      pp[2 * t] = phi[t];
+      pp[2 * t + 1] = 0.0;
+    }
+    // the perturbed entry is the complex sum state + (eps, 0) or + (0, eps),
+    // both parts added as the reference adds them (0.0 turns -0.0 into +0.0)
+    const size_t j = b % n, c = b / n;
+    double* e = c == 2 ? pp + 2 * j : zp + 2 * j;
+    e[0] = e[0] + (c == 1 ? 0.0 : epsilon);
+    e[1] = e[1] + (c == 1 ? epsilon : 0.0);
+  }
+  return 0;
 }
 
 int calculateVorticities256FromVectors(const double* Z, const double* phi, double* a, double* Zp, double* Zpp,

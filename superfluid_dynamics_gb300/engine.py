@@ -20,6 +20,7 @@ device-side calls.  Errors raise SfdError; nothing falls back to the CPU.
 from __future__ import annotations
 
 import ctypes
+import os
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -530,6 +531,27 @@ class SimulationManager:
         finally:
             self.lib.integrateSimulationGL2_freeMemory(states, times)
         return rc, T, S
+
+    def calculate_rhs256(self, input_file: str, output_file: str, L, rho, kappa, depth) -> int:
+        """rhs.py:91-99: RHS of the 256-node state file `input_file`, written to
+        `output_file` as a state file (calculateRHS256FromFile)."""
+        return self.lib.calculateRHS256FromFile(os.fsencode(input_file), os.fsencode(output_file), L, rho, kappa,
+                                                depth)
+
+    def calculate_perturbed_states256(self, x, y, phi, L, rho, kappa, depth, epsilon=1e-6):
+        """rhs.py:197-211: (rc, Zperturbed), the 6 N^2 complex values of the 3N
+        perturbed states at N = 256 (calculatePerturbedStates256)."""
+        x, y, phi = _f64(x), _f64(y), _f64(phi)
+        if y.shape[0] != x.shape[0] or phi.shape[0] != x.shape[0]:
+            raise ValueError("Input arrays must have the same length")
+        if x.shape[0] != 256:
+            raise ValueError("Input arrays must hold 256 nodes")
+        n = x.shape[0]
+        Z = np.empty(6 * n * n, dtype=np.complex128)
+        rc = self.lib.calculatePerturbedStates256(_dp(x), _dp(y), _dp(phi),
+                                                  Z.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), L, rho, kappa,
+                                                  depth, epsilon)
+        return rc, Z
 
     def calculate_jacobian(self, x, y, phi, L, rho, kappa, depth, epsilon=1e-6):
         """rhs.py:213-222: (rc, J) with J[row, col] = d rhs_row / d state_col, a

@@ -203,6 +203,37 @@ def test_vorticities_and_fft_exports():
     assert rel(out, O.fft_derivative(sig)) < 1e-13
 
 
+def test_rhs256_from_file_export(tmp_path):
+    """calculateRHS256FromFile (Export.cu:42-113): the state file's y is scaled
+    by 2 pi / L, the RHS is the 256-node helium RHS of the vector export, and
+    the output state file carries (dx, dy), dphi and the nondimensional
+    properties with initial_amplitude = (max y - min y) / 2 and rhs = true."""
+    from superfluid_dynamics_gb300 import h5io
+    L, depth = 1e-3, 2e-8
+    h = nondim(L, 145.0, 0.0, depth)
+    n = 256
+    xi = W.nodes(n)
+    scale = 2 * np.pi / L
+    y_file = (0.02 * h * np.cos(2 * xi)) / scale
+    phi = 0.001 * np.sin(2 * xi)
+    src, out = str(tmp_path / "state.h5"), str(tmp_path / "rhs.h5")
+    h5io.save_state_file(src, xi + 1j * y_file, phi, {"depth": depth})
+    sm = sfd.SimulationManager()
+    assert sm.calculate_rhs256(src, out, L, 145.0, 0.0, depth) == 0
+    y = scale * y_file
+    rc, vx, vy, dphi = sm.calculate_rhs256_from_vectors(xi, y, phi, L, 145.0, 0.0, depth)
+    assert rc == 0
+    ds, attrs = h5io.read(out)
+    itf, pot = ds["interface"], ds["potential"]
+    assert itf.shape == (n, 2) and pot.shape == (n,)
+    assert rel(itf[:, 0] + 1j * itf[:, 1], vx + 1j * vy) < 1e-13 and rel(pot, dphi) < 1e-13
+    (ox, oy, op), _ = O.rhs(O.Problem(physics=O.HELIUM, depth=h), xi, y, phi)
+    assert rel(itf[:, 0] + 1j * itf[:, 1], ox + 1j * oy) < 1e-11 and rel(pot, op) < 1e-9
+    assert attrs["rhs"] is True and attrs["U"] == 0.0 and attrs["kappa"] == 0.0
+    assert attrs["initial_amplitude"] == (y.max() - y.min()) / 2.0
+    assert np.isclose(attrs["depth"], h, rtol=1e-14, atol=0) and np.isclose(attrs["rho"], 145.0 / 150.0, rtol=1e-15, atol=0)
+
+
 def test_integrate_simulation_rk4_export():
     L, depth = 1e-3, 2e-8
     n = 64
