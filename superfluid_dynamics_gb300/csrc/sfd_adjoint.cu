@@ -516,7 +516,7 @@ int record_rhs(sfd_engine* e, AdjWork* W, AdjStage& st) {
 }
 
 int spectral(sfd_engine* e, AdjWork* W, int job, const double* re, const double* im, cd* out) {
-  DerivArgs D{e->d_surf, 1, re, im, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, out};
+  DerivArgs D{e->d_surf, 1, re, im, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, out, nullptr};
   cudaError_t err = sfd_launch_spectral(D, W->jobs + job, 1, W->n, e->stream);
   if (err != cudaSuccess) return sfd_internal_cuda(err, "spectral derivative");
   return 0;

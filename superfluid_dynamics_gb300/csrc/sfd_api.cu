@@ -250,7 +250,7 @@ int enqueue_precond(sfd_engine* e) {
 // writes C, D and r; the transform reads a and writes a').  The fork is
 // skipped under per-kernel profiling, whose events live on the engine stream.
 int enqueue_ap(sfd_engine* e, bool fork) {
-  DerivArgs D{e->d_surf, e->nsurf, nullptr, nullptr, nullptr, nullptr, e->a, e->zp, e->zpp, e->phip, e->ap};
+  DerivArgs D{e->d_surf, e->nsurf, nullptr, nullptr, nullptr, nullptr, e->a, e->zp, e->zpp, e->phip, e->ap, nullptr};
   if (fork && e->aux && !e->profile) {
     CK(cudaEventRecord(e->ev_fork, e->stream));
     CK(cudaStreamWaitEvent(e->aux, e->ev_fork, 0));
@@ -1492,7 +1492,7 @@ int calculateDerivativeFFT256(const double* input, double* output) {
     if (cudaMalloc(&dj, sizeof(int2)) != cudaSuccess) rc = SFD_ERR_CUDA;
     if (!rc) cudaMemcpy(dj, &job, sizeof(int2), cudaMemcpyHostToDevice);
     const int nt = e->ntot;
-    DerivArgs D{e->d_surf, e->nsurf, e->y0, e->y0 + nt, e->y0 + 2 * nt, nullptr, e->a, e->zp, e->zpp, e->phip, e->ap};
+    DerivArgs D{e->d_surf, e->nsurf, e->y0, e->y0 + nt, e->y0 + 2 * nt, nullptr, e->a, e->zp, e->zpp, e->phip, e->ap, nullptr};
     if (!rc && sfd_launch_spectral(D, dj, 1, n, e->stream) != cudaSuccess) rc = SFD_ERR_CUDA;  // single-CTA job
     if (!rc) {
       cudaStreamSynchronize(e->stream);
