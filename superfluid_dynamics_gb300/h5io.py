@@ -255,8 +255,19 @@ class _Reader:
 
 def read(path: str):
     """Datasets (name -> array) and root attributes (name -> value) of an HDF5
-    file in the subset this module writes."""
-    b = open(path, "rb").read()
+    file in the subset this module writes.  A truncated or malformed file
+    raises H5FormatError."""
+    with open(path, "rb") as f:
+        b = f.read()
+    try:
+        return _read(path, b)
+    except H5FormatError:
+        raise
+    except (struct.error, IndexError, ValueError) as e:  # a field or block outside the file
+        raise H5FormatError(f"{path}: truncated or malformed ({e})") from e
+
+
+def _read(path: str, b: bytes):
     if b[:8] != _SIG:
         raise H5FormatError(f"{path}: not an HDF5 file")
     if b[8] != 0 or b[13] != 8 or b[14] != 8:

@@ -184,3 +184,23 @@ def test_cpp_reader_reads_the_reference_trajectories(tmp_path, i):
     exe = _cxx_tool(tmp_path)
     r = subprocess.run([exe, "traj", path], capture_output=True, text=True)
     assert r.returncode == 0 and r.stdout.startswith("ok"), r.stdout + r.stderr
+
+
+def test_truncated_files_fail_cleanly(tmp_path):
+    """Every truncation of a valid state file is refused with a format error:
+    the Python reader raises H5FormatError, the C++ reader exits with status 1
+    (a crash would be a negative status), and neither reads past the end."""
+    import subprocess
+    n = 8
+    p = str(tmp_path / "state.h5")
+    h5io.save_state_file(p, np.arange(n) + 0.25j, np.ones(n), {"depth": 2.0, "rho": 0.5})
+    raw = open(p, "rb").read()
+    exe = _cxx_tool(tmp_path)
+    cut = str(tmp_path / "cut.h5")
+    cuts = sorted(set(list(range(0, 128, 7)) + list(range(128, len(raw), max(1, len(raw) // 40))) + [len(raw) - 1]))
+    for k in cuts:
+        open(cut, "wb").write(raw[:k])
+        with pytest.raises(h5io.H5FormatError):
+            h5io.load_state_file(cut, n)
+        r = subprocess.run([exe, "read", cut, str(n)], capture_output=True, text=True)
+        assert r.returncode == 1, (k, r.returncode, r.stderr)
