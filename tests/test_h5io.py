@@ -204,3 +204,28 @@ def test_truncated_files_fail_cleanly(tmp_path):
             h5io.load_state_file(cut, n)
         r = subprocess.run([exe, "read", cut, str(n)], capture_output=True, text=True)
         assert r.returncode == 1, (k, r.returncode, r.stderr)
+
+
+def test_corrupted_files_never_crash(tmp_path):
+    """Seeded random byte corruptions of a state file: the C++ reader either
+    reads it or exits with status 1 (never a signal, never a hang), and the
+    Python reader returns or raises a format or shape error."""
+    import subprocess
+    n = 8
+    p = str(tmp_path / "state.h5")
+    h5io.save_state_file(p, np.arange(n) + 0.25j, np.ones(n), {"depth": 2.0, "rho": 0.5})
+    raw = open(p, "rb").read()
+    exe = _cxx_tool(tmp_path)
+    rng = np.random.default_rng(5)
+    bad = str(tmp_path / "bad.h5")
+    for _ in range(150):
+        b = bytearray(raw)
+        for _ in range(int(rng.integers(1, 4))):
+            b[int(rng.integers(0, len(b)))] = int(rng.integers(0, 256))
+        open(bad, "wb").write(b)
+        r = subprocess.run([exe, "read", bad, str(n)], capture_output=True, timeout=20)
+        assert r.returncode in (0, 1), r.returncode
+        try:
+            h5io.load_state_file(bad, n)
+        except (h5io.H5FormatError, RuntimeError):
+            pass
