@@ -74,3 +74,25 @@ def _build_facade_check(tmp_path):
 
 def test_cpp_facade_compiles_and_links(tmp_path):
     assert os.path.exists(_build_facade_check(tmp_path))
+
+
+def test_c_caller_compiles_links_and_runs(tmp_path):
+    """include/sfd.h is a C header: a C11 program (-pedantic) compiles against
+    it, links to libsfd.so and gets the documented defaults and error codes
+    without a device."""
+    import shutil
+    import subprocess
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    lib = _lib.load()
+    libdir = os.path.dirname(lib._name)
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    exe = str(tmp_path / "abi_check")
+    subprocess.check_call([cc, "-std=c11", "-Wall", "-Wextra", "-pedantic", "-Werror",
+                           os.path.join(root, "tests", "c", "abi_check.c"), "-I", os.path.join(root, "include"),
+                           "-L", libdir, "-lsfd", f"-Wl,-rpath,{libdir}",
+                           f"-Wl,-rpath-link,{os.path.join(cuda, 'lib64')}", "-o", exe])
+    out = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0 and out.stdout.strip() == "ok", out.stdout + out.stderr
