@@ -20,10 +20,12 @@ reference measures on no dataset.
            sample (one RK4 step at N = 4096) on this host's cores
 
 --impl reference runs the reference-side CPU path (the oracle port: the
-reference's CUDA build needs Windows/MSVC-only pieces and its NumPy calculator
-cannot be shipped) on the same workload and prints the same line with
-"impl": "reference".  Under torchrun (N > 1) every rank runs an independent
-replica (a single surface does not shard); value = all ranks' steps / max time.
+reference's CUDA path does not compile from its sources as they lie and its
+NumPy calculator cannot be shipped) on the same workload and prints the same
+line with "impl": "reference"; under torchrun rank 0 alone runs it.
+
+Our arm under torchrun (N > 1) runs an independent replica per rank (a single
+surface does not shard); value = all ranks' steps / max time.
 """
 from __future__ import annotations
 
