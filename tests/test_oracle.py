@@ -180,3 +180,26 @@ def test_oracle_drive_terms_known_answers():
     (dx2, dy2, dphi2), _ = O.rhs_driven(P, O.Drive(**{**d.__dict__, "augmented": False}), xi, np.zeros(n),
                                         np.zeros(n), D)
     assert np.allclose(dphi2, d.strength * inten, rtol=0, atol=1e-14)
+
+
+def test_oracle_conserves_energy_and_mass():
+    """Physics pin independent of the reference's vectors: along an RK4
+    trajectory of a water wave the oracle's kinetic + potential energy
+    (Energies.cuh:136-204) and mass drift only at the integrator's order.
+    Halving dt shrinks the energy drift by more than 2^4."""
+    from superfluid_dynamics_gb300 import workloads as W
+    s = W.random_modes(64, seed=2)
+    P = O.Problem()
+
+    def invariants(x, y, phi):
+        (dx, dy, _), _ = O.rhs(P, x, y, phi)
+        return O.invariants(P, x, y, phi, dx, dy)
+
+    i0 = invariants(s.x, s.y, s.phi)
+    drift = []
+    for steps, dt in ((200, 0.005), (400, 0.0025)):
+        (x, y, p), _ = O.rk4_steps(P, s.x, s.y, s.phi, dt, steps)
+        i1 = invariants(x, y, p)
+        drift.append(abs((i1[0] + i1[1]) - (i0[0] + i0[1])) / abs(i0[0] + i0[1]))
+        assert abs(i1[4] - i0[4]) < 1e-14
+    assert drift[0] < 1e-11 and drift[0] / drift[1] > 16.0, drift
