@@ -187,12 +187,17 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         if not build_if_missing:
             raise RuntimeError(f"libsfd.so not built at {path}; run superfluid_dynamics_gb300.build.build()")
         _build.build()
-    L = ctypes.CDLL(path)
+    _lib = bind(ctypes.CDLL(path))
+    return _lib
+
+
+def bind(L: ctypes.CDLL) -> ctypes.CDLL:
+    """Set the argument and result types of every export on a loaded copy of
+    the library (ctypes cannot pass Python floats to an unbound function)."""
     for name, (res, args) in _SIGS.items():
         fn = getattr(L, name)
         fn.restype = res
         fn.argtypes = args
-    _lib = L
     return L
 
 

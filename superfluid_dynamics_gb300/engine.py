@@ -442,7 +442,7 @@ class SimulationManager:
     the same exported symbols, for Linux / this library."""
 
     def __init__(self, dll_path: str | None = None):
-        self.lib = _lib.load() if dll_path is None else ctypes.CDLL(dll_path)
+        self.lib = _lib.load() if dll_path is None else _lib.bind(ctypes.CDLL(dll_path))
 
     def _rhs(self, fn, x, y, phi, *args, nodes=None):
         x, y, phi = _f64(x), _f64(y), _f64(phi)

@@ -73,3 +73,15 @@ def test_engine_state_arrays_checked():
         e.step_host(x, x, np.zeros(96, np.float32), 0.01, 1)
     with pytest.raises(ValueError):  # step_host writes back in place: a strided view is refused
         e.step_host(x, x, np.zeros(192)[::2], 0.01, 1)
+
+
+def test_manager_binds_a_library_loaded_from_a_path():
+    """SimulationManager(dll_path) binds the export signatures like the default
+    load, so float arguments pass and the error code comes back."""
+    from superfluid_dynamics_gb300 import _lib
+    path = _lib.load()._name
+    m = SimulationManager(path)
+    v = np.zeros(256)
+    assert m.lib.calculatePerturbedStates256.argtypes is not None
+    rc, Z = m.calculate_perturbed_states256(v, v, v, 1e-6, 145.0, 0.0, 1.5e-8, 1e-6)
+    assert rc == 0 and Z[0] == 1e-6 + 0j
