@@ -328,9 +328,11 @@ class Engine:
     def rhs_vjp(self, state: np.ndarray, cot: np.ndarray):
         """Host convenience over rhs_vjp_device (device buffers from torch)."""
         import torch
+        state, cot = _f64(state), _f64(cot)
+        self._check_state_size(state, cot)
         dev = torch.device("cuda", self.options.device)
-        s = torch.as_tensor(_f64(state), device=dev)
-        c = torch.as_tensor(_f64(cot), device=dev)
+        s = torch.as_tensor(state, device=dev)
+        c = torch.as_tensor(cot, device=dev)
         g = torch.empty_like(s)
         gp = self.rhs_vjp_device(s.data_ptr(), c.data_ptr(), g.data_ptr())
         return g.cpu().numpy(), gp
@@ -338,8 +340,10 @@ class Engine:
     def jacobian(self, state: np.ndarray) -> np.ndarray:
         """Exact RHS Jacobian J[row, col] at state = [x|y|phi] (reverse sweeps, FP64 engine, one surface)."""
         import torch
+        state = _f64(state)
+        self._check_state_size(state)
         dev = torch.device("cuda", self.options.device)
-        s = torch.as_tensor(_f64(state), device=dev)
+        s = torch.as_tensor(state, device=dev)
         j = torch.empty(s.numel() * s.numel(), dtype=torch.float64, device=dev)
         check(self._L.sfd_jacobian_device(self._h, s.data_ptr(), j.data_ptr()))
         n3 = s.numel()
@@ -348,6 +352,7 @@ class Engine:
     def rk4_record(self, dt: float, steps: int, checkpoint_every: int, state0: np.ndarray) -> np.ndarray:
         """Integrate from state0 = [x|y|phi] keeping checkpoints; returns the final state."""
         s0 = _f64(state0)
+        self._check_state_size(s0)
         out = np.empty_like(s0)
         check(self._L.sfd_rk4_record(self._h, float(dt), int(steps), int(checkpoint_every), _dp(s0), _dp(out)))
         return out
@@ -355,10 +360,19 @@ class Engine:
     def rk4_vjp(self, cot_final: np.ndarray):
         """(d final / d state0)^T cot_final and the parameter derivative of <cot_final, final>."""
         c = _f64(cot_final)
+        self._check_state_size(c)
         g = np.empty_like(c)
         gp = np.zeros(1)
         check(self._L.sfd_rk4_vjp(self._h, _dp(c), _dp(g), _dp(gp)))
         return g, float(gp[0])
+
+    def _check_state_size(self, *arrays) -> None:
+        """Reverse-mode arrays hold the full state [x | y | phi]: the library
+        reads (and the Jacobian writes) exactly that many values."""
+        n3 = 3 * self.ntot
+        for a in arrays:
+            if a.size != n3:
+                raise ValueError(f"state-sized arrays must hold 3 * {self.ntot} = {n3} values, not {a.size}")
 
     def split(self, arr: np.ndarray) -> list[np.ndarray]:
         return [arr[self.offsets[i]:self.offsets[i + 1]] for i in range(self.nsurf)]

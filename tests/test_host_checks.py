@@ -85,3 +85,18 @@ def test_manager_binds_a_library_loaded_from_a_path():
     assert m.lib.calculatePerturbedStates256.argtypes is not None
     rc, Z = m.calculate_perturbed_states256(v, v, v, 1e-6, 145.0, 0.0, 1.5e-8, 1e-6)
     assert rc == 0 and Z[0] == 1e-6 + 0j
+
+
+def test_reverse_mode_arrays_checked_before_device_work():
+    """The Jacobian writes 9 (3 ntot)^2 values and the VJPs read 3 ntot: a
+    state of another length is refused on the host, before any copy."""
+    e = _engine(32)
+    bad, good = np.zeros(95), np.zeros(96)
+    with pytest.raises(ValueError, match="96"):
+        e.jacobian(bad)
+    with pytest.raises(ValueError, match="96"):
+        e.rhs_vjp(good, bad)
+    with pytest.raises(ValueError, match="96"):
+        e.rk4_record(0.01, 1, 1, bad)
+    with pytest.raises(ValueError, match="96"):
+        e.rk4_vjp(bad)
