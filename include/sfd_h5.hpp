@@ -9,8 +9,9 @@
 // - contiguous datasets of little-endian doubles;
 // - version-1 scalar attributes (double, int64, and bool as the FALSE/TRUE
 //   enum over a signed byte, as HighFive and h5py store it).
-// The byte layout is the one of superfluid_dynamics_gb300/h5io.py; files from
-// either side open in the other, in h5py and in HighFive.  Header-only C++17,
+// The byte layout is the one of superfluid_dynamics_gb300/h5io.py and files
+// from either side open in the other; the encoding matches libhdf5's own, the
+// subset h5py and HighFive read.  Header-only C++17,
 // no CUDA; assumes a little-endian host (x86-64, aarch64).
 #pragma once
 

@@ -11,8 +11,9 @@ Layouts:
   ``depth``, ``L``, ``N``, ``t0``, ``t1``, ``initial_amplitude``, ``g``.
 
 The files are written in the subset of the HDF5 format that libhdf5 itself
-writes with its default (earliest) format settings, which h5py and HighFive
-read:
+writes with its default (earliest) format settings (h5py and HighFive read
+that subset; neither is installed beside this package, so the check is
+byte-level against libhdf5-written files):
 - version-0 superblock with 8-byte offsets and lengths;
 - version-1 object headers;
 - the root group as a symbol table (local heap, one version-1 B-tree leaf,
