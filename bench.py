@@ -6,18 +6,33 @@ dispersion relation, g = 1, RK4 dt = 0.005, mixed precision (FP32
 preconditioner + double-float / FP64 refinement).  Synthetic data: the
 reference measures on no dataset.
 
-  value  : steps/s with the state resident in HBM: one CUDA event pair on the
-           engine stream around the K steps and the L2 flush (a 256 MB write)
-           before each, minus K flushes timed alone; the background
-           preconditioner rebuild (refactor_lag) is joined before the end event
+The one JSON line carries:
+  value  : mixed-precision steps/s with the state resident in HBM: one CUDA
+           event pair on the engine stream around the K steps and the L2 flush
+           (a 256 MB write) before each, minus K flushes timed alone; the
+           background preconditioner rebuild (refactor_lag) is joined before
+           the end event
   e2e    : steps/s through the C ABI with host buffers (pinned host -> device
            copy of the state, one step, device -> host copy, every step)
-  roofline: the RK4 step against the tensor roofline of its algorithmic FLOP
-           (dense LU + matvecs, bf16 peak / 3); per-kernel-class times from a
-           CUDA-event pass over the same workload (graphs off in that pass);
-           traffic = DRAM bytes per step from the committed ncu summary
-  cpu_baseline: the FP64 CPU oracle (a port of the reference path) on a bounded
-           sample (one RK4 step at N = 4096) on this host's cores
+  fp64   : the plain FP64 GPU step (the engine in FP64 mode: assembled FP64
+           matrix, blocked FP64 LU, FP64 sums) on the same surface, event-timed;
+           mixed_over_fp64 = value / its steps/s (the metric's ratio)
+  accuracy: max|z_mixed - z_fp64| / max|z_fp64| and the same for phi after 25,
+           50 and 100 steps (the benchmarked mixed settings), beside the FP64
+           round-off envelope: the FP64 run against an FP64 run whose x was
+           perturbed by 1e-15 relative
+  roofline: the dominant kernel class of the step (largest device time per
+           step in an event-timed pass, graphs off) against the measured peak
+           of the unit that bounds it; every class with its algorithmic work,
+           achieved rate and fraction in roofline.classes.  Peaks: HBM and
+           bf16 from MEASURED_PEAKS.json, FP64 and FP32 (SIMT) from cuBLAS
+           DGEMM / SGEMM (TF32 off) timed here before the timed region
+  cpu_baseline: the FP64 CPU oracle (a port of the reference path, OpenMP over
+           the host's cores), median of 3 RK4 steps at N = 4096
+  adjoint: the hand-written adjoint on the fit workload against the recorded
+           FP64 forward and against the mixed forward of the same trajectory
+  helium_batch: 512 uneven helium films in one mixed engine (surface-steps/s,
+           error against the FP64 engine after 5 steps, per-surface status)
 
 --impl reference runs the reference-side CPU path (the oracle port: the
 reference's CUDA path does not compile from its sources as they lie and its
@@ -31,6 +46,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -41,7 +57,6 @@ import time
 import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
-FP64_NOMINAL_TFLOPS = 1.25  # GB300 dense FP64, nominal
 sys.path.insert(0, ROOT)
 
 METRIC = "RK4 steps/s at N=4096, mixed vs FP64 GPU at ≤1e-9 rel error; adjoint/fwd ratio"
@@ -56,6 +71,38 @@ def peaks():
         return float(d["hbm_gbs"]), float(d["bf16_tflops"]), float(d.get("bf16_tflops_sustained", d["bf16_tflops"])), "measured"
     except Exception:
         return 6800.0, 1900.0, 1700.0, "fallback"
+
+
+def simt_peaks(device: int) -> dict:
+    """FP64 and FP32 (SIMT) peaks of this GPU, measured as cuBLAS DGEMM and
+    SGEMM with TF32 off (best of 5 after 3 warm-ups, CUDA events): the
+    denominators of the FP64- and FP32-bound kernel classes."""
+    import torch
+    dev = torch.device("cuda", device)
+    out = {}
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    try:
+        for name, dtype, n in (("fp64_tflops", torch.float64, 4096), ("fp32_tflops", torch.float32, 8192)):
+            a = torch.randn(n, n, device=dev, dtype=dtype)
+            b = torch.randn(n, n, device=dev, dtype=dtype)
+            for _ in range(3):
+                torch.matmul(a, b)
+            best = float("inf")
+            for _ in range(5):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                torch.matmul(a, b)
+                e1.record()
+                torch.cuda.synchronize()
+                best = min(best, e0.elapsed_time(e1) * 1e-3)
+            out[name] = 2.0 * n ** 3 / best / 1e12
+            del a, b
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = prev
+    torch.cuda.empty_cache()
+    out["method"] = "cuBLAS DGEMM n=4096 / SGEMM n=8192 (TF32 off), best of 5, CUDA events"
+    return out
 
 
 class ClockSampler:
@@ -110,20 +157,71 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(rows)}
 
 
-def step_traffic(n, args):
-    """DRAM bytes per RK4 step (read + write, all kernels of one step) from the
-    committed ncu summary of this configuration, or None when there is none."""
-    key = (f"traffic_bytes_per_step n={n} precision={args.precision} pre_iters={args.pre_iters} "
-           f"refine_iters={args.refine_iters} refactor_every={args.refactor_every}:")
+def kernel_traffic(kernel: str, n: int):
+    """DRAM bytes (read + write) per launch of `kernel` at N = n from the
+    committed ncu summaries under profiles/ (a line
+    `dram_bytes_per_launch kernel=<name> n=<N>: <bytes>`), or None."""
+    key = f"dram_bytes_per_launch kernel={kernel} n={n}:"
+    d = os.path.join(ROOT, "profiles")
     try:
-        with open(os.path.join(ROOT, "profiles", "rk4_step_n4096_launches.md")) as f:
-            for line in f:
-                line = line.strip().strip("`")
-                if line.startswith(key):
-                    return float(line[len(key):].split()[0])
+        names = sorted(os.listdir(d))
     except OSError:
-        pass
+        return None
+    for name in names:
+        try:
+            with open(os.path.join(d, name)) as f:
+                for line in f:
+                    line = line.strip().strip("`")
+                    if line.startswith(key):
+                        return float(line[len(key):].split()[0])
+        except OSError:
+            continue
     return None
+
+
+# Algorithmic work of the kernel classes, per unit, as the roofline counts it.
+#   spectral_deriv     : per transform job (forward + inverse complex FFT of n
+#                        points, 5 n log2 n FLOP each): 10 n log2 n FP64 FLOP
+#   boundary_sums_fp32 : per (target, source) pair, water: 15 FP32 FLOP (two
+#                        double-float-split differences, |d|^2, reciprocal
+#                        estimate, weight, two FMA accumulations)
+#   boundary_sums_df   : per pair, water: 94 FP32 FLOP (double-float
+#                        differences, squared norm, reciprocal with one Newton
+#                        step, three products, two cascaded accumulations)
+#   boundary_sums_fp64 : per pair, water: 11 FP64 FLOP
+#   gemv               : per product: 2 n^2 bytes (the FP16 preconditioner)
+#   node_prep, velocity_bernoulli, rk4_combine: O(n), reported by time only
+FLOP_PER_PAIR = {"boundary_sums_fp32": 15.0, "boundary_sums_df": 94.0, "boundary_sums_fp64": 11.0}
+
+
+def class_roofline(prof: dict, prof_steps: int, n: int, sums_per_step: dict, jobs_per_step: int,
+                   gemv_per_step: int, pk: dict) -> dict:
+    """Per kernel class: ms per step, algorithmic work per step, achieved rate
+    and fraction of the bounding unit's measured peak."""
+    classes = {}
+    for name, (tms, cnt) in prof.items():
+        if not cnt:
+            continue
+        ms = tms / prof_steps
+        c = {"ms_per_step": round(ms, 5), "launches_per_step": round(cnt / prof_steps, 3)}
+        sec = ms * 1e-3
+        if name == "spectral_deriv":
+            work = jobs_per_step * 10.0 * n * math.log2(n)
+            c.update(bound="fp64", unit="TFLOP/s", work_per_step=work, achieved=work / sec / 1e12,
+                     peak=pk["fp64_tflops"])
+        elif name in FLOP_PER_PAIR:
+            passes = sums_per_step.get(name, 0)
+            work = passes * float(n) * (n - 1) * FLOP_PER_PAIR[name]
+            bound = "fp64" if name.endswith("fp64") else "fp32"
+            c.update(bound=bound, unit="TFLOP/s", work_per_step=work, achieved=work / sec / 1e12,
+                     peak=pk["fp64_tflops"] if bound == "fp64" else pk["fp32_tflops"])
+        elif name == "gemv":
+            work = gemv_per_step * 2.0 * n * n
+            c.update(bound="hbm", unit="GB/s", work_per_step=work, achieved=work / sec / 1e9, peak=pk["hbm_gbs"])
+        if "achieved" in c:
+            c["frac"] = c["achieved"] / c["peak"]
+        classes[name] = c
+    return classes
 
 
 def adjoint_ratio(device: int):
@@ -132,14 +230,16 @@ def adjoint_ratio(device: int):
     initial y from 64 seeded Fourier coefficients, checkpoints every 50 steps,
     loss = 0.5 |y_final - y_target|^2.  Forward = the recorded FP64 trajectory
     (sfd_rk4_record); adjoint = sfd_rk4_vjp (segment recomputation with every
-    stage recorded, then the reverse sweep).  Wall-clock, synchronous."""
+    stage recorded, then the reverse sweep).  The mixed forward of the same
+    trajectory (the production forward) is timed beside it.  Wall-clock,
+    synchronous."""
     import superfluid_dynamics_gb300 as sfd
     from superfluid_dynamics_gb300 import workloads
     n, steps, dt, every = 512, 500, 1e-3, 50
     s, c0, target = workloads.helium_fit(n)
     state0 = np.concatenate([s.x, s.y, s.phi])
-    eng = sfd.Engine(n, sfd.HeliumBoundaryProblem(depth=10.0, A3=1e3),
-                     sfd.Options(precision=sfd.PRECISION_FP64, use_graphs=False, device=device))
+    phys = sfd.HeliumBoundaryProblem(depth=10.0, A3=1e3)
+    eng = sfd.Engine(n, phys, sfd.Options(precision=sfd.PRECISION_FP64, use_graphs=False, device=device))
     eng.rk4_record(dt, 5, every, state0)          # warm-up (workspace, first launches)
     eng.rk4_vjp(np.zeros(3 * n))
     t0 = time.perf_counter()
@@ -151,22 +251,36 @@ def adjoint_ratio(device: int):
     g, gp = eng.rk4_vjp(cot)
     t_adj = time.perf_counter() - t0
     eng.close()
+    mixed = sfd.Engine(n, phys, sfd.Options(precision=sfd.PRECISION_MIXED, refactor_every=50, pre_iters=2,
+                                            device=device))
+    mixed.set_state(s.x, s.y, s.phi)
+    mixed.step(dt, 5)
+    mixed.set_state(s.x, s.y, s.phi)
+    t0 = time.perf_counter()
+    mixed.step(dt, steps)
+    t_mixed = time.perf_counter() - t0
+    mixed.close()
     return {"workload": "helium film N=512, h0=10, A3=1e3, 500 RK4 steps dt=1e-3, 64 Fourier coefficients, "
                         "checkpoints every 50", "forward_s": t_fwd, "adjoint_s": t_adj, "ratio": t_adj / t_fwd,
+            "mixed_forward_s": t_mixed, "ratio_vs_mixed_forward": t_adj / t_mixed,
             "loss": 0.5 * float(cot[n:2 * n] @ cot[n:2 * n]), "grad_A3": gp}
 
 
 def cpu_sample(steps: int = 1, n: int = N_NODES):
-    """Oracle port (FP64, OpenMP over all host cores): time `steps` RK4 steps."""
+    """Oracle port (FP64, OpenMP over all host cores): time `steps` RK4 steps
+    one by one; returns (steps/s from the median step, cores, per-step s)."""
     from oracle import oracle
     from superfluid_dynamics_gb300 import workloads
     cores = os.cpu_count() or 1
     oracle.set_threads(cores)
     s = workloads.random_modes(n, seed=2)
-    t0 = time.perf_counter()
-    oracle.rk4_steps(oracle.Problem(), s.x, s.y, s.phi, DT, steps)
-    dt = time.perf_counter() - t0
-    return steps / dt, cores
+    x, y, phi = s.x, s.y, s.phi
+    times = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        (x, y, phi), _ = oracle.rk4_steps(oracle.Problem(), x, y, phi, DT, 1)
+        times.append(time.perf_counter() - t0)
+    return 1.0 / statistics.median(times), cores, times
 
 
 def run_reference(args, rank, world):
@@ -176,16 +290,113 @@ def run_reference(args, rank, world):
     steps = max(1, min(args.steps, 2))
     if warm:
         cpu_sample(warm)
-    rate, cores = cpu_sample(steps)
+    rate, cores, _ = cpu_sample(steps)
     line = {"metric": METRIC, "value": rate, "unit": "steps/s", "n_gpus": world, "steps": steps, "warmup": warm,
             "ms_per_step": 1e3 / rate, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic (seeded 8-mode gravity wave)", "impl": "reference",
             "config": {"workload": f"gravity wave N={N_NODES}, 8 modes seed 2, RK4 dt={DT}", "N": N_NODES,
                        "precision": "fp64", "path": "CPU FP64 oracle port of the reference RHS + RK4"},
             "cpu_baseline": {"value": rate, "unit": "steps/s", "cores": cores, "kind": "port",
-                             "sample": f"{steps} RK4 step(s) at N={N_NODES} (of the requested {args.steps})"},
+                             "sample": f"median of {steps} RK4 step(s) at N={N_NODES} (of the requested {args.steps})"},
             "e2e": {"value": rate, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def _timed_steps(eng, dt, steps, stream):
+    import torch
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        eng.step(dt, steps, sync=False)
+        e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) * 1e-3
+
+
+def fp64_and_accuracy(args, opts_mixed, device, stream, checkpoints=(25, 50, 100)):
+    """The plain FP64 GPU step on the headline surface (event-timed over the
+    accuracy run) and the mixed-vs-FP64 error at the checkpoints beside the
+    FP64 round-off envelope."""
+    import superfluid_dynamics_gb300 as sfd
+    from superfluid_dynamics_gb300 import workloads
+    n = args.n
+    s = workloads.random_modes(n, seed=2)
+    fp64 = sfd.Options(precision=sfd.PRECISION_FP64, device=device)
+    runs = {}
+    for name, opt, eps in (("mixed", opts_mixed, 0.0), ("fp64", fp64, 0.0), ("fp64_perturbed", fp64, 1e-15)):
+        eng = sfd.Engine(n, sfd.WaterBoundaryProblem(), opt)
+        eng.set_stream(stream.cuda_stream)
+        x = s.x * (1 + eps * np.random.default_rng(7).standard_normal(n)) if eps else s.x
+        eng.set_state(x, s.y, s.phi)
+        traj, t, done = [], 0.0, 0
+        for c in checkpoints:
+            t += _timed_steps(eng, DT, c - done, stream)
+            done = c
+            traj.append(np.concatenate(eng.get_state()))
+        st = eng.status()
+        runs[name] = (traj, done / t, st, eng.refinement() if name == "mixed" else None)
+        eng.close()
+    fp64_rate = runs["fp64"][1]
+    return {
+        "fp64": {"steps_per_s": fp64_rate, "steps": checkpoints[-1], "ms_per_step": 1e3 / fp64_rate,
+                 "path": "engine FP64 mode: FP64 M assembled, blocked FP64 LU (64-wide), FP64 sums, FP64 FFT",
+                 "status_or": int(np.bitwise_or.reduce(runs["fp64"][2][0]))},
+        "accuracy": {"steps": list(checkpoints),
+                     "mixed_vs_fp64_z_phi": [_state_err(a, b, n) for a, b in zip(runs["mixed"][0], runs["fp64"][0])],
+                     "fp64_perturbed_vs_fp64_z_phi": [_state_err(a, b, n) for a, b in
+                                                      zip(runs["fp64_perturbed"][0], runs["fp64"][0])],
+                     "perturbation": "x * (1 + 1e-15 N(0,1)), seed 7",
+                     "mixed_status_or": int(np.bitwise_or.reduce(runs["mixed"][2][0])),
+                     "mixed_max_rel_residual": float(runs["mixed"][3]["rel_residual"].max()),
+                     "mixed_extra_corrections": int(runs["mixed"][3]["extra_iters"].sum()),
+                     "mixed_stall_rebuilds": runs["mixed"][3]["stall_rebuilds"]},
+    }
+
+
+def helium_batch_summary(args, device, stream, timed_steps=50):
+    """512 uneven helium films (N = 32 U{4..64}, seed 3) in one mixed engine:
+    surface-steps/s over `timed_steps` steps after 5 checked ones, error of
+    those 5 steps against the FP64 engine, per-surface status counts."""
+    import superfluid_dynamics_gb300 as sfd
+    from superfluid_dynamics_gb300 import workloads
+    surfs = workloads.helium_batch(512, seed=3)
+    ns = [sf.n for sf in surfs]
+    phys = [sfd.HeliumBoundaryProblem(depth=sf.depth, A3=sf.A3) for sf in surfs]
+    x = np.concatenate([sf.x for sf in surfs])
+    y = np.concatenate([sf.y for sf in surfs])
+    ph = np.concatenate([sf.phi for sf in surfs])
+    dt = 1e-3
+    opt = sfd.Options(precision=sfd.PRECISION_MIXED, refine_iters=args.refine_iters, pre_iters=args.pre_iters,
+                      refactor_every=args.refactor_every, device=device)
+    eng = sfd.Engine(ns, phys, opt)
+    eng.set_stream(stream.cuda_stream)
+    eng.set_state(x, y, ph)
+    _timed_steps(eng, dt, 5, stream)
+    m5 = np.concatenate(eng.get_state())
+    t = _timed_steps(eng, dt, timed_steps, stream)
+    st = eng.status()[0]
+    eng.close()
+    ref = sfd.Engine(ns, phys, sfd.Options(precision=sfd.PRECISION_FP64, device=device))
+    ref.set_state(x, y, ph)
+    ref.step(dt, 5)
+    f5 = np.concatenate(ref.get_state())
+    ref.close()
+    nt = sum(ns)
+    off = np.concatenate([[0], np.cumsum(ns)])
+    errs = []
+    for i in range(len(ns)):
+        sl = [slice(k * nt + off[i], k * nt + off[i + 1]) for k in range(3)]
+        errs.append(_state_err(np.concatenate([m5[q] for q in sl]), np.concatenate([f5[q] for q in sl]), ns[i]))
+    errs = np.array(errs)
+    return {"workload": "512 helium films, N = 32 U{4..64} (seed 3), h0 ~ U(5,20), A3 ~ U(0.5,2)e3, dt=1e-3",
+            "surface_steps_per_s": len(ns) * timed_steps / t, "steps_per_s": timed_steps / t,
+            "timed_steps": timed_steps, "total_nodes": int(nt),
+            "max_err_vs_fp64_after_5_steps_z_phi": [float(errs[:, 0].max()), float(errs[:, 1].max())],
+            "surfaces_nonfinite": int(((st & sfd._lib.STATUS_NONFINITE) != 0).sum()),
+            "surfaces_refine_stall": int(((st & sfd._lib.STATUS_REFINE_STALL) != 0).sum()),
+            "surfaces_zero_pivot": int(((st & sfd._lib.STATUS_ZERO_PIVOT) != 0).sum())}
 
 
 def run_ours(args, rank, world, local_rank):
@@ -195,6 +406,9 @@ def run_ours(args, rank, world, local_rank):
 
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
+    pk = {}
+    if rank == 0 and not args.no_roofline:
+        pk = simt_peaks(local_rank)
     s = workloads.random_modes(args.n, seed=2)
     prec = sfd.PRECISION_MIXED if args.precision == "mixed" else sfd.PRECISION_FP64
     opts = sfd.Options(precision=prec, refine_iters=args.refine_iters, refactor_every=args.refactor_every,
@@ -232,6 +446,7 @@ def run_ours(args, rank, world, local_rank):
         torch.cuda.synchronize()
     flush_ms = f0.elapsed_time(f1)
     launches0 = eng.kernel_launches
+    eng.clear_status()
     with ClockSampler(local_rank) as clk:
         with torch.cuda.stream(stream):
             e0 = torch.cuda.Event(enable_timing=True)
@@ -244,6 +459,8 @@ def run_ours(args, rank, world, local_rank):
             e1.record(stream)
             torch.cuda.synchronize()
     gpu_launches = eng.kernel_launches - launches0
+    timed_refinement = eng.refinement()
+    timed_status = int(np.bitwise_or.reduce(eng.status()[0]))
     tuning = eng.tuning()
     ms = e0.elapsed_time(e1) - flush_ms
     if world > 1:
@@ -292,55 +509,72 @@ def run_ours(args, rank, world, local_rank):
         return
     hbm, bf16, bf16s, peak_kind = peaks()
     n = args.n
-    per_launch = {name: (tms / cnt, cnt) for name, (tms, cnt) in prof.items() if cnt}
-    # Roofline of the step: the dense second-kind solve is a contraction, so the
-    # tensor pipe bounds it.  Algorithmic FLOP per RK4 step (one surface):
-    #   F(N) = 4 [ (2/3) N^3 (LU) + 2 N^2 (triangular solves) + 2 N^2 (FP64
-    #          residual matvec) + 8 N^2 (complex velocity matvec) ]
-    # against the bf16 dense peak / 3 (the FP32-equivalent rate of a 3-product
-    # bf16 split).  The mixed path replaces most of the LU by a reused FP32
-    # preconditioner plus refinement, so this is an equivalent rate.
-    flop_step = 4.0 * (2.0 / 3.0 * n ** 3 + 2.0 * n * n + 2.0 * n * n + 8.0 * n * n)
-    step_ms = ms / args.steps
-    roof = {"bound": "tensor", "kernel": "rk4_step (one CUDA graph launch per step)",
-            "achieved": flop_step / (step_ms * 1e-3) / 1e12, "peak": bf16 / 3.0, "unit": "TFLOP/s",
-            "algorithmic_flop_per_step": flop_step, "peak_source": f"{peak_kind} bf16 burst / 3"}
-    roof["frac"] = roof["achieved"] / roof["peak"]
-    # the same algorithmic rate against GB300's FP64 peak (nominal; the
-    # measured-peaks file holds no FP64 figure): the plain FP64 method would
-    # have to run at this fraction of the FP64 units to match the step
-    roof["fp64_variant"] = {"achieved": roof["achieved"], "peak": FP64_NOMINAL_TFLOPS, "unit": "TFLOP/s",
-                            "peak_source": "nominal GB300 FP64 (not measured)",
-                            "frac": roof["achieved"] / FP64_NOMINAL_TFLOPS}
-    roof["traffic"] = step_traffic(n, args)
-    roof["classes_ms_per_step"] = {k: round(v[0] * v[1] / prof_steps, 4) for k, v in per_launch.items()}
-    dom = max(per_launch, key=lambda k: per_launch[k][0] * per_launch[k][1])
-    roof["dominant_class"] = {"name": dom, "avg_launch_ms": round(per_launch[dom][0], 5),
-                              "launches_per_step": per_launch[dom][1] / prof_steps}
-
-    adj = None if args.no_adjoint else adjoint_ratio(local_rank)
-    cpu = None
-    if not args.no_cpu and world >= 1:
-        rate, cores = cpu_sample(1, n)
-        cpu = {"value": rate, "unit": "steps/s", "cores": cores, "kind": "port",
-               "sample": f"1 RK4 step at N={n} (FP64 oracle, OpenMP)"}
+    mixed = args.precision == "mixed"
     line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": warm, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64+df32 (mixed)" if args.precision == "mixed" else "f64",
+            "vs_baseline": None, "dtype": "f64+df32 (mixed)" if mixed else "f64",
             "data": "synthetic (seeded 8-mode gravity wave)",
             "config": {"workload": f"gravity wave N={n}, 8 modes seed 2, RK4 dt={DT}", "N": n,
                        "precision": args.precision, "refine_iters": args.refine_iters, "pre_iters": args.pre_iters,
                        "refactor_every": args.refactor_every, "refactor_lag": args.refactor_lag,
+                       "extra_iters": opts.extra_iters, "refine_tol": opts.refine_tol,
                        "precond_storage": "fp32" if args.precond_fp32 else "fp16",
                        "sum_groups_per_cta": tuning,
                        "l2": "flushed (256 MB write) before every timed step",
                        "timing": "CUDA events around the K steps and their L2 flushes (background rebuild joined), "
                                  "minus K flushes timed alone",
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
-            "roofline": roof, "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": 3 * n * 8,
                     "d2h_bytes_per_step": 3 * n * 8},
-            "gpu_launches": gpu_launches, "clocks": clk.summary(), "adjoint": adj}
+            "gpu_launches": gpu_launches, "clocks": clk.summary(),
+            "timed_region": {"status_or": timed_status,
+                             "max_rel_residual": float(timed_refinement["rel_residual"].max()),
+                             "extra_corrections": int(timed_refinement["extra_iters"].sum()),
+                             "stall_rebuilds": timed_refinement["stall_rebuilds"]}}
+
+    # ---- the metric's denominator and error bound
+    if not args.no_accuracy:
+        acc = fp64_and_accuracy(args, opts, local_rank, stream)
+        line["fp64"] = acc["fp64"]
+        line["fp64_steps_per_s"] = acc["fp64"]["steps_per_s"]
+        line["mixed_over_fp64"] = value / acc["fp64"]["steps_per_s"]
+        line["accuracy"] = acc["accuracy"]
+
+    # ---- roofline of the dominant kernel class, with every class listed
+    if pk:
+        pk.update({"hbm_gbs": hbm, "bf16_tflops": bf16, "source_hbm_bf16": peak_kind})
+        passes = {"boundary_sums_fp32": 4 * (args.pre_iters + args.refine_iters) if mixed else 0,
+                  "boundary_sums_df": 4 if mixed else 0, "boundary_sums_fp64": 0 if mixed else 4}
+        gemv = 4 * (1 + args.pre_iters + args.refine_iters) if mixed else 0
+        classes = class_roofline(prof, prof_steps, n, passes, 16, gemv, pk)
+        dom = max(classes, key=lambda k: classes[k]["ms_per_step"])
+        d = classes[dom]
+        kname = {"spectral_deriv": "k_spectral_cluster", "boundary_sums_fp32": "k_boundary_sums<FP32>",
+                 "boundary_sums_df": "k_boundary_sums<DF>", "gemv": "k_gemv_h"}.get(dom, dom)
+        per_launch_work = d.get("work_per_step", 0.0) / max(d["launches_per_step"], 1e-9)
+        traffic = kernel_traffic(kname, n)
+        line["roofline"] = {
+            "bound": d.get("bound"), "kernel": kname, "class": dom, "achieved": d.get("achieved"),
+            "peak": d.get("peak"), "unit": d.get("unit"), "frac": d.get("frac"),
+            "traffic": traffic, "algorithmic_work_per_launch": per_launch_work,
+            "avg_launch_ms": d["ms_per_step"] / max(d["launches_per_step"], 1e-9),
+            "peak_source": ("measured cuBLAS DGEMM" if d.get("bound") == "fp64" else
+                            "measured cuBLAS SGEMM (TF32 off)" if d.get("bound") == "fp32" else
+                            f"{peak_kind} HBM copy"),
+            "peaks": pk, "classes": classes,
+            "note": "achieved = algorithmic work of the class per step / its event-timed device time per step "
+                    "(eager pass over one preconditioner period, graphs off); the step is neither HBM- nor "
+                    "tensor-bound: the boundary sums run on the FP32 pipes, the transforms on the FP64 pipe"}
+
+    if not args.no_adjoint:
+        line["adjoint"] = adjoint_ratio(local_rank)
+    if not args.no_batch:
+        line["helium_batch"] = helium_batch_summary(args, local_rank, stream)
+    if not args.no_cpu:
+        rate, cores, times = cpu_sample(3, n)
+        line["cpu_baseline"] = {"value": rate, "unit": "steps/s", "cores": cores, "kind": "port",
+                                "sample": f"median of 3 RK4 steps at N={n} (FP64 oracle, OpenMP)",
+                                "step_s": times}
     print(json.dumps(line), flush=True)
 
 
@@ -352,19 +586,6 @@ def _state_err(sa, sb, n):
     """max |z_a - z_b| / max |z_b| and the same for phi, from [x|y|phi] arrays."""
     za, zb = sa[:n] + 1j * sa[n:2 * n], sb[:n] + 1j * sb[n:2 * n]
     return [_rel(za, zb), _rel(sa[2 * n:], sb[2 * n:])]
-
-
-def _timed_steps(eng, dt, steps, stream):
-    import torch
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    with torch.cuda.stream(stream):
-        e0.record(stream)
-        eng.step(dt, steps, sync=False)
-        e1.record(stream)
-    torch.cuda.synchronize()
-    return e0.elapsed_time(e1) * 1e-3
 
 
 def _empty_graph_ms(kernels: int, replays: int = 50) -> float:
@@ -537,6 +758,32 @@ def run_workload(args, rank, world, local_rank):
     print(json.dumps(line), flush=True)
 
 
+def run_profile_window(args, local_rank):
+    """The headline engine stepped past its first preconditioner rebuild and
+    background switch (60 steps), then --steps steady-state steps between
+    cudaProfilerStart and cudaProfilerStop, for captures with
+    `ncu --profile-from-start off`.  Prints one informational JSON line."""
+    import torch
+    import superfluid_dynamics_gb300 as sfd
+    from superfluid_dynamics_gb300 import workloads
+    torch.cuda.set_device(local_rank)
+    s = workloads.random_modes(args.n, seed=2)
+    opts = sfd.Options(precision=sfd.PRECISION_MIXED, refine_iters=args.refine_iters,
+                       refactor_every=args.refactor_every, pre_iters=args.pre_iters, device=local_rank,
+                       refactor_lag=args.refactor_lag)
+    with sfd.Engine(args.n, sfd.WaterBoundaryProblem(), opts) as eng:
+        eng.set_state(s.x, s.y, s.phi)
+        eng.step(DT, 60)
+        torch.cuda.synchronize()
+        l0 = eng.kernel_launches
+        torch.cuda.cudart().cudaProfilerStart()
+        eng.step(DT, args.steps)
+        torch.cuda.synchronize()
+        torch.cuda.cudart().cudaProfilerStop()
+        print(json.dumps({"workload": "profile window", "N": args.n, "steps": args.steps,
+                          "kernel_launches": eng.kernel_launches - l0}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -552,8 +799,12 @@ def main():
                     help="rebuild the preconditioner on a side stream and switch to it this many steps later")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the FP64 step and the accuracy study")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 512-film helium batch summary")
+    ap.add_argument("--no-roofline", action="store_true", help="skip the peak probes and the class roofline")
     ap.add_argument("--precond-fp32", action="store_true", help="apply the preconditioner from FP32 (default FP16 copy)")
-    ap.add_argument("--workload", default="headline", choices=["headline", "modes1024", "helium-batch", "steep8192"],
+    ap.add_argument("--workload", default="headline",
+                    choices=["headline", "modes1024", "helium-batch", "steep8192", "profile"],
                     help="headline = the metric's configuration; the others print their own line")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -561,6 +812,10 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.workload == "profile":
+        if rank == 0:
+            run_profile_window(args, local_rank)
         return
     if args.workload != "headline":
         if world > 1 and args.workload == "helium-batch":

@@ -40,14 +40,18 @@ extern "C" {
 #define SFD_WATER 0              /* WaterBoundaryProblem  (createMKernel path)          */
 #define SFD_HELIUM 1             /* HeliumBoundaryProblem (createFiniteDepthMKernel)    */
 
-#define SFD_PRECISION_FP64 0     /* every stage in FP64 (LU without exchanges)          */
+#define SFD_PRECISION_FP64 0     /* every stage in FP64 (LU without exchanges, FP64
+                                    refinement where its residual is above refine_tol)  */
 #define SFD_PRECISION_MIXED 1    /* FP32 preconditioner + double-float/FP64 refinement  */
 
 /* per-surface status bits (sfd_get_status) */
 #define SFD_STATUS_NONFINITE 0x1u
-#define SFD_STATUS_PIVOT_SWAP 0x2u      /* |l_ij| > 1: partial pivoting would have exchanged rows */
+#define SFD_STATUS_PIVOT_SWAP 0x2u      /* engine: an FP64 factorisation had |l_ij| > 1, so partial
+                                           pivoting would have exchanged rows (the residual check
+                                           and FP64 refinement then carry the accuracy); dense
+                                           solver: rows were exchanged */
 #define SFD_STATUS_ZERO_PIVOT 0x4u
-#define SFD_STATUS_REFINE_STALL 0x8u
+#define SFD_STATUS_REFINE_STALL 0x8u    /* the solve's final residual stayed above refine_tol */
 #define SFD_STATUS_TIMEOUT 0x20u        /* a bounded in-kernel wait ran out; that work was skipped */
 
 /* Nondimensional physics of one surface; mirrors the fields of
@@ -82,6 +86,15 @@ typedef struct sfd_options {
                              side stream from the state at that step and switches to it k
                              steps later (k < refactor_every), so the rebuild overlaps the
                              stepping.  Deterministic: the switch step is fixed.          */
+    int extra_iters;      /* 0..4 (default 2): extra corrections of the solve, each run only
+                             for surfaces whose residual after the regular passes (or the
+                             previous extra one) is above refine_tol * max |phi'|; FP64 mode
+                             corrects with the LU factors and FP64 sums, mixed mode with the
+                             preconditioner and FP32 sums.  A final residual still above the
+                             tolerance raises SFD_STATUS_REFINE_STALL; in mixed mode the next
+                             step enqueued after the host sees it rebuilds the preconditioner */
+    double refine_tol;    /* relative residual tolerance max |phi' - M a| / max |phi'| of
+                             the solve (default 1e-10); <= 0 turns the check off          */
 } sfd_options;
 
 /* Optomechanical drive of a helium film, nondimensional (the reference's
@@ -173,10 +186,17 @@ int sfd_join_background(sfd_engine* e);
  * and mass = sum y x'.  `kappa` scales the surface energy as in the reference. */
 int sfd_invariants(sfd_engine* e, double kappa, double* out);
 
-/* Per-surface status words (SFD_STATUS_* bits), max |l_ij| of the last
- * factorisation and max |residual| of the last refinement (each nullable). */
+/* Per-surface status words (SFD_STATUS_* bits), max |l_ij| over the FP64
+ * factorisations and max over RHS evaluations of the final solve residual
+ * max |phi' - M a| (each nullable), all since the last sfd_clear_status. */
 int sfd_get_status(sfd_engine* e, unsigned int* status, double* lmax, double* rnorm);
 int sfd_clear_status(sfd_engine* e);
+/* Refinement record since the last sfd_clear_status (each nullable):
+ * rel_residual[s] = max over RHS evaluations of the final relative residual
+ * max |phi' - M a| / max |phi'|, extra_iters[s] = extra corrections run for
+ * surface s, *stall_rebuilds = preconditioner rebuilds that a refinement
+ * stall triggered (since creation). */
+int sfd_get_refinement(sfd_engine* e, double* rel_residual, long long* extra_iters, long long* stall_rebuilds);
 
 /* Number of kernel launches the engine issued since creation (graph replays
  * count every kernel node). */
@@ -202,11 +222,15 @@ const char* sfd_version(void);
  * 3n doubles (same results as sfd_rhs_device on an FP64 engine).  Scratch is
  * one static device array of about 8.7 MB, held by every GPU that loads the
  * library until exit; n is limited to 1..1024 (larger n returns
- * SFD_ERR_INVALID).  The call is asynchronous on `stream` (NULL = legacy
- * default stream).  Its first call on a device resolves the array's device
- * address, so make that first call before any stream capture.  All calls share
- * the array, so calls that overlap on the GPU (different streams or threads)
- * race; serialise them. */
+ * SFD_ERR_INVALID).  The call issues its kernels on `stream` (NULL = legacy
+ * default stream) and returns without waiting for them; it makes no host to
+ * device copy (its descriptors are written by a kernel).  Its first call on a
+ * device resolves the array's device address (cudaGetSymbolAddress) and sets
+ * the kernels' shared-memory limits, so make that first call before any stream
+ * capture.  All calls share the array, so calls that overlap on the GPU
+ * (different streams or threads) race; serialise them.  No status words are
+ * reported: a non-finite input or a breakdown shows as non-finite entries of
+ * rhs_out. */
 int sfd_rhs_device_noalloc(const sfd_problem* problem, int n, const void* state_in, void* rhs_out, void* stream);
 
 /* ------------------------------------------------------------ adaptive RKF45
@@ -318,9 +342,10 @@ int sfd_rk4_stage_device(long long n, const void* y0, const void* k, void* kacc,
                          double cy, int first, void* stream);
 int sfd_rk4_final_device(long long n, void* y0, const void* kacc, double c, void* stream);
 /* MatrixSolver::solve (MatrixSolver.cuh:113-172): `batch` column-major n x n
- * systems M a = b on the device, FP64 blocked LU without row exchanges; the
- * optional host status words get SFD_STATUS_PIVOT_SWAP where partial pivoting
- * would have exchanged rows and SFD_STATUS_ZERO_PIVOT on a zero pivot. */
+ * systems M a = b on the device, FP64 blocked LU with partial pivoting (the
+ * pivot choice of cusolverDnDgetrf, MatrixSolver.cuh:123-125); the optional
+ * host status words get SFD_STATUS_PIVOT_SWAP where rows were exchanged and
+ * SFD_STATUS_ZERO_PIVOT on a zero pivot (the call then waits for the device). */
 typedef struct sfd_dense_solver sfd_dense_solver;
 int sfd_dense_solver_create(int n, int batch, sfd_dense_solver** out);
 int sfd_dense_solver_set_stream(sfd_dense_solver* d, void* stream);

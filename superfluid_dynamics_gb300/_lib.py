@@ -34,7 +34,8 @@ class SfdProblem(ctypes.Structure):
 class SfdOptions(ctypes.Structure):
     _fields_ = [("precision", c_int), ("refine_iters", c_int), ("refactor_every", c_int),
                 ("use_graphs", c_int), ("device", c_int), ("tensor_cores", c_int), ("pre_iters", c_int),
-                ("precond_half", c_int), ("autotune", c_int), ("refactor_lag", c_int)]
+                ("precond_half", c_int), ("autotune", c_int), ("refactor_lag", c_int), ("extra_iters", c_int),
+                ("refine_tol", c_double)]
 
 
 class SimProperties(ctypes.Structure):
@@ -113,6 +114,11 @@ _SIGS = {
     "sfd_invariants": (c_int, [c_void_p, c_double, _dp]),
     "sfd_get_status": (c_int, [c_void_p, POINTER(c_uint), _dp, _dp]),
     "sfd_clear_status": (c_int, [c_void_p]),
+    "sfd_get_refinement": (c_int, [c_void_p, _dp, POINTER(c_longlong), POINTER(c_longlong)]),
+    "sfd_dense_solver_create": (c_int, [c_int, c_int, POINTER(c_void_p)]),
+    "sfd_dense_solver_set_stream": (c_int, [c_void_p, c_void_p]),
+    "sfd_dense_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, POINTER(c_uint)]),
+    "sfd_dense_solver_destroy": (c_int, [c_void_p]),
     "sfd_kernel_launches": (c_longlong, [c_void_p]),
     "sfd_profile": (c_int, [c_void_p, c_int]),
     "sfd_profile_read": (c_int, [c_void_p, _dp, POINTER(c_longlong), c_int]),

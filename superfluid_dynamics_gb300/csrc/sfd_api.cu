@@ -19,6 +19,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/sfd.h"
@@ -177,34 +178,61 @@ void drain_profile(sfd_engine* e) {
 
 inline int blocks_for(long long n, int t) { return (int)((n + t - 1) / t); }
 
+// Extra corrections of the solve this engine runs (0 when the residual check
+// is off).
+int extra_iters(const sfd_engine* e) {
+  if (!e->rslot || !(e->opt.refine_tol > 0.0)) return 0;
+  return std::max(0, std::min(SFD_MAX_EXTRA, e->opt.extra_iters));
+}
+
+// Gate on the residual slot `slot` of the current evaluation (-1: ungated).
+Gate make_gate(const sfd_engine* e, int slot) {
+  if (slot < 0 || !e->rslot) return Gate{nullptr, nullptr, 0, 0.0};
+  return Gate{e->rslot + slot, e->bnorm, SFD_RSLOTS, e->opt.refine_tol};
+}
+
 // One boundary-sum pass over every surface with weights `weights`
 // (`weights_df` its double-float copy for the DF / FP32 passes); the fused
 // epilogue writes C, D and the residual (mode 0: r = phi' - M a, C/D
-// overwritten; mode 1: r -= M a, C/D accumulated).
-int enqueue_sums(sfd_engine* e, int prec, const double* weights, const float2* weights_df, int mode, bool track_norm) {
+// overwritten; mode 1: r -= M a, C/D accumulated).  track >= 0: the pass
+// records max |r| in that residual slot; gate >= 0: it runs only for the
+// surfaces whose residual in that slot is above the tolerance.
+int enqueue_sums(sfd_engine* e, int prec, const double* weights, const float2* weights_df, int mode, bool track,
+                 int gate = -1) = delete;  // the slot is an index: a bool would silently mean slot 0 or 1
+int enqueue_sums(sfd_engine* e, int prec, const double* weights, const float2* weights_df, int mode, int track,
+                 int gate = -1) {
   SumArgs A{e->d_surf, e->d_sum_items, e->nsurf, e->ntot, e->nd.w, e->nd.p, weights, e->nd.wdf,
             e->nd.pdf, weights_df, e->nd.mdiag, e->zp, e->phip,
-            e->cacc, e->dacc, e->r, track_norm ? e->rnorm : nullptr, mode, e->rf};
+            e->cacc, e->dacc, e->r, (track >= 0 && e->rslot) ? e->rslot + track : nullptr, mode, e->rf,
+            (mode == 0 && e->rslot) ? e->bnorm : nullptr, make_gate(e, gate),
+            e->d_f32_work, e->f32_part, e->f32_wsum, e->f32_count};
+  if (prec == SFD_PREC_F32 && e->d_f32_work) {
+    LAUNCHC(e, SFD_K_SUMS32, sfd_launch_sums_f32(A, e->nf32, e->max_n, e->stream));
+    return 0;
+  }
   int cls = prec == SFD_PREC_F64 ? SFD_K_SUMS64 : prec == SFD_PREC_DF ? SFD_K_SUMSDF : SFD_K_SUMS32;
   LAUNCHC(e, cls, sfd_launch_sums(prec, A, e->nsum, e->max_n, e->sum_groups[prec], e->stream));
   return 0;
 }
 
 // y = X v with the current preconditioner (FP16 copy or FP32); ydf: optional
-// double-float copy of y.
-int enqueue_gemv(sfd_engine* e, const float* vf, double* y, float2* ydf, double* acc, float2* accdf) {
+// double-float copy of y; gate >= 0: only where that residual slot is above
+// the tolerance.
+int enqueue_gemv(sfd_engine* e, const float* vf, double* y, float2* ydf, double* acc, float2* accdf,
+                 int gate = -1) {
+  const Gate G = make_gate(e, gate);
   if (e->m16 && e->nsurf == 1 && e->nsm > 0) {
     // one surface: a whole number of waves of two CTAs per SM, rows interleaved
     const int wave = 2 * e->nsm, need = (e->max_n + kGemvRows - 1) / kGemvRows;
     const int grid = (need + wave - 1) / wave * wave;
     LAUNCHC(e, SFD_K_GEMV, k_gemv_h<<<grid, 512, e->max_np * sizeof(float), e->stream>>>(
-                               e->d_surf, nullptr, e->m16, e->rscale, vf, y, ydf, acc, accdf));
+                               e->d_surf, nullptr, e->m16, e->rscale, vf, y, ydf, acc, accdf, G));
   } else if (e->m16)
     LAUNCHC(e, SFD_K_GEMV, k_gemv_h<<<e->ngemv, 512, e->max_np * sizeof(float), e->stream>>>(
-                               e->d_surf, e->d_gemv_rows, e->m16, e->rscale, vf, y, ydf, acc, accdf));
+                               e->d_surf, e->d_gemv_rows, e->m16, e->rscale, vf, y, ydf, acc, accdf, G));
   else
     LAUNCHC(e, SFD_K_GEMV, k_gemv<<<e->ngemv, 256, e->max_np * sizeof(float), e->stream>>>(
-                               e->d_surf, e->d_gemv_rows, e->m32, vf, y, ydf, acc, accdf));
+                               e->d_surf, e->d_gemv_rows, e->m32, vf, y, ydf, acc, accdf, G));
   return 0;
 }
 
@@ -244,6 +272,38 @@ int enqueue_precond(sfd_engine* e) {
   return 0;
 }
 
+// The spectral transforms of one evaluation step on stream `st`: the first
+// jobs (z', z'', phi') or the a' jobs, as single-CTA transforms, cluster
+// transforms and four-step transforms (power-of-two surfaces; `scr` is
+// their scratch).  *nlaunch counts the kernels launched.
+cudaError_t launch_transforms(const sfd_engine* e, const DerivArgs& D, bool first, cudaStream_t st, cd* scr,
+                              int* nlaunch) {
+  const int nj = first ? e->njobs_first : e->njobs_ap, ncj = first ? e->ncjobs_first : e->ncjobs_ap;
+  cudaError_t err = cudaSuccess;
+  if (nj) {
+    err = sfd_launch_spectral(D, first ? e->d_jobs_first : e->d_jobs_ap, nj, e->max_n_single, st);
+    ++*nlaunch;
+  }
+  if (err == cudaSuccess && ncj) {
+    err = sfd_launch_spectral_cluster(D, first ? e->d_cjobs_first : e->d_cjobs_ap, ncj, e->max_n_cluster, st);
+    ++*nlaunch;
+  }
+  const F4Plan& p = first ? e->f4_first : e->f4_ap;
+  for (int ph = 1; ph <= 3 && err == cudaSuccess && p.njobs; ++ph) {
+    err = sfd_launch_f4(D, p, scr, st, ph);
+    ++*nlaunch;
+  }
+  return err;
+}
+
+// The same on the engine stream as one profiled launch group.
+int enqueue_transforms(sfd_engine* e, const DerivArgs& D, bool first) {
+  int nl = 0;
+  LAUNCHC(e, SFD_K_SPECTRAL, launch_transforms(e, D, first, e->stream, e->f4_scr, &nl));
+  e->launches += nl - 1;  // LAUNCHC counted one
+  return 0;
+}
+
 // a' = d a / d xi (FftDerivative on a, BaseBoundaryIntegrator.cuh:201-203):
 // on the engine stream, or forked onto the auxiliary stream so that it runs
 // beside the last boundary-sum pass (that pass reads the weights delta and
@@ -254,19 +314,14 @@ int enqueue_ap(sfd_engine* e, bool fork) {
   if (fork && e->aux && !e->profile) {
     CK(cudaEventRecord(e->ev_fork, e->stream));
     CK(cudaStreamWaitEvent(e->aux, e->ev_fork, 0));
-    if (e->njobs_ap) CK(sfd_launch_spectral(D, e->d_jobs_ap, e->njobs_ap, e->max_n_single, e->aux));
-    if (e->ncjobs_ap) CK(sfd_launch_spectral_cluster(D, e->d_cjobs_ap, e->ncjobs_ap, e->max_n_cluster, e->aux));
+    int nl = 0;
+    CK(launch_transforms(e, D, false, e->aux, e->f4_scr, &nl));
     CK(cudaEventRecord(e->ev_join, e->aux));
-    e->launches += (e->njobs_ap ? 1 : 0) + (e->ncjobs_ap ? 1 : 0);
+    e->launches += nl;
     e->ap_forked = true;
     return 0;
   }
-  if (e->njobs_ap)
-    LAUNCHC(e, SFD_K_SPECTRAL, sfd_launch_spectral(D, e->d_jobs_ap, e->njobs_ap, e->max_n_single, e->stream));
-  if (e->ncjobs_ap)
-    LAUNCHC(e, SFD_K_SPECTRAL,
-            sfd_launch_spectral_cluster(D, e->d_cjobs_ap, e->ncjobs_ap, e->max_n_cluster, e->stream));
-  return 0;
+  return enqueue_transforms(e, D, false);
 }
 
 // First half of an RHS evaluation (calculateVorticities,
@@ -276,13 +331,13 @@ int enqueue_solve(sfd_engine* e, const double* st, const double* phi_im, bool re
   const int nt = e->ntot;
   const double *x = st, *y = st + nt, *phi = st + 2 * nt;
   DerivArgs D{e->d_surf, e->nsurf, x, y, phi, phi_im, e->a, e->zp, e->zpp, e->phip, e->ap, e->phipf};
-  if (e->njobs_first)
-    LAUNCHC(e, SFD_K_SPECTRAL, sfd_launch_spectral(D, e->d_jobs_first, e->njobs_first, e->max_n_single, e->stream));
-  if (e->ncjobs_first)
-    LAUNCHC(e, SFD_K_SPECTRAL,
-            sfd_launch_spectral_cluster(D, e->d_cjobs_first, e->ncjobs_first, e->max_n_cluster, e->stream));
+  {
+    int rc = enqueue_transforms(e, D, true);
+    if (rc) return rc;
+  }
   LAUNCHC(e, SFD_K_NODE, k_node_prep<<<blocks_for(nt, 32), 64, 0, e->stream>>>(e->d_surf, e->d_node_surf, nt, x, y, e->zp,
-                                                                     e->zpp, e->nd));
+                                                                     e->zpp, e->nd, e->rslot, e->bnorm));
+  const int extra = extra_iters(e);
   if (e->opt.precision == SFD_PRECISION_FP64) {
     LAUNCHC(e, SFD_K_ASSEMBLE, sfd_launch_assemble64(e->d_surf, e->d_asm_tiles, e->nasm, e->nd.w, e->nd.p, e->zp, e->nd.mdiag,
                                     e->m64, e->stream));
@@ -295,14 +350,23 @@ int enqueue_solve(sfd_engine* e, const double* st, const double* phi_im, bool re
         LAUNCHC(e, SFD_K_UPDATE, k_lu64_gemm<<<dim3(2 * rem, 2 * rem, e->nsurf), 256, 0, e->stream>>>(e->d_surf, e->nsurf, kb, e->m64));
       }
     }
-    LAUNCHC(e, SFD_K_TRSV, k_lu64_solve<<<e->nsurf, 256, e->max_np * sizeof(double), e->stream>>>(e->d_surf, e->m64, e->phip,
-                                                                                       e->a));
+    LAUNCHC(e, SFD_K_TRSV, k_lu64_solve<<<e->nsurf, 256, e->max_np * sizeof(double), e->stream>>>(
+                               e->d_surf, e->m64, e->phip, e->a, nullptr, nullptr, Gate{}, e->lmax, e->status));
     if (fork_ap) {
       int rc = enqueue_ap(e, true);
       if (rc) return rc;
     }
-    int rc = enqueue_sums(e, SFD_PREC_F64, e->a, nullptr, 0, true);
+    int rc = enqueue_sums(e, SFD_PREC_F64, e->a, nullptr, 0, 0);
     if (rc) return rc;
+    // FP64 refinement where the residual is above the tolerance (an LU
+    // without exchanges that lost accuracy where partial pivoting would have
+    // exchanged rows): delta = (LU)^-1 r, a += delta, r -= M delta
+    for (int i = 1; i <= extra; ++i) {
+      LAUNCHC(e, SFD_K_TRSV, k_lu64_solve<<<e->nsurf, 256, e->max_np * sizeof(double), e->stream>>>(
+                                 e->d_surf, e->m64, e->r, e->delta, e->a, nullptr, make_gate(e, i - 1), nullptr, nullptr));
+      rc = enqueue_sums(e, SFD_PREC_F64, e->delta, nullptr, 1, i, i - 1);
+      if (rc) return rc;
+    }
   } else {
     if (refactor || !e->have_precond) {
       int rc = enqueue_precond(e);
@@ -318,7 +382,7 @@ int enqueue_solve(sfd_engine* e, const double* st, const double* phi_im, bool re
     int rc = enqueue_gemv(e, e->phipf, e->a, e->adf, nullptr, nullptr);
     if (rc) return rc;
     for (int it = 0; it < e->opt.pre_iters; ++it) {
-      rc = enqueue_sums(e, SFD_PREC_F32, e->a, e->adf, 0, false);
+      rc = enqueue_sums(e, SFD_PREC_F32, e->a, e->adf, 0, -1);
       if (rc) return rc;
       rc = enqueue_gemv(e, e->rf, nullptr, nullptr, e->a, e->adf);
       if (rc) return rc;
@@ -327,7 +391,7 @@ int enqueue_solve(sfd_engine* e, const double* st, const double* phi_im, bool re
       rc = enqueue_ap(e, true);
       if (rc) return rc;
     }
-    rc = enqueue_sums(e, SFD_PREC_DF, e->a, e->adf, 0, e->opt.refine_iters == 0);
+    rc = enqueue_sums(e, SFD_PREC_DF, e->a, e->adf, 0, e->opt.refine_iters == 0 ? 0 : -1);
     if (rc) return rc;
     for (int it = 0; it < e->opt.refine_iters; ++it) {
       rc = enqueue_gemv(e, e->rf, e->delta, e->ddf, e->a, nullptr);
@@ -336,7 +400,15 @@ int enqueue_solve(sfd_engine* e, const double* st, const double* phi_im, bool re
         rc = enqueue_ap(e, true);
         if (rc) return rc;
       }
-      rc = enqueue_sums(e, SFD_PREC_F32, e->delta, e->ddf, 1, it == e->opt.refine_iters - 1);
+      rc = enqueue_sums(e, SFD_PREC_F32, e->delta, e->ddf, 1, it == e->opt.refine_iters - 1 ? 0 : -1);
+      if (rc) return rc;
+    }
+    // extra corrections where the residual of the regular passes is above the
+    // tolerance (a stale or inaccurate preconditioner)
+    for (int i = 1; i <= extra; ++i) {
+      rc = enqueue_gemv(e, e->rf, e->delta, e->ddf, e->a, nullptr, i - 1);
+      if (rc) return rc;
+      rc = enqueue_sums(e, SFD_PREC_F32, e->delta, e->ddf, 1, i, i - 1);
       if (rc) return rc;
     }
   }
@@ -351,16 +423,28 @@ int enqueue_rhs(sfd_engine* e, const double* st, double* out, bool refactor) {
   const int nt = e->ntot;
   const double* y = st + nt;
   // a' (forked during the solve, or here) and the velocity / Bernoulli epilogue
+  const int extra = extra_iters(e);
   if (e->ap_forked) {
     CK(cudaStreamWaitEvent(e->stream, e->ev_join, 0));
     e->ap_forked = false;
+    if (extra > 0) {
+      // the forked transform read a before any extra correction: where one ran
+      // (the residual of the regular passes is above the tolerance), a' is
+      // transformed again from the final a
+      DerivArgs D{e->d_surf, e->nsurf, nullptr, nullptr, nullptr, nullptr, e->a, e->zp, e->zpp, e->phip, e->ap,
+                  nullptr, make_gate(e, 0)};
+      rc = enqueue_transforms(e, D, false);
+      if (rc) return rc;
+    }
   } else {
     rc = enqueue_ap(e, false);
     if (rc) return rc;
   }
   VelArgs V{e->d_surf, e->d_node_surf, e->nsurf, nt, e->cacc, e->dacc, e->a, e->ap, e->nd.v1low, e->nd.v1up,
             e->nd.v2, y, st, e->nblk == 4 ? st + 3 * nt : nullptr, e->nblk == 4 ? out + 3 * nt : nullptr,
-            e->zp, e->zpp, e->vel_low1, out, out + nt, out + 2 * nt, e->status};
+            e->zp, e->zpp, e->vel_low1, out, out + nt, out + 2 * nt, e->status,
+            e->rslot, 1 + extra, e->bnorm, e->opt.refine_tol, e->rnorm, e->rrel, e->extra_count,
+            e->opt.precision == SFD_PRECISION_MIXED ? e->stall_dev : nullptr};
   if (e->any_rho) LAUNCHC(e, SFD_K_VELOCITY, k_velocity_node1<<<1, 32, 0, e->stream>>>(V));
   LAUNCHC(e, SFD_K_VELOCITY, k_velocity_bernoulli<<<blocks_for(nt, 32), 32, 0, e->stream>>>(V));
   return 0;
@@ -432,21 +516,22 @@ int autotune_sums(sfd_engine* e) {
   int rc = enqueue_rhs(e, e->y0, e->kcur, true);
   if (rc) return rc;
   const bool mixed = e->opt.precision == SFD_PRECISION_MIXED;
-  const int precs[2] = {mixed ? SFD_PREC_F32 : SFD_PREC_F64, SFD_PREC_DF};
+  // the FP32 pass (slice-parallel kernel) has no CTA shape to choose
+  const int prec_tuned = mixed ? SFD_PREC_DF : SFD_PREC_F64;
   cudaEvent_t a = nullptr, b = nullptr;
   CK(cudaEventCreate(&a));
   CK(cudaEventCreate(&b));
-  for (int pi = 0; pi < (mixed ? 2 : 1) && !rc; ++pi) {
-    const int prec = precs[pi];
+  for (int pi = 0; pi < 1 && !rc; ++pi) {
+    const int prec = prec_tuned;
     const float2* wdf = prec == SFD_PREC_F64 ? nullptr : e->adf;
     float best = 0.f, t4 = 0.f;
     int best_g = 4;
     for (int g : kSumGroupChoices) {
       e->sum_groups[prec] = g;
-      rc = enqueue_sums(e, prec, e->a, wdf, 0, false);  // warm-up
+      rc = enqueue_sums(e, prec, e->a, wdf, 0, -1);  // warm-up
       if (rc) break;
       cudaEventRecord(a, e->stream);
-      for (int r = 0; r < 3 && !rc; ++r) rc = enqueue_sums(e, prec, e->a, wdf, 0, false);
+      for (int r = 0; r < 3 && !rc; ++r) rc = enqueue_sums(e, prec, e->a, wdf, 0, -1);
       cudaEventRecord(b, e->stream);
       if (rc) break;
       cudaError_t err = cudaEventSynchronize(b);
@@ -507,6 +592,7 @@ int bg_alloc(sfd_engine* e) {
   CK(dalloc(&B.nd.v2, nt));
   CK(dalloc(&B.m16_next, e->mat_elems));
   CK(dalloc(&B.rscale_next, nt));
+  if (e->f4_first.njobs) CK(dalloc(&B.f4_scr, 3LL * nt));
   return 0;
 }
 
@@ -522,9 +608,11 @@ int bg_start(sfd_engine* e) {
   CK(cudaStreamWaitEvent(side, B.ev_snap, 0));
   const double *x = B.snap, *y = B.snap + nt, *phi = B.snap + 2 * nt;
   DerivArgs D{e->d_surf, e->nsurf, x, y, phi, nullptr, nullptr, B.zp, B.zpp, B.phip, nullptr, nullptr};
-  if (e->njobs_first) CK(sfd_launch_spectral(D, e->d_jobs_first, e->njobs_first, e->max_n_single, side));
-  if (e->ncjobs_first) CK(sfd_launch_spectral_cluster(D, e->d_cjobs_first, e->ncjobs_first, e->max_n_cluster, side));
-  k_node_prep<<<blocks_for(nt, 32), 64, 0, side>>>(e->d_surf, e->d_node_surf, nt, x, y, B.zp, B.zpp, B.nd);
+  int nl = 0;
+  CK(launch_transforms(e, D, true, side, B.f4_scr, &nl));
+  e->launches += nl;
+  k_node_prep<<<blocks_for(nt, 32), 64, 0, side>>>(e->d_surf, e->d_node_surf, nt, x, y, B.zp, B.zpp, B.nd, nullptr,
+                                                    nullptr);
   CK(cudaGetLastError());
   CK(sfd_launch_assemble32(e->d_surf, e->d_asm_tiles, e->nasm, B.nd.w, B.nd.p, B.zp, B.nd.mdiag, e->m32, side));
   const int nb = e->max_np / 128, tiles = e->max_np / 64;
@@ -602,6 +690,22 @@ int run_steps(sfd_engine* e, double dt, int steps) {
       }
       refactor = false;
     }
+    // A refinement stall seen by a step that already ran (the kernels set the
+    // host-mapped word; the GPU may be several steps behind the host, so this
+    // is the first step enqueued after the host sees it) rebuilds the
+    // preconditioner inside this step.  A background rebuild in flight owns
+    // the inverse's work buffers, so it is switched in first.
+    if (mixed && e->have_precond && e->stall_host && *reinterpret_cast<volatile unsigned int*>(e->stall_host)) {
+      *reinterpret_cast<volatile unsigned int*>(e->stall_host) = 0u;
+      if (!refactor) {
+        refactor = true;
+        e->stall_rebuilds++;
+        if (e->bg.swap_at >= 0) {
+          int rc = bg_swap(e);
+          if (rc) return rc;
+        }
+      }
+    }
     if (graphs) {
       const int variant = refactor ? 1 : 0;
       if (!e->g_step[variant]) {
@@ -626,17 +730,19 @@ void free_engine(sfd_engine* e) {
   if (e->stream) cudaStreamSynchronize(e->stream);
   if (e->bg.side) cudaStreamSynchronize(e->bg.side);  // a background rebuild uses the inverse's buffers
   destroy_graphs(e);
-  void* ptrs[] = {e->d_surf, e->d_node_surf, e->d_jobs_first, e->d_jobs_ap, e->d_cjobs_first, e->d_cjobs_ap, e->d_sum_items, e->d_asm_tiles,
+  void* ptrs[] = {e->d_surf, e->d_node_surf, e->d_jobs_first, e->d_jobs_ap, e->d_cjobs_first, e->d_cjobs_ap, e->d_sum_items,
+                  e->d_f32_work, e->f32_part, e->f32_wsum, e->f32_count, e->d_asm_tiles,
                   e->d_gemv_rows, e->d_poff, e->y0, e->ys, e->kacc, e->kcur, e->zp, e->zpp, e->ap, e->phip, e->a,
                   e->r, e->delta, e->phi_im, e->nd.w, e->nd.p, e->nd.wdf, e->nd.pdf, e->adf, e->ddf, e->nd.mdiag, e->nd.v1low, e->nd.v1up, e->nd.v2,
-                  e->cacc, e->dacc, e->vel_low1, e->status, e->lmax, e->rnorm,
+                  e->cacc, e->dacc, e->vel_low1, e->status, e->lmax, e->rnorm, e->rslot, e->bnorm, e->rrel,
+                  e->extra_count,
                   e->inv_out, e->m64, e->m32, e->m16, e->rscale, e->fc_in, e->fc_out, e->rf, e->phipf, e->pbuf, e->rbuf, e->cbuf, e->cparts, e->rparts};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   {
     auto& B = e->bg;
     void* bp[] = {B.snap, B.zp, B.zpp, B.phip, B.nd.w, B.nd.p, B.nd.wdf, B.nd.pdf, B.nd.mdiag, B.nd.v1low, B.nd.v1up,
-                  B.nd.v2, B.m16_next, B.rscale_next};
+                  B.nd.v2, B.m16_next, B.rscale_next, B.f4_scr};
     for (void* p : bp)
       if (p) cudaFree(p);
     if (B.ev_snap) cudaEventDestroy(B.ev_snap);
@@ -648,6 +754,12 @@ void free_engine(sfd_engine* e) {
   sfd_gl2_free(e);
   drain_profile(e);
   for (cudaEvent_t ev : e->event_pool) cudaEventDestroy(ev);
+  for (F4Plan* p : {&e->f4_first, &e->f4_ap}) {
+    if (p->jobs) cudaFree(p->jobs);
+    for (int ph = 0; ph < 3; ++ph)
+      if (p->units[ph]) cudaFree(p->units[ph]);
+  }
+  if (e->f4_scr) cudaFree(e->f4_scr);
   for (auto& kv : e->d_tw) cudaFree(kv.second);
   for (auto& kv : e->d_ctw) cudaFree(kv.second);
   if (e->aux) cudaStreamSynchronize(e->aux);
@@ -655,6 +767,7 @@ void free_engine(sfd_engine* e) {
   if (e->ev_join) cudaEventDestroy(e->ev_join);
   if (e->aux) cudaStreamDestroy(e->aux);
   if (e->own_stream) cudaStreamDestroy(e->own_stream);
+  if (e->stall_host) cudaFreeHost(e->stall_host);
   delete e;
 }
 
@@ -708,6 +821,7 @@ cudaError_t sfd_solve_configure() {
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_lu64_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, 8320 * (int)sizeof(double));
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_lu64_trsm, cudaFuncAttributeMaxDynamicSharedMemorySize, kTrsmSmem);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_lu64_trsm_u, cudaFuncAttributeMaxDynamicSharedMemorySize, kTrsmSmem);
   return e;
 }
 
@@ -736,6 +850,8 @@ void sfd_default_options(sfd_options* o) {
   o->precond_half = 1;
   o->autotune = 1;
   o->refactor_lag = 0;
+  o->extra_iters = 2;
+  o->refine_tol = 1e-10;
 }
 
 void sfd_default_problem(sfd_problem* p) {
@@ -765,17 +881,18 @@ int sfd_create_driven(const int* n, int nsurf, const sfd_problem* problems, cons
                       int shared_problem, const sfd_options* opts, sfd_engine** out) {
   if (!out || !n || !problems || nsurf <= 0) return set_error(SFD_ERR_INVALID, "sfd_create: bad arguments");
   *out = nullptr;
+  sfd_options opt;
+  if (opts) opt = *opts;
+  else sfd_default_options(&opt);
+  if (opt.precision != SFD_PRECISION_FP64 && opt.precision != SFD_PRECISION_MIXED)
+    return set_error(SFD_ERR_INVALID, "unknown precision %d", opt.precision);
+  if (opt.extra_iters < 0 || opt.extra_iters > SFD_MAX_EXTRA || !(opt.refine_tol == opt.refine_tol))
+    return set_error(SFD_ERR_INVALID, "extra_iters must be 0..%d and refine_tol a number", SFD_MAX_EXTRA);
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
     return set_error(SFD_ERR_NO_DEVICE, "no CUDA device available");
   sfd_engine* e = new sfd_engine();
-  if (opts) e->opt = *opts;
-  else sfd_default_options(&e->opt);
-  if (e->opt.precision != SFD_PRECISION_FP64 && e->opt.precision != SFD_PRECISION_MIXED) {
-    const int precision = e->opt.precision;
-    delete e;
-    return set_error(SFD_ERR_INVALID, "unknown precision %d", precision);
-  }
+  e->opt = opt;
   if (e->opt.refine_iters < 0) e->opt.refine_iters = 0;
   e->tune_pending = e->opt.autotune != 0;
   if (e->opt.pre_iters < 0) e->opt.pre_iters = 0;
@@ -878,13 +995,20 @@ int sfd_create_driven(const int* n, int nsurf, const sfd_problem* problems, cons
   // work lists
   std::vector<int> node_surf(nt);
   std::vector<int2> jf, ja, cjf, cja;
+  std::vector<F4Job> f4f, f4a;
   std::vector<int2> items;
+  std::vector<int4> f32work;
   std::vector<int4> tiles;
   std::vector<int2> rows;
   for (int s = 0; s < nsurf; ++s) {
     const SurfaceDesc& S = e->hs[s];
     for (int k = 0; k < S.n; ++k) node_surf[S.off + k] = s;
-    if (S.nrad_m > 0) {
+    if (sfd_f4_eligible(S.n)) {
+      // four-step transforms over the whole GPU; scratch regions by node offset
+      f4f.push_back({s, SFD_F4_Z, 0LL * nt + S.off, 1LL * nt + S.off});
+      f4f.push_back({s, SFD_F4_PHI, 2LL * nt + S.off, 0});
+      f4a.push_back({s, SFD_F4_AP, 3LL * nt + S.off, 0});
+    } else if (S.nrad_m > 0) {
       cjf.push_back({s, SFD_JOB_ZP});  // z', z'' and phi' on three clusters side by side
       cjf.push_back({s, SFD_JOB_ZPP});
       cjf.push_back({s, SFD_JOB_PHIP});
@@ -897,7 +1021,11 @@ int sfd_create_driven(const int* n, int nsurf, const sfd_problem* problems, cons
       ja.push_back({s, SFD_JOB_AP});
       e->max_n_single = std::max(e->max_n_single, S.n);
     }
-    for (int t0 = 0; t0 < S.n; t0 += kSumTile) items.push_back({s, t0});
+    for (int t0 = 0; t0 < S.n; t0 += kSumTile) {
+      const int it = (int)items.size(), ns = sfd_f32_slices(S.n);
+      for (int sl = 0; sl < ns; ++sl) f32work.push_back({it, sl, (int)f32work.size() - sl, ns});
+      items.push_back({s, t0});
+    }
     int np = pad_n(S.n);
     for (int r0 = 0; r0 < np; r0 += 64)
       for (int c0 = 0; c0 < np; c0 += 64) tiles.push_back({s, r0, c0, 0});
@@ -922,8 +1050,40 @@ int sfd_create_driven(const int* n, int nsurf, const sfd_problem* problems, cons
   CKE(cudaMemcpy(e->d_cjobs_first, cjf.data(), cjf.size() * sizeof(int2), cudaMemcpyHostToDevice));
   CKE(dalloc(&e->d_cjobs_ap, cja.size()));
   CKE(cudaMemcpy(e->d_cjobs_ap, cja.data(), cja.size() * sizeof(int2), cudaMemcpyHostToDevice));
+  // four-step plans: per phase the (job, unit) list; units of a job are
+  // contiguous and their counts multiples of 4 (64 columns, n / 64 rows)
+  for (int pi = 0; pi < 2; ++pi) {
+    const std::vector<F4Job>& jl = pi == 0 ? f4f : f4a;
+    F4Plan& p = pi == 0 ? e->f4_first : e->f4_ap;
+    if (jl.empty()) continue;
+    std::vector<int2> ul[3];
+    for (int j = 0; j < (int)jl.size(); ++j) {
+      const int n = e->hs[jl[j].surf].n;
+      for (int u = 0; u < 64; ++u) ul[0].push_back({j, u});
+      for (int u = 0; u < n / 64; ++u) ul[1].push_back({j, u});
+      for (int u = 0; u < (jl[j].kind == SFD_F4_Z ? 128 : 64); ++u) ul[2].push_back({j, u});
+    }
+    p.njobs = (int)jl.size();
+    CKE(dalloc(&p.jobs, jl.size()));
+    CKE(cudaMemcpy(p.jobs, jl.data(), jl.size() * sizeof(F4Job), cudaMemcpyHostToDevice));
+    for (int ph = 0; ph < 3; ++ph) {
+      p.nunits[ph] = (int)ul[ph].size();
+      CKE(dalloc(&p.units[ph], ul[ph].size()));
+      CKE(cudaMemcpy(p.units[ph], ul[ph].data(), ul[ph].size() * sizeof(int2), cudaMemcpyHostToDevice));
+    }
+  }
+  if (!f4f.empty()) CKE(dalloc(&e->f4_scr, 4LL * nt));
   CKE(dalloc(&e->d_sum_items, items.size()));
   CKE(cudaMemcpy(e->d_sum_items, items.data(), items.size() * sizeof(int2), cudaMemcpyHostToDevice));
+  if (e->opt.precision == SFD_PRECISION_MIXED) {
+    e->nf32 = (int)f32work.size();
+    CKE(dalloc(&e->d_f32_work, f32work.size()));
+    CKE(cudaMemcpy(e->d_f32_work, f32work.data(), f32work.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    CKE(dalloc(&e->f32_part, 64LL * f32work.size()));
+    CKE(dalloc(&e->f32_wsum, f32work.size()));
+    CKE(dalloc(&e->f32_count, items.size()));
+    CKE(cudaMemset(e->f32_count, 0, items.size() * sizeof(unsigned int)));
+  }
   CKE(dalloc(&e->d_asm_tiles, tiles.size()));
   CKE(cudaMemcpy(e->d_asm_tiles, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice));
   CKE(dalloc(&e->d_gemv_rows, rows.size()));
@@ -962,10 +1122,23 @@ int sfd_create_driven(const int* n, int nsurf, const sfd_problem* problems, cons
   CKE(dalloc(&e->status, nsurf));
   CKE(dalloc(&e->lmax, nsurf));
   CKE(dalloc(&e->rnorm, nsurf));
+  CKE(dalloc(&e->rslot, (long long)SFD_RSLOTS * nsurf));
+  CKE(dalloc(&e->bnorm, nsurf));
+  CKE(dalloc(&e->rrel, nsurf));
+  CKE(dalloc(&e->extra_count, nsurf));
   CKE(dalloc(&e->inv_out, 5LL * nsurf));
   CKE(cudaMemset(e->status, 0, nsurf * sizeof(unsigned int)));
   CKE(cudaMemset(e->lmax, 0, nsurf * sizeof(double)));
   CKE(cudaMemset(e->rnorm, 0, nsurf * sizeof(double)));
+  CKE(cudaMemset(e->rslot, 0, (size_t)SFD_RSLOTS * nsurf * sizeof(double)));
+  CKE(cudaMemset(e->bnorm, 0, nsurf * sizeof(double)));
+  CKE(cudaMemset(e->rrel, 0, nsurf * sizeof(double)));
+  CKE(cudaMemset(e->extra_count, 0, nsurf * sizeof(unsigned long long)));
+  if (e->opt.precision == SFD_PRECISION_MIXED) {
+    CKE(cudaHostAlloc(reinterpret_cast<void**>(&e->stall_host), sizeof(unsigned int), cudaHostAllocMapped));
+    *e->stall_host = 0u;
+    CKE(cudaHostGetDevicePointer(reinterpret_cast<void**>(&e->stall_dev), e->stall_host, 0));
+  }
   CKE(cudaMemset(e->y0, 0, (long long)e->nblk * nt * sizeof(double)));
   CKE(cudaMemset(e->nd.p, 0, nt * sizeof(cd)));
   CKE(cudaMemset(e->nd.pdf, 0, nt * sizeof(float4)));
@@ -1244,6 +1417,18 @@ int sfd_clear_status(sfd_engine* e) {
   CK(cudaMemsetAsync(e->status, 0, e->nsurf * sizeof(unsigned int), e->stream));
   CK(cudaMemsetAsync(e->lmax, 0, e->nsurf * sizeof(double), e->stream));
   CK(cudaMemsetAsync(e->rnorm, 0, e->nsurf * sizeof(double), e->stream));
+  CK(cudaMemsetAsync(e->rrel, 0, e->nsurf * sizeof(double), e->stream));
+  CK(cudaMemsetAsync(e->extra_count, 0, e->nsurf * sizeof(unsigned long long), e->stream));
+  return 0;
+}
+
+int sfd_get_refinement(sfd_engine* e, double* rel_residual, long long* extra, long long* stall_rebuilds) {
+  if (!e) return set_error(SFD_ERR_INVALID, "null engine");
+  CK(cudaSetDevice(e->device));
+  CK(cudaStreamSynchronize(e->stream));
+  if (rel_residual) CK(cudaMemcpy(rel_residual, e->rrel, e->nsurf * sizeof(double), cudaMemcpyDeviceToHost));
+  if (extra) CK(cudaMemcpy(extra, e->extra_count, e->nsurf * sizeof(long long), cudaMemcpyDeviceToHost));
+  if (stall_rebuilds) *stall_rebuilds = e->stall_rebuilds;
   return 0;
 }
 
@@ -1845,6 +2030,42 @@ int noalloc_base(unsigned char** out) {
 
 }  // namespace
 
+// Descriptors of the allocation-free call, written on the device by one
+// kernel from values passed by value (the twiddles travel in the kernel
+// parameters, 16 KB at the 1024-node maximum), so the call issues no host to
+// device copy.
+struct NoallocSetup {
+  SurfaceDesc S;  // S.tw already points into the scratch
+  int n, np, nitems, ntiles;
+  cd tw[noalloc::kMaxN];
+};
+static_assert(sizeof(NoallocSetup) < 32000, "kernel parameters are limited to 32 KB");
+
+__global__ void k_noalloc_setup(const __grid_constant__ NoallocSetup P, SurfaceDesc* d_surf, cd* tw, int2* jobs_first,
+                                int2* jobs_ap, int2* items, int4* tiles, int* node_surf, unsigned int* status,
+                                double* lmax, double* rnorm) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t == 0) {
+    *d_surf = P.S;
+    jobs_first[0] = make_int2(0, SFD_JOB_ZP);
+    jobs_first[1] = make_int2(0, SFD_JOB_ZPP);
+    jobs_first[2] = make_int2(0, SFD_JOB_PHIP);
+    jobs_ap[0] = make_int2(0, SFD_JOB_AP);
+    *status = 0u;
+    *lmax = 0.0;
+    *rnorm = 0.0;
+  }
+  if (t < P.n) {
+    tw[t] = P.tw[t];
+    node_surf[t] = 0;
+  }
+  if (t < P.nitems) items[t] = make_int2(0, t * kSumTile);
+  if (t < P.ntiles) {
+    const int per_row = P.np / 64;
+    tiles[t] = make_int4(0, (t / per_row) * 64, (t % per_row) * 64, 0);
+  }
+}
+
 extern "C" int sfd_rhs_device_noalloc(const sfd_problem* problem, int n, const void* state_in, void* rhs_out,
                                       void* stream) {
   if (!problem || !state_in || !rhs_out) return set_error(SFD_ERR_INVALID, "sfd_rhs_device_noalloc: null argument");
@@ -1859,43 +2080,28 @@ extern "C" int sfd_rhs_device_noalloc(const sfd_problem* problem, int n, const v
   cudaStream_t st = (cudaStream_t)stream;
   const int np = pad_n(n);
 
-  // host-side descriptors, all on the stack
-  SurfaceDesc S;
-  std::memset(&S, 0, sizeof(S));
+  // host-side descriptors (host memory only; the same radices and twiddles as
+  // an engine's, from the same functions)
+  static_assert(std::is_trivially_copyable<NoallocSetup>::value, "passed by value to a kernel");
+  NoallocSetup P;
+  std::memset(&P, 0, sizeof(P));
+  SurfaceDesc& S = P.S;
   rc = fill_surface(S, *problem);
   if (rc) return rc;
   S.n = n;
   S.off = 0;
   S.moff = 0;
-  {
-    int m = n, k = 0;
-    while (m % 4 == 0 && k < SFD_MAX_RADICES) { S.rad[k++] = 4; m /= 4; }
-    while (m % 2 == 0 && k < SFD_MAX_RADICES) { S.rad[k++] = 2; m /= 2; }
-    for (int q = 3; m > 1 && k < SFD_MAX_RADICES; q += 2)
-      while (m % q == 0 && k < SFD_MAX_RADICES) { S.rad[k++] = q; m /= q; }
-    if (m != 1) return set_error(SFD_ERR_INVALID, "sfd_rhs_device_noalloc: n = %d has too many factors", n);
-    S.nrad = k;
-  }
-  cd tw[noalloc::kMaxN];
-  {
-    const long double two_pi = 6.283185307179586476925286766559005768L;
-    for (int e = 0; e < n; ++e) {
-      long double ang = two_pi * (long double)e / (long double)n;
-      tw[e] = cd{(double)cosl(ang), (double)(-sinl(ang))};
-    }
-    tw[0] = {1.0, 0.0};
-    if (n % 2 == 0) tw[n / 2] = {-1.0, 0.0};
-    if (n % 4 == 0) { tw[n / 4] = {0.0, -1.0}; tw[3 * n / 4] = {0.0, 1.0}; }
-  }
-  int2 jf[3] = {{0, SFD_JOB_ZP}, {0, SFD_JOB_ZPP}, {0, SFD_JOB_PHIP}};
-  int2 ja[1] = {{0, SFD_JOB_AP}};
-  int2 items[noalloc::kMaxItems];
-  int nitems = 0;
-  for (int t0 = 0; t0 < n; t0 += kSumTile) items[nitems++] = {0, t0};
-  int4 tiles[noalloc::kMaxTiles];
-  int ntiles = 0;
-  for (int r0 = 0; r0 < np; r0 += 64)
-    for (int c0 = 0; c0 < np; c0 += 64) tiles[ntiles++] = {0, r0, c0, 0};
+  std::vector<int> rad;
+  if (!factorize(n, rad))
+    return set_error(SFD_ERR_INVALID, "sfd_rhs_device_noalloc: n = %d has too many factors", n);
+  S.nrad = (int)rad.size();
+  for (size_t i = 0; i < rad.size(); ++i) S.rad[i] = rad[i];
+  const std::vector<cd> tw = twiddles(n);
+  std::memcpy(P.tw, tw.data(), n * sizeof(cd));
+  P.n = n;
+  P.np = np;
+  P.nitems = (n + kSumTile - 1) / kSumTile;
+  P.ntiles = (np / 64) * (np / 64);
 
   // carve the static scratch (same order as its size computation)
   Bump b{base};
@@ -1932,18 +2138,12 @@ extern "C" int sfd_rhs_device_noalloc(const sfd_problem* problem, int n, const v
   if ((size_t)(b.p - base) > noalloc::kBytes) return set_error(SFD_ERR_INVALID, "scratch layout overflow");
   S.tw = d_tw;
 
-  // upload descriptors; zero what the kernels accumulate into
-  CK(cudaMemcpyAsync(d_tw, tw, n * sizeof(cd), cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(e.d_surf, &S, sizeof(S), cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(e.d_jobs_first, jf, sizeof(jf), cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(e.d_jobs_ap, ja, sizeof(ja), cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(e.d_sum_items, items, nitems * sizeof(int2), cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(e.d_asm_tiles, tiles, ntiles * sizeof(int4), cudaMemcpyHostToDevice, st));
-  CK(cudaMemsetAsync(e.d_node_surf, 0, n * sizeof(int), st));
-  CK(cudaMemsetAsync(e.status, 0, sizeof(unsigned int), st));
-  CK(cudaMemsetAsync(e.lmax, 0, sizeof(double), st));
-  CK(cudaMemsetAsync(e.rnorm, 0, sizeof(double), st));
-
+  // descriptors on the device, then the evaluation, all on `stream`
+  const int setup_threads = std::max(n, P.ntiles);
+  k_noalloc_setup<<<(setup_threads + 255) / 256, 256, 0, st>>>(P, e.d_surf, d_tw, e.d_jobs_first, e.d_jobs_ap,
+                                                               e.d_sum_items, e.d_asm_tiles, e.d_node_surf, e.status,
+                                                               e.lmax, e.rnorm);
+  CK(cudaGetLastError());
   CK(cudaGetDevice(&e.device));
   e.stream = st;
   sfd_default_options(&e.opt);
@@ -1951,6 +2151,7 @@ extern "C" int sfd_rhs_device_noalloc(const sfd_problem* problem, int n, const v
   e.opt.use_graphs = 0;
   e.opt.refine_iters = 0;
   e.opt.pre_iters = 0;
+  e.opt.extra_iters = 0;
   e.nsurf = 1;
   e.ntot = n;
   e.max_n = n;
@@ -1958,8 +2159,8 @@ extern "C" int sfd_rhs_device_noalloc(const sfd_problem* problem, int n, const v
   e.max_np = np;
   e.njobs_first = 3;
   e.njobs_ap = 1;
-  e.nsum = nitems;
-  e.nasm = ntiles;
+  e.nsum = P.nitems;
+  e.nasm = P.ntiles;
   e.any_rho = (S.physics == 0 && S.rho != 0.0);
   return enqueue_rhs(&e, static_cast<const double*>(state_in), static_cast<double*>(rhs_out), true);
 }

@@ -49,6 +49,28 @@ enum : int {
   SFD_JOB_RAW2 = 5, // d^2/dj^2 of (x + i y), likewise unscaled -> ap (reverse mode)
 };
 
+// Residual slots of one RHS evaluation: slot 0 holds max |r| of the last
+// regular pass of the solve, slot i the residual after extra correction i.
+// k_node_prep clears them (and max |phi'|) for every evaluation.
+#define SFD_MAX_EXTRA 4
+#define SFD_RSLOTS (1 + SFD_MAX_EXTRA)
+
+// Refinement gate.  A kernel given an open gate (slot != null) does its work
+// only for the surfaces whose residual in `slot` is above tol * max |phi'|;
+// for the others it returns at once.  This keeps the extra corrections inside
+// a fixed launch sequence (and a fixed CUDA graph) while costing only a launch
+// when they are not needed.  A NaN residual counts as above (slots store 1e300
+// for NaN); a NaN scale counts as below.
+struct Gate {
+  const double* slot;   // rslot + (pass - 1): the previous tracked pass; null = ungated
+  const double* bnorm;  // per-surface max |phi'|
+  int stride;           // slots per surface (SFD_RSLOTS)
+  double tol;           // relative residual tolerance
+};
+__device__ __forceinline__ bool gate_open(const Gate& G, int s) {
+  return !G.slot || (G.slot[(long long)s * G.stride] > G.tol * G.bnorm[s]);
+}
+
 struct DerivArgs {
   const SurfaceDesc* surf;
   int nsurf;
@@ -62,4 +84,5 @@ struct DerivArgs {
   double* phip;
   cd* ap;
   float* phipf;  // FP32 copy of phi' for the preconditioner product (nullable)
+  Gate gate;     // jobs run only where the gate is open (ungated by default)
 };

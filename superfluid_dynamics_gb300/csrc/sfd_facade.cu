@@ -136,12 +136,14 @@ extern "C" int sfd_dense_solver_create(int n, int batch, sfd_dense_solver** out)
   if (err == cudaSuccess) err = cudaMemcpy(d->d_surf, hs.data(), batch * sizeof(SurfaceDesc), cudaMemcpyHostToDevice);
   if (err == cudaSuccess) err = cudaMalloc(&d->mat, (size_t)batch * d->np * d->np * sizeof(double));
   if (err == cudaSuccess) err = cudaMalloc(&d->lmax, batch * sizeof(double));
+  if (err == cudaSuccess) err = cudaMalloc(&d->piv, (size_t)batch * d->np * sizeof(int));
   if (err == cudaSuccess) err = cudaMalloc(&d->status, batch * sizeof(unsigned int));
   if (err == cudaSuccess) err = sfd_solve_configure();
   if (err != cudaSuccess) {
     cudaFree(d->d_surf);
     cudaFree(d->mat);
     cudaFree(d->lmax);
+    cudaFree(d->piv);
     cudaFree(d->status);
     delete d;
     return sfd_internal_cuda(err, "sfd_dense_solver_create");
@@ -161,31 +163,39 @@ extern "C" int sfd_dense_solve(sfd_dense_solver* d, const double* M, const doubl
   dim3 blk(16, 16), grid(nb(d->np, 16), nb(d->np, 16), d->batch);
   k_colmajor_to_padded<<<grid, blk, 0, d->stream>>>(d->n, d->np, M, d->mat);
   FCK(cudaGetLastError());
-  return sfd_internal_dense_factor_solve(d, b, x, status);
+  // MatrixSolver::solve factors with cusolverDnDgetrf / getrs (partial pivoting)
+  return sfd_internal_dense_factor_solve(d, b, x, status, true);
 }
 
-int sfd_internal_dense_factor_solve(sfd_dense_solver* d, const double* b, double* x, unsigned int* status) {
+int sfd_internal_dense_factor_solve(sfd_dense_solver* d, const double* b, double* x, unsigned int* status,
+                                    bool pivoted) {
   cudaStream_t s = d->stream;
   FCK(cudaMemsetAsync(d->status, 0, d->batch * sizeof(unsigned int), s));
   FCK(cudaMemsetAsync(d->lmax, 0, d->batch * sizeof(double), s));
   const int nbk = d->np / 64;
   for (int kb = 0; kb < nbk; ++kb) {
-    k_lu64_diag<<<d->batch, 256, 0, s>>>(d->d_surf, d->batch, kb, d->mat, d->status, d->lmax);
     const int rem = nbk - kb - 1;
-    if (rem > 0) {
-      k_lu64_trsm<<<dim3(rem, 2, d->batch), 64, kTrsmSmem, s>>>(d->d_surf, d->batch, kb, d->mat, d->lmax);
-      k_lu64_gemm<<<dim3(2 * rem, 2 * rem, d->batch), 256, 0, s>>>(d->d_surf, d->batch, kb, d->mat);
+    if (pivoted) {
+      k_lu64_panel_piv<<<d->batch, 1024, 0, s>>>(d->d_surf, d->batch, kb, d->mat, d->piv, d->status);
+      if (nbk > 1) k_lu64_swap<<<dim3(nb(d->np - 64, 256), d->batch), 256, 0, s>>>(d->d_surf, d->batch, kb, d->mat, d->piv);
+      if (rem > 0) k_lu64_trsm_u<<<dim3(rem, 1, d->batch), 64, kTrsmSmem, s>>>(d->d_surf, d->batch, kb, d->mat);
+    } else {
+      k_lu64_diag<<<d->batch, 256, 0, s>>>(d->d_surf, d->batch, kb, d->mat, d->status, d->lmax);
+      if (rem > 0) k_lu64_trsm<<<dim3(rem, 2, d->batch), 64, kTrsmSmem, s>>>(d->d_surf, d->batch, kb, d->mat, d->lmax);
     }
+    if (rem > 0) k_lu64_gemm<<<dim3(2 * rem, 2 * rem, d->batch), 256, 0, s>>>(d->d_surf, d->batch, kb, d->mat);
   }
-  k_lu64_solve<<<d->batch, 256, d->np * sizeof(double), s>>>(d->d_surf, d->mat, b, x);
+  k_lu64_solve<<<d->batch, 256, d->np * sizeof(double), s>>>(d->d_surf, d->mat, b, x, nullptr,
+                                                               pivoted ? d->piv : nullptr, Gate{}, nullptr, nullptr);
   FCK(cudaGetLastError());
   if (status) {
     std::vector<double> lm(d->batch);
     FCK(cudaMemcpyAsync(status, d->status, d->batch * sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
     FCK(cudaMemcpyAsync(lm.data(), d->lmax, d->batch * sizeof(double), cudaMemcpyDeviceToHost, s));
     FCK(cudaStreamSynchronize(s));
-    for (int i = 0; i < d->batch; ++i)
-      if (lm[i] > 1.0) status[i] |= SFD_STATUS_PIVOT_SWAP;
+    if (!pivoted)
+      for (int i = 0; i < d->batch; ++i)
+        if (lm[i] > 1.0) status[i] |= SFD_STATUS_PIVOT_SWAP;
   }
   return 0;
 }
@@ -196,6 +206,7 @@ extern "C" int sfd_dense_solver_destroy(sfd_dense_solver* d) {
   cudaFree(d->d_surf);
   cudaFree(d->mat);
   cudaFree(d->lmax);
+  cudaFree(d->piv);
   cudaFree(d->status);
   delete d;
   return 0;

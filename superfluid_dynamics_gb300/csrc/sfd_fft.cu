@@ -161,6 +161,7 @@ __global__ void __launch_bounds__(kFftThreads, 1) k_spectral_deriv(DerivArgs A, 
   extern __shared__ double2 smem_raw[];
   cd* buf = reinterpret_cast<cd*>(smem_raw);
   const int2 job = jobs[blockIdx.x];
+  if (!gate_open(A.gate, job.x)) return;
   const SurfaceDesc& S = A.surf[job.x];  // read in place: copying would put rad[] on the stack
   const int n = S.n, off = S.off, kind = job.y;
   const double rho = S.physics == 0 ? S.rho : 0.0;
@@ -260,6 +261,7 @@ __global__ void __cluster_dims__(SFD_FFT_CLUSTER, 1, 1) __launch_bounds__(kCT)
   static_assert(C == 8, "the exchange step is written for 8-CTA clusters");
   extern __shared__ double2 csmem_raw[];
   const int2 job = jobs[blockIdx.y];
+  if (!gate_open(A.gate, job.x)) return;  // every CTA of the cluster has the same job
   const SurfaceDesc& S = A.surf[job.x];
   const int n = S.n, off = S.off, kind = job.y;
   const int M = n / C, R = M / C;

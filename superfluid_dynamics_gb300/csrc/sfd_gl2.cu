@@ -363,8 +363,17 @@ int attempt(sfd_engine* e, Gl2Work* W, const sfd_gl2_options& o, bool exact, dou
                                                                       W->lu->mat);
     GCK(cudaGetLastError());
     unsigned int lst = 0;
-    rc = sfd_internal_dense_factor_solve(W->lu, W->R, W->d, &lst);  // M d = R; the update is k - alpha d
+    rc = sfd_internal_dense_factor_solve(W->lu, W->R, W->d, &lst, false);  // M d = R; the update is k - alpha d
     if (rc) return rc;
+    if (lst & SFD_STATUS_PIVOT_SWAP) {
+      // partial pivoting would have exchanged rows: assemble the Newton matrix
+      // again and factor it with the exchanges (the reference's getrf)
+      k_gl2_newton_matrix<<<dim3(np / 32, np / 32), dim3(32, 8), 0, s>>>(n, np, h, W->J0, frozen ? W->J0 : W->J1,
+                                                                        W->lu->mat);
+      GCK(cudaGetLastError());
+      rc = sfd_internal_dense_factor_solve(W->lu, W->R, W->d, &lst, true);
+      if (rc) return rc;
+    }
     if (lst & (SFD_STATUS_ZERO_PIVOT | SFD_STATUS_NONFINITE)) return 0;  // not converged
     const double phi = 0.5 * r2;
     double alpha = 1.0;

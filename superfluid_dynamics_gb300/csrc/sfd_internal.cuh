@@ -65,7 +65,17 @@ struct sfd_engine {
   int2* d_cjobs_first = nullptr; int ncjobs_first = 0;  // cluster-distributed transforms
   int2* d_cjobs_ap = nullptr; int ncjobs_ap = 0;
   int max_n_single = 0, max_n_cluster = 0;
+  // four-step transforms of the power-of-two surfaces: z', z'', phi' and a'
+  // plans, and their L2 scratch (4 ntot complex: z' rows, z'' rows, phi' rows,
+  // a' rows; a' runs on the auxiliary stream beside the main stream's work)
+  F4Plan f4_first, f4_ap;
+  cd* f4_scr = nullptr;
   int2* d_sum_items = nullptr; int nsum = 0;
+  // FP32 pass: (tile, source slice) work entries, per-entry partials, per-tile counters
+  int4* d_f32_work = nullptr; int nf32 = 0;
+  float4* f32_part = nullptr;
+  float2* f32_wsum = nullptr;
+  unsigned int* f32_count = nullptr;
   int4* d_asm_tiles = nullptr; int nasm = 0;
   int2* d_gemv_rows = nullptr; int ngemv = 0;
   long long* d_poff = nullptr;
@@ -81,6 +91,17 @@ struct sfd_engine {
   cd *cacc = nullptr, *dacc = nullptr, *vel_low1 = nullptr;
   unsigned int* status = nullptr;
   double *lmax = nullptr, *rnorm = nullptr, *inv_out = nullptr;
+  // refinement bookkeeping: per-evaluation residual slots (SFD_RSLOTS per
+  // surface) and max |phi'|, cleared by k_node_prep; per-surface max final
+  // relative residual and count of extra corrections since the last clear
+  double *rslot = nullptr, *bnorm = nullptr, *rrel = nullptr;
+  unsigned long long* extra_count = nullptr;
+  // host-mapped word the velocity kernel sets on a refinement stall (mixed
+  // mode): the next step the host enqueues after seeing it rebuilds the
+  // preconditioner in-step
+  unsigned int* stall_host = nullptr;
+  unsigned int* stall_dev = nullptr;
+  long long stall_rebuilds = 0;
   // matrices
   double* m64 = nullptr;
   float* m32 = nullptr;
@@ -124,6 +145,7 @@ struct sfd_engine {
     NodeData nd{};
     __half* m16_next = nullptr;
     float* rscale_next = nullptr;
+    cd* f4_scr = nullptr;       // four-step scratch of the side stream's transforms (3 ntot)
     long long swap_at = -1;     // step index of the switch; -1: none pending
     long long rebuilds = 0;
   } bg;
@@ -140,13 +162,17 @@ struct sfd_dense_solver {
   SurfaceDesc* d_surf = nullptr;
   double* mat = nullptr;
   double* lmax = nullptr;
+  int* piv = nullptr;  // row exchanges of the pivoted factorisation, batch x np
   unsigned int* status = nullptr;
   cudaStream_t stream = nullptr;
 };
-// Factor d->mat in place (blocked LU without row exchanges) and solve for
-// each system's right-hand side b (batch x n) into x; status (host, nullable,
-// batch words) as sfd_dense_solve.  Asynchronous unless status is given.
-int sfd_internal_dense_factor_solve(sfd_dense_solver* d, const double* b, double* x, unsigned int* status);
+// Factor d->mat in place and solve for each system's right-hand side b
+// (batch x n) into x: with `pivoted`, blocked LU with partial pivoting (getrf /
+// getrs semantics); otherwise blocked LU without row exchanges, recording
+// max |l_ij|.  status (host, nullable, batch words) as sfd_dense_solve.
+// Asynchronous unless status is given.
+int sfd_internal_dense_factor_solve(sfd_dense_solver* d, const double* b, double* x, unsigned int* status,
+                                    bool pivoted);
 
 // Entry points of sfd_api.cu used by the reverse mode.
 int sfd_internal_error(int code, const char* msg);

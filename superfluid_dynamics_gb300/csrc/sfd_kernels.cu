@@ -23,6 +23,7 @@
 #include "sfd_engine.cuh"
 #include "sfd_kernels.cuh"
 
+#include <algorithm>
 #include <cooperative_groups.h>
 #include <type_traits>
 
@@ -33,12 +34,21 @@
 // 32 nodes (GB300's FP64 pipe is narrow, so the chains' latency is the cost):
 // warp 0 the exponentials (w, p), warp 1 the z' / z'' terms, which share one
 // reciprocal 1 / z'.
+// The thread of a surface's first node also clears the surface's residual
+// slots and max |phi'| (rslot, bnorm nullable): every boundary-sum pass of the
+// evaluation runs after this kernel.
 __global__ void __launch_bounds__(64) k_node_prep(const SurfaceDesc* surf, const int* node_surf, int ntot,
                                                   const double* x, const double* y, const cd* zp, const cd* zpp,
-                                                  NodeData nd) {
+                                                  NodeData nd, double* rslot, double* bnorm) {
   const int g = blockIdx.x * 32 + (threadIdx.x & 31);
   if (g >= ntot) return;
-  const SurfaceDesc& S = surf[node_surf[g]];
+  const int sidx = node_surf[g];
+  const SurfaceDesc& S = surf[sidx];
+  if (threadIdx.x >= 32 && g == S.off && rslot) {
+#pragma unroll
+    for (int i = 0; i < SFD_RSLOTS; ++i) rslot[(long long)sidx * SFD_RSLOTS + i] = 0.0;
+    bnorm[sidx] = 0.0;
+  }
   if (threadIdx.x < 32) {
     double s, c;
     sincos(x[g], &s, &c);
@@ -318,6 +328,7 @@ __global__ void __cluster_dims__(kSumCL, 1, 1) __launch_bounds__(G * kSumTile, 1
   const int rank = (int)cluster.block_rank();
   const int2 item = A.items[blockIdx.x / kSumCL];
   const int sidx = item.x, t0 = item.y;
+  if (!gate_open(A.gate, sidx)) return;  // every CTA of the cluster has the same surface
   const SurfaceDesc& S = A.surf[sidx];
   const int n = S.n, off = S.off;
   const bool image = (S.physics == 1 && !S.infinite_depth);
@@ -408,22 +419,28 @@ __global__ void __cluster_dims__(kSumCL, 1, 1) __launch_bounds__(G * kSumTile, 1
       red_add(v, shfl_x(v, o));
       aw = wsum_add(aw, shfl_x(aw, o));
     }
-    double rv = 0.0;
+    double rv = 0.0, bv = 0.0;
     const int tkk = t0 + lt;
     if (q == 0 && tkk < n) {
       const cd sum_s = {to_d(v.sr), to_d(v.si)};
       const cd sum_t = {to_d(v.tr), to_d(v.ti)};
       rv = sums_finish(A, S, off + tkk, sum_s, sum_t, to_d(aw), image);
+      if (A.bnorm) {
+        const double b = fabs(A.phip[off + tkk]);
+        bv = (b == b) ? b : 1e300;
+      }
     }
-    if (A.rnorm) {
-      // |r| max per surface: non-negative doubles order like their bit patterns
-      unsigned long long m = (unsigned long long)__double_as_longlong(rv);
+    // per-surface maxima: non-negative doubles order like their bit patterns
+    auto warp_max_to = [&](double val, double* dst) {
+      unsigned long long m = (unsigned long long)__double_as_longlong(val);
       for (int o = 16; o > 0; o >>= 1) {
         unsigned long long u = __shfl_xor_sync(0xffffffffu, m, o);
         m = u > m ? u : m;
       }
-      if (lane == 0) atomicMax(reinterpret_cast<unsigned long long*>(A.rnorm) + sidx, m);
-    }
+      if (lane == 0) atomicMax(reinterpret_cast<unsigned long long*>(dst), m);
+    };
+    if (A.rtrack) warp_max_to(rv, A.rtrack + (long long)sidx * SFD_RSLOTS);
+    if (A.bnorm) warp_max_to(bv, A.bnorm + sidx);
   }
   cluster.sync();  // peers may still be reading this CTA's shared memory
 }
@@ -467,6 +484,250 @@ cudaError_t sfd_launch_sums(int prec, const SumArgs& A, int nitems, int max_n, i
   else if (prec == SFD_PREC_DF) launch_prec<SFD_PREC_DF>(A, grid, groups, smem, st);
   else launch_prec<SFD_PREC_F32>(A, grid, groups, smem, st);
   return cudaPeekAtLastError();  // the caller's launch check reads and clears it
+}
+
+// ----------------------------------------------------------------- FP32 pass
+// The FP32 correction passes move small weights (corrections delta ~ 1e-7 a
+// and smaller), so their sums and epilogue only need FP32 accuracy.  Layout:
+// one independent CTA per (64-target tile, slice of about 256 sources), two
+// targets per thread (every shared-memory source read serves both), four
+// source groups per CTA.  Each CTA writes its 64 partials and its weight-sum
+// partial, then counts itself done on the tile's counter; the CTA that
+// finishes last (no CTA ever waits) reduces the tile's slices in slice order,
+// so the result does not depend on which CTA that is, and runs the epilogue in
+// FP32 with only the final accumulations into C, D and r in FP64.
+namespace {
+constexpr int kF32Groups = 4;
+constexpr int kF32Threads = 32 * kF32Groups;
+
+// S part (sources j != k) and T part (image, every j) of one pair; sources
+// are staged as {w.re hi, w.re lo, w.im hi, w.im lo} and {a, p.re, p.im, -}.
+__device__ __forceinline__ void f32_s(const float (&t)[6], float4 s0, float a, float4& acc) {
+  const float dr = (t[0] - s0.x) + (t[1] - s0.y);
+  const float di = (t[2] - s0.z) + (t[3] - s0.w);
+  const float inv = a * rcp_approx(fmaf(dr, dr, di * di));
+  acc.x = fmaf(inv, dr, acc.x);
+  acc.y = fmaf(-inv, di, acc.y);
+}
+__device__ __forceinline__ void f32_t(const float (&t)[6], float4 s1, float4& acc) {
+  const float qr = t[4] * s1.y + t[5] * s1.z, qi = t[5] * s1.y - t[4] * s1.z;
+  const float dr = 1.f - qr, di = -qi;
+  const float inv = s1.x * rcp_approx(fmaf(dr, dr, di * di));
+  acc.z = fmaf(inv, dr, acc.z);
+  acc.w = fmaf(-inv, di, acc.w);
+}
+
+template <bool IMAGE>
+__device__ __forceinline__ void f32_slice_loop(const float4* src, int jn, int grp, int lo, int hi, int self0,
+                                               int self1, const float (&T0)[6], const float (&T1)[6], float4& acc0,
+                                               float4& acc1) {
+  auto first = [&](int a) { return a + ((grp - a) % kF32Groups + kF32Groups) % kF32Groups; };
+  auto pair = [&](int jj, bool check) {
+    const float4 s0 = src[2 * jj], s1 = src[2 * jj + 1];
+    if (!check || jj != self0) f32_s(T0, s0, s1.x, acc0);
+    if (!check || jj != self1) f32_s(T1, s0, s1.x, acc1);
+    if (IMAGE) {
+      f32_t(T0, s1, acc0);
+      f32_t(T1, s1, acc1);
+    }
+  };
+  int jj = grp;
+#pragma unroll 4
+  for (; jj < lo; jj += kF32Groups) pair(jj, false);
+  for (jj = first(lo); jj < hi; jj += kF32Groups) pair(jj, true);
+#pragma unroll 4
+  for (jj = first(hi); jj < jn; jj += kF32Groups) pair(jj, false);
+}
+
+__device__ __forceinline__ void load_target(const SumArgs& A, int g, bool image, float (&T)[6]) {
+  const float4 w = A.wdf[g];
+  T[0] = w.x; T[1] = w.y; T[2] = w.z; T[3] = w.w;
+  if (image) {
+    const float4 p = A.pdf[g];
+    T[4] = p.x; T[5] = p.z;
+  } else {
+    T[4] = 0.f; T[5] = 0.f;
+  }
+}
+}  // namespace
+
+__global__ void __launch_bounds__(kF32Threads, 8) k_sums_f32(SumArgs A) {
+  const int4 wk = A.swork[blockIdx.x];  // item, slice, first work entry of the item, slices
+  const int2 item = A.items[wk.x];
+  const int sidx = item.x, t0 = item.y;
+  if (!gate_open(A.gate, sidx)) return;  // every slice of the tile skips together
+  const SurfaceDesc& S = A.surf[sidx];
+  const int n = S.n, off = S.off;
+  const bool image = (S.physics == 1 && !S.infinite_depth);
+  const int per = (n + wk.w - 1) / wk.w;
+  const int j_lo = min(n, wk.y * per), j_hi = min(n, j_lo + per), jn = j_hi - j_lo;
+  extern __shared__ float4 f32_src[];  // 2 float4 per source
+  __shared__ float4 red[kF32Groups][64];
+  __shared__ df wred[kF32Groups];
+  __shared__ int last;
+  const int tid = threadIdx.x, lane = tid & 31, grp = tid >> 5;
+
+  // ---- stage this slice's sources and its weight sum
+  df wpart{0.f, 0.f};
+  for (int jj = tid; jj < jn; jj += kF32Threads) {
+    const int g = off + j_lo + jj;
+    const float2 ad = A.adf[g];
+    const float4 p = image ? A.pdf[g] : make_float4(0.f, 0.f, 0.f, 0.f);
+    wpart = df_add(wpart, df{ad.x, ad.y});
+    f32_src[2 * jj] = A.wdf[g];
+    f32_src[2 * jj + 1] = make_float4(ad.x, p.x, p.z, 0.f);
+  }
+  for (int o = 16; o > 0; o >>= 1)
+    wpart = df_add(wpart, df{__shfl_xor_sync(0xffffffffu, wpart.hi, o), __shfl_xor_sync(0xffffffffu, wpart.lo, o)});
+  if (lane == 0) wred[grp] = wpart;
+
+  // ---- targets t0 + lane and t0 + 32 + lane
+  const int tk0 = t0 + lane, tk1 = t0 + 32 + lane;
+  float T0[6], T1[6];
+  load_target(A, off + (tk0 < n ? tk0 : 0), image, T0);
+  load_target(A, off + (tk1 < n ? tk1 : 0), image, T1);
+  __syncthreads();
+  // only the sources of the tile's own nodes need the j == k test
+  int lo = jn, hi = jn;
+  if (t0 < j_hi && t0 + 64 > j_lo) {
+    lo = max(0, t0 - j_lo);
+    hi = min(jn, t0 + 64 - j_lo);
+  }
+  const int self0 = tk0 < n ? tk0 - j_lo : -1, self1 = tk1 < n ? tk1 - j_lo : -1;
+  float4 acc0 = make_float4(0.f, 0.f, 0.f, 0.f), acc1 = acc0;
+  if (image) f32_slice_loop<true>(f32_src, jn, grp, lo, hi, self0, self1, T0, T1, acc0, acc1);
+  else f32_slice_loop<false>(f32_src, jn, grp, lo, hi, self0, self1, T0, T1, acc0, acc1);
+  red[grp][lane] = acc0;
+  red[grp][32 + lane] = acc1;
+  __syncthreads();
+
+  // ---- this slice's partials (groups in order), then count the slice done
+  const long long entry = wk.z + wk.y;
+  if (tid < 64) {
+    float4 v = red[0][tid];
+#pragma unroll
+    for (int q = 1; q < kF32Groups; ++q) {
+      const float4 u = red[q][tid];
+      v.x += u.x; v.y += u.y; v.z += u.z; v.w += u.w;
+    }
+    A.spart[entry * 64 + tid] = v;
+  }
+  if (tid == 0) {
+    df w = wred[0];
+    for (int q = 1; q < kF32Groups; ++q) w = df_add(w, wred[q]);
+    A.swsum[entry] = make_float2(w.hi, w.lo);
+  }
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) last = atomicAdd(A.scount + wk.x, 1u) == (unsigned)(wk.w - 1);
+  __syncthreads();
+  if (!last) return;
+  __threadfence();  // the other slices' partials are visible from here
+
+  // ---- the last slice of the tile: reduce in slice order, FP32 epilogue.
+  // Two threads per target: half h loads slices [8h, 8h + 8) at once (one L2
+  // round trip) and sums them in order; half 1 hands its sum to half 0, which
+  // adds it last, so the order is fixed.
+  if (tid == 0) A.scount[wk.x] = 0u;  // every slice has counted: ready for the next pass
+  __shared__ float hsum[64][10];
+  df sr{0.f, 0.f}, si{0.f, 0.f}, tr{0.f, 0.f}, ti{0.f, 0.f}, aw{0.f, 0.f};
+  {
+    const int t = tid & 63, h = tid >> 6;
+    float4 pv[8];
+    float2 pw[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int sl = 8 * h + i;
+      pv[i] = sl < wk.w ? __ldcg(A.spart + (wk.z + sl) * 64LL + t) : make_float4(0.f, 0.f, 0.f, 0.f);
+      pw[i] = sl < wk.w ? __ldcg(A.swsum + wk.z + sl) : make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      if (8 * h + i < wk.w) {
+        sr = df_add(sr, df{pv[i].x, 0.f});
+        si = df_add(si, df{pv[i].y, 0.f});
+        tr = df_add(tr, df{pv[i].z, 0.f});
+        ti = df_add(ti, df{pv[i].w, 0.f});
+        aw = df_add(aw, df{pw[i].x, pw[i].y});
+      }
+    }
+    if (h == 1) {
+      float* o = hsum[t];
+      o[0] = sr.hi; o[1] = sr.lo; o[2] = si.hi; o[3] = si.lo; o[4] = tr.hi;
+      o[5] = tr.lo; o[6] = ti.hi; o[7] = ti.lo; o[8] = aw.hi; o[9] = aw.lo;
+    }
+    __syncthreads();
+    if (h == 1) return;
+    const float* o = hsum[t];
+    sr = df_add(sr, df{o[0], o[1]});
+    si = df_add(si, df{o[2], o[3]});
+    tr = df_add(tr, df{o[4], o[5]});
+    ti = df_add(ti, df{o[6], o[7]});
+    aw = df_add(aw, df{o[8], o[9]});
+  }
+  const int tk = t0 + tid;
+  double rv = 0.0, bv = 0.0;
+  if (tk < n) {
+    const int g = off + tk;
+    constexpr float inv4pi = (float)(0.25 / SFD_PI);
+    const float c1 = S.physics == 0 ? (float)(0.25 * (1 - S.rho) / SFD_PI) : inv4pi;
+    const float4 wv = A.wdf[g];
+    const float wr = wv.x + wv.y, wi = wv.z + wv.w;
+    const float ak = (float)A.a[g];
+    const float Sr = sr.hi + sr.lo, Si = si.hi + si.lo, Af = aw.hi + aw.lo;
+    // C = i (2 w S - (A - a_k)),  D = -i (2 T - A)
+    const float ur = 2.f * (wr * Sr - wi * Si) - (Af - ak), ui = 2.f * (wr * Si + wi * Sr);
+    const float Cr = -ui, Ci = ur;
+    float Dr = 0.f, Di = 0.f;
+    if (image) {
+      Dr = 2.f * (ti.hi + ti.lo);
+      Di = -(2.f * (tr.hi + tr.lo) - Af);
+    }
+    const cd zp = A.zp[g];
+    float ma = (float)A.mdiag[g] * ak + c1 * ((float)zp.re * Ci + (float)zp.im * Cr);
+    if (image) ma -= inv4pi * Di;
+    double rnew;
+    if (A.mode == 0) {
+      A.cacc[g] = cd{(double)Cr, (double)Ci};
+      if (image) A.dacc[g] = cd{(double)Dr, (double)Di};
+      rnew = A.phip[g] - (double)ma;
+    } else {
+      const cd c = A.cacc[g];
+      A.cacc[g] = cd{c.re + (double)Cr, c.im + (double)Ci};
+      if (image) {
+        const cd d = A.dacc[g];
+        A.dacc[g] = cd{d.re + (double)Dr, d.im + (double)Di};
+      }
+      rnew = A.r[g] - (double)ma;
+    }
+    A.r[g] = rnew;
+    if (A.rf) A.rf[g] = (float)rnew;
+    rv = fabs(rnew);
+    rv = (rv == rv) ? rv : 1e300;
+    if (A.bnorm) {
+      const double b = fabs(A.phip[g]);
+      bv = (b == b) ? b : 1e300;
+    }
+  }
+  auto warp_max_to = [&](double val, double* dst) {
+    unsigned long long m = (unsigned long long)__double_as_longlong(val);
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long u = __shfl_xor_sync(0xffffffffu, m, o);
+      m = u > m ? u : m;
+    }
+    if (lane == 0) atomicMax(reinterpret_cast<unsigned long long*>(dst), m);
+  };
+  if (A.rtrack) warp_max_to(rv, A.rtrack + (long long)sidx * SFD_RSLOTS);
+  if (A.bnorm) warp_max_to(bv, A.bnorm + sidx);
+}
+
+cudaError_t sfd_launch_sums_f32(const SumArgs& A, int nwork, int max_n, cudaStream_t st) {
+  if (nwork == 0) return cudaSuccess;
+  // the widest slice of any surface: at most 256 sources up to n = 4096 (16
+  // slices), then ceil(n / 16) <= 512
+  const size_t smem = (size_t)std::max(256, (max_n + 15) / 16) * 2 * sizeof(float4);
+  k_sums_f32<<<nwork, kF32Threads, smem, st>>>(A);
+  return cudaPeekAtLastError();
 }
 
 // Velocities and Bernoulli:
@@ -544,6 +805,27 @@ __global__ void k_velocity_bernoulli(VelArgs V) {
   V.dphi[g] = out;
   if (V.daux && !S.drive_aug) V.daux[g] = 0.0;
   if (!isfinite(out) || !isfinite(low.re) || !isfinite(low.im)) atomicOr(V.status + s, SFD_ST_NONFINITE);
+  if (V.rslot && g == S.off) {
+    // Refinement summary of this evaluation: the final residual is the first
+    // slot at or below tol * max |phi'| (the gated passes after it did not
+    // run), else the last slot; a final residual above it is a stall.
+    const double* sl = V.rslot + (long long)s * SFD_RSLOTS;
+    const double b = V.bnorm[s];
+    const double lim = V.tol * b;
+    int i = 0;
+    double fin = sl[0];
+    if (V.tol > 0.0)
+      while (!(fin <= lim) && i + 1 < V.nslots) fin = sl[++i];
+    if (i > 0) atomicAdd(V.extra_count + s, (unsigned long long)i);
+    atomicMax(reinterpret_cast<unsigned long long*>(V.rnorm) + s, (unsigned long long)__double_as_longlong(fin));
+    const double rel = b > 0.0 ? fin / b : (fin > 0.0 ? 1e300 : 0.0);
+    atomicMax(reinterpret_cast<unsigned long long*>(V.rrel) + s,
+              (unsigned long long)__double_as_longlong(rel == rel ? rel : 1e300));
+    if (V.tol > 0.0 && !(fin <= lim)) {
+      atomicOr(V.status + s, SFD_ST_REFINE_STALL);
+      if (V.stall_host) *reinterpret_cast<volatile unsigned int*>(V.stall_host) = 1u;
+    }
+  }
 }
 
 // The water cross term reads the lower velocity of concatenated node 1

@@ -41,10 +41,25 @@ struct SumArgs {
   cd* cacc;
   cd* dacc;
   double* r;
-  double* rnorm;        // per-surface max |r| (nullable)
+  double* rtrack;       // residual slot of this pass: per-surface max |r| at rtrack[s * SFD_RSLOTS] (nullable)
   int mode;             // 0: overwrite C/D and r = phi' - M a; 1: accumulate, r -= M a
   float* rf;            // FP32 copy of r for the preconditioner product (nullable)
+  double* bnorm;        // mode 0: per-surface max |phi'| (nullable)
+  Gate gate;            // extra corrections: skip surfaces whose previous residual is converged
+  // FP32 pass (k_sums_f32): one CTA per (tile, source slice); the last CTA
+  // of a tile to finish reduces the slices in order and runs the epilogue
+  const int4* swork;    // (item, slice, first work entry of the item, slices of the item)
+  float4* spart;        // per work entry: 64 target partials (S re, S im, T re, T im)
+  float2* swsum;        // per work entry: weight-sum partial (double-float)
+  unsigned int* scount; // per item: slices finished (the last one resets it)
 };
+
+// Source slices of one 64-target tile in the FP32 pass: about 256 sources
+// each, at most 16.
+__host__ __device__ __forceinline__ int sfd_f32_slices(int n) {
+  const int s = (n + 255) / 256;
+  return s < 1 ? 1 : (s > 16 ? 16 : s);
+}
 
 struct VelArgs {
   const SurfaceDesc* surf;
@@ -69,11 +84,23 @@ struct VelArgs {
   double* dy;
   double* dphi;
   unsigned int* status;
+  // refinement bookkeeping of the solve (rslot null: none)
+  const double* rslot;  // residual slots, SFD_RSLOTS per surface
+  int nslots;           // slots the solve can fill: 1 + extra corrections
+  const double* bnorm;  // per-surface max |phi'|
+  double tol;           // relative residual tolerance (<= 0: no stall check)
+  double* rnorm;        // per-surface max over evaluations of the final |r| (absolute)
+  double* rrel;         // the same relative to max |phi'|
+  unsigned long long* extra_count;  // per-surface count of extra corrections run
+  unsigned int* stall_host;         // host-mapped word set on a refinement stall (nullable)
 };
 
 __global__ void k_node_prep(const SurfaceDesc* surf, const int* node_surf, int ntot, const double* x,
-                            const double* y, const cd* zp, const cd* zpp, NodeData nd);
+                            const double* y, const cd* zp, const cd* zpp, NodeData nd, double* rslot,
+                            double* bnorm);
 cudaError_t sfd_launch_sums(int prec, const SumArgs& A, int nitems, int max_n, int groups, cudaStream_t st);
+// FP32 pass over `nwork` (tile, slice) entries (A.swork).
+cudaError_t sfd_launch_sums_f32(const SumArgs& A, int nwork, int max_n, cudaStream_t st);
 cudaError_t sfd_sums_configure();
 __global__ void k_velocity_bernoulli(VelArgs V);
 __global__ void k_velocity_node1(VelArgs V);
@@ -82,6 +109,24 @@ __global__ void k_rk4_stage(int n3, const double* y0, const double* k, double* k
 __global__ void k_rk4_final(int n3, double* y0, const double* kacc, double c);
 __global__ void k_invariants(const SurfaceDesc* surf, const double* x, const double* y, const double* phi,
                              const cd* zp, const double* u, const double* v, double kappa, double* out);
+
+// Four-step transforms of power-of-two surfaces (sfd_fft4.cu): jobs write z'
+// and z'' (from one forward transform), phi', or a'.
+enum : int { SFD_F4_Z = 0, SFD_F4_PHI = 1, SFD_F4_AP = 2 };
+struct F4Job {
+  int surf;
+  int kind;
+  long long scr0, scr1;  // scratch offsets (complex elements): rows of the job, and z'' rows for SFD_F4_Z
+};
+// The jobs of one spectral launch and their unit lists (job, unit) per phase.
+struct F4Plan {
+  F4Job* jobs = nullptr;
+  int2* units[3] = {nullptr, nullptr, nullptr};
+  int nunits[3] = {0, 0, 0};
+  int njobs = 0;
+};
+bool sfd_f4_eligible(int n);
+cudaError_t sfd_launch_f4(const DerivArgs& A, const F4Plan& p, cd* scr, cudaStream_t st, int phase);
 
 cudaError_t sfd_launch_spectral(const DerivArgs& A, const int2* jobs, int njobs, int max_n, cudaStream_t st);
 cudaError_t sfd_launch_spectral_cluster(const DerivArgs& A, const int2* jobs, int njobs, int max_n, cudaStream_t st);

@@ -218,6 +218,130 @@ __global__ void __launch_bounds__(64) k_lu64_trsm(const SurfaceDesc* surf, int n
   }
 }
 
+// Partial-pivoting panel of step kb (LAPACK getf2 on the tall panel): one CTA
+// per surface walks the 64 columns of [k0, np) x [k0, k0 + 64) in global
+// memory (L2-resident): pivot search (largest |a_ik|, first row on ties, as
+// idamax), row exchange inside the panel, scaling by the pivot, rank-1 update
+// of the panel's remaining columns.  The exchanges outside the panel are
+// applied afterwards by k_lu64_swap.  A zero pivot sets SFD_ST_ZERO_PIVOT and
+// an exchange SFD_ST_PIVOT_SWAP.  This is the fallback / reference-semantics
+// path, so it favours simplicity over speed: the exchange-free LU above is the
+// fast path.
+__global__ void __launch_bounds__(1024) k_lu64_panel_piv(const SurfaceDesc* surf, int nsurf, int kb, double* mat,
+                                                         int* piv, unsigned int* status) {
+  const int s = blockIdx.x;
+  if (s >= nsurf) return;
+  const SurfaceDesc& S = surf[s];
+  const int np = pad_n(S.n), k0 = kb * 64;
+  if (k0 >= np) return;
+  double* A = mat + S.moff;
+  __shared__ double rv[32];
+  __shared__ int ri[32];
+  __shared__ int sp;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+  for (int c = 0; c < 64; ++c) {
+    const int k = k0 + c;
+    // pivot search over rows [k, np)
+    double best = -1.0;
+    int bi = np;
+    for (int i = k + tid; i < np; i += blockDim.x) {
+      const double v = fabs(A[(long long)i * np + k]);
+      if (v > best) { best = v; bi = i; }  // rows ascend per thread: first maximum kept
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const double ov = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+    }
+    if (lane == 0) { rv[warp] = best; ri[warp] = bi; }
+    __syncthreads();
+    if (tid == 0) {
+      double b = rv[0];
+      int i0 = ri[0];
+      for (int w = 1; w < nw; ++w)
+        if (rv[w] > b || (rv[w] == b && ri[w] < i0)) { b = rv[w]; i0 = ri[w]; }
+      if (i0 >= np) i0 = k;  // NaN column: keep the diagonal
+      if (!(b > 0.0)) atomicOr(status + s, SFD_ST_ZERO_PIVOT);
+      if (i0 != k) atomicOr(status + s, SFD_ST_PIVOT_SWAP);
+      piv[(long long)s * np + k] = i0;
+      sp = i0;
+    }
+    __syncthreads();
+    const int p = sp;
+    if (p != k && tid < 64) {
+      double* rk = A + (long long)k * np + k0;
+      double* rp = A + (long long)p * np + k0;
+      const double t = rk[tid];
+      rk[tid] = rp[tid];
+      rp[tid] = t;
+    }
+    __syncthreads();
+    const double inv = 1.0 / A[(long long)k * np + k];
+    for (int i = k + 1 + tid; i < np; i += blockDim.x) A[(long long)i * np + k] *= inv;
+    __syncthreads();
+    const int w = 63 - c;  // remaining panel columns
+    if (w > 0) {
+      const double* rk = A + (long long)k * np + k + 1;
+      for (long long e = tid; e < (long long)(np - k - 1) * w; e += blockDim.x) {
+        const int i = k + 1 + (int)(e / w), j = (int)(e % w);
+        double* ai = A + (long long)i * np + k;
+        ai[1 + j] -= ai[0] * rk[j];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Row exchanges of panel kb applied to the columns outside the panel, one
+// thread per column, the panel's 64 exchanges in order.
+__global__ void __launch_bounds__(256) k_lu64_swap(const SurfaceDesc* surf, int nsurf, int kb, double* mat,
+                                                   const int* piv) {
+  const int s = blockIdx.y;
+  if (s >= nsurf) return;
+  const SurfaceDesc& S = surf[s];
+  const int np = pad_n(S.n), k0 = kb * 64;
+  if (k0 >= np) return;
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= np - 64) return;
+  if (j >= k0) j += 64;  // skip the panel's own columns
+  double* A = mat + S.moff;
+  const int* P = piv + (long long)s * np;
+  for (int c = 0; c < 64; ++c) {
+    const int k = k0 + c, p = P[k];
+    if (p != k) {
+      const double t = A[(long long)k * np + j];
+      A[(long long)k * np + j] = A[(long long)p * np + j];
+      A[(long long)p * np + j] = t;
+    }
+  }
+}
+
+// U12 tiles of step kb: columns tile*64 + t solve L11 x = a (L11 unit lower),
+// the U12 branch of k_lu64_trsm on its own (the pivoted panel already holds L21).
+__global__ void __launch_bounds__(64) k_lu64_trsm_u(const SurfaceDesc* surf, int nsurf, int kb, double* mat) {
+  const int s = blockIdx.z;
+  if (s >= nsurf) return;
+  const SurfaceDesc& S = surf[s];
+  const int np = pad_n(S.n), k0 = kb * 64;
+  const int tile = kb + 1 + blockIdx.x;
+  if (tile * 64 >= np) return;
+  double* A = mat + S.moff;
+  extern __shared__ double trsm_smem[];  // 2 x 64 x 65 doubles (kTrsmSmem bytes)
+  double(*D)[65] = reinterpret_cast<double(*)[65]>(trsm_smem);
+  double(*X)[65] = reinterpret_cast<double(*)[65]>(trsm_smem + 64 * 65);
+  load_tile<64, 16>(&D[0][0], 65, A + (long long)k0 * np + k0, np, 64, 64);
+  load_tile<64, 16, true>(&X[0][0], 65, A + (long long)k0 * np + tile * 64, np, 64, 64);
+  __syncthreads();
+  const int t = threadIdx.x;
+  for (int r = 0; r < 64; ++r) {
+    double v = X[t][r];
+    for (int q = 0; q < r; ++q) v -= D[r][q] * X[t][q];
+    X[t][r] = v;
+  }
+  __syncthreads();
+  for (int e = t; e < 64 * 64; e += 64) A[(long long)(k0 + (e >> 6)) * np + tile * 64 + (e & 63)] = X[e & 63][e >> 6];
+}
+
 // Trailing update A22 -= L21 U12 for step kb: 32x32 output tiles (four per
 // 64x64 block, so small matrices still fill the GPU), K = 64, 2x2 outputs per
 // thread.  grid = (2 rem, 2 rem, surfaces).
@@ -254,13 +378,31 @@ __global__ void __launch_bounds__(256) k_lu64_gemm(const SurfaceDesc* surf, int 
 // 64-row blocks: block dot products by all warps, then warp 0 finishes the
 // 64x64 triangle.  x (length n) is overwritten with the solution.
 __global__ void __launch_bounds__(256) k_lu64_solve(const SurfaceDesc* surf, const double* mat, const double* b,
-                                                    double* x) {
-  const SurfaceDesc& S = surf[blockIdx.x];
+                                                    double* x, double* acc, const int* piv, Gate gate,
+                                                    const double* lmax, unsigned int* status) {
+  const int s = blockIdx.x;
+  if (!gate_open(gate, s)) return;
+  const SurfaceDesc& S = surf[s];
   const int n = S.n, np = pad_n(n), off = S.off;
   const double* A = mat + S.moff;
+  if (lmax && threadIdx.x == 0 && lmax[s] > 1.0) atomicOr(status + s, SFD_ST_PIVOT_SWAP);
   extern __shared__ double xs[];  // np doubles
   for (int i = threadIdx.x; i < np; i += 256) xs[i] = i < n ? b[off + i] : 0.0;
   __syncthreads();
+  if (piv) {  // row exchanges of the factorisation, in order (getrs applies them to b first)
+    if (threadIdx.x == 0) {
+      const int* P = piv + (long long)s * np;
+      for (int k = 0; k < n; ++k) {
+        const int p = P[k];
+        if (p != k && p >= 0 && p < np) {
+          const double t = xs[k];
+          xs[k] = xs[p];
+          xs[p] = t;
+        }
+      }
+    }
+    __syncthreads();
+  }
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nblk = np / 64;
   // forward: x_i = b_i - sum_{j<i} L_ij x_j
@@ -306,7 +448,10 @@ __global__ void __launch_bounds__(256) k_lu64_solve(const SurfaceDesc* surf, con
     }
     __syncthreads();
   }
-  for (int i = threadIdx.x; i < n; i += 256) x[off + i] = xs[i];
+  for (int i = threadIdx.x; i < n; i += 256) {
+    if (x) x[off + i] = xs[i];
+    if (acc) acc[off + i] += xs[i];
+  }
 }
 
 // =============================================================== FP32 Gauss-Jordan inverse
@@ -613,8 +758,10 @@ __device__ __forceinline__ void gemv_store(float yr, int g, double* y, float2* y
 }
 
 __global__ void __launch_bounds__(256) k_gemv(const SurfaceDesc* surf, const int2* rowblk, const float* mat,
-                                              const float* v, double* y, float2* ydf, double* accv, float2* accdf) {
+                                              const float* v, double* y, float2* ydf, double* accv, float2* accdf,
+                                              Gate gate) {
   const int2 rb = rowblk[blockIdx.x];  // (surface, first row)
+  if (!gate_open(gate, rb.x)) return;
   const SurfaceDesc& S = surf[rb.x];
   const int n = S.n, np = pad_n(n), off = S.off;
   extern __shared__ float4 vs4[];
@@ -693,7 +840,7 @@ __global__ void __launch_bounds__(256) k_precond_to_half(const SurfaceDesc* surf
 // latency overlaps the first matrix loads.
 __global__ void __launch_bounds__(512) k_gemv_h(const SurfaceDesc* surf, const int2* rowblk, const __half* mat16,
                                                 const float* rscale, const float* v, double* y, float2* ydf,
-                                                double* accv, float2* accdf) {
+                                                double* accv, float2* accdf, Gate gate) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   // row blocks from the list, or (rowblk null: one surface) rows interleaved
   // over the grid, r = block + grid * warp, so every SM gets the same number
@@ -707,6 +854,7 @@ __global__ void __launch_bounds__(512) k_gemv_h(const SurfaceDesc* surf, const i
     sidx = 0;
     r = blockIdx.x + gridDim.x * warp;
   }
+  if (!gate_open(gate, sidx)) return;
   const SurfaceDesc& S = surf[sidx];
   const int n = S.n, np = pad_n(n), off = S.off;
   extern __shared__ float4 vsh[];

@@ -19,7 +19,22 @@ __global__ void k_lu64_diag(const SurfaceDesc* surf, int nsurf, int kb, double* 
                             double* lmax);
 __global__ void k_lu64_trsm(const SurfaceDesc* surf, int nsurf, int kb, double* mat, double* lmax);
 __global__ void k_lu64_gemm(const SurfaceDesc* surf, int nsurf, int kb, double* mat);
-__global__ void k_lu64_solve(const SurfaceDesc* surf, const double* mat, const double* b, double* x);
+// x = (LU)^-1 b per surface (b, x at the surface's node offset; x may be
+// null); acc (nullable) += the solution; piv (nullable) = row exchanges of a
+// pivoted factorisation, applied to b first; where lmax[s] > 1 the surface's
+// status gets SFD_ST_PIVOT_SWAP (lmax, status nullable); gated surfaces skip.
+__global__ void k_lu64_solve(const SurfaceDesc* surf, const double* mat, const double* b, double* x, double* acc,
+                             const int* piv, Gate gate, const double* lmax, unsigned int* status);
+// Blocked LU with partial pivoting (getrf semantics: the first row of largest
+// magnitude in the column is the pivot).  Step kb: k_lu64_panel_piv factors
+// the 64-column panel [k0, np) x [k0, k0 + 64) in place and records the
+// pivot rows piv[s * np + k] (absolute row indices); k_lu64_swap applies the
+// panel's exchanges to the columns outside it; then the U12 part of
+// k_lu64_trsm (blockIdx.y == 1) and k_lu64_gemm complete the step.
+__global__ void k_lu64_panel_piv(const SurfaceDesc* surf, int nsurf, int kb, double* mat, int* piv,
+                                 unsigned int* status);
+__global__ void k_lu64_swap(const SurfaceDesc* surf, int nsurf, int kb, double* mat, const int* piv);
+__global__ void k_lu64_trsm_u(const SurfaceDesc* surf, int nsurf, int kb, double* mat);
 __global__ void k_gj_diag(const SurfaceDesc* surf, int nsurf, int kb, float* mat, float* pbuf, unsigned int* status);
 __global__ void k_gj_panel(const SurfaceDesc* surf, int nsurf, int kb, const float* mat, const float* pbuf,
                            float* rbuf, float* cbuf, const long long* poff, __nv_bfloat16* cparts,
@@ -30,10 +45,10 @@ __global__ void k_precond_to_half(const SurfaceDesc* surf, const int2* rowblk, c
                                   float* rscale);
 // y = X v (v FP32); optional double-float copy of y and in-place acc += y
 __global__ void k_gemv_h(const SurfaceDesc* surf, const int2* rowblk, const __half* mat16, const float* rscale,
-                         const float* v, double* y, float2* ydf, double* acc, float2* accdf);
+                         const float* v, double* y, float2* ydf, double* acc, float2* accdf, Gate gate);
 cudaError_t sfd_tc_configure();
 cudaError_t sfd_launch_gj_update_tc(const SurfaceDesc* surf, int nsurf, int kb, int max_np, float* mat,
                                     const __nv_bfloat16* cparts, const __nv_bfloat16* rparts, long long part_stride,
                                     const long long* poff, unsigned int* status, cudaStream_t st);
 __global__ void k_gemv(const SurfaceDesc* surf, const int2* rowblk, const float* mat, const float* v, double* y,
-                       float2* ydf, double* acc, float2* accdf);
+                       float2* ydf, double* acc, float2* accdf, Gate gate);

@@ -99,6 +99,10 @@ class Options:
     autotune       time the boundary-sum CTA shapes on the first steps
     refactor_lag   mixed, stepping: rebuild on a side stream and switch k steps
                    later (0 < k < refactor_every; 0 rebuilds inside the step)
+    extra_iters    extra corrections of the solve (0..4), run only where the
+                   relative residual is above refine_tol
+    refine_tol     relative residual tolerance max|phi' - M a| / max|phi'|
+                   (<= 0: no check)
     """
     precision: int = PRECISION_MIXED
     refine_iters: int = 2
@@ -110,12 +114,14 @@ class Options:
     precond_half: bool = True
     autotune: bool = True
     refactor_lag: int = 0
+    extra_iters: int = 2
+    refine_tol: float = 1e-10
 
     def to_c(self) -> _lib.SfdOptions:
         return _lib.SfdOptions(self.precision, self.refine_iters, self.refactor_every,
                                1 if self.use_graphs else 0, self.device, 1 if self.tensor_cores else 0,
                                self.pre_iters, 1 if self.precond_half else 0, 1 if self.autotune else 0,
-                               self.refactor_lag)
+                               self.refactor_lag, self.extra_iters, float(self.refine_tol))
 
 
 class Engine:
@@ -287,6 +293,17 @@ class Engine:
 
     def clear_status(self) -> None:
         check(self._L.sfd_clear_status(self._h))
+
+    def refinement(self) -> dict:
+        """Refinement record since the last clear_status: per-surface max final
+        relative residual and extra corrections run, and the preconditioner
+        rebuilds a refinement stall triggered."""
+        rel = np.empty(self.nsurf)
+        extra = (ctypes.c_longlong * self.nsurf)()
+        rb = ctypes.c_longlong(0)
+        check(self._L.sfd_get_refinement(self._h, _dp(rel), extra, ctypes.byref(rb)))
+        return {"rel_residual": rel, "extra_iters": np.array(list(extra), dtype=np.int64),
+                "stall_rebuilds": int(rb.value)}
 
     def set_stream(self, stream_ptr: int) -> None:
         check(self._L.sfd_set_stream(self._h, stream_ptr))

@@ -16,10 +16,15 @@ int main(void) {
   sfd_options o;
   sfd_default_options(&o);
   if (o.precision != SFD_PRECISION_MIXED || o.use_graphs != 1 || o.refactor_lag != 0) return fail("default options");
+  if (o.extra_iters != 2 || o.refine_tol != 1e-10) return fail("default refinement options");
   sfd_problem p;
   sfd_default_problem(&p);
   if (p.physics != SFD_WATER || p.gravity != 1.0) return fail("default problem");
   sfd_engine* e = NULL;
+  const int n64[1] = {64};
+  o.extra_iters = 5;
+  if (sfd_create(n64, 1, &p, 1, &o, &e) != SFD_ERR_INVALID || e != NULL) return fail("extra_iters > 4 refused");
+  o.extra_iters = 2;
   if (sfd_create(NULL, 1, &p, 1, &o, &e) != SFD_ERR_INVALID || e != NULL) return fail("null sizes refused");
   if (strlen(sfd_last_error()) == 0) return fail("error message set");
   if (sfd_rk4_steps(NULL, 0.01, 1) != SFD_ERR_INVALID) return fail("null engine refused");

@@ -12,6 +12,7 @@ Sources of truth:
     (the point used by ComplexFunctionsTests.cuh:169-244).
 
 Usage: python tests/golden/make_golden.py [/path/to/reference]
+The reference location is the argument, else $SFD_REFERENCE_DIR.
 """
 import json
 import os
@@ -20,7 +21,9 @@ import sys
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SFD_REFERENCE_DIR", "")
+if not REF or not os.path.isdir(REF):
+    raise SystemExit("give the reference checkout as the argument or in SFD_REFERENCE_DIR")
 sys.path.insert(0, os.path.join(REF, "CuSuperHelium", "Python"))
 sys.path.insert(0, os.path.join(HERE, "..", ".."))
 

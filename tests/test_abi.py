@@ -25,6 +25,8 @@ def test_version_and_defaults_without_gpu():
     o = _lib.SfdOptions()
     L.sfd_default_options(ctypes.byref(o))
     assert o.precision == _lib.PRECISION_MIXED and o.refine_iters >= 1
+    # the refinement fields sit after refactor_lag, past 4 bytes of padding
+    assert o.extra_iters == 2 and o.refine_tol == 1e-10 and ctypes.sizeof(_lib.SfdOptions) == 56
     p = _lib.SfdProblem()
     L.sfd_default_problem(ctypes.byref(p))
     assert p.physics == _lib.WATER and p.gravity == 1.0

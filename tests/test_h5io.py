@@ -11,7 +11,8 @@ import pytest
 
 from superfluid_dynamics_gb300 import h5io
 
-_REF = "/root/reference/CuSuperHelium/Python"
+# the reference checkout, when this machine has one (SFD_REFERENCE_DIR)
+_REF = os.path.join(os.environ.get("SFD_REFERENCE_DIR", ""), "CuSuperHelium", "Python")
 _FILES = [os.path.join(_REF, "integration", "simulation_15modes.h5"),
           os.path.join(_REF, "simulation_gaussian_highampl0.1.h5")]
 
