@@ -85,6 +85,21 @@ def test_golden_reference_numpy(name):
     assert rel(a, d["a"]) < 1e-11
 
 
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+@pytest.mark.parametrize("name", ["ref_helium_n128_h10", "ref_helium_n128_h5", "ref_helium_n256_h8",
+                                  "ref_water_n128_modes"])
+def test_golden_reference_cuda_path(name, prec):
+    """The engine against outputs of the reference's own FP64 CUDA path
+    (tests/golden/make_ref_fixtures.py): helium with A3 = h^4/3, and water."""
+    d = np.load(os.path.join(GOLD, name + ".npz"))
+    n, h = d["x"].size, float(d["depth"])
+    phys = sfd.HeliumBoundaryProblem(h) if "helium" in name else sfd.WaterBoundaryProblem()
+    (dx, dy, dphi, a, zp, zpp), _ = engine_rhs(n, phys, d["x"], d["y"], d["phi"], prec)
+    assert rel(dx + 1j * dy, d["vx"] + 1j * d["vy"]) < TOL[prec]
+    assert rel(dphi, d["dphi"]) < TOL[prec]
+    assert rel(a, d["a"]) < TOL[prec]
+
+
 def stokes(N, h, omega, t):
     j = 2 * np.pi * np.arange(N) / N
     X = j - h * np.sin(j - omega * t)

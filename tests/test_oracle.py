@@ -7,6 +7,10 @@ known-answer tests of the reference's gtest suite, re-derived here:
   MatrixMTests.cuh:51-67,477-607   spectral derivatives of a Lagrangian Stokes wave, N=1024
   MatrixMTests.cuh:735-820         water Bernoulli, N=32
   ComplexFunctionsTests.cuh:169-244 cot Green's function vs a 50-digit value
+and against outputs of the reference's own FP64 CUDA path (fixtures made by
+tests/golden/make_ref_fixtures.py with oracle/ref_harness.cu): finite-depth
+helium films (createFiniteDepthMKernel, createHeliumVelocityMatrices,
+compute_rhs_helium_phi_expression with A3 = h^4/3) and a water surface.
 """
 import cmath
 import json
@@ -203,3 +207,18 @@ def test_oracle_conserves_energy_and_mass():
         drift.append(abs((i1[0] + i1[1]) - (i0[0] + i0[1])) / abs(i0[0] + i0[1]))
         assert abs(i1[4] - i0[4]) < 1e-14
     assert drift[0] < 1e-11 and drift[0] / drift[1] > 16.0, drift
+
+
+# --- the reference's own FP64 CUDA path (oracle/ref_harness.cu)
+REF_CASES = ["ref_helium_n128_h10", "ref_helium_n128_h5", "ref_helium_n256_h8", "ref_water_n128_modes"]
+
+
+@pytest.mark.parametrize("name", REF_CASES)
+def test_oracle_matches_reference_cuda_path(name):
+    d = np.load(os.path.join(GOLD, name + ".npz"))
+    h = float(d["depth"])
+    prob = O.Problem(physics=O.HELIUM, depth=h) if "helium" in name else O.Problem()
+    (vx, vy, dphi, a, _, _), info = O.rhs(prob, d["x"], d["y"], d["phi"], diagnostics=True)
+    assert rel(vx + 1j * vy, d["vx"] + 1j * d["vy"]) < 1e-12
+    assert rel(dphi, d["dphi"]) < 1e-12
+    assert rel(a, d["a"]) < 1e-12
