@@ -15,13 +15,15 @@
 //            multiplier of the global mode k = k2 + N2 k1, the inverse row
 //            FFTs (z' and z'' share the forward row FFT), times W_n^{-n1 k2}
 //   phase 3  inverse column FFTs over k2, scaling, output
-// Each FFT of length L = 8 P is one unit of 8 threads: thread t holds
-// x[t + 8 j] (j < P), does a P-point DFT in registers, multiplies by
-// W_L^{t ka}, exchanges through shared memory and finishes with 8-point DFTs
-// (thread t then holds X[t + 8 q + P kb]).  The row phase needs no exchange
-// between the forward and the inverse transform: the forward leaves thread t
-// holding exactly the inputs its inverse needs.  Units of one job are
-// contiguous and a multiple of 4, so a warp's four units share their length.
+// Each FFT of length L (8 <= L <= 128) belongs to one warp: lane l holds the
+// elements l + 32 q (q < L / 32; for L < 32 lanes l >= L idle), and the
+// transform is radix-2 across lanes by shuffles (and across a lane's own
+// elements for spans of 64 and more), so a lane's dependent chain is about
+// 3 FP64 operations and one shuffle per pass.  The forward transform is the
+// decimation in frequency (natural order in, bit-reversed out), the inverse
+// the decimation in time (bit-reversed in, natural out), so the row phase
+// runs forward, multiplier and inverse on the same registers.  Each CTA is
+// one warp; its shared memory holds W_L^e.
 // Intermediate rows and columns go through an L2-resident scratch (16 bytes
 // per node and output).
 #include "sfd_engine.cuh"
@@ -29,116 +31,97 @@
 
 namespace {
 
-constexpr double kH = 0.70710678118654752440;          // cos(pi/4)
-constexpr double kC8 = 0.92387953251128675613;         // cos(pi/8)
-constexpr double kS8 = 0.38268343236508977173;         // sin(pi/8)
-
-__device__ __forceinline__ cd rot(cd a, int sign) { return sign < 0 ? cd{a.im, -a.re} : cd{-a.im, a.re}; }
-
-// Natural-order DFTs in registers (sign -1: exp(-2 pi i jk / P), +1: inverse
-// without 1/P).
-__device__ __forceinline__ void dft2(cd* v) {
-  const cd a = v[0], b = v[1];
-  v[0] = a + b;
-  v[1] = a - b;
-}
-__device__ __forceinline__ void dft4(cd* v, int sign) {
-  const cd a0 = v[0] + v[2], a1 = v[0] - v[2];
-  const cd b0 = v[1] + v[3], b1 = rot(v[1] - v[3], sign);
-  v[0] = a0 + b0;
-  v[1] = a1 + b1;
-  v[2] = a0 - b0;
-  v[3] = a1 - b1;
-}
-// W_8^k (k < 4) times a, for the given sign
-__device__ __forceinline__ cd w8mul(cd a, int k, int sign) {
-  const double s = sign < 0 ? -1.0 : 1.0;
-  switch (k) {
-    case 0: return a;
-    case 1: return cd{kH * (a.re - s * a.im), kH * (a.im + s * a.re)};
-    case 2: return rot(a, sign);
-    default: return cd{kH * (-a.re - s * a.im), kH * (-a.im + s * a.re)};
-  }
-}
-__device__ __forceinline__ void dft8(cd* v, int sign) {
-  cd e[4] = {v[0], v[2], v[4], v[6]}, o[4] = {v[1], v[3], v[5], v[7]};
-  dft4(e, sign);
-  dft4(o, sign);
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const cd t = w8mul(o[k], k, sign);
-    v[k] = e[k] + t;
-    v[k + 4] = e[k] - t;
-  }
-}
-// W_16^k (k < 8) times a
-__device__ __forceinline__ cd w16mul(cd a, int k, int sign) {
-  if ((k & 1) == 0) return w8mul(a, k >> 1, sign);
-  const double s = sign < 0 ? -1.0 : 1.0;
-  double c, sn;  // cos and sin of 2 pi k / 16 for odd k
-  switch (k) {
-    case 1: c = kC8; sn = kS8; break;
-    case 3: c = kS8; sn = kC8; break;
-    case 5: c = -kS8; sn = kC8; break;
-    default: c = -kC8; sn = kS8; break;
-  }
-  sn *= s;  // exp(s i 2 pi k / 16)
-  return cd{a.re * c - a.im * sn, a.re * sn + a.im * c};
-}
-__device__ __forceinline__ void dft16(cd* v, int sign) {
-  cd e[8], o[8];
-#pragma unroll
-  for (int j = 0; j < 8; ++j) {
-    e[j] = v[2 * j];
-    o[j] = v[2 * j + 1];
-  }
-  dft8(e, sign);
-  dft8(o, sign);
-#pragma unroll
-  for (int k = 0; k < 8; ++k) {
-    const cd t = w16mul(o[k], k, sign);
-    v[k] = e[k] + t;
-    v[k + 8] = e[k] - t;
-  }
-}
-template <int P>
-__device__ __forceinline__ void dftP(cd* v, int sign) {
-  if constexpr (P == 2) dft2(v);
-  else if constexpr (P == 4) dft4(v, sign);
-  else if constexpr (P == 8) dft8(v, sign);
-  else if constexpr (P == 16) dft16(v, sign);
-}
-
-__device__ __forceinline__ cd twid(const cd* tw, long long e, int sign) {
+__device__ __forceinline__ cd twid(const cd* tw, int e, int sign) {
   const cd t = tw[e];
   return sign < 0 ? t : cd{t.re, -t.im};
 }
+__device__ __forceinline__ cd shfl_xor_cd(cd a, int m) {
+  return {__shfl_xor_sync(0xffffffffu, a.re, m), __shfl_xor_sync(0xffffffffu, a.im, m)};
+}
 
-// Length L = 8 P FFT of one unit (8 threads, t = lane % 8).  In: v[j] =
-// x[t + 8 j], j < P.  Out: v[q * 8 + kb] = X[ka + P kb] for ka = t + 8 q
-// (q < max(1, P / 8); for P < 8 only threads t < P hold outputs).  tw: W_n^e
-// with n = L * tws; sm: 8 P complex values of shared memory for this unit.
-template <int P>
-__device__ __forceinline__ void unit_fft(cd* v, cd* sm, int t, const cd* tw, int tws, int sign) {
-  dftP<P>(v, sign);
+// 1 / n for a power of two n, built from the exponent bits (no FP64 division)
+__device__ __forceinline__ double inv_pow2(int n) {
+  const int e = __ffs(n) - 1;
+  return __longlong_as_double((long long)(1023 - e) << 52);
+}
+
+template <int L>
+struct WF {
+  static constexpr int Q = L >= 32 ? L / 32 : 1;  // elements per lane
+  static constexpr int LOG = L == 8 ? 3 : L == 16 ? 4 : L == 32 ? 5 : L == 64 ? 6 : 7;
+};
+template <int L>
+__device__ __forceinline__ int bitrev(int i) {
+  return (int)(__brev((unsigned)i) >> (32 - WF<L>::LOG));
+}
+
+// Forward-direction decimation in frequency (sign -1) or its conjugate (+1):
+// natural-order input, bit-reversed output.  twL[e] = W_L^e.
+template <int L>
+__device__ __forceinline__ void warp_dif(cd* v, const cd* twL, int lane, int sign) {
+  constexpr int Q = WF<L>::Q;
 #pragma unroll
-  for (int ka = 1; ka < P; ++ka)
-    if (t) v[ka] = v[ka] * twid(tw, (long long)t * ka * tws, sign);
+  for (int half = L / 2; half >= 1; half >>= 1) {
+    const int step = L / (2 * half);  // W_{2 half}^j = W_L^{j step}
+    if (half >= 32) {
+      const int h = half / 32;
 #pragma unroll
-  for (int ka = 0; ka < P; ++ka) sm[t * P + ka] = v[ka];
-  __syncwarp();
-  constexpr int Q = P >= 8 ? P / 8 : 1;
+      for (int q = 0; q < Q; ++q) {
+        if ((q / h) % 2 == 0) {
+          const int j = (lane + 32 * q) % (2 * half);
+          const cd a = v[q], b = v[q + h];
+          v[q] = a + b;
+          v[q + h] = (a - b) * twid(twL, j * step, sign);
+        }
+      }
+    } else {
+      const bool upper = (lane & half) != 0;
+      const int j = upper ? (lane % (2 * half)) - half : 0;
+      const cd w = upper ? twid(twL, j * step, sign) : cd{1.0, 0.0};
+      const double sg = upper ? -1.0 : 1.0;
 #pragma unroll
-  for (int q = 0; q < Q; ++q) {
-    const int ka = t + 8 * q;
-    cd b[8];
-#pragma unroll
-    for (int tt = 0; tt < 8; ++tt) b[tt] = (ka < P) ? sm[tt * P + ka] : cd{0.0, 0.0};
-    dft8(b, sign);
-#pragma unroll
-    for (int kb = 0; kb < 8; ++kb) v[q * 8 + kb] = b[kb];
+      for (int q = 0; q < Q; ++q) {
+        const cd own = v[q];
+        const cd p = shfl_xor_cd(own, half);
+        // upper lanes hold b and form (a - b) W, lower lanes a + b: one FMA per part
+        const cd t = {fma(sg, own.re, p.re), fma(sg, own.im, p.im)};
+        v[q] = t * w;
+      }
+    }
   }
-  __syncwarp();  // the unit's shared memory is reused by the caller
+}
+
+// Decimation in time: bit-reversed input, natural-order output.
+template <int L>
+__device__ __forceinline__ void warp_dit(cd* v, const cd* twL, int lane, int sign) {
+  constexpr int Q = WF<L>::Q;
+#pragma unroll
+  for (int half = 1; half < L; half <<= 1) {
+    const int step = L / (2 * half);
+    if (half >= 32) {
+      const int h = half / 32;
+#pragma unroll
+      for (int q = 0; q < Q; ++q) {
+        if ((q / h) % 2 == 0) {
+          const int j = (lane + 32 * q) % (2 * half);
+          const cd a = v[q], b = v[q + h] * twid(twL, j * step, sign);
+          v[q] = a + b;
+          v[q + h] = a - b;
+        }
+      }
+    } else {
+      const bool upper = (lane & half) != 0;
+      const int j = upper ? (lane % (2 * half)) - half : 0;
+      const cd w = upper ? twid(twL, j * step, sign) : cd{1.0, 0.0};
+      const double sg = upper ? -1.0 : 1.0;
+#pragma unroll
+      for (int q = 0; q < Q; ++q) {
+        const cd t = v[q] * w;  // upper lanes: b W; lower lanes: a
+        const cd p = shfl_xor_cd(t, half);
+        v[q] = {fma(sg, t.re, p.re), fma(sg, t.im, p.im)};  // upper: a - b W, lower: a + b W
+      }
+    }
+  }
 }
 
 // spectral multipliers, as in sfd_fft.cu (utilities.cuh:106-148, :178-200)
@@ -163,142 +146,154 @@ __device__ __forceinline__ double xi_node(int j, double dn, double inv_n) {
   return fma(r, inv_n, q0);
 }
 
-constexpr int kUnitsPerCta = 4;  // one warp
-constexpr int kF4Threads = 8 * kUnitsPerCta;
+// One warp (one unit: a row or column of one job) per CTA, so the units
+// spread over as many SMs as there are units: GB300's FP64 pipe issues a
+// warp's FP64 instruction about every 16 cycles, so an SM's FP64 pipe, not
+// latency, bounds a CTA of several units.
+constexpr int kWarpsPerCta = 1;
+constexpr int kF4Threads = 32 * kWarpsPerCta;
 
 }  // namespace
 
-// Phase 1: column FFTs.  Unit u of a job: n1 = u (64 units).
-template <int P>
-__device__ __forceinline__ void f4_phase1(const DerivArgs& A, const F4Job& J, const SurfaceDesc& S, int u, int t,
-                                          cd* sm, cd* scr) {
-  const int n = S.n, off = S.off;
-  const int n1 = u;
-  const double dn = (double)n, inv_n = 1.0 / dn;
+// Phase 1: forward column FFT over n2 for n1 = u, times W_n^{n1 k2}.
+template <int L>
+__device__ __forceinline__ void f4_phase1(const DerivArgs& A, const F4Job& J, const SurfaceDesc& S, int u,
+                                          int lane, const cd* twL, cd* scr) {
+  constexpr int Q = WF<L>::Q;
+  const int n = S.n, off = S.off, n1 = u;
+  const double dn = (double)n, inv_n = inv_pow2(n);
   const double rho = S.physics == 0 ? S.rho : 0.0;
-  const double uq = -(1 + rho) * SFD_PI * S.U / n;
-  cd v[P >= 8 ? P : 8];
-#pragma unroll
-  for (int j = 0; j < P; ++j) {
-    const int m = n1 + 64 * (t + 8 * j);  // node index
-    if (J.kind == SFD_F4_Z) v[j] = {A.x[off + m] - xi_node(m, dn, inv_n), A.y[off + m]};        // Derivatives.cuh:285,317
-    else if (J.kind == SFD_F4_PHI) v[j] = {A.phi[off + m] - uq * (double)m, A.phi_im ? A.phi_im[off + m] : 0.0};  // :286,318
-    else v[j] = {A.a[off + m], 0.0};                                                            // real_to_complex(a)
-  }
-  unit_fft<P>(v, sm, t, S.tw, n / (8 * P), -1);
-  constexpr int Q = P >= 8 ? P / 8 : 1;
+  const double uq = -(1 + rho) * SFD_PI * S.U * inv_n;  // n a power of two: exact as the division
+  cd v[Q], pw[Q];
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
-    const int ka = t + 8 * q;
-    if (ka < P) {
-#pragma unroll
-      for (int kb = 0; kb < 8; ++kb) {
-        const int k2 = ka + P * kb;
-        scr[J.scr0 + (long long)k2 * 64 + n1] = v[q * 8 + kb] * twid(S.tw, ((long long)n1 * k2) % n, -1);
-      }
+    const int i = lane + 32 * q;
+    const int k2 = bitrev<L>(i & (L - 1));
+    pw[q] = twid(S.tw, (n1 * k2) & (n - 1), -1);  // issued before the transform: its index is known
+    if (i < L) {
+      const int m = n1 + 64 * i;  // node index
+      if (J.kind == SFD_F4_Z) v[q] = {A.x[off + m] - xi_node(m, dn, inv_n), A.y[off + m]};          // Derivatives.cuh:285,317
+      else if (J.kind == SFD_F4_PHI) v[q] = {A.phi[off + m] - uq * (double)m, A.phi_im ? A.phi_im[off + m] : 0.0};  // :286,318
+      else v[q] = {A.a[off + m], 0.0};                                                              // real_to_complex(a)
+    } else {
+      v[q] = {0.0, 0.0};
     }
+  }
+  warp_dif<L>(v, twL, lane, -1);
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    const int i = lane + 32 * q;
+    if (i < L) scr[J.scr0 + (long long)bitrev<L>(i) * 64 + n1] = v[q] * pw[q];
   }
 }
 
-// Phase 2: row k2 = u: forward 64-point FFT, multiplier, inverse FFT(s).
-__device__ __forceinline__ void f4_phase2(const F4Job& J, const SurfaceDesc& S, int u, int t, cd* sm, cd* scr) {
+// Phase 2: row k2 = u: forward 64-point FFT, multiplier of mode k2 + N2 k1,
+// inverse FFT(s), times W_n^{-n1 k2}.
+__device__ __forceinline__ void f4_phase2(const F4Job& J, const SurfaceDesc& S, int u, int lane, const cd* twL,
+                                          cd* scr) {
+  constexpr int Q = 2;
   const int n = S.n, N2 = n / 64, k2 = u;
-  const double inv_n = 1.0 / (double)n;
+  const double inv_n = inv_pow2(n);
   cd* row = scr + J.scr0 + (long long)k2 * 64;
-  cd v[8];
+  cd v[Q], w[Q], pw[Q];
 #pragma unroll
-  for (int j = 0; j < 8; ++j) v[j] = row[t + 8 * j];
-  unit_fft<8>(v, sm, t, S.tw, n / 64, -1);  // v[kb] = X[k2 + N2 (t + 8 kb)]
+  for (int q = 0; q < Q; ++q) {
+    const int i = lane + 32 * q;
+    v[q] = row[i];
+    pw[q] = twid(S.tw, (i * k2) & (n - 1), +1);
+  }
+  warp_dif<64>(v, twL, lane, -1);  // element i holds X[k2 + N2 bitrev(i)]
   const bool second_too = J.kind == SFD_F4_Z;
-  cd w[8];
 #pragma unroll
-  for (int kb = 0; kb < 8; ++kb) {
-    const int k = k2 + N2 * (t + 8 * kb);
-    w[kb] = second_too ? second_mult(v[kb], k, n, inv_n) : v[kb];
-    v[kb] = first_mult(v[kb], k, n, inv_n);
+  for (int q = 0; q < Q; ++q) {
+    const int k = k2 + N2 * bitrev<64>(lane + 32 * q);
+    w[q] = second_too ? second_mult(v[q], k, n, inv_n) : v[q];
+    v[q] = first_mult(v[q], k, n, inv_n);
   }
-  // thread t holds the inverse transform's inputs m = t + 8 kb
-  unit_fft<8>(v, sm, t, S.tw, n / 64, +1);  // v[kb] = Y'[n1 = t + 8 kb]
+  warp_dit<64>(v, twL, lane, +1);  // element i holds Y'[n1 = i]
 #pragma unroll
-  for (int kb = 0; kb < 8; ++kb) {
-    const int n1 = t + 8 * kb;
-    row[n1] = v[kb] * twid(S.tw, ((long long)n1 * k2) % n, +1);
-  }
+  for (int q = 0; q < Q; ++q) row[lane + 32 * q] = v[q] * pw[q];
   if (second_too) {
-    unit_fft<8>(w, sm, t, S.tw, n / 64, +1);
+    warp_dit<64>(w, twL, lane, +1);
     cd* row2 = scr + J.scr1 + (long long)k2 * 64;
 #pragma unroll
-    for (int kb = 0; kb < 8; ++kb) {
-      const int n1 = t + 8 * kb;
-      row2[n1] = w[kb] * twid(S.tw, ((long long)n1 * k2) % n, +1);
-    }
+    for (int q = 0; q < Q; ++q) row2[lane + 32 * q] = w[q] * pw[q];
   }
 }
 
-// Phase 3: inverse column FFTs.  Unit u: output o = u / 64 (z' then z''
-// for the z job), column n1 = u % 64.
-template <int P>
-__device__ __forceinline__ void f4_phase3(const DerivArgs& A, const F4Job& J, const SurfaceDesc& S, int u, int t,
-                                          cd* sm, const cd* scr) {
+// Phase 3: inverse column FFT over k2.  Unit u: output o = u / 64 (z' then
+// z'' for the z job), column n1 = u % 64.
+template <int L>
+__device__ __forceinline__ void f4_phase3(const DerivArgs& A, const F4Job& J, const SurfaceDesc& S, int u,
+                                          int lane, const cd* twL, const cd* scr) {
+  constexpr int Q = WF<L>::Q;
   const int n = S.n, off = S.off;
   const int o = u >> 6, n1 = u & 63;
   const cd* col = scr + (o ? J.scr1 : J.scr0) + n1;
-  cd v[P >= 8 ? P : 8];
-#pragma unroll
-  for (int j = 0; j < P; ++j) v[j] = col[(long long)(t + 8 * j) * 64];
-  unit_fft<P>(v, sm, t, S.tw, n / (8 * P), +1);
-  const double s1 = 2.0 * SFD_PI / n;
-  const double s2 = 4.0 * SFD_PI * SFD_PI / ((double)n * n);
-  const double rho = S.physics == 0 ? S.rho : 0.0;
-  const double uq = -(1 + rho) * SFD_PI * S.U / n;
-  constexpr int Q = P >= 8 ? P / 8 : 1;
+  cd v[Q];
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
-    const int ka = t + 8 * q;
-    if (ka < P) {
+    const int i = lane + 32 * q;
+    v[q] = i < L ? col[(long long)bitrev<L>(i) * 64] : cd{0.0, 0.0};  // bit-reversed input
+  }
+  warp_dit<L>(v, twL, lane, +1);
+  // n is a power of two, so scaling by 1/n is exact and equals the division
+  const double inv_n = inv_pow2(n);
+  const double s1 = 2.0 * SFD_PI * inv_n;
+  const double s2 = 4.0 * SFD_PI * SFD_PI * inv_n * inv_n;
+  const double rho = S.physics == 0 ? S.rho : 0.0;
+  const double uq = -(1 + rho) * SFD_PI * S.U * inv_n;
 #pragma unroll
-      for (int kb = 0; kb < 8; ++kb) {
-        const int j = off + n1 + 64 * (ka + P * kb);
-        const cd x = v[q * 8 + kb];
-        if (J.kind == SFD_F4_Z) {
-          if (o == 0) A.zp[j] = {x.re * s1 + s1, x.im * s1};  // Derivatives.cuh:323,374
-          else A.zpp[j] = {x.re * s2, x.im * s2};           // :321
-        } else if (J.kind == SFD_F4_PHI) {
-          double r = x.re * s1;                             // :324, complex_to_real
-          if (S.U != 0) r += uq;                            // :380-383
-          A.phip[j] = r;
-          if (A.phipf) A.phipf[j] = (float)r;
-        } else {
-          A.ap[j] = {x.re * s1, x.im * s1};                 // BaseBoundaryIntegrator.cuh:203
-        }
-      }
+  for (int q = 0; q < Q; ++q) {
+    const int i = lane + 32 * q;
+    if (i >= L) continue;
+    const int j = off + n1 + 64 * i;
+    const cd x = v[q];
+    if (J.kind == SFD_F4_Z) {
+      if (o == 0) A.zp[j] = {x.re * s1 + s1, x.im * s1};  // Derivatives.cuh:323,374
+      else A.zpp[j] = {x.re * s2, x.im * s2};           // :321
+    } else if (J.kind == SFD_F4_PHI) {
+      double r = x.re * s1;                             // :324, complex_to_real
+      if (S.U != 0) r += uq;                            // :380-383
+      A.phip[j] = r;
+      if (A.phipf) A.phipf[j] = (float)r;
+    } else {
+      A.ap[j] = {x.re * s1, x.im * s1};                 // BaseBoundaryIntegrator.cuh:203
     }
   }
+}
+
+template <int PHASE, int L>
+__device__ __forceinline__ void f4_run(const DerivArgs& A, const F4Job& J, const SurfaceDesc& S, int u, int lane,
+                                       cd* twL, cd* scr) {
+  // W_L^e for this CTA's transform length (the CTA's units share one job)
+  for (int e = threadIdx.x; e < L; e += kF4Threads) twL[e] = S.tw[(long long)e * (S.n / L)];
+  __syncthreads();
+  if (PHASE == 1) f4_phase1<L>(A, J, S, u, lane, twL, scr);
+  else if (PHASE == 2) f4_phase2(J, S, u, lane, twL, scr);
+  else f4_phase3<L>(A, J, S, u, lane, twL, scr);
 }
 
 template <int PHASE>
 __global__ void __launch_bounds__(kF4Threads) k_fft4(DerivArgs A, const F4Job* jobs, const int2* units, int nunits,
                                                      cd* scr) {
-  __shared__ cd sm_all[kUnitsPerCta][8 * 16];
-  const int lane = threadIdx.x & 31, unit_in_cta = lane >> 3, t = lane & 7;
-  const int ui = blockIdx.x * kUnitsPerCta + unit_in_cta;
-  if (ui >= nunits) return;  // unit counts are multiples of 4: whole warps leave together
+  __shared__ cd twL[128];
+  const int lane = threadIdx.x & 31;
+  const int ui = blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);  // grid = units / kWarpsPerCta: ui < nunits
   const int2 uw = units[ui];
   const F4Job J = jobs[uw.x];
-  if (!gate_open(A.gate, J.surf)) return;  // a job's units share the surface: whole warps leave together
+  if (!gate_open(A.gate, J.surf)) return;  // uniform over the CTA
   const SurfaceDesc& S = A.surf[J.surf];
-  cd* sm = sm_all[unit_in_cta];
   if (PHASE == 2) {
-    f4_phase2(J, S, uw.y, t, sm, scr);
+    f4_run<2, 64>(A, J, S, uw.y, lane, twL, scr);
     return;
   }
-  const int P = (S.n / 64) / 8;
-  switch (P) {
-    case 1: PHASE == 1 ? f4_phase1<1>(A, J, S, uw.y, t, sm, scr) : f4_phase3<1>(A, J, S, uw.y, t, sm, scr); break;
-    case 2: PHASE == 1 ? f4_phase1<2>(A, J, S, uw.y, t, sm, scr) : f4_phase3<2>(A, J, S, uw.y, t, sm, scr); break;
-    case 4: PHASE == 1 ? f4_phase1<4>(A, J, S, uw.y, t, sm, scr) : f4_phase3<4>(A, J, S, uw.y, t, sm, scr); break;
-    case 8: PHASE == 1 ? f4_phase1<8>(A, J, S, uw.y, t, sm, scr) : f4_phase3<8>(A, J, S, uw.y, t, sm, scr); break;
-    default: PHASE == 1 ? f4_phase1<16>(A, J, S, uw.y, t, sm, scr) : f4_phase3<16>(A, J, S, uw.y, t, sm, scr); break;
+  switch (S.n / 64) {
+    case 8: f4_run<PHASE, 8>(A, J, S, uw.y, lane, twL, scr); break;
+    case 16: f4_run<PHASE, 16>(A, J, S, uw.y, lane, twL, scr); break;
+    case 32: f4_run<PHASE, 32>(A, J, S, uw.y, lane, twL, scr); break;
+    case 64: f4_run<PHASE, 64>(A, J, S, uw.y, lane, twL, scr); break;
+    default: f4_run<PHASE, 128>(A, J, S, uw.y, lane, twL, scr); break;
   }
 }
 
@@ -307,7 +302,7 @@ bool sfd_f4_eligible(int n) { return n >= 512 && n <= 8192 && (n & (n - 1)) == 0
 cudaError_t sfd_launch_f4(const DerivArgs& A, const F4Plan& p, cd* scr, cudaStream_t st, int phase) {
   const int nu = p.nunits[phase - 1];
   if (nu == 0) return cudaSuccess;
-  const int grid = (nu + kUnitsPerCta - 1) / kUnitsPerCta;
+  const int grid = nu / kWarpsPerCta;  // every job contributes a multiple of 4 units
   if (phase == 1) k_fft4<1><<<grid, kF4Threads, 0, st>>>(A, p.jobs, p.units[0], nu, scr);
   else if (phase == 2) k_fft4<2><<<grid, kF4Threads, 0, st>>>(A, p.jobs, p.units[1], nu, scr);
   else k_fft4<3><<<grid, kF4Threads, 0, st>>>(A, p.jobs, p.units[2], nu, scr);
