@@ -144,6 +144,79 @@ __device__ __forceinline__ void df_div_acc(df nr, df ni, df a, df& sr, df& si) {
   df_acc(si, -pi.hi, -pi.lo);
 }
 
+// ---- packed double-float pairs.  GB300 issues one FP32x2 instruction
+// (add / mul / fma .f32x2, each lane rounded to nearest as the scalar
+// instruction) per pair of FP32 operations, so the double-float pass keeps
+// the real and imaginary parts of a complex double-float side by side and
+// runs the identical operation sequence on both at once: the error-free
+// transforms stay exact per lane and the sums are bitwise those of the
+// scalar sequence, with about half the instructions.
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, neg2(b)); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
+// two double-float numbers: lane x and lane y
+struct df2 {
+  float2 hi, lo;
+};
+__device__ __forceinline__ df2 two_sum2(float2 a, float2 b) {
+  const float2 s = add2(a, b);
+  const float2 bb = sub2(s, a);
+  return {s, add2(sub2(a, sub2(s, bb)), sub2(b, bb))};
+}
+__device__ __forceinline__ df2 quick_two_sum2(float2 a, float2 b) {
+  const float2 s = add2(a, b);
+  return {s, sub2(b, sub2(s, a))};
+}
+__device__ __forceinline__ df2 two_prod2(float2 a, float2 b) {
+  const float2 p = mul2(a, b);
+  return {p, fma2(a, b, neg2(p))};
+}
+// df_diff per lane
+__device__ __forceinline__ df2 df_diff2(float2 a_hi, float2 a_lo, float2 b_hi, float2 b_lo) {
+  const df2 s = two_sum2(a_hi, neg2(b_hi));
+  return two_sum2(s.hi, add2(s.lo, sub2(a_lo, b_lo)));
+}
+// df_mul per lane (normalised)
+__device__ __forceinline__ df2 df_mul2(float2 a_hi, float2 a_lo, float2 b_hi, float2 b_lo) {
+  const df2 p = two_prod2(a_hi, b_hi);
+  return quick_two_sum2(p.hi, fma2(a_hi, b_lo, fma2(a_lo, b_hi, p.lo)));
+}
+// df_add per lane
+__device__ __forceinline__ df2 df_add2(df2 a, df2 b) {
+  const df2 s = two_sum2(a.hi, b.hi);
+  return quick_two_sum2(s.hi, add2(s.lo, add2(a.lo, b.lo)));
+}
+// df_acc per lane
+__device__ __forceinline__ void df_acc2(df2& acc, float2 xh, float2 xl) {
+  const df2 s = two_sum2(acc.hi, xh);
+  acc.hi = s.hi;
+  acc.lo = add2(acc.lo, add2(s.lo, xl));
+}
+// (acc.x, acc.y) += a / (d.x + i d.y) = (a d.x / |d|^2, -a d.y / |d|^2): the
+// packed form of df_div_acc
+__device__ __forceinline__ void df_div_acc2(df2 d, df a, df2& acc) {
+  const df2 P = two_prod2(d.hi, d.hi);
+  const float2 E = fma2(mul2(d.hi, make_float2(2.f, 2.f)), d.lo, P.lo);
+  const df s = two_sum(P.hi.x, P.hi.y);
+  const df q = {s.hi, __fadd_rn(s.lo, __fadd_rn(E.x, E.y))};
+  const df t = df_mul_raw(a, df_rcp_raw(q));
+  const float2 th = make_float2(t.hi, t.hi), tl = make_float2(t.lo, t.lo);
+  const df2 p = two_prod2(th, d.hi);
+  const float2 e = fma2(th, d.lo, fma2(tl, d.hi, p.lo));
+  df_acc2(acc, make_float2(p.hi.x, -p.hi.y), make_float2(e.x, -e.y));
+}
+
+// double-float source of the packed pass: hi parts and lo parts of w (and p)
+// as register pairs {re, im}
+struct SrcDF2 {
+  float4 w;  // w.re hi, w.im hi, w.re lo, w.im lo
+  float4 p;  // p.re hi, p.im hi, p.re lo, p.im lo
+  float a_hi, a_lo;
+};
+
 }  // namespace
 
 struct Src64 {
@@ -159,7 +232,8 @@ struct Acc<SFD_PREC_F64> {
 };
 template <>
 struct Acc<SFD_PREC_DF> {
-  df sr{0.f, 0.f}, si{0.f, 0.f}, tr{0.f, 0.f}, ti{0.f, 0.f};
+  df2 s{{0.f, 0.f}, {0.f, 0.f}};  // (S re, S im)
+  df2 t{{0.f, 0.f}, {0.f, 0.f}};  // (T re, T im)
 };
 template <>
 struct Acc<SFD_PREC_F32> {
@@ -176,10 +250,13 @@ struct Tgt<SFD_PREC_F64> {
 };
 template <>
 struct Tgt<SFD_PREC_DF> {
-  df wr, wi, pr, pi;
+  float2 w_hi, w_lo;    // (re, im) of w
+  float2 p_hi, p_lo;    // (re, im) of p
+  float2 ps_hi, ps_lo;  // (im, re) of p
   __device__ void load(float4 w_, float4 p_) {
-    wr = {w_.x, w_.y}; wi = {w_.z, w_.w};
-    pr = {p_.x, p_.y}; pi = {p_.z, p_.w};
+    w_hi = {w_.x, w_.z}; w_lo = {w_.y, w_.w};
+    p_hi = {p_.x, p_.z}; p_lo = {p_.y, p_.w};
+    ps_hi = {p_.z, p_.x}; ps_lo = {p_.w, p_.y};
   }
 };
 template <>
@@ -208,19 +285,24 @@ __device__ __forceinline__ void pair_acc(const Tgt<SFD_PREC_F64>& t, const Src64
     A.ti -= inv * di;
   }
 }
-__device__ __forceinline__ void pair_acc(const Tgt<SFD_PREC_DF>& t, const SrcDF& s, bool self, bool image,
+__device__ __forceinline__ void pair_acc(const Tgt<SFD_PREC_DF>& t, const SrcDF2& s, bool self, bool image,
                                          Acc<SFD_PREC_DF>& A) {
-  df aj{s.a_hi, s.a_lo};
+  const df aj{s.a_hi, s.a_lo};
   if (!self) {
-    df dr = df_diff(t.wr, df{s.wr_hi, s.wr_lo});
-    df di = df_diff(t.wi, df{s.wi_hi, s.wi_lo});
-    df_div_acc(dr, di, aj, A.sr, A.si);
+    // (w_k - w_j) as a packed pair, then a_j / (w_k - w_j) accumulated into S
+    const df2 d = df_diff2(t.w_hi, t.w_lo, make_float2(s.w.x, s.w.y), make_float2(s.w.z, s.w.w));
+    df_div_acc2(d, aj, A.s);
   }
   if (image) {
-    df prj{s.pr_hi, s.pr_lo}, pij{s.pi_hi, s.pi_lo};
-    df qr = df_add(df_mul(t.pr, prj), df_mul(t.pi, pij));
-    df qi = df_sub(df_mul(t.pi, prj), df_mul(t.pr, pij));
-    df_div_acc(df_sub(df{1.f, 0.f}, qr), df_neg(qi), aj, A.tr, A.ti);
+    // q = p_k conj(p_j): (qr, qi) = (pr prj + pi pij, pi prj - pr pij)
+    const float2 prj_hi = make_float2(s.p.x, s.p.x), prj_lo = make_float2(s.p.z, s.p.z);
+    const float2 pij_hi = make_float2(s.p.y, s.p.y), pij_lo = make_float2(s.p.w, s.p.w);
+    const df2 m1 = df_mul2(t.p_hi, t.p_lo, prj_hi, prj_lo);    // (pr prj, pi prj)
+    const df2 m2 = df_mul2(t.ps_hi, t.ps_lo, pij_hi, pij_lo);  // (pi pij, pr pij)
+    const df2 q = df_add2(m1, df2{make_float2(m2.hi.x, -m2.hi.y), make_float2(m2.lo.x, -m2.lo.y)});
+    // (1 - qr, -qi)
+    const df2 d = df_add2(df2{make_float2(1.f, 0.f), make_float2(0.f, 0.f)}, df2{neg2(q.hi), neg2(q.lo)});
+    df_div_acc2(d, aj, A.t);
   }
 }
 __device__ __forceinline__ void pair_acc(const Tgt<SFD_PREC_F32>& t, const SrcDF& s, bool self, bool image,
@@ -241,7 +323,8 @@ __device__ __forceinline__ void pair_acc(const Tgt<SFD_PREC_F32>& t, const SrcDF
   }
 }
 template <int PREC>
-using SrcT = typename std::conditional<PREC == SFD_PREC_F64, Src64, SrcDF>::type;
+using SrcT = typename std::conditional<PREC == SFD_PREC_F64, Src64,
+                                       typename std::conditional<PREC == SFD_PREC_DF, SrcDF2, SrcDF>::type>::type;
 
 // Fixed-order reduction values of one target: FP64 for the FP64 pass,
 // double-float for the DF and FP32 passes.
@@ -258,7 +341,8 @@ using WSum = typename std::conditional<PREC == SFD_PREC_F64, double, df>::type;
 
 __device__ __forceinline__ Red<SFD_PREC_F64> to_red(const Acc<SFD_PREC_F64>& A) { return {A.sr, A.si, A.tr, A.ti}; }
 __device__ __forceinline__ Red<SFD_PREC_DF> to_red(const Acc<SFD_PREC_DF>& A) {
-  return {df_acc_done(A.sr), df_acc_done(A.si), df_acc_done(A.tr), df_acc_done(A.ti)};
+  const df2 s = two_sum2(A.s.hi, A.s.lo), t = two_sum2(A.t.hi, A.t.lo);  // df_acc_done per lane
+  return {df{s.hi.x, s.lo.x}, df{s.hi.y, s.lo.y}, df{t.hi.x, t.lo.x}, df{t.hi.y, t.lo.y}};
 }
 __device__ __forceinline__ Red<SFD_PREC_F32> to_red(const Acc<SFD_PREC_F32>& A) {
   return {df{A.sr, 0.f}, df{A.si, 0.f}, df{A.tr, 0.f}, df{A.ti, 0.f}};
@@ -352,12 +436,18 @@ __global__ void __cluster_dims__(kSumCL, 1, 1) __launch_bounds__(G * kSumTile, 1
       wpart += aj;
       cd p = image ? A.p[g] : cd{0.0, 0.0};
       src[jj] = Src64{w.re, w.im, p.re, p.im, aj};
+    } else if constexpr (PREC == SFD_PREC_DF) {
+      const float4 w = A.wdf[g];
+      const float2 ad = A.adf[g];
+      const float4 p = image ? A.pdf[g] : make_float4(0.f, 0.f, 0.f, 0.f);
+      wpart = df_add(wpart, df{ad.x, ad.y});
+      src[jj] = SrcDF2{make_float4(w.x, w.z, w.y, w.w), make_float4(p.x, p.z, p.y, p.w), ad.x, ad.y};
     } else {
       float4 w = A.wdf[g];
       float2 ad = A.adf[g];
       float4 p = image ? A.pdf[g] : make_float4(0.f, 0.f, 0.f, 0.f);
       wpart = df_add(wpart, df{ad.x, ad.y});
-      src[jj] = SrcDF{w.x, w.y, w.z, w.w, p.x, p.y, p.z, p.w, ad.x, PREC == SFD_PREC_DF ? ad.y : 0.f};
+      src[jj] = SrcDF{w.x, w.y, w.z, w.w, p.x, p.y, p.z, p.w, ad.x, 0.f};
     }
   }
   for (int o = 16; o > 0; o >>= 1) wpart = wsum_add(wpart, shfl_x(wpart, o));
@@ -447,7 +537,7 @@ __global__ void __cluster_dims__(kSumCL, 1, 1) __launch_bounds__(G * kSumTile, 1
 
 size_t sfd_sums_smem(int prec, int max_n) {
   const size_t per = (size_t)(max_n + kSumCL - 1) / kSumCL;
-  return per * (prec == SFD_PREC_F64 ? sizeof(Src64) : sizeof(SrcDF));
+  return per * (prec == SFD_PREC_F64 ? sizeof(Src64) : prec == SFD_PREC_DF ? sizeof(SrcDF2) : sizeof(SrcDF));
 }
 
 namespace {
@@ -469,7 +559,9 @@ void launch_prec(const SumArgs& A, dim3 grid, int groups, size_t smem, cudaStrea
 }  // namespace
 
 cudaError_t sfd_sums_configure() {
-  const int bytes = (int)sfd_sums_smem(SFD_PREC_F64, 8192);
+  // the largest staged source (the packed double-float one is 48 bytes) at n = 8192
+  const int bytes = (int)std::max(std::max(sfd_sums_smem(SFD_PREC_F64, 8192), sfd_sums_smem(SFD_PREC_DF, 8192)),
+                                  sfd_sums_smem(SFD_PREC_F32, 8192));
   cudaError_t e = configure_prec<SFD_PREC_F64>(bytes);
   if (e == cudaSuccess) e = configure_prec<SFD_PREC_DF>(bytes);
   if (e == cudaSuccess) e = configure_prec<SFD_PREC_F32>(bytes);
@@ -517,26 +609,58 @@ __device__ __forceinline__ void f32_t(const float (&t)[6], float4 s1, float4& ac
   acc.w = fmaf(-inv, di, acc.w);
 }
 
+// Both targets of a thread as packed pairs (lane x: target t0, lane y:
+// target t1), for the sources away from the tile's own nodes.
+struct F32Pair {
+  float2 wr_hi, wr_lo, wi_hi, wi_lo, pr, pi;
+};
+template <bool IMAGE>
+__device__ __forceinline__ void f32_pair2(const F32Pair& T, float4 s0, float4 s1, float2& sr, float2& si,
+                                          float2& tr, float2& ti) {
+  const float2 dr = add2(sub2(T.wr_hi, make_float2(s0.x, s0.x)), sub2(T.wr_lo, make_float2(s0.y, s0.y)));
+  const float2 di = add2(sub2(T.wi_hi, make_float2(s0.z, s0.z)), sub2(T.wi_lo, make_float2(s0.w, s0.w)));
+  const float2 d2 = fma2(dr, dr, mul2(di, di));
+  const float2 inv = mul2(make_float2(s1.x, s1.x), make_float2(rcp_approx(d2.x), rcp_approx(d2.y)));
+  sr = fma2(inv, dr, sr);
+  si = fma2(neg2(inv), di, si);
+  if (IMAGE) {
+    const float2 qr = fma2(T.pr, make_float2(s1.y, s1.y), mul2(T.pi, make_float2(s1.z, s1.z)));
+    const float2 qi = fma2(T.pi, make_float2(s1.y, s1.y), neg2(mul2(T.pr, make_float2(s1.z, s1.z))));
+    const float2 er = sub2(make_float2(1.f, 1.f), qr), ei = neg2(qi);
+    const float2 e2 = fma2(er, er, mul2(ei, ei));
+    const float2 inv2 = mul2(make_float2(s1.x, s1.x), make_float2(rcp_approx(e2.x), rcp_approx(e2.y)));
+    tr = fma2(inv2, er, tr);
+    ti = fma2(neg2(inv2), ei, ti);
+  }
+}
+
 template <bool IMAGE>
 __device__ __forceinline__ void f32_slice_loop(const float4* src, int jn, int grp, int lo, int hi, int self0,
                                                int self1, const float (&T0)[6], const float (&T1)[6], float4& acc0,
                                                float4& acc1) {
   auto first = [&](int a) { return a + ((grp - a) % kF32Groups + kF32Groups) % kF32Groups; };
-  auto pair = [&](int jj, bool check) {
+  const F32Pair P{{T0[0], T1[0]}, {T0[1], T1[1]}, {T0[2], T1[2]}, {T0[3], T1[3]}, {T0[4], T1[4]}, {T0[5], T1[5]}};
+  float2 sr = {acc0.x, acc1.x}, si = {acc0.y, acc1.y}, tr = {acc0.z, acc1.z}, ti = {acc0.w, acc1.w};
+  int jj = grp;
+#pragma unroll 4
+  for (; jj < lo; jj += kF32Groups) f32_pair2<IMAGE>(P, src[2 * jj], src[2 * jj + 1], sr, si, tr, ti);
+  acc0 = make_float4(sr.x, si.x, tr.x, ti.x);
+  acc1 = make_float4(sr.y, si.y, tr.y, ti.y);
+  // the tile's own nodes: j == k is skipped per target
+  for (jj = first(lo); jj < hi; jj += kF32Groups) {
     const float4 s0 = src[2 * jj], s1 = src[2 * jj + 1];
-    if (!check || jj != self0) f32_s(T0, s0, s1.x, acc0);
-    if (!check || jj != self1) f32_s(T1, s0, s1.x, acc1);
+    if (jj != self0) f32_s(T0, s0, s1.x, acc0);
+    if (jj != self1) f32_s(T1, s0, s1.x, acc1);
     if (IMAGE) {
       f32_t(T0, s1, acc0);
       f32_t(T1, s1, acc1);
     }
-  };
-  int jj = grp;
+  }
+  sr = {acc0.x, acc1.x}; si = {acc0.y, acc1.y}; tr = {acc0.z, acc1.z}; ti = {acc0.w, acc1.w};
 #pragma unroll 4
-  for (; jj < lo; jj += kF32Groups) pair(jj, false);
-  for (jj = first(lo); jj < hi; jj += kF32Groups) pair(jj, true);
-#pragma unroll 4
-  for (jj = first(hi); jj < jn; jj += kF32Groups) pair(jj, false);
+  for (jj = first(hi); jj < jn; jj += kF32Groups) f32_pair2<IMAGE>(P, src[2 * jj], src[2 * jj + 1], sr, si, tr, ti);
+  acc0 = make_float4(sr.x, si.x, tr.x, ti.x);
+  acc1 = make_float4(sr.y, si.y, tr.y, ti.y);
 }
 
 __device__ __forceinline__ void load_target(const SumArgs& A, int g, bool image, float (&T)[6]) {
