@@ -205,8 +205,8 @@ long long sfd_kernel_launches(const sfd_engine* e);
 /* Per-kernel-class device time: while enabled, RK4 steps run eagerly (no
  * graph) and every kernel launch is bracketed by CUDA events on the engine
  * stream; sfd_profile_read returns accumulated milliseconds and launch counts
- * per class (names from sfd_profile_class_name; 16 classes). */
-#define SFD_PROFILE_CLASSES 16
+ * per class (names from sfd_profile_class_name; 19 classes). */
+#define SFD_PROFILE_CLASSES 19
 int sfd_profile(sfd_engine* e, int enable);
 int sfd_profile_read(sfd_engine* e, double* ms, long long* counts, int nclass);
 const char* sfd_profile_class_name(int cls);
@@ -310,7 +310,9 @@ int sfd_rhs_vjp_device(sfd_engine* e, const void* state, const void* cotangent, 
 /* Integrate `steps` RK4 steps of size dt from state0 (host, 3n) keeping a
  * checkpoint every `checkpoint_every` steps on the device; the final state is
  * written to state_final (host, 3n; nullable).  Same arithmetic as
- * sfd_rk4_steps on an FP64 engine. */
+ * sfd_rk4_steps on an FP64 engine with the same boundary-sum shape: bitwise
+ * equal with autotune off, or once the autotuning first sfd_rk4_steps call has
+ * run (it may keep another shape, which changes the summation order). */
 int sfd_rk4_record(sfd_engine* e, double dt, int steps, int checkpoint_every, const double* state0,
                    double* state_final);
 /* Reverse the recorded trajectory: grad_state0 = (d state_final / d state0)^T

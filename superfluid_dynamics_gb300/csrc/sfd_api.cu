@@ -207,7 +207,7 @@ int enqueue_sums(sfd_engine* e, int prec, const double* weights, const float2* w
             (mode == 0 && e->rslot) ? e->bnorm : nullptr, make_gate(e, gate),
             e->d_f32_work, e->f32_part, e->f32_wsum, e->f32_count};
   if (prec == SFD_PREC_F32 && e->d_f32_work) {
-    LAUNCHC(e, SFD_K_SUMS32, sfd_launch_sums_f32(A, e->nf32, e->max_n, e->stream));
+    LAUNCHC(e, SFD_K_SUMS32, sfd_launch_sums_f32(A, e->nf32, e->f32_max_per, e->stream));
     return 0;
   }
   int cls = prec == SFD_PREC_F64 ? SFD_K_SUMS64 : prec == SFD_PREC_DF ? SFD_K_SUMSDF : SFD_K_SUMS32;
@@ -225,14 +225,14 @@ int enqueue_gemv(sfd_engine* e, const float* vf, double* y, float2* ydf, double*
     // one surface: a whole number of waves of two CTAs per SM, rows interleaved
     const int wave = 2 * e->nsm, need = (e->max_n + kGemvRows - 1) / kGemvRows;
     const int grid = (need + wave - 1) / wave * wave;
-    LAUNCHC(e, SFD_K_GEMV, k_gemv_h<<<grid, 512, e->max_np * sizeof(float), e->stream>>>(
-                               e->d_surf, nullptr, e->m16, e->rscale, vf, y, ydf, acc, accdf, G));
+    LAUNCHC(e, SFD_K_GEMV, sfd_launch(k_gemv_h, dim3(grid), dim3(512), e->max_np * sizeof(float), e->stream, true,
+                                      e->d_surf, (const int2*)nullptr, e->m16, e->rscale, vf, y, ydf, acc, accdf, G));
   } else if (e->m16)
-    LAUNCHC(e, SFD_K_GEMV, k_gemv_h<<<e->ngemv, 512, e->max_np * sizeof(float), e->stream>>>(
-                               e->d_surf, e->d_gemv_rows, e->m16, e->rscale, vf, y, ydf, acc, accdf, G));
+    LAUNCHC(e, SFD_K_GEMV, sfd_launch(k_gemv_h, dim3(e->ngemv), dim3(512), e->max_np * sizeof(float), e->stream, true,
+                                      e->d_surf, e->d_gemv_rows, e->m16, e->rscale, vf, y, ydf, acc, accdf, G));
   else
-    LAUNCHC(e, SFD_K_GEMV, k_gemv<<<e->ngemv, 256, e->max_np * sizeof(float), e->stream>>>(
-                               e->d_surf, e->d_gemv_rows, e->m32, vf, y, ydf, acc, accdf, G));
+    LAUNCHC(e, SFD_K_GEMV, sfd_launch(k_gemv, dim3(e->ngemv), dim3(256), e->max_np * sizeof(float), e->stream, true,
+                                      e->d_surf, e->d_gemv_rows, e->m32, vf, y, ydf, acc, accdf, G));
   return 0;
 }
 
@@ -297,10 +297,23 @@ cudaError_t launch_transforms(const sfd_engine* e, const DerivArgs& D, bool firs
 }
 
 // The same on the engine stream as one profiled launch group.
+// The same on the engine stream, each kernel a profiled launch of its own
+// class (the four-step phases separately, so that per-kernel times compare
+// with single-kernel classes).
 int enqueue_transforms(sfd_engine* e, const DerivArgs& D, bool first) {
-  int nl = 0;
-  LAUNCHC(e, SFD_K_SPECTRAL, launch_transforms(e, D, first, e->stream, e->f4_scr, &nl));
-  e->launches += nl - 1;  // LAUNCHC counted one
+  const int nj = first ? e->njobs_first : e->njobs_ap, ncj = first ? e->ncjobs_first : e->ncjobs_ap;
+  if (nj)
+    LAUNCHC(e, SFD_K_SPECTRAL,
+            sfd_launch_spectral(D, first ? e->d_jobs_first : e->d_jobs_ap, nj, e->max_n_single, e->stream));
+  if (ncj)
+    LAUNCHC(e, SFD_K_SPECTRAL, sfd_launch_spectral_cluster(D, first ? e->d_cjobs_first : e->d_cjobs_ap, ncj,
+                                                           e->max_n_cluster, e->stream));
+  const F4Plan& p = first ? e->f4_first : e->f4_ap;
+  if (p.njobs) {
+    LAUNCHC(e, SFD_K_F4_COLS, sfd_launch_f4(D, p, e->f4_scr, e->stream, 1));
+    LAUNCHC(e, SFD_K_F4_ROWS, sfd_launch_f4(D, p, e->f4_scr, e->stream, 2));
+    LAUNCHC(e, SFD_K_F4_ICOLS, sfd_launch_f4(D, p, e->f4_scr, e->stream, 3));
+  }
   return 0;
 }
 
@@ -335,8 +348,8 @@ int enqueue_solve(sfd_engine* e, const double* st, const double* phi_im, bool re
     int rc = enqueue_transforms(e, D, true);
     if (rc) return rc;
   }
-  LAUNCHC(e, SFD_K_NODE, k_node_prep<<<blocks_for(nt, 32), 64, 0, e->stream>>>(e->d_surf, e->d_node_surf, nt, x, y, e->zp,
-                                                                     e->zpp, e->nd, e->rslot, e->bnorm));
+  LAUNCHC(e, SFD_K_NODE, sfd_launch(k_node_prep, dim3(blocks_for(nt, 32)), dim3(64), 0, e->stream, true, e->d_surf,
+                                    e->d_node_surf, nt, x, y, e->zp, e->zpp, e->nd, e->rslot, e->bnorm));
   const int extra = extra_iters(e);
   if (e->opt.precision == SFD_PRECISION_FP64) {
     LAUNCHC(e, SFD_K_ASSEMBLE, sfd_launch_assemble64(e->d_surf, e->d_asm_tiles, e->nasm, e->nd.w, e->nd.p, e->zp, e->nd.mdiag,
@@ -445,8 +458,9 @@ int enqueue_rhs(sfd_engine* e, const double* st, double* out, bool refactor) {
             e->zp, e->zpp, e->vel_low1, out, out + nt, out + 2 * nt, e->status,
             e->rslot, 1 + extra, e->bnorm, e->opt.refine_tol, e->rnorm, e->rrel, e->extra_count,
             e->opt.precision == SFD_PRECISION_MIXED ? e->stall_dev : nullptr};
-  if (e->any_rho) LAUNCHC(e, SFD_K_VELOCITY, k_velocity_node1<<<1, 32, 0, e->stream>>>(V));
-  LAUNCHC(e, SFD_K_VELOCITY, k_velocity_bernoulli<<<blocks_for(nt, 32), 32, 0, e->stream>>>(V));
+  if (e->any_rho) LAUNCHC(e, SFD_K_VELOCITY, sfd_launch(k_velocity_node1, dim3(1), dim3(32), 0, e->stream, true, V));
+  LAUNCHC(e, SFD_K_VELOCITY,
+          sfd_launch(k_velocity_bernoulli, dim3(blocks_for(nt, 32)), dim3(32), 0, e->stream, true, V));
   return 0;
 }
 
@@ -459,10 +473,10 @@ int enqueue_step(sfd_engine* e, double dt, bool refactor) {
     const double* in = s == 0 ? e->y0 : e->ys;
     int rc = enqueue_rhs(e, in, e->kcur, refactor && s == 0);
     if (rc) return rc;
-    LAUNCHC(e, SFD_K_RK4, k_rk4_stage<<<nb, 256, 0, e->stream>>>(n3, e->y0, e->kcur, e->kacc, s < 3 ? e->ys : nullptr, wk[s],
-                                                       cy[s], s == 0));
+    LAUNCHC(e, SFD_K_RK4, sfd_launch(k_rk4_stage, dim3(nb), dim3(256), 0, e->stream, true, n3, e->y0, e->kcur, e->kacc,
+                                     s < 3 ? e->ys : nullptr, wk[s], cy[s], s == 0 ? 1 : 0));
   }
-  LAUNCHC(e, SFD_K_RK4, k_rk4_final<<<nb, 256, 0, e->stream>>>(n3, e->y0, e->kacc, dt / 6.0));
+  LAUNCHC(e, SFD_K_RK4, sfd_launch(k_rk4_final, dim3(nb), dim3(256), 0, e->stream, true, n3, e->y0, e->kacc, dt / 6.0));
   return 0;
 }
 
@@ -877,6 +891,28 @@ int sfd_create(const int* n, int nsurf, const sfd_problem* problems, int shared_
   return sfd_create_driven(n, nsurf, problems, nullptr, shared_problem, opts, out);
 }
 
+// Source slices per surface for the FP32 pass, so that one launch fills the
+// GPU evenly: the total work (tiles x sources) is spread over `slots`
+// resident CTAs (in as many waves as keep a slice within kF32MaxPer
+// sources), each surface's slice count proportional to its node count (the
+// floor, so the entries never exceed the slots of the waves), with at least
+// kF32MinPer sources per slice and at most kF32MaxSlices slices.
+static void plan_f32_slices(const std::vector<SurfaceDesc>& hs, int nsurf, int slots, std::vector<int>& out) {
+  int cap = kF32MaxSlices;
+  if (const char* v = std::getenv("SFD_F32_SLICES")) cap = std::min(64, std::max(1, std::atoi(v)));
+  long long total = 0;
+  for (int s = 0; s < nsurf; ++s) total += (long long)((hs[s].n + kSumTile - 1) / kSumTile) * hs[s].n;
+  const long long waves = std::max(1LL, (total + (long long)slots * kF32MaxPer - 1) / ((long long)slots * kF32MaxPer));
+  out.assign(nsurf, 1);
+  for (int s = 0; s < nsurf; ++s) {
+    const long long n = hs[s].n;
+    long long ns = total > 0 ? n * waves * slots / total : 1;
+    ns = std::min(ns, (n + kF32MinPer - 1) / kF32MinPer);
+    ns = std::max(ns, (n + kF32MaxPer - 1) / kF32MaxPer);  // slices within kF32MaxPer sources
+    out[s] = (int)std::max(1LL, std::min<long long>(ns, cap));
+  }
+}
+
 int sfd_create_driven(const int* n, int nsurf, const sfd_problem* problems, const sfd_drive* drives,
                       int shared_problem, const sfd_options* opts, sfd_engine** out) {
   if (!out || !n || !problems || nsurf <= 0) return set_error(SFD_ERR_INVALID, "sfd_create: bad arguments");
@@ -997,9 +1033,15 @@ int sfd_create_driven(const int* n, int nsurf, const sfd_problem* problems, cons
   std::vector<int2> jf, ja, cjf, cja;
   std::vector<F4Job> f4f, f4a;
   std::vector<int2> items;
-  std::vector<int4> f32work;
+  std::vector<F32Work> f32work;
   std::vector<int4> tiles;
   std::vector<int2> rows;
+  std::vector<int> f32_slices;
+  if (e->opt.precision == SFD_PRECISION_MIXED) {
+    int ctas = 0;
+    CKE(sfd_f32_ctas_per_sm(kF32MaxPer, &ctas));
+    plan_f32_slices(e->hs, nsurf, std::max(1, ctas) * std::max(1, e->nsm), f32_slices);
+  }
   for (int s = 0; s < nsurf; ++s) {
     const SurfaceDesc& S = e->hs[s];
     for (int k = 0; k < S.n; ++k) node_surf[S.off + k] = s;
@@ -1022,8 +1064,23 @@ int sfd_create_driven(const int* n, int nsurf, const sfd_problem* problems, cons
       e->max_n_single = std::max(e->max_n_single, S.n);
     }
     for (int t0 = 0; t0 < S.n; t0 += kSumTile) {
-      const int it = (int)items.size(), ns = sfd_f32_slices(S.n);
-      for (int sl = 0; sl < ns; ++sl) f32work.push_back({it, sl, (int)f32work.size() - sl, ns});
+      const int it = (int)items.size(), ns = f32_slices.empty() ? 0 : f32_slices[s];
+      const int base = (int)f32work.size();
+      if (ns) e->f32_max_per = std::max(e->f32_max_per, (S.n + ns - 1) / ns);
+      for (int sl = 0; sl < ns; ++sl) {
+        F32Work w{};
+        w.item = it;
+        w.slice = sl;
+        w.base = base;
+        w.nsl = ns;
+        w.sidx = s;
+        w.t0 = t0;
+        w.n = S.n;
+        w.off = S.off;
+        w.image = (S.physics == 1 && !S.infinite_depth) ? 1 : 0;
+        w.c1 = S.physics == 0 ? (float)(0.25 * (1 - S.rho) / SFD_PI) : (float)(0.25 / SFD_PI);
+        f32work.push_back(w);
+      }
       items.push_back({s, t0});
     }
     int np = pad_n(S.n);
@@ -1077,8 +1134,10 @@ int sfd_create_driven(const int* n, int nsurf, const sfd_problem* problems, cons
   CKE(cudaMemcpy(e->d_sum_items, items.data(), items.size() * sizeof(int2), cudaMemcpyHostToDevice));
   if (e->opt.precision == SFD_PRECISION_MIXED) {
     e->nf32 = (int)f32work.size();
+    int ctas = 0;  // shared-memory opt-in for the widest slice
+    CKE(sfd_f32_ctas_per_sm(std::max(e->f32_max_per, kF32MaxPer), &ctas));
     CKE(dalloc(&e->d_f32_work, f32work.size()));
-    CKE(cudaMemcpy(e->d_f32_work, f32work.data(), f32work.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    CKE(cudaMemcpy(e->d_f32_work, f32work.data(), f32work.size() * sizeof(F32Work), cudaMemcpyHostToDevice));
     CKE(dalloc(&e->f32_part, 64LL * f32work.size()));
     CKE(dalloc(&e->f32_wsum, f32work.size()));
     CKE(dalloc(&e->f32_count, items.size()));
@@ -1346,7 +1405,8 @@ const char* sfd_profile_class_name(int cls) {
   static const char* names[SFD_NCLASS] = {"other", "spectral_deriv", "node_prep", "boundary_sums_fp64",
                                           "boundary_sums_df", "boundary_sums_fp32", "sum_epilogue", "assemble",
                                           "factor_diag", "factor_panel", "factor_update", "lu_trsv", "gemv",
-                                          "velocity_bernoulli", "rk4_combine", "factor_update_tcgen05"};
+                                          "velocity_bernoulli", "rk4_combine", "factor_update_tcgen05",
+                                          "fft4_columns", "fft4_rows", "fft4_inverse_columns"};
   return (cls >= 0 && cls < SFD_NCLASS) ? names[cls] : "";
 }
 

@@ -67,6 +67,18 @@ struct Gate {
   int stride;           // slots per surface (SFD_RSLOTS)
   double tol;           // relative residual tolerance
 };
+// Programmatic dependent launch.  A kernel launched with sfd_launch(..., pdl
+// = true) may be scheduled while its predecessor in the stream still runs;
+// every CTA calls sfd_pdl_begin() before its first global memory access: it
+// waits until the predecessor grid has completed and its writes are visible,
+// then lets the next kernel of the stream be scheduled in turn.  Every CTA
+// waits, also one that returns early, so completion stays transitive along the
+// stream.  In a launch without the attribute both instructions return at once.
+__device__ __forceinline__ void sfd_pdl_begin() {
+  asm volatile("griddepcontrol.wait;\n" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+}
+
 __device__ __forceinline__ bool gate_open(const Gate& G, int s) {
   return !G.slot || (G.slot[(long long)s * G.stride] > G.tol * G.bnorm[s]);
 }
@@ -86,3 +98,39 @@ struct DerivArgs {
   float* phipf;  // FP32 copy of phi' for the preconditioner product (nullable)
   Gate gate;     // jobs run only where the gate is open (ungated by default)
 };
+
+#ifdef __CUDACC__
+#include <cstdlib>
+#include <utility>
+// Programmatic dependent launch is on unless SFD_PDL=0 is set in the
+// environment (read once per process).
+inline bool sfd_pdl_enabled() {
+  static const bool on = [] {
+    const char* v = std::getenv("SFD_PDL");
+    return !(v && v[0] == '0');
+  }();
+  return on;
+}
+
+// Launch `k` on `st`; with pdl (and sfd_pdl_enabled()) the launch carries the
+// programmatic stream-serialization attribute (a programmatic edge when the
+// stream is captured into a graph).  Only kernels that call sfd_pdl_begin()
+// first may be launched with pdl.
+template <typename... KArgs, typename... Args>
+cudaError_t sfd_launch(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, bool pdl,
+                       Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  if (pdl && sfd_pdl_enabled()) {
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+  }
+  return cudaLaunchKernelEx(&cfg, k, std::forward<Args>(args)...);
+}
+#endif

@@ -158,6 +158,7 @@ __device__ __forceinline__ double xi_node(int j, double dn, double inv_n) {
 }  // namespace
 
 __global__ void __launch_bounds__(kFftThreads, 1) k_spectral_deriv(DerivArgs A, const int2* jobs) {
+  sfd_pdl_begin();
   extern __shared__ double2 smem_raw[];
   cd* buf = reinterpret_cast<cd*>(smem_raw);
   const int2 job = jobs[blockIdx.x];
@@ -255,6 +256,7 @@ __device__ __forceinline__ void dft4(cd* y, int sign) {
 
 __global__ void __cluster_dims__(SFD_FFT_CLUSTER, 1, 1) __launch_bounds__(kCT)
     k_spectral_cluster(DerivArgs A, const int2* jobs) {
+  sfd_pdl_begin();
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();
   constexpr int C = SFD_FFT_CLUSTER;
@@ -391,8 +393,7 @@ cudaError_t sfd_launch_spectral_cluster(const DerivArgs& A, const int2* jobs, in
   if (njobs == 0) return cudaSuccess;
   const int M = max_n / SFD_FFT_CLUSTER;
   size_t smem = (size_t)3 * M * sizeof(cd);
-  k_spectral_cluster<<<dim3(SFD_FFT_CLUSTER, njobs), kCT, smem, st>>>(A, jobs);
-  return cudaPeekAtLastError();  // the caller's launch check reads and clears it
+  return sfd_launch(k_spectral_cluster, dim3(SFD_FFT_CLUSTER, njobs), dim3(kCT), smem, st, true, A, jobs);
 }
 
 cudaError_t sfd_fft_configure() {
@@ -407,6 +408,5 @@ cudaError_t sfd_fft_configure() {
 cudaError_t sfd_launch_spectral(const DerivArgs& A, const int2* jobs, int njobs, int max_n, cudaStream_t st) {
   if (njobs == 0) return cudaSuccess;
   size_t smem = (size_t)max_n * sizeof(cd);
-  k_spectral_deriv<<<njobs, kFftThreads, smem, st>>>(A, jobs);
-  return cudaPeekAtLastError();
+  return sfd_launch(k_spectral_deriv, dim3(njobs), dim3(kFftThreads), smem, st, true, A, jobs);
 }

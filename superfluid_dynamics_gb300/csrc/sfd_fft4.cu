@@ -277,6 +277,7 @@ __device__ __forceinline__ void f4_run(const DerivArgs& A, const F4Job& J, const
 template <int PHASE>
 __global__ void __launch_bounds__(kF4Threads) k_fft4(DerivArgs A, const F4Job* jobs, const int2* units, int nunits,
                                                      cd* scr) {
+  sfd_pdl_begin();
   __shared__ cd twL[128];
   const int lane = threadIdx.x & 31;
   const int ui = blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);  // grid = units / kWarpsPerCta: ui < nunits
@@ -303,8 +304,9 @@ cudaError_t sfd_launch_f4(const DerivArgs& A, const F4Plan& p, cd* scr, cudaStre
   const int nu = p.nunits[phase - 1];
   if (nu == 0) return cudaSuccess;
   const int grid = nu / kWarpsPerCta;  // every job contributes a multiple of 4 units
-  if (phase == 1) k_fft4<1><<<grid, kF4Threads, 0, st>>>(A, p.jobs, p.units[0], nu, scr);
-  else if (phase == 2) k_fft4<2><<<grid, kF4Threads, 0, st>>>(A, p.jobs, p.units[1], nu, scr);
-  else k_fft4<3><<<grid, kF4Threads, 0, st>>>(A, p.jobs, p.units[2], nu, scr);
-  return cudaPeekAtLastError();  // the caller's launch check reads and clears it
+  const F4Job* jobs = p.jobs;
+  const int2* units = p.units[phase - 1];
+  if (phase == 1) return sfd_launch(k_fft4<1>, dim3(grid), dim3(kF4Threads), 0, st, true, A, jobs, units, nu, scr);
+  if (phase == 2) return sfd_launch(k_fft4<2>, dim3(grid), dim3(kF4Threads), 0, st, true, A, jobs, units, nu, scr);
+  return sfd_launch(k_fft4<3>, dim3(grid), dim3(kF4Threads), 0, st, true, A, jobs, units, nu, scr);
 }

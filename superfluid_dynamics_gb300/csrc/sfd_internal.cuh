@@ -32,6 +32,9 @@ enum {
   SFD_K_VELOCITY,
   SFD_K_RK4,
   SFD_K_UPDATE_TC,
+  SFD_K_F4_COLS,   // four-step transforms: forward column FFTs
+  SFD_K_F4_ROWS,   // row FFTs, multipliers, inverse row FFTs
+  SFD_K_F4_ICOLS,  // inverse column FFTs and outputs
   SFD_NCLASS
 };
 
@@ -72,7 +75,8 @@ struct sfd_engine {
   cd* f4_scr = nullptr;
   int2* d_sum_items = nullptr; int nsum = 0;
   // FP32 pass: (tile, source slice) work entries, per-entry partials, per-tile counters
-  int4* d_f32_work = nullptr; int nf32 = 0;
+  F32Work* d_f32_work = nullptr; int nf32 = 0;
+  int f32_max_per = 0;  // sources of the widest slice
   float4* f32_part = nullptr;
   float2* f32_wsum = nullptr;
   unsigned int* f32_count = nullptr;

@@ -40,6 +40,7 @@
 __global__ void __launch_bounds__(64) k_node_prep(const SurfaceDesc* surf, const int* node_surf, int ntot,
                                                   const double* x, const double* y, const cd* zp, const cd* zpp,
                                                   NodeData nd, double* rslot, double* bnorm) {
+  sfd_pdl_begin();
   const int g = blockIdx.x * 32 + (threadIdx.x & 31);
   if (g >= ntot) return;
   const int sidx = node_surf[g];
@@ -405,6 +406,7 @@ __device__ __forceinline__ double sums_finish(const SumArgs& A, const SurfaceDes
 template <int PREC, int G>
 __global__ void __cluster_dims__(kSumCL, 1, 1) __launch_bounds__(G * kSumTile, 1024 / (G * kSumTile))
     k_boundary_sums(SumArgs A) {
+  sfd_pdl_begin();
   constexpr int kSumGroups = G;                  // source groups per CTA (tuned per engine)
   constexpr int kSumThreads = G * kSumTile;
   namespace cg = cooperative_groups;
@@ -551,10 +553,10 @@ cudaError_t configure_prec(int bytes) {
   return e;
 }
 template <int PREC>
-void launch_prec(const SumArgs& A, dim3 grid, int groups, size_t smem, cudaStream_t st) {
-  if (groups == 2) k_boundary_sums<PREC, 2><<<grid, 2 * kSumTile, smem, st>>>(A);
-  else if (groups == 8) k_boundary_sums<PREC, 8><<<grid, 8 * kSumTile, smem, st>>>(A);
-  else k_boundary_sums<PREC, 4><<<grid, 4 * kSumTile, smem, st>>>(A);
+cudaError_t launch_prec(const SumArgs& A, dim3 grid, int groups, size_t smem, cudaStream_t st) {
+  if (groups == 2) return sfd_launch(k_boundary_sums<PREC, 2>, grid, dim3(2 * kSumTile), smem, st, true, A);
+  if (groups == 8) return sfd_launch(k_boundary_sums<PREC, 8>, grid, dim3(8 * kSumTile), smem, st, true, A);
+  return sfd_launch(k_boundary_sums<PREC, 4>, grid, dim3(4 * kSumTile), smem, st, true, A);
 }
 }  // namespace
 
@@ -572,10 +574,9 @@ cudaError_t sfd_launch_sums(int prec, const SumArgs& A, int nitems, int max_n, i
   if (nitems == 0) return cudaSuccess;
   const dim3 grid(nitems * kSumCL);
   const size_t smem = sfd_sums_smem(prec, max_n);
-  if (prec == SFD_PREC_F64) launch_prec<SFD_PREC_F64>(A, grid, groups, smem, st);
-  else if (prec == SFD_PREC_DF) launch_prec<SFD_PREC_DF>(A, grid, groups, smem, st);
-  else launch_prec<SFD_PREC_F32>(A, grid, groups, smem, st);
-  return cudaPeekAtLastError();  // the caller's launch check reads and clears it
+  if (prec == SFD_PREC_F64) return launch_prec<SFD_PREC_F64>(A, grid, groups, smem, st);
+  if (prec == SFD_PREC_DF) return launch_prec<SFD_PREC_DF>(A, grid, groups, smem, st);
+  return launch_prec<SFD_PREC_F32>(A, grid, groups, smem, st);
 }
 
 // ----------------------------------------------------------------- FP32 pass
@@ -675,16 +676,39 @@ __device__ __forceinline__ void load_target(const SumArgs& A, int g, bool image,
 }
 }  // namespace
 
+// Asynchronous global -> shared copies (cp.async): the copy needs no
+// register; the issuing thread waits for its own copies before reading them.
+__device__ __forceinline__ void cp_async16(void* sdst, const void* gsrc) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((unsigned)__cvta_generic_to_shared(sdst)),
+               "l"(gsrc)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* sdst, const void* gsrc) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"((unsigned)__cvta_generic_to_shared(sdst)),
+               "l"(gsrc)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// Epilogue operands of one target of the FP32 pass (16-byte aligned fields
+// for the 16-byte copies).
+struct __align__(16) F32Epi {
+  float4 w;  // w as double-float pairs
+  cd zp;     // z'
+  double a, md, b;  // weight, M diagonal, phi' (first pass) or r (correction)
+  double pad;
+};
+
 __global__ void __launch_bounds__(kF32Threads, 8) k_sums_f32(SumArgs A) {
-  const int4 wk = A.swork[blockIdx.x];  // item, slice, first work entry of the item, slices
-  const int2 item = A.items[wk.x];
-  const int sidx = item.x, t0 = item.y;
+  sfd_pdl_begin();
+  const F32Work wk = A.swork[blockIdx.x];
+  const int sidx = wk.sidx, t0 = wk.t0;
   if (!gate_open(A.gate, sidx)) return;  // every slice of the tile skips together
-  const SurfaceDesc& S = A.surf[sidx];
-  const int n = S.n, off = S.off;
-  const bool image = (S.physics == 1 && !S.infinite_depth);
-  const int per = (n + wk.w - 1) / wk.w;
-  const int j_lo = min(n, wk.y * per), j_hi = min(n, j_lo + per), jn = j_hi - j_lo;
+  const int n = wk.n, off = wk.off;
+  const bool image = wk.image != 0;
+  const int per = (n + wk.nsl - 1) / wk.nsl;
+  const int j_lo = min(n, wk.slice * per), j_hi = min(n, j_lo + per), jn = j_hi - j_lo;
   extern __shared__ float4 f32_src[];  // 2 float4 per source
   __shared__ float4 red[kF32Groups][64];
   __shared__ df wred[kF32Groups];
@@ -726,7 +750,7 @@ __global__ void __launch_bounds__(kF32Threads, 8) k_sums_f32(SumArgs A) {
   __syncthreads();
 
   // ---- this slice's partials (groups in order), then count the slice done
-  const long long entry = wk.z + wk.y;
+  const long long entry = wk.base + wk.slice;
   if (tid < 64) {
     float4 v = red[0][tid];
 #pragma unroll
@@ -743,36 +767,55 @@ __global__ void __launch_bounds__(kF32Threads, 8) k_sums_f32(SumArgs A) {
   }
   __threadfence();
   __syncthreads();
-  if (tid == 0) last = atomicAdd(A.scount + wk.x, 1u) == (unsigned)(wk.w - 1);
+  if (tid == 0) last = atomicAdd(A.scount + wk.item, 1u) == (unsigned)(wk.nsl - 1);
   __syncthreads();
   if (!last) return;
   __threadfence();  // the other slices' partials are visible from here
 
   // ---- the last slice of the tile: reduce in slice order, FP32 epilogue.
-  // Two threads per target: half h loads slices [8h, 8h + 8) at once (one L2
-  // round trip) and sums them in order; half 1 hands its sum to half 0, which
-  // adds it last, so the order is fixed.
-  if (tid == 0) A.scount[wk.x] = 0u;  // every slice has counted: ready for the next pass
+  // Two threads per target: half h sums its half of the slices in order (8
+  // loads per L2 round trip); half 1 hands its sum to half 0, which adds it
+  // last, so the order is fixed.
+  if (tid == 0) A.scount[wk.item] = 0u;  // every slice has counted: ready for the next pass
   __shared__ float hsum[64][10];
+  // epilogue operands of target t0 + tid: asynchronous copies into shared
+  // memory, in flight together with the partial loads below (no registers
+  // held across them)
+  __shared__ F32Epi epi[64];
+  const int tk = t0 + tid;
+  const int ge = off + (tk < n ? tk : 0);
+  if (tid < 64) {
+    F32Epi& E = epi[tid];
+    cp_async16(&E.w, A.wdf + ge);
+    cp_async16(&E.zp, A.zp + ge);
+    cp_async8(&E.a, A.a + ge);
+    cp_async8(&E.md, A.mdiag + ge);
+    cp_async8(&E.b, (A.mode == 0 ? A.phip : A.r) + ge);
+    cp_async_commit();
+  }
   df sr{0.f, 0.f}, si{0.f, 0.f}, tr{0.f, 0.f}, ti{0.f, 0.f}, aw{0.f, 0.f};
   {
     const int t = tid & 63, h = tid >> 6;
-    float4 pv[8];
-    float2 pw[8];
+    const int half = (wk.nsl + 1) >> 1;
+    const int s_lo = h * half, s_hi = min(wk.nsl, s_lo + half);
+    for (int c0 = s_lo; c0 < s_hi; c0 += 8) {  // 8 loads in flight per round trip
+      float4 pv[8];
+      float2 pw[8];
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      const int sl = 8 * h + i;
-      pv[i] = sl < wk.w ? __ldcg(A.spart + (wk.z + sl) * 64LL + t) : make_float4(0.f, 0.f, 0.f, 0.f);
-      pw[i] = sl < wk.w ? __ldcg(A.swsum + wk.z + sl) : make_float2(0.f, 0.f);
-    }
+      for (int i = 0; i < 8; ++i) {
+        const int sl = c0 + i;
+        pv[i] = sl < s_hi ? __ldcg(A.spart + (wk.base + sl) * 64LL + t) : make_float4(0.f, 0.f, 0.f, 0.f);
+        pw[i] = sl < s_hi ? __ldcg(A.swsum + wk.base + sl) : make_float2(0.f, 0.f);
+      }
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      if (8 * h + i < wk.w) {
-        sr = df_add(sr, df{pv[i].x, 0.f});
-        si = df_add(si, df{pv[i].y, 0.f});
-        tr = df_add(tr, df{pv[i].z, 0.f});
-        ti = df_add(ti, df{pv[i].w, 0.f});
-        aw = df_add(aw, df{pw[i].x, pw[i].y});
+      for (int i = 0; i < 8; ++i) {
+        if (c0 + i < s_hi) {
+          sr = df_add(sr, df{pv[i].x, 0.f});
+          si = df_add(si, df{pv[i].y, 0.f});
+          tr = df_add(tr, df{pv[i].z, 0.f});
+          ti = df_add(ti, df{pv[i].w, 0.f});
+          aw = df_add(aw, df{pw[i].x, pw[i].y});
+        }
       }
     }
     if (h == 1) {
@@ -789,15 +832,18 @@ __global__ void __launch_bounds__(kF32Threads, 8) k_sums_f32(SumArgs A) {
     ti = df_add(ti, df{o[6], o[7]});
     aw = df_add(aw, df{o[8], o[9]});
   }
-  const int tk = t0 + tid;
+  cp_async_wait_all();  // this thread's own copies: no barrier needed
   double rv = 0.0, bv = 0.0;
   if (tk < n) {
-    const int g = off + tk;
+    const int g = ge;
+    const F32Epi& E = epi[tid];
+    const float4 ew = E.w;
+    const cd ezp = E.zp;
+    const double emd = E.md, eb = E.b;
     constexpr float inv4pi = (float)(0.25 / SFD_PI);
-    const float c1 = S.physics == 0 ? (float)(0.25 * (1 - S.rho) / SFD_PI) : inv4pi;
-    const float4 wv = A.wdf[g];
-    const float wr = wv.x + wv.y, wi = wv.z + wv.w;
-    const float ak = (float)A.a[g];
+    const float c1 = wk.c1;
+    const float wr = ew.x + ew.y, wi = ew.z + ew.w;
+    const float ak = (float)E.a;
     const float Sr = sr.hi + sr.lo, Si = si.hi + si.lo, Af = aw.hi + aw.lo;
     // C = i (2 w S - (A - a_k)),  D = -i (2 T - A)
     const float ur = 2.f * (wr * Sr - wi * Si) - (Af - ak), ui = 2.f * (wr * Si + wi * Sr);
@@ -807,14 +853,13 @@ __global__ void __launch_bounds__(kF32Threads, 8) k_sums_f32(SumArgs A) {
       Dr = 2.f * (ti.hi + ti.lo);
       Di = -(2.f * (tr.hi + tr.lo) - Af);
     }
-    const cd zp = A.zp[g];
-    float ma = (float)A.mdiag[g] * ak + c1 * ((float)zp.re * Ci + (float)zp.im * Cr);
+    float ma = (float)emd * ak + c1 * ((float)ezp.re * Ci + (float)ezp.im * Cr);
     if (image) ma -= inv4pi * Di;
     double rnew;
     if (A.mode == 0) {
       A.cacc[g] = cd{(double)Cr, (double)Ci};
       if (image) A.dacc[g] = cd{(double)Dr, (double)Di};
-      rnew = A.phip[g] - (double)ma;
+      rnew = eb - (double)ma;
     } else {
       const cd c = A.cacc[g];
       A.cacc[g] = cd{c.re + (double)Cr, c.im + (double)Ci};
@@ -822,14 +867,14 @@ __global__ void __launch_bounds__(kF32Threads, 8) k_sums_f32(SumArgs A) {
         const cd d = A.dacc[g];
         A.dacc[g] = cd{d.re + (double)Dr, d.im + (double)Di};
       }
-      rnew = A.r[g] - (double)ma;
+      rnew = eb - (double)ma;
     }
     A.r[g] = rnew;
     if (A.rf) A.rf[g] = (float)rnew;
     rv = fabs(rnew);
     rv = (rv == rv) ? rv : 1e300;
-    if (A.bnorm) {
-      const double b = fabs(A.phip[g]);
+    if (A.bnorm) {  // mode 0: eb = phi'
+      const double b = fabs(eb);
       bv = (b == b) ? b : 1e300;
     }
   }
@@ -845,13 +890,18 @@ __global__ void __launch_bounds__(kF32Threads, 8) k_sums_f32(SumArgs A) {
   if (A.bnorm) warp_max_to(bv, A.bnorm + sidx);
 }
 
-cudaError_t sfd_launch_sums_f32(const SumArgs& A, int nwork, int max_n, cudaStream_t st) {
+static size_t f32_smem(int max_per) { return (size_t)std::max(1, max_per) * 2 * sizeof(float4); }
+
+cudaError_t sfd_f32_ctas_per_sm(int max_per, int* ctas) {
+  const size_t smem = f32_smem(max_per);
+  cudaError_t e = cudaFuncSetAttribute(k_sums_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctas, k_sums_f32, kF32Threads, smem);
+  return e;
+}
+
+cudaError_t sfd_launch_sums_f32(const SumArgs& A, int nwork, int max_per, cudaStream_t st) {
   if (nwork == 0) return cudaSuccess;
-  // the widest slice of any surface: at most 256 sources up to n = 4096 (16
-  // slices), then ceil(n / 16) <= 512
-  const size_t smem = (size_t)std::max(256, (max_n + 15) / 16) * 2 * sizeof(float4);
-  k_sums_f32<<<nwork, kF32Threads, smem, st>>>(A);
-  return cudaPeekAtLastError();
+  return sfd_launch(k_sums_f32, dim3(nwork), dim3(kF32Threads), f32_smem(max_per), st, true, A);
 }
 
 // Velocities and Bernoulli:
@@ -861,6 +911,7 @@ cudaError_t sfd_launch_sums_f32(const SumArgs& A, int nwork, int max_n, cudaStre
 //   driven helium adds damping * v + strength * I(y, x) [+ D, dD = beta I - D / tau]
 // Output goes to the RHS slot (dx, dy, dphi [, dD]).  Status bit on non-finite values.
 __global__ void k_velocity_bernoulli(VelArgs V) {
+  sfd_pdl_begin();
   int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= V.ntot) return;
   const int s = V.node_surf[g];
@@ -955,6 +1006,7 @@ __global__ void k_velocity_bernoulli(VelArgs V) {
 // The water cross term reads the lower velocity of concatenated node 1
 // (createM.cuh:104).  For rho != 0 that value is computed first (one thread).
 __global__ void k_velocity_node1(VelArgs V) {
+  sfd_pdl_begin();
   if (blockIdx.x != 0 || threadIdx.x != 0) return;
   int g = V.ntot > 1 ? 1 : 0;
   const SurfaceDesc& S = V.surf[V.node_surf[g]];
@@ -970,6 +1022,7 @@ __global__ void k_velocity_node1(VelArgs V) {
 //   kacc = (first ? k : kacc + wk * k);  ystage = y0 + cy * k  (if cy != 0)
 __global__ void k_rk4_stage(int n3, const double* __restrict__ y0, const double* __restrict__ k,
                             double* __restrict__ kacc, double* __restrict__ ystage, double wk, double cy, int first) {
+  sfd_pdl_begin();
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n3) return;
   double kv = k[i];
@@ -977,6 +1030,7 @@ __global__ void k_rk4_stage(int n3, const double* __restrict__ y0, const double*
   if (ystage) ystage[i] = y0[i] + cy * kv;
 }
 __global__ void k_rk4_final(int n3, double* __restrict__ y0, const double* __restrict__ kacc, double c) {
+  sfd_pdl_begin();
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n3) return;
   y0[i] = y0[i] + c * kacc[i];

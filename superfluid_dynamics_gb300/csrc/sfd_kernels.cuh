@@ -48,18 +48,36 @@ struct SumArgs {
   Gate gate;            // extra corrections: skip surfaces whose previous residual is converged
   // FP32 pass (k_sums_f32): one CTA per (tile, source slice); the last CTA
   // of a tile to finish reduces the slices in order and runs the epilogue
-  const int4* swork;    // (item, slice, first work entry of the item, slices of the item)
+  const struct F32Work* swork;  // one entry per CTA
   float4* spart;        // per work entry: 64 target partials (S re, S im, T re, T im)
   float2* swsum;        // per work entry: weight-sum partial (double-float)
   unsigned int* scount; // per item: slices finished (the last one resets it)
 };
 
-// Source slices of one 64-target tile in the FP32 pass: about 256 sources
-// each, at most 16.
-__host__ __device__ __forceinline__ int sfd_f32_slices(int n) {
-  const int s = (n + 255) / 256;
-  return s < 1 ? 1 : (s > 16 ? 16 : s);
-}
+// One CTA of the FP32 pass: everything it needs before its first source
+// (no dependent loads of the item list or the surface descriptor).
+struct F32Work {
+  int item;    // index of the (surface, tile) item: its counter
+  int slice;   // this CTA's slice of the sources
+  int base;    // work entry of the item's slice 0 (partials are base + slice)
+  int nsl;     // slices of the item
+  int sidx;    // surface
+  int t0;      // first target of the tile
+  int n, off;  // surface nodes and node offset
+  int image;   // finite-depth helium: image sums
+  float c1;    // (1 - rho) / 4 pi (water), 1 / 4 pi (helium): factor of z' C in M a
+  int pad[2];
+};
+
+// Source slices of the FP32 pass: at least kF32MinPer sources and at most
+// kF32MaxSlices slices per tile (SFD_F32_SLICES in the environment lowers or
+// raises the cap, up to 64); slices above kF32MaxPer sources take a second
+// wave rather than more shared memory (planned at engine creation).
+constexpr int kF32MinPer = 64;
+constexpr int kF32MaxPer = 512;
+constexpr int kF32MaxSlices = 16;
+// Resident CTAs per SM of the FP32 pass with slices of up to max_per sources.
+cudaError_t sfd_f32_ctas_per_sm(int max_per, int* ctas);
 
 struct VelArgs {
   const SurfaceDesc* surf;
@@ -99,8 +117,9 @@ __global__ void k_node_prep(const SurfaceDesc* surf, const int* node_surf, int n
                             const double* y, const cd* zp, const cd* zpp, NodeData nd, double* rslot,
                             double* bnorm);
 cudaError_t sfd_launch_sums(int prec, const SumArgs& A, int nitems, int max_n, int groups, cudaStream_t st);
-// FP32 pass over `nwork` (tile, slice) entries (A.swork).
-cudaError_t sfd_launch_sums_f32(const SumArgs& A, int nwork, int max_n, cudaStream_t st);
+// FP32 pass over `nwork` (tile, slice) entries (A.swork), slices of at most
+// max_per sources.
+cudaError_t sfd_launch_sums_f32(const SumArgs& A, int nwork, int max_per, cudaStream_t st);
 cudaError_t sfd_sums_configure();
 __global__ void k_velocity_bernoulli(VelArgs V);
 __global__ void k_velocity_node1(VelArgs V);

@@ -760,6 +760,7 @@ __device__ __forceinline__ void gemv_store(float yr, int g, double* y, float2* y
 __global__ void __launch_bounds__(256) k_gemv(const SurfaceDesc* surf, const int2* rowblk, const float* mat,
                                               const float* v, double* y, float2* ydf, double* accv, float2* accdf,
                                               Gate gate) {
+  sfd_pdl_begin();
   const int2 rb = rowblk[blockIdx.x];  // (surface, first row)
   if (!gate_open(gate, rb.x)) return;
   const SurfaceDesc& S = surf[rb.x];
@@ -841,6 +842,7 @@ __global__ void __launch_bounds__(256) k_precond_to_half(const SurfaceDesc* surf
 __global__ void __launch_bounds__(512) k_gemv_h(const SurfaceDesc* surf, const int2* rowblk, const __half* mat16,
                                                 const float* rscale, const float* v, double* y, float2* ydf,
                                                 double* accv, float2* accdf, Gate gate) {
+  sfd_pdl_begin();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   // row blocks from the list, or (rowblk null: one surface) rows interleaved
   // over the grid, r = block + grid * warp, so every SM gets the same number

@@ -28,6 +28,14 @@ def test_class_roofline_counts_the_work_actually_run():
     assert c["gemv"]["bound"] == "hbm" and math.isclose(c["gemv"]["work_per_step"], 20 * 2.0 * n * n)
 
 
+def test_fft4_work_counts_five_n_log_n_per_transform():
+    n = 4096  # N2 = 64: per stage 3 forward column sets, 7 row sets, 4 inverse column sets of 64 FFTs of 64 points
+    per_fft = 5.0 * 64 * 6
+    assert math.isclose(bench.fft4_work_per_step("fft4_columns", n), 4 * 3 * 64 * per_fft)
+    assert math.isclose(bench.fft4_work_per_step("fft4_rows", n), 4 * 7 * 64 * per_fft)
+    assert math.isclose(bench.fft4_work_per_step("fft4_inverse_columns", n), 4 * 4 * 64 * per_fft)
+
+
 def test_traffic_lookup_misses_cleanly():
     assert bench.kernel_traffic("no_such_kernel", 4096) is None
 
