@@ -197,6 +197,10 @@ def kernel_traffic(kernel: str, n: int):
 #                        3 x 64 forward columns (L = N2), 7 x N2 rows
 #                        (L = 64), 4 x 64 inverse columns per stage
 #   node_prep, velocity_bernoulli, rk4_combine: O(n), reported by time only
+#   extra_corrections, ap_redo: the gated extra corrections and the a'
+#                        transform repeated after them; they return at once
+#                        where the residual is converged (no work counted),
+#                        reported by time only
 FLOP_PER_PAIR = {"boundary_sums_fp32": 15.0, "boundary_sums_df": 94.0, "boundary_sums_fp64": 11.0}
 
 
@@ -583,9 +587,10 @@ def run_ours(args, rank, world, local_rank):
                             f"{peak_kind} HBM copy"),
             "peaks": pk, "classes": classes,
             "note": "achieved = algorithmic work of the class per step / its event-timed device time per step "
-                    "(eager pass over one preconditioner period, graphs off; launches_per_step includes the gated "
-                    "extra-correction launches that return at once); the step is neither HBM- nor tensor-bound: "
-                    "the boundary sums run on the FP32 pipes, the transforms on the FP64 pipe"}
+                    "(eager pass over one preconditioner period, graphs off); the gated extra corrections and the "
+                    "repeated a' transform are the classes extra_corrections and ap_redo, timed but counted as no "
+                    "work; the step is neither HBM- nor tensor-bound: the boundary sums run on the FP32 pipes, "
+                    "the transforms on the FP64 pipe"}
 
     if not args.no_adjoint:
         line["adjoint"] = adjoint_ratio(local_rank)

@@ -205,8 +205,11 @@ long long sfd_kernel_launches(const sfd_engine* e);
 /* Per-kernel-class device time: while enabled, RK4 steps run eagerly (no
  * graph) and every kernel launch is bracketed by CUDA events on the engine
  * stream; sfd_profile_read returns accumulated milliseconds and launch counts
- * per class (names from sfd_profile_class_name; 19 classes). */
-#define SFD_PROFILE_CLASSES 19
+ * per class (names from sfd_profile_class_name; 21 classes).  The gated extra
+ * corrections and the a' transform repeated after them have classes of their
+ * own ("extra_corrections", "ap_redo"), so the other classes hold working
+ * launches only. */
+#define SFD_PROFILE_CLASSES 21
 int sfd_profile(sfd_engine* e, int enable);
 int sfd_profile_read(sfd_engine* e, double* ms, long long* counts, int nclass);
 const char* sfd_profile_class_name(int cls);

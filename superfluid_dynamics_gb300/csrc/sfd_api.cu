@@ -207,10 +207,11 @@ int enqueue_sums(sfd_engine* e, int prec, const double* weights, const float2* w
             (mode == 0 && e->rslot) ? e->bnorm : nullptr, make_gate(e, gate),
             e->d_f32_work, e->f32_part, e->f32_wsum, e->f32_count};
   if (prec == SFD_PREC_F32 && e->d_f32_work) {
-    LAUNCHC(e, SFD_K_SUMS32, sfd_launch_sums_f32(A, e->nf32, e->f32_max_per, e->stream));
+    LAUNCHC(e, gate >= 0 ? SFD_K_EXTRA : SFD_K_SUMS32, sfd_launch_sums_f32(A, e->nf32, e->f32_max_per, e->stream));
     return 0;
   }
   int cls = prec == SFD_PREC_F64 ? SFD_K_SUMS64 : prec == SFD_PREC_DF ? SFD_K_SUMSDF : SFD_K_SUMS32;
+  if (gate >= 0) cls = SFD_K_EXTRA;
   LAUNCHC(e, cls, sfd_launch_sums(prec, A, e->nsum, e->max_n, e->sum_groups[prec], e->stream));
   return 0;
 }
@@ -221,17 +222,18 @@ int enqueue_sums(sfd_engine* e, int prec, const double* weights, const float2* w
 int enqueue_gemv(sfd_engine* e, const float* vf, double* y, float2* ydf, double* acc, float2* accdf,
                  int gate = -1) {
   const Gate G = make_gate(e, gate);
+  const int cls = gate >= 0 ? SFD_K_EXTRA : SFD_K_GEMV;
   if (e->m16 && e->nsurf == 1 && e->nsm > 0) {
     // one surface: a whole number of waves of two CTAs per SM, rows interleaved
     const int wave = 2 * e->nsm, need = (e->max_n + kGemvRows - 1) / kGemvRows;
     const int grid = (need + wave - 1) / wave * wave;
-    LAUNCHC(e, SFD_K_GEMV, sfd_launch(k_gemv_h, dim3(grid), dim3(512), e->max_np * sizeof(float), e->stream, true,
+    LAUNCHC(e, cls, sfd_launch(k_gemv_h, dim3(grid), dim3(512), e->max_np * sizeof(float), e->stream, true,
                                       e->d_surf, (const int2*)nullptr, e->m16, e->rscale, vf, y, ydf, acc, accdf, G));
   } else if (e->m16)
-    LAUNCHC(e, SFD_K_GEMV, sfd_launch(k_gemv_h, dim3(e->ngemv), dim3(512), e->max_np * sizeof(float), e->stream, true,
+    LAUNCHC(e, cls, sfd_launch(k_gemv_h, dim3(e->ngemv), dim3(512), e->max_np * sizeof(float), e->stream, true,
                                       e->d_surf, e->d_gemv_rows, e->m16, e->rscale, vf, y, ydf, acc, accdf, G));
   else
-    LAUNCHC(e, SFD_K_GEMV, sfd_launch(k_gemv, dim3(e->ngemv), dim3(256), e->max_np * sizeof(float), e->stream, true,
+    LAUNCHC(e, cls, sfd_launch(k_gemv, dim3(e->ngemv), dim3(256), e->max_np * sizeof(float), e->stream, true,
                                       e->d_surf, e->d_gemv_rows, e->m32, vf, y, ydf, acc, accdf, G));
   return 0;
 }
@@ -302,17 +304,19 @@ cudaError_t launch_transforms(const sfd_engine* e, const DerivArgs& D, bool firs
 // with single-kernel classes).
 int enqueue_transforms(sfd_engine* e, const DerivArgs& D, bool first) {
   const int nj = first ? e->njobs_first : e->njobs_ap, ncj = first ? e->ncjobs_first : e->ncjobs_ap;
+  const bool redo = D.gate.slot != nullptr;  // gated a' after extra corrections: a class of its own
   if (nj)
-    LAUNCHC(e, SFD_K_SPECTRAL,
+    LAUNCHC(e, redo ? SFD_K_AP_REDO : SFD_K_SPECTRAL,
             sfd_launch_spectral(D, first ? e->d_jobs_first : e->d_jobs_ap, nj, e->max_n_single, e->stream));
   if (ncj)
-    LAUNCHC(e, SFD_K_SPECTRAL, sfd_launch_spectral_cluster(D, first ? e->d_cjobs_first : e->d_cjobs_ap, ncj,
-                                                           e->max_n_cluster, e->stream));
+    LAUNCHC(e, redo ? SFD_K_AP_REDO : SFD_K_SPECTRAL,
+            sfd_launch_spectral_cluster(D, first ? e->d_cjobs_first : e->d_cjobs_ap, ncj, e->max_n_cluster,
+                                        e->stream));
   const F4Plan& p = first ? e->f4_first : e->f4_ap;
   if (p.njobs) {
-    LAUNCHC(e, SFD_K_F4_COLS, sfd_launch_f4(D, p, e->f4_scr, e->stream, 1));
-    LAUNCHC(e, SFD_K_F4_ROWS, sfd_launch_f4(D, p, e->f4_scr, e->stream, 2));
-    LAUNCHC(e, SFD_K_F4_ICOLS, sfd_launch_f4(D, p, e->f4_scr, e->stream, 3));
+    LAUNCHC(e, redo ? SFD_K_AP_REDO : SFD_K_F4_COLS, sfd_launch_f4(D, p, e->f4_scr, e->stream, 1));
+    LAUNCHC(e, redo ? SFD_K_AP_REDO : SFD_K_F4_ROWS, sfd_launch_f4(D, p, e->f4_scr, e->stream, 2));
+    LAUNCHC(e, redo ? SFD_K_AP_REDO : SFD_K_F4_ICOLS, sfd_launch_f4(D, p, e->f4_scr, e->stream, 3));
   }
   return 0;
 }
@@ -375,8 +379,8 @@ int enqueue_solve(sfd_engine* e, const double* st, const double* phi_im, bool re
     // without exchanges that lost accuracy where partial pivoting would have
     // exchanged rows): delta = (LU)^-1 r, a += delta, r -= M delta
     for (int i = 1; i <= extra; ++i) {
-      LAUNCHC(e, SFD_K_TRSV, k_lu64_solve<<<e->nsurf, 256, e->max_np * sizeof(double), e->stream>>>(
-                                 e->d_surf, e->m64, e->r, e->delta, e->a, nullptr, make_gate(e, i - 1), nullptr, nullptr));
+      LAUNCHC(e, SFD_K_EXTRA, k_lu64_solve<<<e->nsurf, 256, e->max_np * sizeof(double), e->stream>>>(
+                                  e->d_surf, e->m64, e->r, e->delta, e->a, nullptr, make_gate(e, i - 1), nullptr, nullptr));
       rc = enqueue_sums(e, SFD_PREC_F64, e->delta, nullptr, 1, i, i - 1);
       if (rc) return rc;
     }
@@ -1406,7 +1410,8 @@ const char* sfd_profile_class_name(int cls) {
                                           "boundary_sums_df", "boundary_sums_fp32", "sum_epilogue", "assemble",
                                           "factor_diag", "factor_panel", "factor_update", "lu_trsv", "gemv",
                                           "velocity_bernoulli", "rk4_combine", "factor_update_tcgen05",
-                                          "fft4_columns", "fft4_rows", "fft4_inverse_columns"};
+                                          "fft4_columns", "fft4_rows", "fft4_inverse_columns", "extra_corrections",
+                                          "ap_redo"};
   return (cls >= 0 && cls < SFD_NCLASS) ? names[cls] : "";
 }
 

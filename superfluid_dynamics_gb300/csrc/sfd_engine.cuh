@@ -75,8 +75,8 @@ struct Gate {
 // waits, also one that returns early, so completion stays transitive along the
 // stream.  In a launch without the attribute both instructions return at once.
 __device__ __forceinline__ void sfd_pdl_begin() {
-  asm volatile("griddepcontrol.wait;\n" ::: "memory");
-  asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+  cudaGridDependencySynchronize();
+  cudaTriggerProgrammaticLaunchCompletion();
 }
 
 __device__ __forceinline__ bool gate_open(const Gate& G, int s) {

@@ -35,6 +35,8 @@ enum {
   SFD_K_F4_COLS,   // four-step transforms: forward column FFTs
   SFD_K_F4_ROWS,   // row FFTs, multipliers, inverse row FFTs
   SFD_K_F4_ICOLS,  // inverse column FFTs and outputs
+  SFD_K_EXTRA,     // extra corrections (gated: they return at once where the residual is converged)
+  SFD_K_AP_REDO,   // a' transformed again after extra corrections (gated likewise)
   SFD_NCLASS
 };
 

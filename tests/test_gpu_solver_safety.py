@@ -8,7 +8,7 @@
   gated extra corrections where it is above: forced on (a tolerance below
   round-off) the FP64 refinement runs, reports the stall and still matches
   the oracle.
-* A deliberately stale preconditioner (never rebuilt while a steep wave
+* A deliberately stale preconditioner (never rebuilt while a water wave
   evolves) is caught: without extra corrections the stall bit comes up and
   the host rebuilds the preconditioner; with them the residual is brought
   back under the tolerance.  Either way the trajectory stays on the FP64 one.
