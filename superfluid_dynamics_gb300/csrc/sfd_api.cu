@@ -1541,11 +1541,15 @@ sfd_problem helium_problem(const NondimProps& np, bool use_exp = false, int orde
   return p;
 }
 
+// Engines of the compatibility exports: eager launches, and no autotuning of
+// the sum shape, so that repeated calls give bitwise the same results (the
+// tuner keeps the fastest shape by timing, which sets the summation order).
 int make_engine(int n, int batch, const sfd_problem& p, sfd_engine** e, const sfd_drive* drive = nullptr) {
   sfd_options o;
   sfd_default_options(&o);
   o.precision = g_default_precision;
   o.use_graphs = 0;
+  o.autotune = 0;
   std::vector<int> ns(batch, n);
   return sfd_create_driven(ns.data(), batch, &p, drive, 1, &o, e);
 }
@@ -1906,6 +1910,7 @@ int calculateJacobian(const double* state, double* jac, double L, double rho, do
   sfd_default_options(&o);
   o.precision = SFD_PRECISION_FP64;
   o.use_graphs = 0;
+  o.autotune = 0;
   std::vector<double> hx, hy, hp, dx, dy, dp;
   for (size_t c0 = 0; c0 < n3; c0 += chunk) {
     const size_t nc = std::min(chunk, n3 - c0), ns = 2 * nc;
