@@ -324,11 +324,14 @@ int enqueue_transforms(sfd_engine* e, const DerivArgs& D, bool first) {
 // a' = d a / d xi (FftDerivative on a, BaseBoundaryIntegrator.cuh:201-203):
 // on the engine stream, or forked onto the auxiliary stream so that it runs
 // beside the last boundary-sum pass (that pass reads the weights delta and
-// writes C, D and r; the transform reads a and writes a').  The fork is
-// skipped under per-kernel profiling, whose events live on the engine stream.
+// writes C, D and r; the transform reads a and writes a').  Where the fork
+// is not possible (no auxiliary stream, or per-kernel profiling, whose events
+// live on the engine stream) nothing is launched here: enqueue_rhs transforms
+// a once the solve, extra corrections included, is done.
 int enqueue_ap(sfd_engine* e, bool fork) {
   DerivArgs D{e->d_surf, e->nsurf, nullptr, nullptr, nullptr, nullptr, e->a, e->zp, e->zpp, e->phip, e->ap, nullptr};
-  if (fork && e->aux && !e->profile) {
+  if (fork) {
+    if (!e->aux || e->profile) return 0;
     CK(cudaEventRecord(e->ev_fork, e->stream));
     CK(cudaStreamWaitEvent(e->aux, e->ev_fork, 0));
     int nl = 0;
