@@ -906,7 +906,7 @@ int sfd_create(const int* n, int nsurf, const sfd_problem* problems, int shared_
 // kF32MinPer sources per slice and at most kF32MaxSlices slices.
 static void plan_f32_slices(const std::vector<SurfaceDesc>& hs, int nsurf, int slots, std::vector<int>& out) {
   int cap = kF32MaxSlices;
-  if (const char* v = std::getenv("SFD_F32_SLICES")) cap = std::min(64, std::max(1, std::atoi(v)));
+  if (const char* v = std::getenv("SFD_F32_SLICES")) cap = std::min(kF32MaxSlices, std::max(1, std::atoi(v)));
   long long total = 0;
   for (int s = 0; s < nsurf; ++s) total += (long long)((hs[s].n + kSumTile - 1) / kSumTile) * hs[s].n;
   const long long waves = std::max(1LL, (total + (long long)slots * kF32MaxPer - 1) / ((long long)slots * kF32MaxPer));

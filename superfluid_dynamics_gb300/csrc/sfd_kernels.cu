@@ -175,10 +175,13 @@ __device__ __forceinline__ df2 two_prod2(float2 a, float2 b) {
   const float2 p = mul2(a, b);
   return {p, fma2(a, b, neg2(p))};
 }
-// df_diff per lane
+// df_diff per lane, for the node differences w_k - w_j (k != j): the
+// renormalisation is a quick two-sum, exact because |hi(w_k) - hi(w_j)| is at
+// least the node spacing (about 2 pi / n), far above the low parts' sum
+// (ulps of |w| ~ 1), whenever the two nodes are distinct in FP32
 __device__ __forceinline__ df2 df_diff2(float2 a_hi, float2 a_lo, float2 b_hi, float2 b_lo) {
   const df2 s = two_sum2(a_hi, neg2(b_hi));
-  return two_sum2(s.hi, add2(s.lo, sub2(a_lo, b_lo)));
+  return quick_two_sum2(s.hi, add2(s.lo, sub2(a_lo, b_lo)));
 }
 // df_mul per lane (normalised)
 __device__ __forceinline__ df2 df_mul2(float2 a_hi, float2 a_lo, float2 b_hi, float2 b_lo) {
@@ -196,8 +199,10 @@ __device__ __forceinline__ void df_acc2(df2& acc, float2 xh, float2 xl) {
   acc.hi = s.hi;
   acc.lo = add2(acc.lo, add2(s.lo, xl));
 }
-// (acc.x, acc.y) += a / (d.x + i d.y) = (a d.x / |d|^2, -a d.y / |d|^2): the
-// packed form of df_div_acc
+// (acc.x, acc.y) += (a d.x / |d|^2, a d.y / |d|^2): the packed form of
+// df_div_acc for a / (d.x + i d.y) = (a d.x, -a d.y) / |d|^2, with the
+// imaginary lane accumulated negated (no per-pair sign flips; negation is
+// exact, so to_red's flip gives bitwise the sums of the unflipped sequence)
 __device__ __forceinline__ void df_div_acc2(df2 d, df a, df2& acc) {
   const df2 P = two_prod2(d.hi, d.hi);
   const float2 E = fma2(mul2(d.hi, make_float2(2.f, 2.f)), d.lo, P.lo);
@@ -207,7 +212,7 @@ __device__ __forceinline__ void df_div_acc2(df2 d, df a, df2& acc) {
   const float2 th = make_float2(t.hi, t.hi), tl = make_float2(t.lo, t.lo);
   const df2 p = two_prod2(th, d.hi);
   const float2 e = fma2(th, d.lo, fma2(tl, d.hi, p.lo));
-  df_acc2(acc, make_float2(p.hi.x, -p.hi.y), make_float2(e.x, -e.y));
+  df_acc2(acc, p.hi, e);
 }
 
 // double-float source of the packed pass: hi parts and lo parts of w (and p)
@@ -233,8 +238,8 @@ struct Acc<SFD_PREC_F64> {
 };
 template <>
 struct Acc<SFD_PREC_DF> {
-  df2 s{{0.f, 0.f}, {0.f, 0.f}};  // (S re, S im)
-  df2 t{{0.f, 0.f}, {0.f, 0.f}};  // (T re, T im)
+  df2 s{{0.f, 0.f}, {0.f, 0.f}};  // (S re, -S im)
+  df2 t{{0.f, 0.f}, {0.f, 0.f}};  // (T re, -T im)
 };
 template <>
 struct Acc<SFD_PREC_F32> {
@@ -343,7 +348,7 @@ using WSum = typename std::conditional<PREC == SFD_PREC_F64, double, df>::type;
 __device__ __forceinline__ Red<SFD_PREC_F64> to_red(const Acc<SFD_PREC_F64>& A) { return {A.sr, A.si, A.tr, A.ti}; }
 __device__ __forceinline__ Red<SFD_PREC_DF> to_red(const Acc<SFD_PREC_DF>& A) {
   const df2 s = two_sum2(A.s.hi, A.s.lo), t = two_sum2(A.t.hi, A.t.lo);  // df_acc_done per lane
-  return {df{s.hi.x, s.lo.x}, df{s.hi.y, s.lo.y}, df{t.hi.x, t.lo.x}, df{t.hi.y, t.lo.y}};
+  return {df{s.hi.x, s.lo.x}, df{-s.hi.y, -s.lo.y}, df{t.hi.x, t.lo.x}, df{-t.hi.y, -t.lo.y}};
 }
 __device__ __forceinline__ Red<SFD_PREC_F32> to_red(const Acc<SFD_PREC_F32>& A) {
   return {df{A.sr, 0.f}, df{A.si, 0.f}, df{A.tr, 0.f}, df{A.ti, 0.f}};
@@ -765,17 +770,24 @@ __global__ void __launch_bounds__(kF32Threads, 8) k_sums_f32(SumArgs A) {
     for (int q = 1; q < kF32Groups; ++q) w = df_add(w, wred[q]);
     A.swsum[entry] = make_float2(w.hi, w.lo);
   }
-  __threadfence();
+  // Count the slice done with one acquire-release atomic instead of fences:
+  // the barrier orders every thread's partial stores before thread 0's
+  // release (release is cumulative), the counter's read-modify-writes form
+  // one release sequence, so the last slice's acquire sees every slice's
+  // partials, and its barrier orders them before its threads' loads.
   __syncthreads();
-  if (tid == 0) last = atomicAdd(A.scount + wk.item, 1u) == (unsigned)(wk.nsl - 1);
+  if (tid == 0) {
+    unsigned prev;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(prev) : "l"(A.scount + wk.item) : "memory");
+    last = prev == (unsigned)(wk.nsl - 1);
+  }
   __syncthreads();
   if (!last) return;
-  __threadfence();  // the other slices' partials are visible from here
 
   // ---- the last slice of the tile: reduce in slice order, FP32 epilogue.
-  // Two threads per target: half h sums its half of the slices in order (8
-  // loads per L2 round trip); half 1 hands its sum to half 0, which adds it
-  // last, so the order is fixed.
+  // Two threads per target: half h loads slices [8h, 8h + 8) at once (one L2
+  // round trip; at most kF32MaxSlices = 16 slices) and sums them in order;
+  // half 1 hands its sum to half 0, which adds it last, so the order is fixed.
   if (tid == 0) A.scount[wk.item] = 0u;  // every slice has counted: ready for the next pass
   __shared__ float hsum[64][10];
   // epilogue operands of target t0 + tid: asynchronous copies into shared
@@ -796,26 +808,22 @@ __global__ void __launch_bounds__(kF32Threads, 8) k_sums_f32(SumArgs A) {
   df sr{0.f, 0.f}, si{0.f, 0.f}, tr{0.f, 0.f}, ti{0.f, 0.f}, aw{0.f, 0.f};
   {
     const int t = tid & 63, h = tid >> 6;
-    const int half = (wk.nsl + 1) >> 1;
-    const int s_lo = h * half, s_hi = min(wk.nsl, s_lo + half);
-    for (int c0 = s_lo; c0 < s_hi; c0 += 8) {  // 8 loads in flight per round trip
-      float4 pv[8];
-      float2 pw[8];
+    float4 pv[8];
+    float2 pw[8];
 #pragma unroll
-      for (int i = 0; i < 8; ++i) {
-        const int sl = c0 + i;
-        pv[i] = sl < s_hi ? __ldcg(A.spart + (wk.base + sl) * 64LL + t) : make_float4(0.f, 0.f, 0.f, 0.f);
-        pw[i] = sl < s_hi ? __ldcg(A.swsum + wk.base + sl) : make_float2(0.f, 0.f);
-      }
+    for (int i = 0; i < 8; ++i) {  // slices [8h, 8h + 8): one L2 round trip
+      const int sl = 8 * h + i;
+      pv[i] = sl < wk.nsl ? __ldcg(A.spart + (wk.base + sl) * 64LL + t) : make_float4(0.f, 0.f, 0.f, 0.f);
+      pw[i] = sl < wk.nsl ? __ldcg(A.swsum + wk.base + sl) : make_float2(0.f, 0.f);
+    }
 #pragma unroll
-      for (int i = 0; i < 8; ++i) {
-        if (c0 + i < s_hi) {
-          sr = df_add(sr, df{pv[i].x, 0.f});
-          si = df_add(si, df{pv[i].y, 0.f});
-          tr = df_add(tr, df{pv[i].z, 0.f});
-          ti = df_add(ti, df{pv[i].w, 0.f});
-          aw = df_add(aw, df{pw[i].x, pw[i].y});
-        }
+    for (int i = 0; i < 8; ++i) {
+      if (8 * h + i < wk.nsl) {
+        sr = df_add(sr, df{pv[i].x, 0.f});
+        si = df_add(si, df{pv[i].y, 0.f});
+        tr = df_add(tr, df{pv[i].z, 0.f});
+        ti = df_add(ti, df{pv[i].w, 0.f});
+        aw = df_add(aw, df{pw[i].x, pw[i].y});
       }
     }
     if (h == 1) {

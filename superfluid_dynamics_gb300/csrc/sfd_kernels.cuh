@@ -70,9 +70,10 @@ struct F32Work {
 };
 
 // Source slices of the FP32 pass: at least kF32MinPer sources and at most
-// kF32MaxSlices slices per tile (SFD_F32_SLICES in the environment lowers or
-// raises the cap, up to 64); slices above kF32MaxPer sources take a second
-// wave rather than more shared memory (planned at engine creation).
+// kF32MaxSlices slices per tile (the last slice's reduction loads them in one
+// round trip; SFD_F32_SLICES in the environment lowers the cap); slices
+// above kF32MaxPer sources take a second wave rather than more shared memory
+// (planned at engine creation).
 constexpr int kF32MinPer = 64;
 constexpr int kF32MaxPer = 512;
 constexpr int kF32MaxSlices = 16;
