@@ -203,12 +203,21 @@ __device__ __forceinline__ void df_acc2(df2& acc, float2 xh, float2 xl) {
 // df_div_acc for a / (d.x + i d.y) = (a d.x, -a d.y) / |d|^2, with the
 // imaginary lane accumulated negated (no per-pair sign flips; negation is
 // exact, so to_red's flip gives bitwise the sums of the unflipped sequence)
+//   |d|^2: the two squares are non-negative, so ordered by size they need
+//   only a quick two-sum; a / |d|^2: one FP32 quotient from the reciprocal
+//   estimate and one correction from its remainder, formed exactly by FMAs
+//   (the double-float division without a separate reciprocal refinement).
 __device__ __forceinline__ void df_div_acc2(df2 d, df a, df2& acc) {
   const df2 P = two_prod2(d.hi, d.hi);
   const float2 E = fma2(mul2(d.hi, make_float2(2.f, 2.f)), d.lo, P.lo);
-  const df s = two_sum(P.hi.x, P.hi.y);
+  const df s = quick_two_sum(fmaxf(P.hi.x, P.hi.y), fminf(P.hi.x, P.hi.y));
   const df q = {s.hi, __fadd_rn(s.lo, __fadd_rn(E.x, E.y))};
-  const df t = df_mul_raw(a, df_rcp_raw(q));
+  float r0;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r0) : "f"(q.hi));
+  const float t0 = __fmul_rn(a.hi, r0);
+  float rem = __fmaf_rn(-t0, q.hi, a.hi);  // a - t0 q, exact in the high parts
+  rem = __fadd_rn(__fmaf_rn(-t0, q.lo, rem), a.lo);
+  const df t = {t0, __fmul_rn(rem, r0)};
   const float2 th = make_float2(t.hi, t.hi), tl = make_float2(t.lo, t.lo);
   const df2 p = two_prod2(th, d.hi);
   const float2 e = fma2(th, d.lo, fma2(tl, d.hi, p.lo));
