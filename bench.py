@@ -185,9 +185,11 @@ def kernel_traffic(kernel: str, n: int):
 #   boundary_sums_fp32 : per (target, source) pair, water: 15 FP32 FLOP (two
 #                        double-float-split differences, |d|^2, reciprocal
 #                        estimate, weight, two FMA accumulations)
-#   boundary_sums_df   : per pair, water: 94 FP32 FLOP (double-float
-#                        differences, squared norm, reciprocal with one Newton
-#                        step, three products, two cascaded accumulations)
+#   boundary_sums_df   : per pair, water: 77 FP32 FLOP, FMA = 2 (double-float
+#                        difference renormalised by a quick two-sum, squared
+#                        norm, quotient with one remainder correction, the two
+#                        products with d, cascaded accumulation; packed
+#                        FP32x2 lanes count twice)
 #   boundary_sums_fp64 : per pair, water: 11 FP64 FLOP
 #   gemv               : per product: 2 n^2 bytes (the FP16 preconditioner)
 #   fft4_columns, fft4_rows, fft4_inverse_columns (four-step transforms of a
@@ -201,7 +203,7 @@ def kernel_traffic(kernel: str, n: int):
 #                        transform repeated after them; they return at once
 #                        where the residual is converged (no work counted),
 #                        reported by time only
-FLOP_PER_PAIR = {"boundary_sums_fp32": 15.0, "boundary_sums_df": 94.0, "boundary_sums_fp64": 11.0}
+FLOP_PER_PAIR = {"boundary_sums_fp32": 15.0, "boundary_sums_df": 77.0, "boundary_sums_fp64": 11.0}
 
 
 def fft4_work_per_step(cls: str, n: int) -> float:
