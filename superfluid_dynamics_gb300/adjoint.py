@@ -2,8 +2,11 @@
 
 The backward pass calls the hand-written CUDA adjoint (sfd_rk4_vjp): each
 checkpoint segment of the trajectory is recomputed once with every RK4 stage
-recorded (LU factors included) and reversed stage by stage.  The reference has
-no reverse mode; it differentiates by finite differences
+recorded and reversed stage by stage.  With an FP64 engine the records include
+the LU factors of M and the transposed solve uses them; with a mixed engine
+(the production forward) the transposed solve is refinement preconditioned by
+the transpose of the engine's approximate inverse.  The reference has no
+reverse mode; it differentiates by finite differences
 (Python/integration/jacobian_tests.py:10-150).
 
     traj = Trajectory(n=512, physics=HeliumBoundaryProblem(depth=10.0, A3=1e3),
@@ -19,7 +22,7 @@ import dataclasses
 import numpy as np
 import torch
 
-from ._lib import HELIUM, PRECISION_FP64
+from ._lib import HELIUM, PRECISION_FP64, PRECISION_MIXED
 from .engine import Engine, Options, Physics
 
 
@@ -47,20 +50,30 @@ class _RK4Trajectory(torch.autograd.Function):
 
 
 class Trajectory:
-    """An FP64 engine for one surface plus the RK4 settings of the trajectory.
+    """An engine for one surface plus the RK4 settings of the trajectory.
 
-    The differentiated parameter is A3 for helium films and g for water.  The
-    engine holds one recording, so the backward of a forward must come before
-    the next forward on the same object (an out-of-order backward raises)."""
+    precision=PRECISION_FP64 (default) records LU factors and reproduces the
+    FP64 engine's steps bitwise; PRECISION_MIXED runs the forward on the
+    mixed engine (captured step graphs, preconditioner rebuilt every
+    `refactor_every` steps) and reverses it with the preconditioned transposed
+    solve.  The differentiated parameter is A3 for helium films and g for
+    water.  The engine holds one recording, so the backward of a forward must
+    come before the next forward on the same object (an out-of-order backward
+    raises)."""
 
     def __init__(self, n: int, physics: Physics, dt: float, steps: int, checkpoint_every: int = 50,
-                 device: int = 0):
+                 device: int = 0, precision: int = PRECISION_FP64, refactor_every: int = 50):
         self.n = int(n)
         self.physics = physics
         self.dt = float(dt)
         self.steps = int(steps)
         self.checkpoint_every = int(checkpoint_every)
-        self.engine = Engine(self.n, physics, Options(precision=PRECISION_FP64, use_graphs=False, device=device))
+        if precision == PRECISION_MIXED:
+            opts = Options(precision=PRECISION_MIXED, pre_iters=2, refactor_every=int(refactor_every),
+                           autotune=False, device=device)
+        else:
+            opts = Options(precision=PRECISION_FP64, use_graphs=False, device=device)
+        self.engine = Engine(self.n, physics, opts)
         self._recordings = 0  # forwards so far; a backward must belong to the latest
 
     def _apply_param(self, value: float) -> None:

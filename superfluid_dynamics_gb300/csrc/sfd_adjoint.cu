@@ -37,6 +37,22 @@
 //   state: gx = Re(gz + gZ),  gy = Im(gz + gZ) + Bernoulli part,  gphi = -s1 Re R1(lambda)
 // RK4 (AutonomousRungeKuttaStepper.cuh:338-375) is reversed stage by stage from
 // per-stage records made by recomputing each checkpoint segment.
+//
+// Two precisions, following the engine's:
+//  * FP64 engines record the LU factors of M per stage and solve M^T lambda = ga
+//    with them (U^T then L^T).
+//  * Mixed engines record O(n) data only.  The transposed solve is iterative
+//    refinement preconditioned by the transpose of the engine's approximate
+//    inverse X (FP16, row-scaled: X = diag(s) H, so X^T r = H^T (s r)):
+//      lambda_0 = X^T ga;  r = ga - M^T lambda (FP64, matrix-free);  lambda += X^T r
+//    where, with gC = i c1 conj(z') lambda and gD = -i cI lambda,
+//      (M^T lambda)_j = Mdiag_j lambda_j + Re(i (sum gC - gC_j) + 2 i conj(Sb_j)) + Re(-i sum gD + 2 i Tb_j)
+//    (Sb, Tb as in the ga line above, here with b_k = -i c1 w_k z'_k lambda_k).
+//    The iterations are gated on the residual (they return at once once
+//    max |r| <= 1e-13 max |ga|); a final residual above the engine's
+//    refine_tol raises SFD_ST_REFINE_STALL.  Every pair sum of one stage reads
+//    the pair reciprocals R_jk = 1 / (w_j - w_k) and I_jk = 1 / (1 - p_j conj p_k),
+//    computed once per stage in FP64 into two n x n complex matrices.
 #include <algorithm>
 #include <cstring>
 
@@ -47,7 +63,7 @@
 struct AdjStage {
   double* Y;   // stage state [x|y|phi]
   double* k;   // stage RHS [dx|dy|dphi]
-  double* lu;  // LU factors of M (np x np, row-major, no row exchanges)
+  double* lu;  // LU factors of M (np x np, row-major, no row exchanges); null for mixed engines
   double* a;
   cd *ap, *zp, *zpp, *C, *D, *w, *p;
 };
@@ -273,9 +289,14 @@ __global__ void __launch_bounds__(kAdjThreads) k_lu_solve_t(int n, int np, const
 }
 
 // M-part cotangents at fixed a (rho = -lambda); totals of gC, gD for pass 2.
+// With rmax (mixed engines' transposed solve), thread 0 also raises the
+// refinement-stall bit when the solve's final residual rmax[last] is above
+// tol * rmax[0] (or NaN).
 __global__ void k_adj_node2(AdjConst K, AdjStage st, const double* lambda, cd* cbar, cd* dbar, double* zpb_re,
-                            double* zpb_im, double* zppb_re, double* zppb_im) {
+                            double* zpb_im, double* zppb_re, double* zppb_im, const double* rmax, int last,
+                            double tol, unsigned int* status) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (rmax && k == 0 && !(rmax[last] <= tol * rmax[0])) atomicOr(status, (unsigned int)SFD_ST_REFINE_STALL);
   if (k >= K.n) return;
   const double rho = -lambda[k];
   const cd zp = st.zp[k], zpp = st.zpp[k];
@@ -340,6 +361,201 @@ __global__ void k_adj_sums2(AdjConst K, AdjStage st, const cd* cbar, const cd* d
   }
 }
 
+// ------------------------------------------------ mixed-precision reverse sweep
+// Pair reciprocals of one stage, row j = target: R_jk = 1 / (w_j - w_k)
+// (0 on the diagonal) and, with the image, I_jk = 1 / (1 - p_j conj p_k).
+// One thread per pair; consecutive threads write consecutive k.
+__global__ void k_adj_pairs(AdjConst K, const cd* w, const cd* p, cd* R, cd* I) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long nn = (long long)K.n * K.n;
+  if (t >= nn) return;
+  const int j = (int)(t / K.n), k = (int)(t - (long long)j * K.n);
+  R[t] = j == k ? cd{0.0, 0.0} : crcp(w[j] - w[k]);
+  if (K.image) I[t] = crcp(cd{1.0, 0.0} - p[j] * cconj(p[k]));
+}
+
+// k_adj_sums1 from the pair reciprocals (one warp per target j).
+__global__ void k_adj_sums1m(AdjConst K, const cd* w, const cd* R, const cd* I, const cd* cbar, const cd* dbar,
+                             cd* sb, cd* tb) {
+  const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (j >= K.n) return;
+  const cd* Rj = R + (long long)j * K.n;
+  const cd* Ij = I + (long long)j * K.n;
+  cd accS = {0, 0}, accT = {0, 0};
+  for (int k = lane; k < K.n; k += 32) {
+    accS = cadd(accS, (w[k] * cconj(cbar[k])) * Rj[k]);  // R_jj = 0
+    if (K.image) accT = cadd(accT, dbar[k] * Ij[k]);
+  }
+  accS = warp_sum(accS);
+  accT = warp_sum(accT);
+  if (lane == 0) {
+    sb[j] = accS;
+    tb[j] = accT;
+  }
+}
+
+// k_adj_sums2 from the pair reciprocals (one warp per target k): R_kj =
+// 1 / (w_k - w_j), I_kj = 1 / (1 - p_k conj p_j).
+__global__ void k_adj_sums2m(AdjConst K, AdjStage st, const cd* R, const cd* I, const cd* cbar, const cd* dbar,
+                             double* gY) {
+  const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (k >= K.n) return;
+  const cd* w = st.w;
+  const cd* p = st.p;
+  const double* a = st.a;
+  const cd* Rk = R + (long long)k * K.n;
+  const cd* Ik = I + (long long)k * K.n;
+  cd S = {0, 0}, S2 = {0, 0}, Q = {0, 0}, T2 = {0, 0}, U = {0, 0};
+  for (int j = lane; j < K.n; j += 32) {
+    const double aj = a[j];
+    const cd inv = Rk[j];  // 0 for j = k
+    const cd inv2 = inv * inv;
+    S = cadd(S, aj * inv);
+    S2 = cadd(S2, aj * inv2);
+    Q = cadd(Q, (w[j] * cconj(cbar[j])) * inv2);
+    if (K.image) {
+      const cd cpj = cconj(p[j]);
+      const cd ie = Ik[j];
+      const cd ie2c = (ie * ie) * cpj;
+      T2 = cadd(T2, aj * ie2c);
+      U = cadd(U, dbar[j] * ie2c);
+    }
+  }
+  S = warp_sum(S);
+  S2 = warp_sum(S2);
+  Q = warp_sum(Q);
+  T2 = warp_sum(T2);
+  U = warp_sum(U);
+  if (lane == 0) {
+    const double ak = a[k];
+    const cd wk = w[k];
+    const cd wb = cmul_i(-2.0 * (cconj(S - wk * S2) * cbar[k])) + cmul_i(-2.0 * ak * cconj(Q));
+    cd zb = cmul_i(-1.0 * (cconj(wk) * wb));
+    if (K.image) {
+      const cd pk = p[k];
+      const cd pb = cmul_i(2.0 * (cconj(T2) * dbar[k])) + cmul_i(-2.0 * ak * cconj(U));
+      zb = zb + cmul_i(-1.0 * (cconj(pk) * pb));
+    }
+    gY[k] += zb.re;
+    gY[K.n + k] += zb.im;
+  }
+}
+
+// Transposed solve, set-up (one CTA): lambda = 0, v = s * ga (FP32, input of
+// the first H^T product), bw = -i c1 w z' (per-node weight of M^T lambda),
+// rmax[0] = max |ga|, residual slots rmax[1..] = 0.
+constexpr int kAdjtIters = 6;   // residual checks (each followed by a gated correction)
+constexpr double kAdjtGateTol = 1e-13;
+__global__ void __launch_bounds__(1024) k_adjt_init(AdjConst K, AdjStage st, const double* ga, const float* rscale,
+                                                   double* lam, float* v, cd* bw, double* rmax) {
+  __shared__ double red[32];
+  double m = 0.0;
+  for (int j = threadIdx.x; j < K.n; j += blockDim.x) {
+    const double g = ga[j];
+    lam[j] = 0.0;
+    v[j] = (float)((double)rscale[j] * g);
+    bw[j] = cmul_i(-K.c1 * (st.w[j] * st.zp[j]));
+    m = fmax(m, fabs(g));  // a NaN entry is caught by the residual slots
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    m = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (threadIdx.x == 0) rmax[0] = m;
+  }
+  if (threadIdx.x >= 1 && threadIdx.x <= kAdjtIters) rmax[threadIdx.x] = 0.0;
+}
+
+__device__ __forceinline__ bool adjt_converged(const double* rmax, int it) {
+  return it > 0 && rmax[it] <= kAdjtGateTol * rmax[0];  // NaN: not converged
+}
+
+// lambda += H^T v (FP32 accumulation) where the residual of slot `it` is above
+// the gate (slot 0: the first product, always).  One CTA per 64 columns, 16
+// warps over the rows, a lane owns 2 columns; fixed-order reduction over the
+// warps in shared memory.
+__global__ void __launch_bounds__(512) k_gemv_ht(int n, int np, const __half* H, const float* v, double* lam,
+                                                 const double* rmax, int it) {
+  if (adjt_converged(rmax, it)) return;
+  __shared__ float2 part[16][32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int c = blockIdx.x * 64 + 2 * lane;  // np is a multiple of 128: c + 1 < np
+  float2 acc = make_float2(0.f, 0.f);
+  for (int i = warp; i < n; i += 16) {
+    const float2 h = __half22float2(*reinterpret_cast<const __half2*>(H + (long long)i * np + c));
+    const float vi = v[i];
+    acc.x = fmaf(h.x, vi, acc.x);
+    acc.y = fmaf(h.y, vi, acc.y);
+  }
+  part[warp][lane] = acc;
+  __syncthreads();
+  if (warp == 0) {
+    float2 t = part[0][lane];
+#pragma unroll
+    for (int w = 1; w < 16; ++w) {
+      t.x += part[w][lane].x;
+      t.y += part[w][lane].y;
+    }
+    if (c < n) lam[c] += (double)t.x;
+    if (c + 1 < n) lam[c + 1] += (double)t.y;
+  }
+}
+
+// r = ga - M^T lambda (FP64) into v = s * r (FP32) and max |r| into slot `it`
+// (one warp per target j; every warp also forms the totals sum conj(z') lambda
+// and sum lambda in its pass over the row).  Where slot it - 1 is converged,
+// slot it inherits it and nothing else runs.
+__global__ void k_adjt_resid(AdjConst K, AdjStage st, const cd* R, const cd* I, const cd* bw, const double* ga,
+                             const double* lam, const float* rscale, float* v, double* rmax, int it) {
+  if (adjt_converged(rmax, it - 1)) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) rmax[it] = rmax[it - 1];
+    return;
+  }
+  const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (j >= K.n) return;
+  const cd* Rj = R + (long long)j * K.n;
+  const cd* Ij = I + (long long)j * K.n;
+  cd sb = {0, 0}, tb = {0, 0}, sz = {0, 0};
+  double sl = 0.0;
+  for (int k = lane; k < K.n; k += 32) {
+    const double lk = lam[k];
+    sb = cadd(sb, lk * (bw[k] * Rj[k]));  // R_jj = 0
+    sz = cadd(sz, lk * cconj(st.zp[k]));
+    if (K.image) {
+      tb = cadd(tb, lk * Ij[k]);
+      sl += lk;
+    }
+  }
+  sb = warp_sum(sb);
+  sz = warp_sum(sz);
+  tb = warp_sum(tb);
+  for (int o = 16; o > 0; o >>= 1) sl += __shfl_xor_sync(0xffffffffu, sl, o);
+  if (lane == 0) {
+    const double lj = lam[j];
+    const cd zp = st.zp[j];
+    const double mdiag = 0.5 + K.c1 * (st.zpp[j] * crcp(zp)).im;
+    const cd gCj = cmul_i(K.c1 * lj * cconj(zp));
+    const cd sumC = cmul_i(K.c1 * sz);
+    double mt = mdiag * lj + (cmul_i(sumC - gCj) + cmul_i(2.0 * cconj(sb))).re;
+    if (K.image) {
+      // sum gD = -i cI sum lambda;  Tb = sum_k gD_k I_jk = -i cI tb
+      const cd sumD = cmul_i(cd{-K.cI * sl, 0.0});
+      const cd Tb = cmul_i(-K.cI * tb);
+      mt += (cmul_i(-1.0 * sumD) + cmul_i(2.0 * Tb)).re;
+    }
+    const double r = ga[j] - mt;
+    v[j] = (float)((double)rscale[j] * r);
+    const double ar = fabs(r);
+    atomicMax(reinterpret_cast<unsigned long long*>(rmax + it),
+              (unsigned long long)__double_as_longlong(ar == ar ? ar : 1e300));
+  }
+}
+
 // spectral part: gZ = -s1 R1(gz') + s2 R2(gz''); gphi = -s1 Re R1(lambda)
 __global__ void k_adj_final(AdjConst K, const cd* r1zpb, const cd* r2zppb, const cd* r1lam, double* gY) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -389,6 +605,14 @@ struct AdjWork {
   cd *cbar = nullptr, *dbar = nullptr, *sb = nullptr, *tb = nullptr, *t1 = nullptr, *t2 = nullptr, *t3 = nullptr;
   cd* sums = nullptr;
   double* gparam = nullptr;    // device accumulator
+  // mixed engines: pair reciprocals of the current stage (n x n each; I with
+  // the image only), the transposed solve's node weights, FP32 product input
+  // and residual slots, and the engine state saved around a recording
+  bool mixed = false;
+  cd *R = nullptr, *I = nullptr, *bw = nullptr;
+  float* v = nullptr;
+  double* rmax = nullptr;
+  double* ysave = nullptr;
   int2* jobs = nullptr;        // {0, RAW}, {0, RAW2}
   std::vector<void*> allocs;
 };
@@ -404,7 +628,8 @@ void sfd_adjoint_free(sfd_engine* e) {
 
 // Why reverse mode does not cover the engine, or null when it does.
 const char* sfd_adjoint_unsupported(const sfd_engine* e) {
-  if (e->opt.precision != SFD_PRECISION_FP64) return "reverse mode needs an engine created with SFD_PRECISION_FP64";
+  if (e->opt.precision == SFD_PRECISION_MIXED && (!e->m16 || !e->rscale))
+    return "reverse mode of a mixed engine needs the FP16 preconditioner (precond_half = 1)";
   if (e->nsurf != 1) return "reverse mode supports engines with one surface";
   const SurfaceDesc& S = e->hs[0];
   if (S.physics == 0 && S.rho != 0.0) return "reverse mode supports water with rho = 0 only";
@@ -462,6 +687,16 @@ int ensure_work(sfd_engine* e, int steps) {
     for (cd** p : cv) ACK(adj_alloc(W, p, (size_t)n));
     ACK(adj_alloc(W, &W->sums, 2));
     ACK(adj_alloc(W, &W->gparam, 1));
+    W->mixed = e->opt.precision == SFD_PRECISION_MIXED;
+    if (W->mixed) {
+      const AdjConst K = adj_const(e->hs[0]);
+      ACK(adj_alloc(W, &W->R, (size_t)n * n));
+      if (K.image) ACK(adj_alloc(W, &W->I, (size_t)n * n));
+      ACK(adj_alloc(W, &W->bw, (size_t)n));
+      ACK(adj_alloc(W, &W->v, (size_t)n));
+      ACK(adj_alloc(W, &W->rmax, (size_t)kAdjtIters + 1));
+      ACK(adj_alloc(W, &W->ysave, n3));
+    }
     ACK(adj_alloc(W, &W->jobs, 2));
     int2 jobs[2] = {{0, SFD_JOB_RAW}, {0, SFD_JOB_RAW2}};
     ACK(cudaMemcpy(W->jobs, jobs, sizeof(jobs), cudaMemcpyHostToDevice));
@@ -469,7 +704,8 @@ int ensure_work(sfd_engine* e, int steps) {
   }
   const size_t n = W->n, np = W->np;
   auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
-  const size_t per = 2 * al(24 * n) + al(8 * np * np) + al(8 * n) + 7 * al(16 * n);
+  const size_t lu_bytes = W->mixed ? 0 : al(8 * np * np);
+  const size_t per = 2 * al(24 * n) + lu_bytes + al(8 * n) + 7 * al(16 * n);
   const size_t nslot = 4 * (size_t)steps;
   ACK(cudaMalloc(&W->slot_mem, per * nslot));
   unsigned char* b = static_cast<unsigned char*>(W->slot_mem);
@@ -483,7 +719,7 @@ int ensure_work(sfd_engine* e, int steps) {
     };
     s.Y = reinterpret_cast<double*>(take(24 * n));
     s.k = reinterpret_cast<double*>(take(24 * n));
-    s.lu = reinterpret_cast<double*>(take(8 * np * np));
+    s.lu = W->mixed ? nullptr : reinterpret_cast<double*>(take(8 * np * np));
     s.a = reinterpret_cast<double*>(take(8 * n));
     s.ap = reinterpret_cast<cd*>(take(16 * n));
     s.zp = reinterpret_cast<cd*>(take(16 * n));
@@ -498,12 +734,14 @@ int ensure_work(sfd_engine* e, int steps) {
 }
 
 // RHS at st.Y into st.k, keeping the intermediates the reverse pass reads.
-int record_rhs(sfd_engine* e, AdjWork* W, AdjStage& st) {
-  int rc = sfd_internal_rhs(e, st.Y, st.k);
+// On a mixed engine `refactor` rebuilds the preconditioner at this
+// evaluation (an FP64 engine factors M at every evaluation anyway).
+int record_rhs(sfd_engine* e, AdjWork* W, AdjStage& st, bool refactor = true) {
+  int rc = sfd_internal_rhs_ex(e, st.Y, st.k, refactor);
   if (rc) return rc;
   const size_t n = W->n, np = W->np;
   cudaStream_t s = e->stream;
-  ACK(cudaMemcpyAsync(st.lu, e->m64, 8 * np * np, cudaMemcpyDeviceToDevice, s));
+  if (st.lu) ACK(cudaMemcpyAsync(st.lu, e->m64, 8 * np * np, cudaMemcpyDeviceToDevice, s));
   ACK(cudaMemcpyAsync(st.a, e->a, 8 * n, cudaMemcpyDeviceToDevice, s));
   ACK(cudaMemcpyAsync(st.ap, e->ap, 16 * n, cudaMemcpyDeviceToDevice, s));
   ACK(cudaMemcpyAsync(st.zp, e->zp, 16 * n, cudaMemcpyDeviceToDevice, s));
@@ -534,12 +772,30 @@ int rhs_vjp(sfd_engine* e, AdjWork* W, const AdjStage& st, const double* gk, dou
   int rc = spectral(e, W, 0, W->apb_re, W->apb_im, W->t1);
   if (rc) return rc;
   k_adj_sum_cd<<<1, kAdjThreads, 0, s>>>(n, W->cbar, W->dbar, W->sums);
-  k_adj_sums1<<<nw, kAdjThreads, 0, s>>>(K, st.w, st.p, W->cbar, W->dbar, W->sb, W->tb);
-  k_adj_a<<<nb, kAdjThreads, 0, s>>>(K, W->sums, W->t1, W->cbar, W->sb, W->tb, W->abar);
-  k_lu_solve_t<<<1, kAdjThreads, K.np * sizeof(double), s>>>(n, K.np, st.lu, W->abar, W->lam);
-  k_adj_node2<<<nb, kAdjThreads, 0, s>>>(K, st, W->lam, W->cbar, W->dbar, W->zpb_re, W->zpb_im, W->zppb_re,
-                                         W->zppb_im);
-  k_adj_sums2<<<nw, kAdjThreads, 0, s>>>(K, st, W->cbar, W->dbar, gYout);
+  if (!W->mixed) {
+    k_adj_sums1<<<nw, kAdjThreads, 0, s>>>(K, st.w, st.p, W->cbar, W->dbar, W->sb, W->tb);
+    k_adj_a<<<nb, kAdjThreads, 0, s>>>(K, W->sums, W->t1, W->cbar, W->sb, W->tb, W->abar);
+    k_lu_solve_t<<<1, kAdjThreads, K.np * sizeof(double), s>>>(n, K.np, st.lu, W->abar, W->lam);
+    k_adj_node2<<<nb, kAdjThreads, 0, s>>>(K, st, W->lam, W->cbar, W->dbar, W->zpb_re, W->zpb_im, W->zppb_re,
+                                           W->zppb_im, nullptr, 0, 0.0, nullptr);
+    k_adj_sums2<<<nw, kAdjThreads, 0, s>>>(K, st, W->cbar, W->dbar, gYout);
+  } else {
+    const long long nn = (long long)n * n;
+    k_adj_pairs<<<nblocks(nn, kAdjThreads), kAdjThreads, 0, s>>>(K, st.w, st.p, W->R, W->I);
+    k_adj_sums1m<<<nw, kAdjThreads, 0, s>>>(K, st.w, W->R, W->I, W->cbar, W->dbar, W->sb, W->tb);
+    k_adj_a<<<nb, kAdjThreads, 0, s>>>(K, W->sums, W->t1, W->cbar, W->sb, W->tb, W->abar);
+    // lambda = M^-T ga by refinement preconditioned with X^T
+    k_adjt_init<<<1, 1024, 0, s>>>(K, st, W->abar, e->rscale, W->lam, W->v, W->bw, W->rmax);
+    k_gemv_ht<<<K.np / 64, 512, 0, s>>>(n, K.np, e->m16, W->v, W->lam, W->rmax, 0);
+    for (int it = 1; it <= kAdjtIters; ++it) {
+      k_adjt_resid<<<nw, kAdjThreads, 0, s>>>(K, st, W->R, W->I, W->bw, W->abar, W->lam, e->rscale, W->v, W->rmax,
+                                              it);
+      if (it < kAdjtIters) k_gemv_ht<<<K.np / 64, 512, 0, s>>>(n, K.np, e->m16, W->v, W->lam, W->rmax, it);
+    }
+    k_adj_node2<<<nb, kAdjThreads, 0, s>>>(K, st, W->lam, W->cbar, W->dbar, W->zpb_re, W->zpb_im, W->zppb_re,
+                                           W->zppb_im, W->rmax, kAdjtIters, e->opt.refine_tol, e->status);
+    k_adj_sums2m<<<nw, kAdjThreads, 0, s>>>(K, st, W->R, W->I, W->cbar, W->dbar, gYout);
+  }
   ACK(cudaGetLastError());
   rc = spectral(e, W, 0, W->zpb_re, W->zpb_im, W->t1);
   if (!rc) rc = spectral(e, W, 1, W->zppb_re, W->zppb_im, W->t2);
@@ -558,7 +814,7 @@ const double kW[4] = {1.0, 2.0, 2.0, 1.0};
 // One RK4 step of W->y in place (the forward path's stage kernels, so the
 // trajectory matches the engine's own steps bitwise).  With rec != nullptr
 // the four stages are recorded in rec[0..3].
-int adj_step(sfd_engine* e, AdjWork* W, double dt, AdjStage* rec) {
+int adj_step(sfd_engine* e, AdjWork* W, double dt, AdjStage* rec, bool refactor = true) {
   const int n3 = 3 * W->n;
   const int nb = nblocks(n3, 256);
   const double cy[4] = {dt * 0.5, dt * 0.5, dt, 0.0};
@@ -568,10 +824,10 @@ int adj_step(sfd_engine* e, AdjWork* W, double dt, AdjStage* rec) {
     double* kout = rec ? rec[st].k : W->ktmp;
     if (rec) {
       if (st == 0) ACK(cudaMemcpyAsync(rec[0].Y, W->y, 8 * (size_t)n3, cudaMemcpyDeviceToDevice, s));
-      int rc = record_rhs(e, W, rec[st]);
+      int rc = record_rhs(e, W, rec[st], refactor && st == 0);
       if (rc) return rc;
     } else {
-      int rc = sfd_internal_rhs(e, in, kout);
+      int rc = sfd_internal_rhs_ex(e, in, kout, refactor && st == 0);
       if (rc) return rc;
     }
     double* ynext = st < 3 ? (rec ? rec[st + 1].Y : W->ys) : nullptr;
@@ -691,6 +947,23 @@ extern "C" int sfd_rk4_record(sfd_engine* e, double dt, int steps, int checkpoin
   W->every = checkpoint_every;
   W->nckpt = nckpt;
   W->dt = dt;
+  if (W->mixed) {
+    // The engine's own stepping (captured step graphs, preconditioner schedule
+    // and background rebuilds as configured) on its resident state, which is
+    // saved before and restored after.
+    ACK(cudaStreamSynchronize(e->stream));
+    ACK(cudaMemcpyAsync(W->ysave, e->y0, 8 * n3, cudaMemcpyDeviceToDevice, e->stream));
+    ACK(cudaMemcpyAsync(e->y0, state0, 8 * n3, cudaMemcpyHostToDevice, e->stream));
+    for (int i = 0; i < steps && !rc; i += checkpoint_every) {
+      ACK(cudaMemcpyAsync(W->ckpt + n3 * (i / checkpoint_every), e->y0, 8 * n3, cudaMemcpyDeviceToDevice,
+                          e->stream));
+      rc = sfd_rk4_steps_async(e, dt, std::min(checkpoint_every, steps - i));
+    }
+    if (!rc && state_final) ACK(cudaMemcpyAsync(state_final, e->y0, 8 * n3, cudaMemcpyDeviceToHost, e->stream));
+    ACK(cudaMemcpyAsync(e->y0, W->ysave, 8 * n3, cudaMemcpyDeviceToDevice, e->stream));
+    ACK(cudaStreamSynchronize(e->stream));
+    return rc;
+  }
   ACK(cudaMemcpyAsync(W->y, state0, 8 * n3, cudaMemcpyHostToDevice, e->stream));
   for (int i = 0; i < steps; ++i) {
     if (i % checkpoint_every == 0)
@@ -718,9 +991,11 @@ extern "C" int sfd_rk4_vjp(sfd_engine* e, const double* cot_final, double* grad_
   for (int seg = nseg - 1; seg >= 0; --seg) {
     const int n0 = seg * W->every, n1 = std::min(W->steps, n0 + W->every);
     // recompute the segment from its checkpoint, recording every stage
+    // (a mixed engine rebuilds its preconditioner at the segment's first
+    // evaluation and keeps it for the segment's recomputation and reversal)
     ACK(cudaMemcpyAsync(W->y, W->ckpt + n3 * seg, 8 * n3, cudaMemcpyDeviceToDevice, s));
     for (int i = n0; i < n1; ++i) {
-      rc = adj_step(e, W, W->dt, &W->slots[4 * (size_t)(i - n0)]);
+      rc = adj_step(e, W, W->dt, &W->slots[4 * (size_t)(i - n0)], i == n0);
       if (rc) return rc;
     }
     for (int i = n1 - 1; i >= n0; --i) {

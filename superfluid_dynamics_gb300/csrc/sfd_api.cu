@@ -244,8 +244,8 @@ int enqueue_precond(sfd_engine* e) {
   int rc = bg_flush(e);  // a rebuild in flight on the side stream owns the work buffers
   if (rc) return rc;
   const int nb = e->max_np / 128;
-  LAUNCHC(e, SFD_K_ASSEMBLE, sfd_launch_assemble32(e->d_surf, e->d_asm_tiles, e->nasm, e->nd.w, e->nd.p, e->zp, e->nd.mdiag, e->m32,
-                                  e->stream));
+  LAUNCHC(e, SFD_K_ASSEMBLE, sfd_launch_assemble32(e->d_surf, e->d_asm_tiles, e->nasm, e->nd.wdf, e->nd.pdf, e->nd.p,
+                                                   e->zp, e->nd.mdiag, e->m32, e->stream));
   const int tiles = e->max_np / 64;
   for (int kb = 0; kb < nb; ++kb) {
     LAUNCHC(e, SFD_K_DIAG, k_gj_diag<<<e->nsurf, 512, kGjDiagSmem, e->stream>>>(e->d_surf, e->nsurf, kb, e->m32,
@@ -635,7 +635,8 @@ int bg_start(sfd_engine* e) {
   k_node_prep<<<blocks_for(nt, 32), 64, 0, side>>>(e->d_surf, e->d_node_surf, nt, x, y, B.zp, B.zpp, B.nd, nullptr,
                                                     nullptr);
   CK(cudaGetLastError());
-  CK(sfd_launch_assemble32(e->d_surf, e->d_asm_tiles, e->nasm, B.nd.w, B.nd.p, B.zp, B.nd.mdiag, e->m32, side));
+  CK(sfd_launch_assemble32(e->d_surf, e->d_asm_tiles, e->nasm, B.nd.wdf, B.nd.pdf, B.nd.p, B.zp, B.nd.mdiag,
+                           e->m32, side));
   const int nb = e->max_np / 128, tiles = e->max_np / 64;
   for (int kb = 0; kb < nb; ++kb) {
     k_gj_diag<<<e->nsurf, 512, kGjDiagSmem, side>>>(e->d_surf, e->nsurf, kb, e->m32, e->pbuf, e->status);

@@ -30,13 +30,13 @@
 // M_kj = c1 Im(z'_k cot((z_k - z_j)/2)) - [image] (1/4pi) Im cot((z_k - conj z_j)/2 + ih)
 // M_kk = mdiag_k - [image] (1/4pi) Im cot(i (y_k + h))          (createM.cuh:43-92)
 // with cot via w = exp(i z) (see sfd_kernels.cu).  Padded rows/cols = identity.
-template <typename T>
-__global__ void k_assemble(const SurfaceDesc* surf, const int4* tiles, const cd* w, const cd* p, const cd* zp,
-                           const double* mdiag, T* mat) {
+// FP64 entries (the FP64 engine's matrix).
+__global__ void k_assemble64(const SurfaceDesc* surf, const int4* tiles, const cd* w, const cd* p, const cd* zp,
+                             const double* mdiag, double* mat) {
   const int4 t = tiles[blockIdx.x];  // (surface, row0, col0, -)
   const SurfaceDesc& S = surf[t.x];
   const int n = S.n, np = pad_n(n), off = S.off;
-  T* A = mat + S.moff;
+  double* A = mat + S.moff;
   const bool image = (S.physics == 1 && !S.infinite_depth);
   const double c1 = S.physics == 0 ? 0.25 * (1 - S.rho) / SFD_PI : 0.25 / SFD_PI;
   const double inv4pi = 0.25 / SFD_PI;
@@ -45,7 +45,7 @@ __global__ void k_assemble(const SurfaceDesc* surf, const int4* tiles, const cd*
     double v;
     if (k >= n || j >= n) {
       v = (k == j) ? 1.0 : 0.0;
-    } else if (sizeof(T) == 8) {
+    } else {
       cd wk = w[off + k];
       if (k == j) {
         v = mdiag[off + k];
@@ -60,51 +60,120 @@ __global__ void k_assemble(const SurfaceDesc* surf, const int4* tiles, const cd*
         cd r = cdiv(cd{1.0 + q.re, q.im}, cd{1.0 - q.re, -q.im});  // cot = -i r  ->  Im cot = -Re r
         v -= inv4pi * (-r.re);
       }
-    } else {
-      // FP32 entries for the preconditioner: w_k - w_j from hi/lo splits so the
-      // near-diagonal difference keeps FP32 relative accuracy.
-      if (k == j) {
-        v = mdiag[off + k];
-        if (image) {
-          cd pk = p[off + k];
-          double q = cabs2(pk);
-          v -= inv4pi * (-(1.0 + q) / (1.0 - q));
-        }
-      } else {
-        cd wk = w[off + k], wj = w[off + j];
-        float kr = (float)wk.re, ki = (float)wk.im, jr = (float)wj.re, ji = (float)wj.im;
-        float dr = (kr - jr) + ((float)(wk.re - (double)kr) - (float)(wj.re - (double)jr));
-        float di = (ki - ji) + ((float)(wk.im - (double)ki) - (float)(wj.im - (double)ji));
-        float sr = kr + jr, si = ki + ji;
-        float den = 1.0f / (dr * dr + di * di);
-        float qr = (sr * dr + si * di) * den, qi = (si * dr - sr * di) * den;  // (w_k+w_j)/(w_k-w_j)
-        // cot = i (qr + i qi) = -qi + i qr
-        float zr = (float)zp[off + k].re, zi = (float)zp[off + k].im;
-        float imv = zr * qr + zi * (-qi);
-        float fv = (float)c1 * imv;
-        if (image) {
-          cd pk = p[off + k], pj = p[off + j];
-          float pkr = (float)pk.re, pki = (float)pk.im, pjr = (float)pj.re, pji = (float)pj.im;
-          float q_r = pkr * pjr + pki * pji, q_i = pki * pjr - pkr * pji;
-          float nr = 1.f + q_r, ni = q_i, er = 1.f - q_r, ei = -q_i;
-          float d2 = 1.0f / (er * er + ei * ei);
-          float rr = (nr * er + ni * ei) * d2;
-          fv -= (float)inv4pi * (-rr);
-        }
-        v = fv;
-      }
     }
-    A[(long long)k * np + j] = (T)v;
+    A[(long long)k * np + j] = v;
   }
 }
+
+// FP32 entries of the preconditioner's matrix, one 64 x 64 tile per CTA of 256
+// threads.  The tile's 64 row nodes and 64 column nodes are staged in shared
+// memory from the double-float copies (wdf, pdf) written by the node-data
+// kernel, so the entry loop runs on the FP32 pipe alone: w_k - w_j as
+// (hi_k - hi_j) + (lo_k - lo_j) keeps FP32 relative accuracy for neighbouring
+// nodes, and 1/|w_k - w_j|^2 is the fast reciprocal (the matrix only feeds the
+// FP16 preconditioner, whose error is far larger).  Each thread writes 4 rows
+// x 4 consecutive columns as float4 stores, a warp two full 256-byte rows.
+// Per tile: 16 KB written, 3 KB read.
+__global__ void __launch_bounds__(256) k_assemble32(const SurfaceDesc* surf, const int4* tiles, const float4* wdf,
+                                                    const float4* pdf, const cd* p, const cd* zp,
+                                                    const double* mdiag, float* mat) {
+  __shared__ float4 s_wj[64];  // (re.hi, re.lo, im.hi, im.lo)
+  __shared__ float2 s_pj[64];
+  __shared__ float4 s_wk[64];
+  __shared__ float2 s_zk[64];
+  __shared__ float2 s_pk[64];
+  __shared__ float s_dk[64];
+  const int4 t = tiles[blockIdx.x];  // (surface, row0, col0, -)
+  const SurfaceDesc& S = surf[t.x];
+  const int n = S.n, np = pad_n(n), off = S.off;
+  const bool image = (S.physics == 1 && !S.infinite_depth);
+  const double inv4pi = 0.25 / SFD_PI;
+  const float c1 = (float)(S.physics == 0 ? 0.25 * (1 - S.rho) / SFD_PI : 0.25 / SFD_PI);
+  {
+    const int i = threadIdx.x & 63;
+    const int part = threadIdx.x >> 6;  // 0: column nodes, 1: row nodes, 2: row diagonal
+    if (part == 0) {
+      const int j = t.z + i;
+      const bool in = j < n;
+      s_wj[i] = in ? wdf[off + j] : make_float4(0.f, 0.f, 0.f, 0.f);
+      s_pj[i] = (in && image) ? make_float2(pdf[off + j].x, pdf[off + j].z) : make_float2(0.f, 0.f);
+    } else if (part == 1) {
+      const int k = t.y + i;
+      const bool in = k < n;
+      s_wk[i] = in ? wdf[off + k] : make_float4(0.f, 0.f, 0.f, 0.f);
+      s_pk[i] = (in && image) ? make_float2(pdf[off + k].x, pdf[off + k].z) : make_float2(0.f, 0.f);
+      s_zk[i] = in ? make_float2((float)zp[off + k].re, (float)zp[off + k].im) : make_float2(0.f, 0.f);
+    } else if (part == 2) {
+      const int k = t.y + i;
+      double v = 1.0;
+      if (k < n) {
+        v = mdiag[off + k];
+        if (image) {
+          const double q = cabs2(p[off + k]);
+          v += inv4pi * (1.0 + q) / (1.0 - q);
+        }
+      }
+      s_dk[i] = (float)v;
+    }
+  }
+  __syncthreads();
+  const int cg = threadIdx.x & 15, rg = threadIdx.x >> 4;
+  const int c0 = 4 * cg;
+  float4 wj[4];
+  float2 pj[4];
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    wj[c] = s_wj[c0 + c];
+    pj[c] = s_pj[c0 + c];
+  }
+  float* A = mat + S.moff;
+  const float fi = (float)inv4pi;
+#pragma unroll
+  for (int rr = 0; rr < 4; ++rr) {
+    const int r = rg + 16 * rr;
+    const int k = t.y + r;
+    const float4 wk = s_wk[r];
+    const float2 zk = s_zk[r], pk = s_pk[r];
+    float v[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const float dr = (wk.x - wj[c].x) + (wk.y - wj[c].y);
+      const float di = (wk.z - wj[c].z) + (wk.w - wj[c].w);
+      const float sr = wk.x + wj[c].x, si = wk.z + wj[c].z;
+      const float den = __fdividef(1.0f, fmaf(dr, dr, di * di));
+      const float qr = fmaf(sr, dr, si * di) * den, qi = fmaf(si, dr, -sr * di) * den;  // (w_k+w_j)/(w_k-w_j)
+      // cot = i (qr + i qi);  Im(z'_k cot) = zr qr - zi qi
+      float fv = c1 * fmaf(zk.x, qr, -zk.y * qi);
+      if (image) {
+        const float q_r = fmaf(pk.x, pj[c].x, pk.y * pj[c].y), q_i = fmaf(pk.y, pj[c].x, -pk.x * pj[c].y);
+        const float er = 1.f - q_r, ei = -q_i;
+        const float d2 = __fdividef(1.0f, fmaf(er, er, ei * ei));
+        fv = fmaf(fi, fmaf(1.f + q_r, er, q_i * ei) * d2, fv);
+      }
+      v[c] = fv;
+    }
+    const int j0 = t.z + c0;
+    if (k >= n || j0 + 3 >= n || (k >= j0 && k <= j0 + 3)) {  // padding or the diagonal: entry by entry
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const int j = j0 + c;
+        if (k >= n || j >= n) v[c] = (k == j) ? 1.f : 0.f;
+        else if (k == j) v[c] = s_dk[r];
+      }
+    }
+    *reinterpret_cast<float4*>(A + (long long)k * np + j0) = make_float4(v[0], v[1], v[2], v[3]);
+  }
+}
+
 cudaError_t sfd_launch_assemble64(const SurfaceDesc* surf, const int4* tiles, int ntiles, const cd* w, const cd* p,
                                   const cd* zp, const double* mdiag, double* mat, cudaStream_t st) {
-  k_assemble<double><<<ntiles, 256, 0, st>>>(surf, tiles, w, p, zp, mdiag, mat);
+  k_assemble64<<<ntiles, 256, 0, st>>>(surf, tiles, w, p, zp, mdiag, mat);
   return cudaPeekAtLastError();  // the caller's launch check reads and clears it
 }
-cudaError_t sfd_launch_assemble32(const SurfaceDesc* surf, const int4* tiles, int ntiles, const cd* w, const cd* p,
-                                  const cd* zp, const double* mdiag, float* mat, cudaStream_t st) {
-  k_assemble<float><<<ntiles, 256, 0, st>>>(surf, tiles, w, p, zp, mdiag, mat);
+cudaError_t sfd_launch_assemble32(const SurfaceDesc* surf, const int4* tiles, int ntiles, const float4* wdf,
+                                  const float4* pdf, const cd* p, const cd* zp, const double* mdiag, float* mat,
+                                  cudaStream_t st) {
+  k_assemble32<<<ntiles, 256, 0, st>>>(surf, tiles, wdf, pdf, p, zp, mdiag, mat);
   return cudaPeekAtLastError();
 }
 

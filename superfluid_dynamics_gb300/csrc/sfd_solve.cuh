@@ -13,8 +13,9 @@ constexpr int kGjDiagSmem = (128 * 129 + 128 * 33 + 32 * 128 + 32 * 33) * 4;  //
 
 cudaError_t sfd_launch_assemble64(const SurfaceDesc* surf, const int4* tiles, int ntiles, const cd* w, const cd* p,
                                   const cd* zp, const double* mdiag, double* mat, cudaStream_t st);
-cudaError_t sfd_launch_assemble32(const SurfaceDesc* surf, const int4* tiles, int ntiles, const cd* w, const cd* p,
-                                  const cd* zp, const double* mdiag, float* mat, cudaStream_t st);
+cudaError_t sfd_launch_assemble32(const SurfaceDesc* surf, const int4* tiles, int ntiles, const float4* wdf,
+                                  const float4* pdf, const cd* p, const cd* zp, const double* mdiag, float* mat,
+                                  cudaStream_t st);
 __global__ void k_lu64_diag(const SurfaceDesc* surf, int nsurf, int kb, double* mat, unsigned int* status,
                             double* lmax);
 __global__ void k_lu64_trsm(const SurfaceDesc* surf, int nsurf, int kb, double* mat, double* lmax);

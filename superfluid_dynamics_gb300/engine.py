@@ -334,7 +334,9 @@ class Engine:
         check(self._L.sfd_set_problem(self._h, int(surface), ctypes.byref(physics.to_c())))
 
     # -------------------------------------------------------------- reverse mode
-    # FP64 engines with one surface (water rho = 0 or helium, standard closure).
+    # Engines with one surface (water rho = 0 or helium, standard closure):
+    # FP64 (LU records) or mixed with the FP16 preconditioner (refinement
+    # preconditioned by its transpose).
     def rhs_vjp_device(self, state_ptr: int, cot_ptr: int, grad_ptr: int) -> float:
         """grad = J(state)^T cot on device arrays of 3n doubles; returns the
         parameter derivative (d/dA3 helium, d/dg water)."""
