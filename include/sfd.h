@@ -300,29 +300,45 @@ int sfd_gl2_evolve_cb(sfd_engine* e, double t0, double t1, const sfd_gl2_options
                       sfd_gl2_step_fn fn, void* user);
 
 /* ------------------------------------------------------------ reverse mode (adjoint)
- * Hand-written adjoint of the FP64 RHS and of RK4 trajectories.  The reference
+ * Hand-written adjoint of the RHS and of RK4 trajectories.  The reference
  * has no reverse mode (it differentiates by finite differences in
  * Python/integration/jacobian_tests.py:10-150); these entry points are new.
- * Requirements: an engine created with SFD_PRECISION_FP64 holding one surface,
- * water with rho = 0 or helium with the standard Bernoulli closure, U = 0.
- * The parameter derivative is d/dA3 for helium and d/dg for water. */
+ * Requirements: an engine holding one surface, water with rho = 0 or helium
+ * with the standard Bernoulli closure, U = 0.  The parameter derivative is
+ * d/dA3 for helium and d/dg for water.
+ * On an FP64 engine the per-stage records hold the LU factors of M and the
+ * transposed solve M^T lambda = g uses them.  On a mixed engine the records
+ * hold O(n) data; the transposed solve is FP64 refinement preconditioned by
+ * the transpose of the engine's FP32 approximate inverse, rebuilt at the
+ * first evaluation of each recomputed checkpoint segment (and of each
+ * sfd_rhs_vjp_device / sfd_jacobian_device call); a final relative residual
+ * above the engine's refine_tol raises SFD_STATUS_REFINE_STALL. */
 /* grad_state = J(state)^T cotangent for the RHS state -> [dx|dy|dphi]; device
  * arrays of 3n doubles; synchronous. */
 int sfd_rhs_vjp_device(sfd_engine* e, const void* state, const void* cotangent, void* grad_state,
                        double* grad_param);
 /* Integrate `steps` RK4 steps of size dt from state0 (host, 3n) keeping a
  * checkpoint every `checkpoint_every` steps on the device; the final state is
- * written to state_final (host, 3n; nullable).  Same arithmetic as
- * sfd_rk4_steps on an FP64 engine with the same boundary-sum shape: bitwise
- * equal with autotune off, or once the autotuning first sfd_rk4_steps call has
- * run (it may keep another shape, which changes the summation order). */
+ * written to state_final (host, 3n; nullable).  FP64 engines: same arithmetic
+ * as sfd_rk4_steps with the same boundary-sum shape (bitwise equal with
+ * autotune off, or once the autotuning first sfd_rk4_steps call has run: it
+ * may keep another shape, which changes the summation order).  Mixed engines:
+ * the engine's own stepping (sfd_rk4_steps, its graphs and preconditioner
+ * schedule) on its resident state, which is saved before and restored after. */
 int sfd_rk4_record(sfd_engine* e, double dt, int steps, int checkpoint_every, const double* state0,
                    double* state_final);
 /* Reverse the recorded trajectory: grad_state0 = (d state_final / d state0)^T
  * cot_final and *grad_param = the parameter derivative of <cot_final,
  * state_final>.  Each checkpoint segment is recomputed once with every stage
- * recorded (LU factors included), then reversed stage by stage. */
+ * recorded, then reversed stage by stage.  With use_graphs, each step of a
+ * segment (recomputation and reversal) runs as a CUDA graph captured on first
+ * use and kept for later calls with the same dt and problem. */
 int sfd_rk4_vjp(sfd_engine* e, const double* cot_final, double* grad_state0, double* grad_param);
+/* Record of the mixed transposed solves of the last sfd_rhs_vjp_device,
+ * sfd_jacobian_device or sfd_rk4_vjp call (each nullable): the largest final
+ * relative residual max |g - M^T lambda| / max |g| and the largest number of
+ * preconditioner products one solve ran.  Zeros for FP64 engines. */
+int sfd_adjoint_residual(sfd_engine* e, double* max_rel_residual, int* max_corrections);
 /* Exact Jacobian of the RHS at `state` (device, 3n) from 3n reverse sweeps
  * over one recorded forward evaluation: jac (device, 9 n^2 doubles) in the
  * column-major layout of calculateJacobian. */

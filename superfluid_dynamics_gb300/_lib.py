@@ -143,6 +143,7 @@ _SIGS = {
     "sfd_rhs_vjp_device": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, _dp]),
     "sfd_rk4_record": (c_int, [c_void_p, c_double, c_int, c_int, _dp, _dp]),
     "sfd_rk4_vjp": (c_int, [c_void_p, _dp, _dp, _dp]),
+    "sfd_adjoint_residual": (c_int, [c_void_p, _dp, POINTER(c_int)]),
     "sfd_jacobian_device": (c_int, [c_void_p, c_void_p, c_void_p]),
     "sfd_default_rkf45_options": (None, [POINTER(SfdRkf45Options)]),
     "sfd_rkf45_evolve": (c_int, [c_void_p, c_double, c_double, POINTER(SfdRkf45Options), POINTER(SfdRkf45Result),

@@ -66,11 +66,31 @@ struct AdjStage {
   double* lu;  // LU factors of M (np x np, row-major, no row exchanges); null for mixed engines
   double* a;
   cd *ap, *zp, *zpp, *C, *D, *w, *p;
+  const float* xt;  // mixed engines: X^T of the preconditioner rebuilt for this stage's block of steps
 };
 
 namespace {
 
 constexpr int kAdjThreads = 256;
+// Transposed solve of mixed engines: residual checks (each but the last
+// followed by a correction, gated on the residual), and the relative residual
+// below which the remaining checks and corrections return at once.  They also
+// stop once a correction gained less than a factor kAdjtStagnation: the
+// residual has reached the noise floor of its FP64 evaluation (a few 1e-12
+// relative at n = 512), where further corrections change nothing.
+constexpr int kAdjtIters = 5;
+constexpr double kAdjtGateTol = 1e-13;
+constexpr double kAdjtStagnation = 0.25;
+// The reverse sweep of a mixed engine rebuilds the preconditioner every
+// kXtEvery steps of a recomputed segment and keeps one X^T per block of steps:
+// with X up to 50 steps old the transposed solve needs five products or more,
+// with X fresh three.
+constexpr int kXtEvery = 10;
+
+// Whether the solve stopped at residual check `it` (NaN: not stopped).
+__device__ __forceinline__ bool adjt_converged(const double* rmax, int it) {
+  return it > 0 && (rmax[it] <= kAdjtGateTol * rmax[0] || (it >= 2 && rmax[it] > kAdjtStagnation * rmax[it - 1]));
+}
 
 __device__ __forceinline__ cd cadd(cd a, cd b) { return {a.re + b.re, a.im + b.im}; }
 __device__ __forceinline__ cd crcp(cd b) {
@@ -101,17 +121,23 @@ AdjConst adj_const(const SurfaceDesc& S) {
 }
 
 // ---------------------------------------------------------------- kernels
-// Output side: E, V1, V2 and the Bernoulli closure.
-__global__ void k_adj_out(AdjConst K, AdjStage st, const double* gk, double* gY, double* apb_re, double* apb_im,
-                          cd* cbar, cd* dbar, double* abar, double* zpb_re, double* zpb_im, double* zppb_re,
-                          double* zppb_im, double* pbar) {
+// Output side: E, V1, V2 and the Bernoulli closure.  The output cotangent is
+// alpha ga + beta gb (gb nullable: the RK4 reverse combines the step's
+// cotangents here).  With rmax (mixed engines), thread 0 clears the
+// transposed solve's residual slots 0..kAdjtIters.
+__global__ void k_adj_out(AdjConst K, AdjStage st, double alpha, const double* ga, double beta, const double* gb,
+                          double* gY, double* apb_re, double* apb_im, cd* cbar, cd* dbar, double* abar,
+                          double* zpb_re, double* zpb_im, double* zppb_re, double* zppb_im, double* pbar,
+                          double* rmax) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int n = K.n;
+  if (rmax && k <= kAdjtIters) rmax[k] = 0.0;
   if (k >= n) return;
   const double inv4pi = 0.25 / SFD_PI;
   const double dx = st.k[k], dy = st.k[n + k], yk = st.Y[n + k];
-  const double gphi = gk[2 * n + k];
-  const double gxt = gk[k] + gphi * dx, gyt = gk[n + k] + gphi * dy;
+  auto cot = [&](int i) { return gb ? alpha * ga[i] + beta * gb[i] : alpha * ga[i]; };
+  const double gphi = cot(2 * n + k);
+  const double gxt = cot(k) + gphi * dx, gyt = cot(n + k) + gphi * dy;
   const cd Eb = {gxt, -gyt};
   const cd zp = st.zp[k], zpp = st.zpp[k];
   const cd izp = crcp(zp);
@@ -175,20 +201,6 @@ __global__ void k_adj_sum_cd(int n, const cd* cbar, const cd* dbar, cd* out) {
     out[0] = sc[0];
     out[1] = sd[0];
   }
-}
-
-// sum of the per-node parameter cotangents (one CTA, fixed order), added to *acc
-__global__ void k_adj_sum_param(int n, const double* pbar, double scale, double* acc) {
-  __shared__ double s[kAdjThreads];
-  double v = 0.0;
-  for (int k = threadIdx.x; k < n; k += kAdjThreads) v += pbar[k];
-  s[threadIdx.x] = v;
-  __syncthreads();
-  for (int h = kAdjThreads / 2; h > 0; h >>= 1) {
-    if (threadIdx.x < h) s[threadIdx.x] += s[threadIdx.x + h];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) *acc += scale * s[0];
 }
 
 __device__ __forceinline__ cd warp_sum(cd v) {
@@ -289,14 +301,24 @@ __global__ void __launch_bounds__(kAdjThreads) k_lu_solve_t(int n, int np, const
 }
 
 // M-part cotangents at fixed a (rho = -lambda); totals of gC, gD for pass 2.
-// With rmax (mixed engines' transposed solve), thread 0 also raises the
-// refinement-stall bit when the solve's final residual rmax[last] is above
-// tol * rmax[0] (or NaN).
+// With rmax (mixed engines' transposed solve, residual slots 0..last), thread
+// 0 also raises the refinement-stall bit when the final residual rmax[last]
+// is above tol * rmax[0] (or NaN), and records the final relative residual
+// and the corrections the solve ran (maxima over the solves of a call).
 __global__ void k_adj_node2(AdjConst K, AdjStage st, const double* lambda, cd* cbar, cd* dbar, double* zpb_re,
                             double* zpb_im, double* zppb_re, double* zppb_im, const double* rmax, int last,
-                            double tol, unsigned int* status) {
+                            double tol, unsigned int* status, double* diag_rel, unsigned int* diag_corr) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (rmax && k == 0 && !(rmax[last] <= tol * rmax[0])) atomicOr(status, (unsigned int)SFD_ST_REFINE_STALL);
+  if (rmax && k == 0) {
+    const double b = rmax[0], rl = rmax[last];
+    if (!(rl <= tol * b)) atomicOr(status, (unsigned int)SFD_ST_REFINE_STALL);
+    const double rel = b > 0.0 ? rl / b : (rl > 0.0 ? 1e300 : 0.0);
+    atomicMax(reinterpret_cast<unsigned long long*>(diag_rel),
+              (unsigned long long)__double_as_longlong(rel == rel ? rel : 1e300));
+    unsigned int corr = 1;  // the first product
+    for (int it = 1; it < last; ++it) corr += adjt_converged(rmax, it) ? 0u : 1u;
+    atomicMax(diag_corr, corr);
+  }
   if (k >= K.n) return;
   const double rho = -lambda[k];
   const cd zp = st.zp[k], zpp = st.zpp[k];
@@ -363,72 +385,123 @@ __global__ void k_adj_sums2(AdjConst K, AdjStage st, const cd* cbar, const cd* d
 
 // ------------------------------------------------ mixed-precision reverse sweep
 // Pair reciprocals of one stage, row j = target: R_jk = 1 / (w_j - w_k)
-// (0 on the diagonal) and, with the image, I_jk = 1 / (1 - p_j conj p_k).
+// (0 on the diagonal), Rb_jk = bw_k R_jk with bw = -i c1 w z' (the weights of
+// M^T lambda) and, with the image, I_jk = 1 / (1 - p_j conj p_k).
 // One thread per pair; consecutive threads write consecutive k.
-__global__ void k_adj_pairs(AdjConst K, const cd* w, const cd* p, cd* R, cd* I) {
+__global__ void k_adj_pairs(AdjConst K, const cd* w, const cd* p, const cd* zp, cd* R, cd* Rb, cd* I) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long nn = (long long)K.n * K.n;
   if (t >= nn) return;
   const int j = (int)(t / K.n), k = (int)(t - (long long)j * K.n);
-  R[t] = j == k ? cd{0.0, 0.0} : crcp(w[j] - w[k]);
+  const cd wk = w[k];
+  const cd r = j == k ? cd{0.0, 0.0} : crcp(w[j] - wk);
+  R[t] = r;
+  Rb[t] = cmul_i(-K.c1 * (wk * zp[k])) * r;
   if (K.image) I[t] = crcp(cd{1.0, 0.0} - p[j] * cconj(p[k]));
 }
 
-// k_adj_sums1 from the pair reciprocals (one warp per target j).
-__global__ void k_adj_sums1m(AdjConst K, const cd* w, const cd* R, const cd* I, const cd* cbar, const cd* dbar,
-                             cd* sb, cd* tb) {
-  const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (j >= K.n) return;
-  const cd* Rj = R + (long long)j * K.n;
-  const cd* Ij = I + (long long)j * K.n;
-  cd accS = {0, 0}, accT = {0, 0};
-  for (int k = lane; k < K.n; k += 32) {
-    accS = cadd(accS, (w[k] * cconj(cbar[k])) * Rj[k]);  // R_jj = 0
-    if (K.image) accT = cadd(accT, dbar[k] * Ij[k]);
-  }
-  accS = warp_sum(accS);
-  accT = warp_sum(accT);
-  if (lane == 0) {
-    sb[j] = accS;
-    tb[j] = accT;
+// The pair sums below give each target kWpt warps (a CTA holds kTpc targets):
+// warp w of a target takes the sources k = lane + 32 (w + kWpt i), and the
+// warps' sums are combined in a fixed order through shared memory, so results
+// are bitwise repeatable.  One warp per target would leave about three warps
+// per SM at n = 512, too few to cover the FP64 latency.
+constexpr int kWpt = 4;
+constexpr int kTpc = 2;
+constexpr int kPairThreads = 32 * kWpt * kTpc;
+
+// Combine NV complex accumulators of the kWpt warps of each target; the
+// result is returned to lane 0 of the target's first warp (others: zeros).
+template <int NV>
+__device__ __forceinline__ void pair_reduce(cd* acc, cd (*sh)[kWpt][NV]) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int t = warp / kWpt, w = warp % kWpt;
+#pragma unroll
+  for (int i = 0; i < NV; ++i) acc[i] = warp_sum(acc[i]);
+  if (lane == 0)
+#pragma unroll
+    for (int i = 0; i < NV; ++i) sh[t][w][i] = acc[i];
+  __syncthreads();
+  if (w == 0 && lane == 0) {
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      cd v = sh[t][0][i];
+#pragma unroll
+      for (int q = 1; q < kWpt; ++q) v = cadd(v, sh[t][q][i]);
+      acc[i] = v;
+    }
   }
 }
 
-// k_adj_sums2 from the pair reciprocals (one warp per target k): R_kj =
-// 1 / (w_k - w_j), I_kj = 1 / (1 - p_k conj p_j).
-__global__ void k_adj_sums2m(AdjConst K, AdjStage st, const cd* R, const cd* I, const cd* cbar, const cd* dbar,
-                             double* gY) {
-  const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (k >= K.n) return;
+// k_adj_sums1 from the pair reciprocals, with k_adj_a's combination and the
+// transposed solve's set-up in the epilogue: ga_j = abar_j - s1 Re R1(ga')_j
+// + Re(i (sum gC - gC_j) + 2 i conj(Sb_j)) + Re(-i sum gD + 2 i Tb_j) is the
+// solve's right-hand side; lambda_j = 0, v_j = ga_j (FP32, input of the first
+// X^T product) and max |ga| into rmax[0] (cleared by k_adj_out).
+__global__ void __launch_bounds__(kPairThreads) k_adj_sums1m(AdjConst K, const cd* w, const cd* R, const cd* I,
+                                                            const cd* cbar, const cd* dbar, const cd* sums,
+                                                            const cd* r1apb, double* abar, double* lam, float* v,
+                                                            double* rmax) {
+  __shared__ cd sh[kTpc][kWpt][2];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int j = blockIdx.x * kTpc + warp / kWpt;
+  const int k0 = lane + 32 * (warp % kWpt);
+  cd acc[2] = {{0, 0}, {0, 0}};
+  if (j < K.n) {
+    const cd* Rj = R + (long long)j * K.n;
+    const cd* Ij = I + (long long)j * K.n;
+    for (int k = k0; k < K.n; k += 32 * kWpt) {
+      acc[0] = cadd(acc[0], (w[k] * cconj(cbar[k])) * Rj[k]);  // R_jj = 0
+      if (K.image) acc[1] = cadd(acc[1], dbar[k] * Ij[k]);
+    }
+  }
+  pair_reduce<2>(acc, sh);
+  if (j < K.n && k0 == 0) {
+    const double s1 = 2.0 * SFD_PI / K.n;
+    double g = abar[j] - s1 * r1apb[j].re;
+    const cd sc = sums[0], sd = sums[1];
+    g += (cmul_i(sc - cbar[j]) + cmul_i(2.0 * cconj(acc[0]))).re;
+    if (K.image) g += (cmul_i(cd{-sd.re, -sd.im}) + cmul_i(2.0 * acc[1])).re;
+    abar[j] = g;
+    lam[j] = 0.0;
+    v[j] = (float)g;
+    const double ag = fabs(g);
+    atomicMax(reinterpret_cast<unsigned long long*>(rmax), (unsigned long long)__double_as_longlong(ag == ag ? ag : 1e300));
+  }
+}
+
+// k_adj_sums2 from the pair reciprocals: R_kj = 1 / (w_k - w_j),
+// I_kj = 1 / (1 - p_k conj p_j).
+__global__ void __launch_bounds__(kPairThreads) k_adj_sums2m(AdjConst K, AdjStage st, const cd* R, const cd* I,
+                                                            const cd* cbar, const cd* dbar, double* gY) {
+  __shared__ cd sh[kTpc][kWpt][5];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int k = blockIdx.x * kTpc + warp / kWpt;
+  const int j0 = lane + 32 * (warp % kWpt);
   const cd* w = st.w;
   const cd* p = st.p;
   const double* a = st.a;
-  const cd* Rk = R + (long long)k * K.n;
-  const cd* Ik = I + (long long)k * K.n;
-  cd S = {0, 0}, S2 = {0, 0}, Q = {0, 0}, T2 = {0, 0}, U = {0, 0};
-  for (int j = lane; j < K.n; j += 32) {
-    const double aj = a[j];
-    const cd inv = Rk[j];  // 0 for j = k
-    const cd inv2 = inv * inv;
-    S = cadd(S, aj * inv);
-    S2 = cadd(S2, aj * inv2);
-    Q = cadd(Q, (w[j] * cconj(cbar[j])) * inv2);
-    if (K.image) {
-      const cd cpj = cconj(p[j]);
-      const cd ie = Ik[j];
-      const cd ie2c = (ie * ie) * cpj;
-      T2 = cadd(T2, aj * ie2c);
-      U = cadd(U, dbar[j] * ie2c);
+  cd acc[5] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}, {0, 0}};  // S, S2, Q, T2, U
+  if (k < K.n) {
+    const cd* Rk = R + (long long)k * K.n;
+    const cd* Ik = I + (long long)k * K.n;
+    for (int j = j0; j < K.n; j += 32 * kWpt) {
+      const double aj = a[j];
+      const cd inv = Rk[j];  // 0 for j = k
+      const cd inv2 = inv * inv;
+      acc[0] = cadd(acc[0], aj * inv);
+      acc[1] = cadd(acc[1], aj * inv2);
+      acc[2] = cadd(acc[2], (w[j] * cconj(cbar[j])) * inv2);
+      if (K.image) {
+        const cd ie = Ik[j];
+        const cd ie2c = (ie * ie) * cconj(p[j]);
+        acc[3] = cadd(acc[3], aj * ie2c);
+        acc[4] = cadd(acc[4], dbar[j] * ie2c);
+      }
     }
   }
-  S = warp_sum(S);
-  S2 = warp_sum(S2);
-  Q = warp_sum(Q);
-  T2 = warp_sum(T2);
-  U = warp_sum(U);
-  if (lane == 0) {
+  pair_reduce<5>(acc, sh);
+  if (k < K.n && j0 == 0) {
+    const cd S = acc[0], S2 = acc[1], Q = acc[2], T2 = acc[3], U = acc[4];
     const double ak = a[k];
     const cd wk = w[k];
     const cd wb = cmul_i(-2.0 * (cconj(S - wk * S2) * cbar[k])) + cmul_i(-2.0 * ak * cconj(Q));
@@ -443,99 +516,124 @@ __global__ void k_adj_sums2m(AdjConst K, AdjStage st, const cd* R, const cd* I, 
   }
 }
 
-// Transposed solve, set-up (one CTA): lambda = 0, v = s * ga (FP32, input of
-// the first H^T product), bw = -i c1 w z' (per-node weight of M^T lambda),
-// rmax[0] = max |ga|, residual slots rmax[1..] = 0.
-constexpr int kAdjtIters = 6;   // residual checks (each followed by a gated correction)
-constexpr double kAdjtGateTol = 1e-13;
-__global__ void __launch_bounds__(1024) k_adjt_init(AdjConst K, AdjStage st, const double* ga, const float* rscale,
-                                                   double* lam, float* v, cd* bw, double* rmax) {
-  __shared__ double red[32];
-  double m = 0.0;
-  for (int j = threadIdx.x; j < K.n; j += blockDim.x) {
-    const double g = ga[j];
-    lam[j] = 0.0;
-    v[j] = (float)((double)rscale[j] * g);
-    bw[j] = cmul_i(-K.c1 * (st.w[j] * st.zp[j]));
-    m = fmax(m, fabs(g));  // a NaN entry is caught by the residual slots
-  }
-  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+// X^T as a row-major FP32 matrix: xt[j][i] = X[i][j] for the np x np padded
+// inverse (the padding keeps its identity).  32 x 32 tiles through shared memory.
+// Record of one evaluation's node data into a stage slot (one launch in place
+// of eight copies).
+__global__ void k_adj_store(int n, const double* a, const cd* ap, const cd* zp, const cd* zpp, const cd* C,
+                            const cd* D, const cd* w, const cd* p, AdjStage st) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  st.a[i] = a[i];
+  st.ap[i] = ap[i];
+  st.zp[i] = zp[i];
+  st.zpp[i] = zpp[i];
+  st.C[i] = C[i];
+  st.D[i] = D[i];
+  st.w[i] = w[i];
+  st.p[i] = p[i];
+}
+
+__global__ void k_adj_transpose(int np, const float* X, float* xt) {
+  __shared__ float tile[32][33];
+  const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) tile[r][threadIdx.x] = X[(long long)(by + r) * np + bx + threadIdx.x];
   __syncthreads();
-  if (threadIdx.x < 32) {
-    m = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
-    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if (threadIdx.x == 0) rmax[0] = m;
-  }
-  if (threadIdx.x >= 1 && threadIdx.x <= kAdjtIters) rmax[threadIdx.x] = 0.0;
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) xt[(long long)(bx + r) * np + by + threadIdx.x] = tile[threadIdx.x][r];
 }
 
-__device__ __forceinline__ bool adjt_converged(const double* rmax, int it) {
-  return it > 0 && rmax[it] <= kAdjtGateTol * rmax[0];  // NaN: not converged
-}
 
-// lambda += H^T v (FP32 accumulation) where the residual of slot `it` is above
-// the gate (slot 0: the first product, always).  One CTA per 64 columns, 16
-// warps over the rows, a lane owns 2 columns; fixed-order reduction over the
-// warps in shared memory.
-__global__ void __launch_bounds__(512) k_gemv_ht(int n, int np, const __half* H, const float* v, double* lam,
-                                                 const double* rmax, int it) {
+// lambda += X^T v (FP32 products, FP64 update) where the residual of slot
+// `it` is above the gate (slot 0: the first product, always): one warp per row
+// j of xt = X^T, kGtRows rows per CTA.  The epilogue also writes the CTA's
+// partial sums of conj(z'_j) lambda_j and lambda_j (fixed order), which the
+// residual kernel totals: part[2 b] = sum conj(z') lambda, part[2 b + 1].re =
+// sum lambda over the CTA's rows.
+constexpr int kGtRows = 16;
+__global__ void __launch_bounds__(32 * kGtRows) k_adjt_gemv(int n, int np, const float* xt, const float* v,
+                                                           const cd* zp, double* lam, cd* part, const double* rmax,
+                                                           int it) {
   if (adjt_converged(rmax, it)) return;
-  __shared__ float2 part[16][32];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int c = blockIdx.x * 64 + 2 * lane;  // np is a multiple of 128: c + 1 < np
-  float2 acc = make_float2(0.f, 0.f);
-  for (int i = warp; i < n; i += 16) {
-    const float2 h = __half22float2(*reinterpret_cast<const __half2*>(H + (long long)i * np + c));
-    const float vi = v[i];
-    acc.x = fmaf(h.x, vi, acc.x);
-    acc.y = fmaf(h.y, vi, acc.y);
-  }
-  part[warp][lane] = acc;
+  extern __shared__ float4 vsh4[];
+  __shared__ cd red[kGtRows][2];
+  float* vsh = reinterpret_cast<float*>(vsh4);
+  const int n4 = (n + 3) & ~3;
+  for (int i = threadIdx.x; i < n4; i += blockDim.x) vsh[i] = i < n ? v[i] : 0.f;
   __syncthreads();
-  if (warp == 0) {
-    float2 t = part[0][lane];
-#pragma unroll
-    for (int w = 1; w < 16; ++w) {
-      t.x += part[w][lane].x;
-      t.y += part[w][lane].y;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int j = blockIdx.x * kGtRows + warp;
+  cd pz = {0, 0}, pl = {0, 0};
+  if (j < n) {
+    const float4* row = reinterpret_cast<const float4*>(xt + (long long)j * np);
+    float acc = 0.f;
+    for (int q = lane; q < n4 / 4; q += 32) {
+      const float4 a = __ldg(row + q), b = vsh4[q];
+      acc = fmaf(a.x, b.x, fmaf(a.y, b.y, fmaf(a.z, b.z, fmaf(a.w, b.w, acc))));
     }
-    if (c < n) lam[c] += (double)t.x;
-    if (c + 1 < n) lam[c + 1] += (double)t.y;
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) {
+      const double l = lam[j] + (double)acc;
+      lam[j] = l;
+      pz = l * cconj(zp[j]);
+      pl = {l, 0.0};
+    }
+  }
+  if (lane == 0) {
+    red[warp][0] = pz;
+    red[warp][1] = pl;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    cd a = red[0][0], b = red[0][1];
+    for (int w = 1; w < kGtRows; ++w) {
+      a = cadd(a, red[w][0]);
+      b = cadd(b, red[w][1]);
+    }
+    part[2 * blockIdx.x] = a;
+    part[2 * blockIdx.x + 1] = b;
   }
 }
 
-// r = ga - M^T lambda (FP64) into v = s * r (FP32) and max |r| into slot `it`
-// (one warp per target j; every warp also forms the totals sum conj(z') lambda
-// and sum lambda in its pass over the row).  Where slot it - 1 is converged,
-// slot it inherits it and nothing else runs.
-__global__ void k_adjt_resid(AdjConst K, AdjStage st, const cd* R, const cd* I, const cd* bw, const double* ga,
-                             const double* lam, const float* rscale, float* v, double* rmax, int it) {
+// r = ga - M^T lambda (FP64) into v = r (FP32) and max |r| into slot `it`
+// (sum conj(z') lambda and sum lambda from the product's partial sums,
+// nparts CTAs).  Where slot it - 1 is converged, slot it inherits it and
+// nothing else runs.
+__global__ void __launch_bounds__(kPairThreads) k_adjt_resid(AdjConst K, AdjStage st, const cd* Rb, const cd* I,
+                                                            const cd* part, int nparts, const double* ga,
+                                                            const double* lam, float* v, double* rmax, int it) {
   if (adjt_converged(rmax, it - 1)) {
     if (blockIdx.x == 0 && threadIdx.x == 0) rmax[it] = rmax[it - 1];
     return;
   }
-  const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (j >= K.n) return;
-  const cd* Rj = R + (long long)j * K.n;
-  const cd* Ij = I + (long long)j * K.n;
-  cd sb = {0, 0}, tb = {0, 0}, sz = {0, 0};
-  double sl = 0.0;
-  for (int k = lane; k < K.n; k += 32) {
-    const double lk = lam[k];
-    sb = cadd(sb, lk * (bw[k] * Rj[k]));  // R_jj = 0
-    sz = cadd(sz, lk * cconj(st.zp[k]));
-    if (K.image) {
-      tb = cadd(tb, lk * Ij[k]);
-      sl += lk;
+  __shared__ cd sh[kTpc][kWpt][2];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int j = blockIdx.x * kTpc + warp / kWpt;
+  const int k0 = lane + 32 * (warp % kWpt);
+  cd acc[2] = {{0, 0}, {0, 0}};  // sb = sum_k lambda_k bw_k R_jk, tb = sum_k lambda_k I_jk
+  if (j < K.n) {
+    const cd* Rj = Rb + (long long)j * K.n;
+    const cd* Ij = I + (long long)j * K.n;
+    for (int k = k0; k < K.n; k += 32 * kWpt) {
+      const double lk = lam[k];
+      const cd rb = Rj[k];
+      acc[0].re = fma(lk, rb.re, acc[0].re);  // Rb_jj = 0
+      acc[0].im = fma(lk, rb.im, acc[0].im);
+      if (K.image) {
+        const cd ie = Ij[k];
+        acc[1].re = fma(lk, ie.re, acc[1].re);
+        acc[1].im = fma(lk, ie.im, acc[1].im);
+      }
     }
   }
-  sb = warp_sum(sb);
-  sz = warp_sum(sz);
-  tb = warp_sum(tb);
-  for (int o = 16; o > 0; o >>= 1) sl += __shfl_xor_sync(0xffffffffu, sl, o);
-  if (lane == 0) {
+  pair_reduce<2>(acc, sh);
+  if (j < K.n && k0 == 0) {
+    cd sz = {0, 0};
+    double sl = 0.0;
+    for (int b = 0; b < nparts; ++b) {
+      sz = cadd(sz, part[2 * b]);
+      sl += part[2 * b + 1].re;
+    }
+    const cd sb = acc[0], tb = acc[1];
     const double lj = lam[j];
     const cd zp = st.zp[j];
     const double mdiag = 0.5 + K.c1 * (st.zpp[j] * crcp(zp)).im;
@@ -549,7 +647,7 @@ __global__ void k_adjt_resid(AdjConst K, AdjStage st, const cd* R, const cd* I, 
       mt += (cmul_i(-1.0 * sumD) + cmul_i(2.0 * Tb)).re;
     }
     const double r = ga[j] - mt;
-    v[j] = (float)((double)rscale[j] * r);
+    v[j] = (float)r;
     const double ar = fabs(r);
     atomicMax(reinterpret_cast<unsigned long long*>(rmax + it),
               (unsigned long long)__double_as_longlong(ar == ar ? ar : 1e300));
@@ -557,7 +655,23 @@ __global__ void k_adjt_resid(AdjConst K, AdjStage st, const cd* R, const cd* I, 
 }
 
 // spectral part: gZ = -s1 R1(gz') + s2 R2(gz''); gphi = -s1 Re R1(lambda)
-__global__ void k_adj_final(AdjConst K, const cd* r1zpb, const cd* r2zppb, const cd* r1lam, double* gY) {
+// Block 0 also adds scale * sum pbar to *acc (the parameter cotangent, fixed
+// order; k_adj_sum_param's work).
+__global__ void __launch_bounds__(kAdjThreads) k_adj_final(AdjConst K, const cd* r1zpb, const cd* r2zppb,
+                                                          const cd* r1lam, double* gY, const double* pbar,
+                                                          double scale, double* acc) {
+  if (blockIdx.x == 0) {
+    __shared__ double sp[kAdjThreads];
+    double v = 0.0;
+    for (int i = threadIdx.x; i < K.n; i += kAdjThreads) v += pbar[i];
+    sp[threadIdx.x] = v;
+    __syncthreads();
+    for (int h = kAdjThreads / 2; h > 0; h >>= 1) {
+      if (threadIdx.x < h) sp[threadIdx.x] += sp[threadIdx.x + h];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) *acc += scale * sp[0];
+  }
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= K.n) return;
   const double s1 = 2.0 * SFD_PI / K.n;
@@ -568,14 +682,7 @@ __global__ void k_adj_final(AdjConst K, const cd* r1zpb, const cd* r2zppb, const
   gY[2 * K.n + k] = -s1 * r1lam[k].re;
 }
 
-// RK4 helpers: out = alpha a + beta b (b nullable); acc += a + b + c + d
-__global__ void k_adj_lin(int n3, double* out, double alpha, const double* a, double beta, const double* b) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n3) return;
-  double v = alpha * a[i];
-  if (b) v += beta * b[i];
-  out[i] = v;
-}
+// RK4 helper: acc += a + b + c + d
 __global__ void k_adj_acc4(int n3, double* acc, const double* a, const double* b, const double* c, const double* d) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n3) return;
@@ -609,16 +716,48 @@ struct AdjWork {
   // the image only), the transposed solve's node weights, FP32 product input
   // and residual slots, and the engine state saved around a recording
   bool mixed = false;
-  cd *R = nullptr, *I = nullptr, *bw = nullptr;
+  cd *R = nullptr, *Rb = nullptr, *I = nullptr;
+  cd* part = nullptr;          // per-CTA partial sums of the X^T product (2 per CTA)
   float* v = nullptr;
+  float* xt = nullptr;         // transpose of the FP32 approximate inverse (np x np)
   double* rmax = nullptr;
   double* ysave = nullptr;
+  double* diag_rel = nullptr;  // max final relative residual of the transposed solves of the last call
+  unsigned int* diag_corr = nullptr;  // max corrections they ran
+  // four-step transforms of the reverse sweep (power-of-two n in [512, 8192]):
+  // plan a' (the a' cotangent) and plan 3 (z', z'' and lambda cotangents)
+  F4Plan f4_ap, f4_3;
+  cd* f4_scr = nullptr;
   int2* jobs = nullptr;        // {0, RAW}, {0, RAW2}
   std::vector<void*> allocs;
+  // captured steps of sfd_rk4_vjp (engines with use_graphs): for step slot i
+  // of a segment, g_rec[i] recomputes the step recording its stages into
+  // slots 4i..4i+3 (slot 0 with the preconditioner rebuild) and g_rev[i]
+  // reverses it; valid for g_dt and the current slots
+  std::vector<cudaGraphExec_t> g_rec, g_rev;
+  std::vector<long long> g_rec_nodes, g_rev_nodes;
+  double g_dt = 0.0;
+  AdjConst g_K{};  // surface constants the graphs' kernels were given
 };
+
+static bool same_const(const AdjConst& a, const AdjConst& b) {
+  return a.n == b.n && a.np == b.np && a.physics == b.physics && a.image == b.image && a.c1 == b.c1 &&
+         a.cI == b.cI && a.depth == b.depth && a.vdw == b.vdw && a.gravity == b.gravity && a.rho == b.rho;
+}
+
+static void adj_destroy_graphs(AdjWork* W) {
+  for (auto* v : {&W->g_rec, &W->g_rev})
+    for (cudaGraphExec_t& g : *v)
+      if (g) {
+        cudaGraphExecDestroy(g);
+        g = nullptr;
+      }
+}
 
 void sfd_adjoint_free(sfd_engine* e) {
   if (!e || !e->adj) return;
+  adj_destroy_graphs(e->adj);
+  if (e->adj->xt) cudaFree(e->adj->xt);
   for (void* p : e->adj->allocs) cudaFree(p);
   if (e->adj->slot_mem) cudaFree(e->adj->slot_mem);
   if (e->adj->ckpt) cudaFree(e->adj->ckpt);
@@ -628,8 +767,6 @@ void sfd_adjoint_free(sfd_engine* e) {
 
 // Why reverse mode does not cover the engine, or null when it does.
 const char* sfd_adjoint_unsupported(const sfd_engine* e) {
-  if (e->opt.precision == SFD_PRECISION_MIXED && (!e->m16 || !e->rscale))
-    return "reverse mode of a mixed engine needs the FP16 preconditioner (precond_half = 1)";
   if (e->nsurf != 1) return "reverse mode supports engines with one surface";
   const SurfaceDesc& S = e->hs[0];
   if (S.physics == 0 && S.rho != 0.0) return "reverse mode supports water with rho = 0 only";
@@ -665,6 +802,7 @@ int ensure_work(sfd_engine* e, int steps) {
   AdjWork* W = e->adj;
   if (W && W->cap_steps >= steps) return 0;
   if (W) {
+    adj_destroy_graphs(W);  // captured with the old slots
     if (W->slot_mem) cudaFree(W->slot_mem);
     W->slot_mem = nullptr;
     W->slots.clear();
@@ -691,11 +829,42 @@ int ensure_work(sfd_engine* e, int steps) {
     if (W->mixed) {
       const AdjConst K = adj_const(e->hs[0]);
       ACK(adj_alloc(W, &W->R, (size_t)n * n));
+      ACK(adj_alloc(W, &W->Rb, (size_t)n * n));
       if (K.image) ACK(adj_alloc(W, &W->I, (size_t)n * n));
-      ACK(adj_alloc(W, &W->bw, (size_t)n));
+      ACK(adj_alloc(W, &W->part, 2 * (size_t)((n + kGtRows - 1) / kGtRows)));
       ACK(adj_alloc(W, &W->v, (size_t)n));
       ACK(adj_alloc(W, &W->rmax, (size_t)kAdjtIters + 1));
       ACK(adj_alloc(W, &W->ysave, n3));
+
+      ACK(adj_alloc(W, &W->diag_rel, 1));
+      ACK(adj_alloc(W, &W->diag_corr, 1));
+    }
+    if (sfd_f4_eligible(n)) {
+      // jobs: a' cotangent -> t1; then z' -> t1, z'' -> t2, lambda -> t3
+      const F4Job ja[1] = {{0, SFD_F4_RAW1, 0, 0, W->apb_re, W->apb_im, W->t1}};
+      const F4Job j3[3] = {{0, SFD_F4_RAW1, 0, 0, W->zpb_re, W->zpb_im, W->t1},
+                           {0, SFD_F4_RAW2, (long long)n, 0, W->zppb_re, W->zppb_im, W->t2},
+                           {0, SFD_F4_RAW1, 2LL * n, 0, W->lam, nullptr, W->t3}};
+      for (int pi = 0; pi < 2; ++pi) {
+        F4Plan& P = pi == 0 ? W->f4_ap : W->f4_3;
+        const F4Job* jl = pi == 0 ? ja : j3;
+        const int nj = pi == 0 ? 1 : 3;
+        std::vector<int2> ul[3];
+        for (int j = 0; j < nj; ++j) {
+          for (int u = 0; u < 64; ++u) ul[0].push_back({j, u});
+          for (int u = 0; u < n / 64; ++u) ul[1].push_back({j, u});
+          for (int u = 0; u < 64; ++u) ul[2].push_back({j, u});
+        }
+        ACK(adj_alloc(W, &P.jobs, (size_t)nj));
+        ACK(cudaMemcpy(P.jobs, jl, nj * sizeof(F4Job), cudaMemcpyHostToDevice));
+        for (int ph = 0; ph < 3; ++ph) {
+          ACK(adj_alloc(W, &P.units[ph], ul[ph].size()));
+          ACK(cudaMemcpy(P.units[ph], ul[ph].data(), ul[ph].size() * sizeof(int2), cudaMemcpyHostToDevice));
+          P.nunits[ph] = (int)ul[ph].size();
+        }
+        P.njobs = nj;
+      }
+      ACK(adj_alloc(W, &W->f4_scr, 3 * (size_t)n));
     }
     ACK(adj_alloc(W, &W->jobs, 2));
     int2 jobs[2] = {{0, SFD_JOB_RAW}, {0, SFD_JOB_RAW2}};
@@ -707,6 +876,11 @@ int ensure_work(sfd_engine* e, int steps) {
   const size_t lu_bytes = W->mixed ? 0 : al(8 * np * np);
   const size_t per = 2 * al(24 * n) + lu_bytes + al(8 * n) + 7 * al(16 * n);
   const size_t nslot = 4 * (size_t)steps;
+  if (W->mixed) {
+    if (W->xt) cudaFree(W->xt);
+    W->xt = nullptr;
+    ACK(cudaMalloc(&W->xt, sizeof(float) * np * np * (size_t)((steps + kXtEvery - 1) / kXtEvery)));
+  }
   ACK(cudaMalloc(&W->slot_mem, per * nslot));
   unsigned char* b = static_cast<unsigned char*>(W->slot_mem);
   W->slots.resize(nslot);
@@ -728,6 +902,7 @@ int ensure_work(sfd_engine* e, int steps) {
     s.D = reinterpret_cast<cd*>(take(16 * n));
     s.w = reinterpret_cast<cd*>(take(16 * n));
     s.p = reinterpret_cast<cd*>(take(16 * n));
+    s.xt = W->mixed ? W->xt + np * np * (i / 4 / kXtEvery) : nullptr;
   }
   W->cap_steps = steps;
   return 0;
@@ -742,14 +917,9 @@ int record_rhs(sfd_engine* e, AdjWork* W, AdjStage& st, bool refactor = true) {
   const size_t n = W->n, np = W->np;
   cudaStream_t s = e->stream;
   if (st.lu) ACK(cudaMemcpyAsync(st.lu, e->m64, 8 * np * np, cudaMemcpyDeviceToDevice, s));
-  ACK(cudaMemcpyAsync(st.a, e->a, 8 * n, cudaMemcpyDeviceToDevice, s));
-  ACK(cudaMemcpyAsync(st.ap, e->ap, 16 * n, cudaMemcpyDeviceToDevice, s));
-  ACK(cudaMemcpyAsync(st.zp, e->zp, 16 * n, cudaMemcpyDeviceToDevice, s));
-  ACK(cudaMemcpyAsync(st.zpp, e->zpp, 16 * n, cudaMemcpyDeviceToDevice, s));
-  ACK(cudaMemcpyAsync(st.C, e->cacc, 16 * n, cudaMemcpyDeviceToDevice, s));
-  ACK(cudaMemcpyAsync(st.D, e->dacc, 16 * n, cudaMemcpyDeviceToDevice, s));
-  ACK(cudaMemcpyAsync(st.w, e->nd.w, 16 * n, cudaMemcpyDeviceToDevice, s));
-  ACK(cudaMemcpyAsync(st.p, e->nd.p, 16 * n, cudaMemcpyDeviceToDevice, s));
+  k_adj_store<<<nblocks((long long)n, kAdjThreads), kAdjThreads, 0, s>>>((int)n, e->a, e->ap, e->zp, e->zpp, e->cacc,
+                                                                          e->dacc, e->nd.w, e->nd.p, st);
+  ACK(cudaGetLastError());
   return 0;
 }
 
@@ -760,16 +930,49 @@ int spectral(sfd_engine* e, AdjWork* W, int job, const double* re, const double*
   return 0;
 }
 
+// The jobs of a four-step plan (unscaled first / second derivatives of the
+// jobs' own inputs) in its three launches.
+int spectral_f4(sfd_engine* e, AdjWork* W, const F4Plan& P) {
+  DerivArgs D{e->d_surf, 1, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  for (int ph = 1; ph <= 3; ++ph) {
+    cudaError_t err = sfd_launch_f4(D, P, W->f4_scr, e->stream, ph);
+    if (err != cudaSuccess) return sfd_internal_cuda(err, "four-step transform");
+  }
+  return 0;
+}
+
+// Start of a reverse-mode call: clear the transposed-solve record.
+int clear_diag(sfd_engine* e, AdjWork* W) {
+  if (!W->mixed) return 0;
+  ACK(cudaMemsetAsync(W->diag_rel, 0, sizeof(double), e->stream));
+  ACK(cudaMemsetAsync(W->diag_corr, 0, sizeof(unsigned int), e->stream));
+  return 0;
+}
+
+// Mixed engines: X^T from the FP32 inverse the last preconditioner rebuild
+// left in e->m32, into the stage's block (call after every evaluation that
+// rebuilt it).
+int refresh_xt(sfd_engine* e, AdjWork* W, const AdjStage& st) {
+  if (!W->mixed) return 0;
+  k_adj_transpose<<<dim3(W->np / 32, W->np / 32), dim3(32, 8), 0, e->stream>>>(W->np, e->m32,
+                                                                               const_cast<float*>(st.xt));
+  ACK(cudaGetLastError());
+  return 0;
+}
+
 // gYout = J(st)^T gk; the parameter cotangent is added to W->gparam.
-int rhs_vjp(sfd_engine* e, AdjWork* W, const AdjStage& st, const double* gk, double* gYout) {
+// The output cotangent is alpha ga + beta gb (gb nullable).
+int rhs_vjp(sfd_engine* e, AdjWork* W, const AdjStage& st, double alpha, const double* ga, double beta,
+            const double* gb, double* gYout) {
   const AdjConst K = adj_const(e->hs[0]);
   const int n = K.n;
   cudaStream_t s = e->stream;
   const int nb = nblocks(n, kAdjThreads), nw = nblocks(32LL * n, kAdjThreads);
-  k_adj_out<<<nb, kAdjThreads, 0, s>>>(K, st, gk, gYout, W->apb_re, W->apb_im, W->cbar, W->dbar, W->abar, W->zpb_re,
-                                       W->zpb_im, W->zppb_re, W->zppb_im, W->pbar);
+  k_adj_out<<<nb, kAdjThreads, 0, s>>>(K, st, alpha, ga, beta, gb, gYout, W->apb_re, W->apb_im, W->cbar, W->dbar,
+                                       W->abar, W->zpb_re, W->zpb_im, W->zppb_re, W->zppb_im, W->pbar,
+                                       W->mixed ? W->rmax : nullptr);
   ACK(cudaGetLastError());
-  int rc = spectral(e, W, 0, W->apb_re, W->apb_im, W->t1);
+  int rc = W->f4_ap.njobs ? spectral_f4(e, W, W->f4_ap) : spectral(e, W, 0, W->apb_re, W->apb_im, W->t1);
   if (rc) return rc;
   k_adj_sum_cd<<<1, kAdjThreads, 0, s>>>(n, W->cbar, W->dbar, W->sums);
   if (!W->mixed) {
@@ -777,34 +980,46 @@ int rhs_vjp(sfd_engine* e, AdjWork* W, const AdjStage& st, const double* gk, dou
     k_adj_a<<<nb, kAdjThreads, 0, s>>>(K, W->sums, W->t1, W->cbar, W->sb, W->tb, W->abar);
     k_lu_solve_t<<<1, kAdjThreads, K.np * sizeof(double), s>>>(n, K.np, st.lu, W->abar, W->lam);
     k_adj_node2<<<nb, kAdjThreads, 0, s>>>(K, st, W->lam, W->cbar, W->dbar, W->zpb_re, W->zpb_im, W->zppb_re,
-                                           W->zppb_im, nullptr, 0, 0.0, nullptr);
+                                           W->zppb_im, nullptr, 0, 0.0, nullptr, nullptr, nullptr);
     k_adj_sums2<<<nw, kAdjThreads, 0, s>>>(K, st, W->cbar, W->dbar, gYout);
   } else {
     const long long nn = (long long)n * n;
-    k_adj_pairs<<<nblocks(nn, kAdjThreads), kAdjThreads, 0, s>>>(K, st.w, st.p, W->R, W->I);
-    k_adj_sums1m<<<nw, kAdjThreads, 0, s>>>(K, st.w, W->R, W->I, W->cbar, W->dbar, W->sb, W->tb);
-    k_adj_a<<<nb, kAdjThreads, 0, s>>>(K, W->sums, W->t1, W->cbar, W->sb, W->tb, W->abar);
-    // lambda = M^-T ga by refinement preconditioned with X^T
-    k_adjt_init<<<1, 1024, 0, s>>>(K, st, W->abar, e->rscale, W->lam, W->v, W->bw, W->rmax);
-    k_gemv_ht<<<K.np / 64, 512, 0, s>>>(n, K.np, e->m16, W->v, W->lam, W->rmax, 0);
-    for (int it = 1; it <= kAdjtIters; ++it) {
-      k_adjt_resid<<<nw, kAdjThreads, 0, s>>>(K, st, W->R, W->I, W->bw, W->abar, W->lam, e->rscale, W->v, W->rmax,
-                                              it);
-      if (it < kAdjtIters) k_gemv_ht<<<K.np / 64, 512, 0, s>>>(n, K.np, e->m16, W->v, W->lam, W->rmax, it);
+    const int np_blocks = (n + kTpc - 1) / kTpc;
+    const int gt_blocks = (n + kGtRows - 1) / kGtRows;
+    const size_t gt_smem = (size_t)((n + 3) & ~3) * sizeof(float);
+    k_adj_pairs<<<nblocks(nn, kAdjThreads), kAdjThreads, 0, s>>>(K, st.w, st.p, st.zp, W->R, W->Rb, W->I);
+    // Sb, Tb and the solve's right-hand side ga (k_adj_a), lambda = 0, v = ga
+    k_adj_sums1m<<<np_blocks, kPairThreads, 0, s>>>(K, st.w, W->R, W->I, W->cbar, W->dbar, W->sums, W->t1,
+                                                    W->abar, W->lam, W->v, W->rmax);
+    // lambda = M^-T ga by refinement preconditioned with X^T (the FP32
+    // inverse's transpose, st.xt): lambda = X^T ga, then r = ga - M^T lambda,
+    // lambda += X^T r while the residual is above the gate
+    for (int it = 0; it < kAdjtIters; ++it) {
+      if (it > 0)
+        k_adjt_resid<<<np_blocks, kPairThreads, 0, s>>>(K, st, W->Rb, W->I, W->part, gt_blocks, W->abar, W->lam,
+                                                        W->v, W->rmax, it);
+      k_adjt_gemv<<<gt_blocks, 32 * kGtRows, gt_smem, s>>>(n, K.np, st.xt, W->v, st.zp, W->lam, W->part, W->rmax,
+                                                           it);
     }
+    k_adjt_resid<<<np_blocks, kPairThreads, 0, s>>>(K, st, W->Rb, W->I, W->part, gt_blocks, W->abar, W->lam, W->v,
+                                                    W->rmax, kAdjtIters);
     k_adj_node2<<<nb, kAdjThreads, 0, s>>>(K, st, W->lam, W->cbar, W->dbar, W->zpb_re, W->zpb_im, W->zppb_re,
-                                           W->zppb_im, W->rmax, kAdjtIters, e->opt.refine_tol, e->status);
-    k_adj_sums2m<<<nw, kAdjThreads, 0, s>>>(K, st, W->R, W->I, W->cbar, W->dbar, gYout);
+                                           W->zppb_im, W->rmax, kAdjtIters, e->opt.refine_tol, e->status,
+                                           W->diag_rel, W->diag_corr);
+    k_adj_sums2m<<<np_blocks, kPairThreads, 0, s>>>(K, st, W->R, W->I, W->cbar, W->dbar, gYout);
   }
   ACK(cudaGetLastError());
-  rc = spectral(e, W, 0, W->zpb_re, W->zpb_im, W->t1);
-  if (!rc) rc = spectral(e, W, 1, W->zppb_re, W->zppb_im, W->t2);
-  if (!rc) rc = spectral(e, W, 0, W->lam, nullptr, W->t3);
+  if (W->f4_3.njobs) {
+    rc = spectral_f4(e, W, W->f4_3);
+  } else {
+    rc = spectral(e, W, 0, W->zpb_re, W->zpb_im, W->t1);
+    if (!rc) rc = spectral(e, W, 1, W->zppb_re, W->zppb_im, W->t2);
+    if (!rc) rc = spectral(e, W, 0, W->lam, nullptr, W->t3);
+  }
   if (rc) return rc;
-  k_adj_final<<<nb, kAdjThreads, 0, s>>>(K, W->t1, W->t2, W->t3, gYout);
   // parameter: d/dA3 = d/dvdw / h^3 (helium), d/dg (water)
   const double scale = K.physics == 1 ? 1.0 / (K.depth * K.depth * K.depth) : 1.0;
-  k_adj_sum_param<<<1, kAdjThreads, 0, s>>>(n, W->pbar, scale, W->gparam);
+  k_adj_final<<<nb, kAdjThreads, 0, s>>>(K, W->t1, W->t2, W->t3, gYout, W->pbar, scale, W->gparam);
   ACK(cudaGetLastError());
   return 0;
 }
@@ -844,21 +1059,45 @@ int adj_step_back(sfd_engine* e, AdjWork* W, double dt, const AdjStage* rec) {
   const int n3 = 3 * W->n;
   const int nb = nblocks(n3, 256);
   cudaStream_t s = e->stream;
-  // stage 4: gk4 = dt/6 gY
-  k_adj_lin<<<nb, 256, 0, s>>>(n3, W->gk, dt / 6.0, W->gY, 0.0, nullptr);
-  int rc = rhs_vjp(e, W, rec[3], W->gk, W->gYs[3]);
+  // stage cotangents: k4: dt/6 gY; k3: dt/3 gY + dt g(Y4); k2: dt/3 gY + dt/2 g(Y3); k1: dt/6 gY + dt/2 g(Y2)
+  int rc = rhs_vjp(e, W, rec[3], dt / 6.0, W->gY, 0.0, nullptr, W->gYs[3]);
   if (rc) return rc;
-  k_adj_lin<<<nb, 256, 0, s>>>(n3, W->gk, dt / 3.0, W->gY, dt, W->gYs[3]);
-  rc = rhs_vjp(e, W, rec[2], W->gk, W->gYs[2]);
+  rc = rhs_vjp(e, W, rec[2], dt / 3.0, W->gY, dt, W->gYs[3], W->gYs[2]);
   if (rc) return rc;
-  k_adj_lin<<<nb, 256, 0, s>>>(n3, W->gk, dt / 3.0, W->gY, dt * 0.5, W->gYs[2]);
-  rc = rhs_vjp(e, W, rec[1], W->gk, W->gYs[1]);
+  rc = rhs_vjp(e, W, rec[1], dt / 3.0, W->gY, dt * 0.5, W->gYs[2], W->gYs[1]);
   if (rc) return rc;
-  k_adj_lin<<<nb, 256, 0, s>>>(n3, W->gk, dt / 6.0, W->gY, dt * 0.5, W->gYs[1]);
-  rc = rhs_vjp(e, W, rec[0], W->gk, W->gYs[0]);
+  rc = rhs_vjp(e, W, rec[0], dt / 6.0, W->gY, dt * 0.5, W->gYs[1], W->gYs[0]);
   if (rc) return rc;
   k_adj_acc4<<<nb, 256, 0, s>>>(n3, W->gY, W->gYs[0], W->gYs[1], W->gYs[2], W->gYs[3]);
   ACK(cudaGetLastError());
+  return 0;
+}
+
+// Run `body` (which enqueues on the engine stream) through the cached graph
+// *g, capturing it first if there is none; *nodes counts its nodes.
+template <typename F>
+int run_captured(sfd_engine* e, cudaGraphExec_t* g, long long* nodes, F&& body) {
+  if (!*g) {
+    cudaGraph_t graph = nullptr;
+    const long long before = e->launches;
+    ACK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = body();
+    cudaError_t ce = cudaStreamEndCapture(e->stream, &graph);
+    e->launches = before;
+    if (rc) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    if (ce != cudaSuccess) return sfd_internal_cuda(ce, "adjoint step capture");
+    size_t nn = 0;
+    cudaGraphGetNodes(graph, nullptr, &nn);
+    *nodes = (long long)nn;
+    ce = cudaGraphInstantiate(g, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ce != cudaSuccess) return sfd_internal_cuda(ce, "adjoint step graph");
+  }
+  ACK(cudaGraphLaunch(*g, e->stream));
+  e->launches += *nodes;
   return 0;
 }
 
@@ -878,9 +1117,11 @@ extern "C" int sfd_rhs_vjp_device(sfd_engine* e, const void* state, const void* 
   AdjStage& st = W->slots[0];
   ACK(cudaMemcpyAsync(st.Y, state, 8 * n3, cudaMemcpyDeviceToDevice, e->stream));
   ACK(cudaMemsetAsync(W->gparam, 0, sizeof(double), e->stream));
-  rc = record_rhs(e, W, st);
+  rc = clear_diag(e, W);
+  if (!rc) rc = record_rhs(e, W, st);
+  if (!rc) rc = refresh_xt(e, W, st);
   if (rc) return rc;
-  rc = rhs_vjp(e, W, st, static_cast<const double*>(cotangent), static_cast<double*>(grad_state));
+  rc = rhs_vjp(e, W, st, 1.0, static_cast<const double*>(cotangent), 0.0, nullptr, static_cast<double*>(grad_state));
   if (rc) return rc;
   double gp = 0.0;
   ACK(cudaMemcpyAsync(&gp, W->gparam, sizeof(double), cudaMemcpyDeviceToHost, e->stream));
@@ -912,12 +1153,14 @@ extern "C" int sfd_jacobian_device(sfd_engine* e, const void* state, void* jac) 
   cudaStream_t s = e->stream;
   AdjStage& st = W->slots[0];
   ACK(cudaMemcpyAsync(st.Y, state, 8 * (size_t)n3, cudaMemcpyDeviceToDevice, s));
-  rc = record_rhs(e, W, st);
+  rc = clear_diag(e, W);
+  if (!rc) rc = record_rhs(e, W, st);
+  if (!rc) rc = refresh_xt(e, W, st);
   if (rc) return rc;
   double* out = static_cast<double*>(jac);
   for (int row = 0; row < n3; ++row) {
     k_jac_unit<<<nblocks(n3, 256), 256, 0, s>>>(n3, row, W->gk);
-    rc = rhs_vjp(e, W, st, W->gk, W->gYs[0]);
+    rc = rhs_vjp(e, W, st, 1.0, W->gk, 0.0, nullptr, W->gYs[0]);
     if (rc) return rc;
     k_jac_scatter_row<<<nblocks(n3, 256), 256, 0, s>>>(n3, row, W->gYs[0], out);
     ACK(cudaGetLastError());
@@ -987,19 +1230,49 @@ extern "C" int sfd_rk4_vjp(sfd_engine* e, const double* cot_final, double* grad_
   cudaStream_t s = e->stream;
   ACK(cudaMemcpyAsync(W->gY, cot_final, 8 * n3, cudaMemcpyHostToDevice, s));
   ACK(cudaMemsetAsync(W->gparam, 0, sizeof(double), s));
+  rc = clear_diag(e, W);
+  if (rc) return rc;
   const int nseg = (W->steps + W->every - 1) / W->every;
+  // With graphs, each step of a segment (recomputation and reversal) is one
+  // captured graph per step slot, replayed for every segment and call.
+  const bool graphs = e->opt.use_graphs && !e->profile;
+  if (graphs) {
+    rc = sfd_internal_bg_flush(e);  // a pending background rebuild cannot be switched in during capture
+    if (rc) return rc;
+    // the reverse kernels take the surface constants (A3, g, ...) by value:
+    // after sfd_set_problem the graphs are captured again
+    const AdjConst K = adj_const(e->hs[0]);
+    if (W->g_dt != W->dt || !same_const(W->g_K, K)) adj_destroy_graphs(W);
+    W->g_dt = W->dt;
+    W->g_K = K;
+    const size_t cap = (size_t)W->cap_steps;
+    W->g_rec.resize(cap, nullptr);
+    W->g_rev.resize(cap, nullptr);
+    W->g_rec_nodes.resize(cap, 0);
+    W->g_rev_nodes.resize(cap, 0);
+  }
   for (int seg = nseg - 1; seg >= 0; --seg) {
     const int n0 = seg * W->every, n1 = std::min(W->steps, n0 + W->every);
     // recompute the segment from its checkpoint, recording every stage
-    // (a mixed engine rebuilds its preconditioner at the segment's first
-    // evaluation and keeps it for the segment's recomputation and reversal)
+    // (a mixed engine rebuilds its preconditioner every kXtEvery steps of the
+    // segment and keeps each X^T for the reversal of its block of steps)
     ACK(cudaMemcpyAsync(W->y, W->ckpt + n3 * seg, 8 * n3, cudaMemcpyDeviceToDevice, s));
     for (int i = n0; i < n1; ++i) {
-      rc = adj_step(e, W, W->dt, &W->slots[4 * (size_t)(i - n0)], i == n0);
+      const int k = i - n0;
+      AdjStage* rec = &W->slots[4 * (size_t)k];
+      const bool rebuild = k % kXtEvery == 0;
+      auto body = [&] {
+        int r = adj_step(e, W, W->dt, rec, rebuild);
+        return (!r && rebuild) ? refresh_xt(e, W, rec[0]) : r;
+      };
+      rc = graphs ? run_captured(e, &W->g_rec[k], &W->g_rec_nodes[k], body) : body();
       if (rc) return rc;
     }
     for (int i = n1 - 1; i >= n0; --i) {
-      rc = adj_step_back(e, W, W->dt, &W->slots[4 * (size_t)(i - n0)]);
+      const int k = i - n0;
+      const AdjStage* rec = &W->slots[4 * (size_t)k];
+      auto body = [&] { return adj_step_back(e, W, W->dt, rec); };
+      rc = graphs ? run_captured(e, &W->g_rev[k], &W->g_rev_nodes[k], body) : body();
       if (rc) return rc;
     }
   }
@@ -1008,5 +1281,21 @@ extern "C" int sfd_rk4_vjp(sfd_engine* e, const double* cot_final, double* grad_
   ACK(cudaMemcpyAsync(&gp, W->gparam, sizeof(double), cudaMemcpyDeviceToHost, s));
   ACK(cudaStreamSynchronize(s));
   if (grad_param) *grad_param = gp;
+  return 0;
+}
+
+extern "C" int sfd_adjoint_residual(sfd_engine* e, double* max_rel_residual, int* max_corrections) {
+  if (!e) return sfd_internal_error(SFD_ERR_INVALID, "null engine");
+  double rel = 0.0;
+  unsigned int corr = 0;
+  AdjWork* W = e->adj;
+  if (W && W->mixed) {
+    ACK(cudaSetDevice(e->device));
+    ACK(cudaMemcpyAsync(&rel, W->diag_rel, sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+    ACK(cudaMemcpyAsync(&corr, W->diag_corr, sizeof(unsigned int), cudaMemcpyDeviceToHost, e->stream));
+    ACK(cudaStreamSynchronize(e->stream));
+  }
+  if (max_rel_residual) *max_rel_residual = rel;
+  if (max_corrections) *max_corrections = (int)corr;
   return 0;
 }

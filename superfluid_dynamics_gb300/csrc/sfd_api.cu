@@ -856,6 +856,7 @@ int sfd_internal_solve(sfd_engine* e, const double* st) { return enqueue_solve(e
 int sfd_internal_rhs_ex(sfd_engine* e, const double* st, double* out, bool refactor) {
   return enqueue_rhs(e, st, out, refactor);
 }
+int sfd_internal_bg_flush(sfd_engine* e) { return bg_flush(e); }
 
 // ====================================================================== C ABI
 extern "C" {

@@ -174,7 +174,8 @@ __device__ __forceinline__ void f4_phase1(const DerivArgs& A, const F4Job& J, co
       const int m = n1 + 64 * i;  // node index
       if (J.kind == SFD_F4_Z) v[q] = {A.x[off + m] - xi_node(m, dn, inv_n), A.y[off + m]};          // Derivatives.cuh:285,317
       else if (J.kind == SFD_F4_PHI) v[q] = {A.phi[off + m] - uq * (double)m, A.phi_im ? A.phi_im[off + m] : 0.0};  // :286,318
-      else v[q] = {A.a[off + m], 0.0};                                                              // real_to_complex(a)
+      else if (J.kind == SFD_F4_AP) v[q] = {A.a[off + m], 0.0};                                     // real_to_complex(a)
+      else v[q] = {J.in_re[off + m], J.in_im ? J.in_im[off + m] : 0.0};                             // RAW jobs
     } else {
       v[q] = {0.0, 0.0};
     }
@@ -204,11 +205,12 @@ __device__ __forceinline__ void f4_phase2(const F4Job& J, const SurfaceDesc& S, 
   }
   warp_dif<64>(v, twL, lane, -1);  // element i holds X[k2 + N2 bitrev(i)]
   const bool second_too = J.kind == SFD_F4_Z;
+  const bool second_only = J.kind == SFD_F4_RAW2;
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
     const int k = k2 + N2 * bitrev<64>(lane + 32 * q);
     w[q] = second_too ? second_mult(v[q], k, n, inv_n) : v[q];
-    v[q] = first_mult(v[q], k, n, inv_n);
+    v[q] = second_only ? second_mult(v[q], k, n, inv_n) : first_mult(v[q], k, n, inv_n);
   }
   warp_dit<64>(v, twL, lane, +1);  // element i holds Y'[n1 = i]
 #pragma unroll
@@ -257,8 +259,10 @@ __device__ __forceinline__ void f4_phase3(const DerivArgs& A, const F4Job& J, co
       if (S.U != 0) r += uq;                            // :380-383
       A.phip[j] = r;
       if (A.phipf) A.phipf[j] = (float)r;
-    } else {
+    } else if (J.kind == SFD_F4_AP) {
       A.ap[j] = {x.re * s1, x.im * s1};                 // BaseBoundaryIntegrator.cuh:203
+    } else {
+      J.out[j] = x;                                     // RAW jobs: unscaled
     }
   }
 }

@@ -190,6 +190,9 @@ int sfd_internal_rhs(sfd_engine* e, const double* st, double* out);
 // As sfd_internal_rhs, for either precision; refactor = rebuild the mixed
 // preconditioner at this evaluation (it is built anyway if there is none).
 int sfd_internal_rhs_ex(sfd_engine* e, const double* st, double* out, bool refactor);
+// Switch in a pending background preconditioner rebuild now (not allowed
+// while the engine stream is being captured).
+int sfd_internal_bg_flush(sfd_engine* e);
 // reverse-mode workspace release (sfd_adjoint.cu)
 void sfd_adjoint_free(sfd_engine* e);
 // adaptive-integrator workspace release (sfd_rkf45.cu)

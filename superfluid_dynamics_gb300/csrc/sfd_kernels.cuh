@@ -131,12 +131,18 @@ __global__ void k_invariants(const SurfaceDesc* surf, const double* x, const dou
                              const cd* zp, const double* u, const double* v, double kappa, double* out);
 
 // Four-step transforms of power-of-two surfaces (sfd_fft4.cu): jobs write z'
-// and z'' (from one forward transform), phi', or a'.
-enum : int { SFD_F4_Z = 0, SFD_F4_PHI = 1, SFD_F4_AP = 2 };
+// and z'' (from one forward transform), phi', or a'; the RAW jobs (reverse
+// mode) transform their own input in_re + i in_im (in_im nullable) into out
+// with the first (RAW1) or second (RAW2) derivative multiplier, unscaled (the
+// d/dj of FftDerivative::exec).
+enum : int { SFD_F4_Z = 0, SFD_F4_PHI = 1, SFD_F4_AP = 2, SFD_F4_RAW1 = 3, SFD_F4_RAW2 = 4 };
 struct F4Job {
   int surf;
   int kind;
   long long scr0, scr1;  // scratch offsets (complex elements): rows of the job, and z'' rows for SFD_F4_Z
+  const double* in_re;   // RAW jobs only
+  const double* in_im;
+  cd* out;
 };
 // The jobs of one spectral launch and their unit lists (job, unit) per phase.
 struct F4Plan {

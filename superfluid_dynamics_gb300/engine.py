@@ -385,6 +385,15 @@ class Engine:
         check(self._L.sfd_rk4_vjp(self._h, _dp(c), _dp(g), _dp(gp)))
         return g, float(gp[0])
 
+    def adjoint_residual(self) -> tuple[float, int]:
+        """Mixed engines: the largest final relative residual of the transposed
+        solves of the last reverse-mode call, and the most preconditioner
+        products one of them ran ((0.0, 0) for FP64 engines)."""
+        rel = np.zeros(1)
+        corr = ctypes.c_int(0)
+        check(self._L.sfd_adjoint_residual(self._h, _dp(rel), ctypes.byref(corr)))
+        return float(rel[0]), int(corr.value)
+
     def _check_state_size(self, *arrays) -> None:
         """Reverse-mode arrays hold the full state [x | y | phi]: the library
         reads (and the Jacobian writes) exactly that many values."""

@@ -11,7 +11,9 @@ against central finite differences of the CUDA path and of the CPU oracle:
   - RK4 trajectory VJPs with uneven checkpoint segments: within 1e-8;
   - the fit workload at full size (N=512, 500 steps at dt=1e-3, checkpoints
     every 50): coefficient and A3 gradients within 1e-7;
-  - the torch.autograd.Function with precision=PRECISION_MIXED.
+  - the torch.autograd.Function with precision=PRECISION_MIXED;
+  - the captured reverse steps after a parameter change (set_problem) against
+    a fresh engine created with the new parameter.
 """
 import numpy as np
 import pytest
@@ -46,6 +48,8 @@ def test_rhs_vjp_matches_fp64(case, n):
         e.clear_status()
         g, gp = e.rhs_vjp(s, c)
         status = e.status()[0]
+        res, corr = e.adjoint_residual()
+    assert res <= 1e-11 and 1 <= corr <= 5, (res, corr)
     assert rel(g, g64) <= 1e-10, rel(g, g64)
     assert abs(gp - gp64) <= 1e-9 * max(abs(gp64), 1e-12), (gp, gp64)
     assert not (status[0] & STATUS_REFINE_STALL), status
@@ -69,6 +73,8 @@ def test_rk4_vjp_matches_fp64(case, dt, steps, every):
         f = e.rk4_record(dt, steps, every, s)
         g, gp = e.rk4_vjp(c)
         status = e.status()[0]
+        res, corr = e.adjoint_residual()
+        assert res <= 1e-11 and 1 <= corr <= 5, (res, corr)
         # the recording leaves the engine's resident state as it was
         x1, y1, p1 = e.get_state()
         assert np.array_equal(x0, x1) and np.array_equal(y0, y1) and np.array_equal(p0, p1)
@@ -127,3 +133,24 @@ def test_autograd_mixed_matches_fp64():
     gc, ga = grads[sfd.PRECISION_MIXED]
     assert rel(gc, gc64) <= 1e-8, rel(gc, gc64)
     assert abs(ga - ga64) <= 1e-8 * abs(ga64), (ga, ga64)
+
+
+def test_captured_steps_follow_set_problem():
+    n, dt, steps, every = 128, 1e-3, 12, 5
+    mk, st = CASES["helium"]
+    phys = mk()
+    s = st(n)
+    c = np.random.default_rng(51).standard_normal(3 * n)
+    phys2 = with_param(phys, 1.5e3)
+    with mixed_engine(n, phys) as e:
+        e.rk4_record(dt, steps, every, s)
+        e.rk4_vjp(c)
+        e.set_problem(phys2)
+        f = e.rk4_record(dt, steps, every, s)
+        g, gp = e.rk4_vjp(c)
+    with mixed_engine(n, phys2) as e:
+        f2 = e.rk4_record(dt, steps, every, s)
+        g2, gp2 = e.rk4_vjp(c)
+    assert rel(f, f2) <= 1e-13, rel(f, f2)
+    assert rel(g, g2) <= 1e-11, rel(g, g2)
+    assert abs(gp - gp2) <= 1e-10 * abs(gp2), (gp, gp2)
