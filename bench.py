@@ -249,7 +249,7 @@ def class_roofline(prof: dict, prof_steps: int, n: int, sums_per_step: dict, job
     return classes
 
 
-def adjoint_ratio(device: int):
+def adjoint_ratio(device: int, steps: int = 500, every: int = 50):
     """Cost of the hand-written adjoint against the forward pass on the fit
     workload: helium film N=512, h0=10, A3=1e3, 500 RK4 steps at dt=1e-3,
     initial y from 64 seeded Fourier coefficients, checkpoints every 50 steps,
@@ -264,12 +264,12 @@ def adjoint_ratio(device: int):
     entry)."""
     import superfluid_dynamics_gb300 as sfd
     from superfluid_dynamics_gb300 import workloads
-    n, steps, dt, every = 512, 500, 1e-3, 50
+    n, dt = 512, 1e-3
     s, c0, target = workloads.helium_fit(n)
     state0 = np.concatenate([s.x, s.y, s.phi])
     phys = sfd.HeliumBoundaryProblem(depth=10.0, A3=1e3)
-    out = {"workload": "helium film N=512, h0=10, A3=1e3, 500 RK4 steps dt=1e-3, 64 Fourier coefficients, "
-                       "checkpoints every 50"}
+    out = {"workload": f"helium film N=512, h0=10, A3=1e3, {steps} RK4 steps dt=1e-3, 64 Fourier coefficients, "
+                       f"checkpoints every {every}"}
     grads = {}
     for name, opts in (("mixed", sfd.Options(precision=sfd.PRECISION_MIXED, refactor_every=50, pre_iters=2,
                                              autotune=False, device=device)),
@@ -848,8 +848,9 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the 512-film helium batch summary")
     ap.add_argument("--no-roofline", action="store_true", help="skip the peak probes and the class roofline")
     ap.add_argument("--precond-fp32", action="store_true", help="apply the preconditioner from FP32 (default FP16 copy)")
+    ap.add_argument("--checkpoint-every", type=int, default=50, help="--workload adjoint: checkpoint spacing")
     ap.add_argument("--workload", default="headline",
-                    choices=["headline", "modes1024", "helium-batch", "steep8192", "profile"],
+                    choices=["headline", "modes1024", "helium-batch", "steep8192", "profile", "adjoint"],
                     help="headline = the metric's configuration; the others print their own line")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -861,6 +862,10 @@ def main():
     if args.workload == "profile":
         if rank == 0:
             run_profile_window(args, local_rank)
+        return
+    if args.workload == "adjoint":  # the fit workload's adjoint alone, --steps RK4 steps
+        if rank == 0:
+            print(json.dumps(adjoint_ratio(local_rank, args.steps, args.checkpoint_every)), flush=True)
         return
     if args.workload != "headline":
         if world > 1 and args.workload == "helium-batch":

@@ -210,6 +210,11 @@ int enqueue_sums(sfd_engine* e, int prec, const double* weights, const float2* w
     LAUNCHC(e, gate >= 0 ? SFD_K_EXTRA : SFD_K_SUMS32, sfd_launch_sums_f32(A, e->nf32, e->f32_max_per, e->stream));
     return 0;
   }
+  if (prec == SFD_PREC_DF && e->d_f32_work && e->df_part) {
+    LAUNCHC(e, gate >= 0 ? SFD_K_EXTRA : SFD_K_SUMSDF,
+            sfd_launch_sums_dfs(A, e->df_part, e->nf32, e->f32_max_per, e->sum_groups[prec], e->stream));
+    return 0;
+  }
   int cls = prec == SFD_PREC_F64 ? SFD_K_SUMS64 : prec == SFD_PREC_DF ? SFD_K_SUMSDF : SFD_K_SUMS32;
   if (gate >= 0) cls = SFD_K_EXTRA;
   LAUNCHC(e, cls, sfd_launch_sums(prec, A, e->nsum, e->max_n, e->sum_groups[prec], e->stream));
@@ -753,7 +758,7 @@ void free_engine(sfd_engine* e) {
   if (e->bg.side) cudaStreamSynchronize(e->bg.side);  // a background rebuild uses the inverse's buffers
   destroy_graphs(e);
   void* ptrs[] = {e->d_surf, e->d_node_surf, e->d_jobs_first, e->d_jobs_ap, e->d_cjobs_first, e->d_cjobs_ap, e->d_sum_items,
-                  e->d_f32_work, e->f32_part, e->f32_wsum, e->f32_count, e->d_asm_tiles,
+                  e->d_f32_work, e->f32_part, e->f32_wsum, e->f32_count, e->df_part, e->d_asm_tiles,
                   e->d_gemv_rows, e->d_poff, e->y0, e->ys, e->kacc, e->kcur, e->zp, e->zpp, e->ap, e->phip, e->a,
                   e->r, e->delta, e->phi_im, e->nd.w, e->nd.p, e->nd.wdf, e->nd.pdf, e->adf, e->ddf, e->nd.mdiag, e->nd.v1low, e->nd.v1up, e->nd.v2,
                   e->cacc, e->dacc, e->vel_low1, e->status, e->lmax, e->rnorm, e->rslot, e->bnorm, e->rrel,
@@ -1148,6 +1153,7 @@ int sfd_create_driven(const int* n, int nsurf, const sfd_problem* problems, cons
     CKE(dalloc(&e->d_f32_work, f32work.size()));
     CKE(cudaMemcpy(e->d_f32_work, f32work.data(), f32work.size() * sizeof(F32Work), cudaMemcpyHostToDevice));
     CKE(dalloc(&e->f32_part, 64LL * f32work.size()));
+    CKE(dalloc(&e->df_part, 128LL * f32work.size()));
     CKE(dalloc(&e->f32_wsum, f32work.size()));
     CKE(dalloc(&e->f32_count, items.size()));
     CKE(cudaMemset(e->f32_count, 0, items.size() * sizeof(unsigned int)));

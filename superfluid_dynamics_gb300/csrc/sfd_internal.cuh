@@ -82,6 +82,7 @@ struct sfd_engine {
   float4* f32_part = nullptr;
   float2* f32_wsum = nullptr;
   unsigned int* f32_count = nullptr;
+  float4* df_part = nullptr;  // double-float pass on the same work entries: 128 float4 per entry
   int4* d_asm_tiles = nullptr; int nasm = 0;
   int2* d_gemv_rows = nullptr; int ngemv = 0;
   long long* d_poff = nullptr;

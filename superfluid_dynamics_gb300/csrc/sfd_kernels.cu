@@ -91,7 +91,9 @@ __global__ void __launch_bounds__(64) k_node_prep(const SurfaceDesc* surf, const
 // shared memory, the cluster's CTA partials over distributed shared memory, in
 // a fixed order (bitwise reproducible), and CTA r finishes targets
 // [r kSumPerRank, (r+1) kSumPerRank) of the tile with the epilogue (C, D, M a,
-// residual).  One launch per pass; no partials leave the chip.
+// residual).  One launch per pass; no partials leave the chip.  This is the
+// FP64 engines' pass; the mixed engines' double-float and FP32 passes run on
+// (tile, source slice) CTAs (k_sums_dfs, k_sums_f32 below).
 
 namespace {
 
@@ -574,13 +576,20 @@ cudaError_t launch_prec(const SumArgs& A, dim3 grid, int groups, size_t smem, cu
 }
 }  // namespace
 
+template <int G>
+__global__ void k_sums_dfs(SumArgs A, float4* dpart);
+
 cudaError_t sfd_sums_configure() {
   // the largest staged source (the packed double-float one is 48 bytes) at n = 8192
   const int bytes = (int)std::max(std::max(sfd_sums_smem(SFD_PREC_F64, 8192), sfd_sums_smem(SFD_PREC_DF, 8192)),
                                   sfd_sums_smem(SFD_PREC_F32, 8192));
   cudaError_t e = configure_prec<SFD_PREC_F64>(bytes);
-  if (e == cudaSuccess) e = configure_prec<SFD_PREC_DF>(bytes);
   if (e == cudaSuccess) e = configure_prec<SFD_PREC_F32>(bytes);
+  // double-float pass on slices: slices of up to kF32MaxPer sources
+  const int dfs = kF32MaxPer * (int)sizeof(SrcDF2);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_sums_dfs<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, dfs);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_sums_dfs<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, dfs);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_sums_dfs<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, dfs);
   return e;
 }
 
@@ -589,7 +598,7 @@ cudaError_t sfd_launch_sums(int prec, const SumArgs& A, int nitems, int max_n, i
   const dim3 grid(nitems * kSumCL);
   const size_t smem = sfd_sums_smem(prec, max_n);
   if (prec == SFD_PREC_F64) return launch_prec<SFD_PREC_F64>(A, grid, groups, smem, st);
-  if (prec == SFD_PREC_DF) return launch_prec<SFD_PREC_DF>(A, grid, groups, smem, st);
+  if (prec == SFD_PREC_DF) return cudaErrorInvalidValue;  // the double-float pass runs on slices (k_sums_dfs)
   return launch_prec<SFD_PREC_F32>(A, grid, groups, smem, st);
 }
 
@@ -919,6 +928,173 @@ cudaError_t sfd_f32_ctas_per_sm(int max_per, int* ctas) {
 cudaError_t sfd_launch_sums_f32(const SumArgs& A, int nwork, int max_per, cudaStream_t st) {
   if (nwork == 0) return cudaSuccess;
   return sfd_launch(k_sums_f32, dim3(nwork), dim3(kF32Threads), f32_smem(max_per), st, true, A);
+}
+
+// ------------------------------------------------- double-float pass on slices
+// The accurate pass of a mixed solve (S_k, T_k in double-float, ~48 bits)
+// with the FP32 pass's layout: one independent CTA per (64-target tile,
+// source slice) work entry, sharing its work entries, tile counters and
+// weight-sum partials (the passes run one after another on one stream).  G
+// groups of 64 threads, one target per thread; group g takes the slice's
+// sources g, g + G, ... in ascending order.  The CTA writes its 64 targets'
+// double-float partials; the last slice of a tile to finish (acquire-release
+// counter, as in the FP32 pass) reduces them in slice order and runs the FP64
+// epilogue.  Compared with one 8-CTA cluster per tile, no CTA waits for its
+// cluster peers, and small surfaces get slices sized to their work.
+template <int G>
+__global__ void __launch_bounds__(64 * G, 1024 / (64 * G)) k_sums_dfs(SumArgs A, float4* dpart) {
+  sfd_pdl_begin();
+  constexpr int NT = 64 * G;
+  const F32Work wk = A.swork[blockIdx.x];
+  const int sidx = wk.sidx, t0 = wk.t0;
+  if (!gate_open(A.gate, sidx)) return;  // every slice of the tile skips together
+  const int n = wk.n, off = wk.off;
+  const bool image = wk.image != 0;
+  const int per = (n + wk.nsl - 1) / wk.nsl;
+  const int j_lo = min(n, wk.slice * per), j_hi = min(n, j_lo + per), jn = j_hi - j_lo;
+  extern __shared__ __align__(16) unsigned char dfs_dyn[];
+  SrcDF2* src = reinterpret_cast<SrcDF2*>(dfs_dyn);
+  __shared__ Red<SFD_PREC_DF> gred[G][kSumTile];
+  __shared__ df wred[NT / 32];
+  __shared__ int last;
+  const int tid = threadIdx.x, lane = tid & 31;
+
+  // ---- stage this slice's sources and its weight sum
+  df wpart{0.f, 0.f};
+  for (int jj = tid; jj < jn; jj += NT) {
+    const int g = off + j_lo + jj;
+    const float4 w = A.wdf[g];
+    const float2 ad = A.adf[g];
+    const float4 p = image ? A.pdf[g] : make_float4(0.f, 0.f, 0.f, 0.f);
+    wpart = df_add(wpart, df{ad.x, ad.y});
+    src[jj] = SrcDF2{make_float4(w.x, w.z, w.y, w.w), make_float4(p.x, p.z, p.y, p.w), ad.x, ad.y};
+  }
+  for (int o = 16; o > 0; o >>= 1) wpart = df_add(wpart, shfl_x(wpart, o));
+  if (lane == 0) wred[tid >> 5] = wpart;
+
+  // ---- one target per thread of each group
+  const int grp = tid / kSumTile, l = tid % kSumTile;
+  const int tk = t0 + l;
+  const int gt = off + (tk < n ? tk : 0);
+  Tgt<SFD_PREC_DF> T;
+  T.load(A.wdf[gt], image ? A.pdf[gt] : make_float4(0.f, 0.f, 0.f, 0.f));
+  __syncthreads();
+  Acc<SFD_PREC_DF> R;
+  // only the sources of the tile's own nodes need the j == k test
+  int lo = jn, hi = jn;
+  if (t0 < j_hi && t0 + kSumTile > j_lo) {
+    lo = max(0, t0 - j_lo);
+    hi = min(jn, t0 + kSumTile - j_lo);
+  }
+  const int self = tk < n ? tk - j_lo : -1;
+  auto first = [&](int a) { return a + ((grp - a) % G + G) % G; };
+  int jj = grp;
+#pragma unroll 4
+  for (; jj < lo; jj += G) pair_acc(T, src[jj], false, image, R);
+  for (jj = first(lo); jj < hi; jj += G) pair_acc(T, src[jj], jj == self, image, R);
+#pragma unroll 4
+  for (jj = first(hi); jj < jn; jj += G) pair_acc(T, src[jj], false, image, R);
+  gred[grp][l] = to_red(R);
+  __syncthreads();
+
+  // ---- this slice's partials (groups in order), then count the slice done
+  const long long entry = wk.base + wk.slice;
+  if (tid < kSumTile) {
+    Red<SFD_PREC_DF> v = gred[0][tid];
+#pragma unroll
+    for (int q = 1; q < G; ++q) red_add(v, gred[q][tid]);
+    dpart[entry * 128 + 2 * tid] = make_float4(v.sr.hi, v.sr.lo, v.si.hi, v.si.lo);
+    dpart[entry * 128 + 2 * tid + 1] = make_float4(v.tr.hi, v.tr.lo, v.ti.hi, v.ti.lo);
+  }
+  if (tid == 0) {
+    df w = wred[0];
+    for (int q = 1; q < NT / 32; ++q) w = df_add(w, wred[q]);
+    A.swsum[entry] = make_float2(w.hi, w.lo);
+  }
+  // one acquire-release atomic per slice (see k_sums_f32)
+  __syncthreads();
+  if (tid == 0) {
+    unsigned prev;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(prev) : "l"(A.scount + wk.item) : "memory");
+    last = prev == (unsigned)(wk.nsl - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+
+  // ---- the last slice of the tile: reduce in slice order, FP64 epilogue.
+  // P parts of 64 threads: part h sums slices [h spp, (h + 1) spp) in order,
+  // four loads in flight at a time; part 0 then adds parts 1 .. P - 1 in
+  // order, so the order is fixed.
+  if (tid == 0) A.scount[wk.item] = 0u;  // every slice has counted: ready for the next pass
+  constexpr int P = G < 4 ? G : 4;
+  constexpr int spp = (kF32MaxSlices + P - 1) / P;
+  __shared__ float hsum[P][kSumTile][10];
+  const int t = tid & 63, h = tid >> 6;
+  Red<SFD_PREC_DF> v;
+  df aw{0.f, 0.f};
+  if (h < P) {
+    for (int b = 0; b < spp; b += 4) {
+      float4 pa[4], pb[4];
+      float2 pw[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int sl = h * spp + b + i;
+        const bool in = b + i < spp && sl < wk.nsl;
+        pa[i] = in ? __ldcg(dpart + (wk.base + sl) * 128LL + 2 * t) : make_float4(0.f, 0.f, 0.f, 0.f);
+        pb[i] = in ? __ldcg(dpart + (wk.base + sl) * 128LL + 2 * t + 1) : make_float4(0.f, 0.f, 0.f, 0.f);
+        pw[i] = in ? __ldcg(A.swsum + wk.base + sl) : make_float2(0.f, 0.f);
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        if (b + i < spp && h * spp + b + i < wk.nsl) {
+          red_add(v, Red<SFD_PREC_DF>{df{pa[i].x, pa[i].y}, df{pa[i].z, pa[i].w}, df{pb[i].x, pb[i].y},
+                                      df{pb[i].z, pb[i].w}});
+          aw = df_add(aw, df{pw[i].x, pw[i].y});
+        }
+      }
+    }
+    if (h > 0) {
+      float* o = hsum[h][t];
+      o[0] = v.sr.hi; o[1] = v.sr.lo; o[2] = v.si.hi; o[3] = v.si.lo; o[4] = v.tr.hi;
+      o[5] = v.tr.lo; o[6] = v.ti.hi; o[7] = v.ti.lo; o[8] = aw.hi; o[9] = aw.lo;
+    }
+  }
+  __syncthreads();
+  if (h != 0) return;
+#pragma unroll
+  for (int q = 1; q < P; ++q) {
+    const float* o = hsum[q][t];
+    red_add(v, Red<SFD_PREC_DF>{df{o[0], o[1]}, df{o[2], o[3]}, df{o[4], o[5]}, df{o[6], o[7]}});
+    aw = df_add(aw, df{o[8], o[9]});
+  }
+  double rv = 0.0, bv = 0.0;
+  if (tk < n) {
+    const SurfaceDesc& S = A.surf[sidx];
+    rv = sums_finish(A, S, off + tk, cd{to_d(v.sr), to_d(v.si)}, cd{to_d(v.tr), to_d(v.ti)}, to_d(aw), image);
+    if (A.bnorm) {
+      const double b = fabs(A.phip[off + tk]);
+      bv = (b == b) ? b : 1e300;
+    }
+  }
+  auto warp_max_to = [&](double val, double* dst) {
+    unsigned long long m = (unsigned long long)__double_as_longlong(val);
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long u = __shfl_xor_sync(0xffffffffu, m, o);
+      m = u > m ? u : m;
+    }
+    if (lane == 0) atomicMax(reinterpret_cast<unsigned long long*>(dst), m);
+  };
+  if (A.rtrack) warp_max_to(rv, A.rtrack + (long long)sidx * SFD_RSLOTS);
+  if (A.bnorm) warp_max_to(bv, A.bnorm + sidx);
+}
+
+cudaError_t sfd_launch_sums_dfs(const SumArgs& A, float4* dpart, int nwork, int max_per, int groups,
+                                cudaStream_t st) {
+  if (nwork == 0) return cudaSuccess;
+  const size_t smem = (size_t)std::max(1, max_per) * sizeof(SrcDF2);
+  if (groups == 2) return sfd_launch(k_sums_dfs<2>, dim3(nwork), dim3(128), smem, st, true, A, dpart);
+  if (groups == 8) return sfd_launch(k_sums_dfs<8>, dim3(nwork), dim3(512), smem, st, true, A, dpart);
+  return sfd_launch(k_sums_dfs<4>, dim3(nwork), dim3(256), smem, st, true, A, dpart);
 }
 
 // Velocities and Bernoulli:

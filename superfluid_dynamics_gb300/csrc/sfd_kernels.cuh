@@ -121,6 +121,11 @@ cudaError_t sfd_launch_sums(int prec, const SumArgs& A, int nitems, int max_n, i
 // FP32 pass over `nwork` (tile, slice) entries (A.swork), slices of at most
 // max_per sources.
 cudaError_t sfd_launch_sums_f32(const SumArgs& A, int nwork, int max_per, cudaStream_t st);
+// Double-float pass on the FP32 pass's (tile, slice) work entries; dpart: 128
+// float4 of double-float partials per work entry; groups: 2, 4 or 8 groups of
+// 64 threads per CTA.
+cudaError_t sfd_launch_sums_dfs(const SumArgs& A, float4* dpart, int nwork, int max_per, int groups,
+                                cudaStream_t st);
 cudaError_t sfd_sums_configure();
 __global__ void k_velocity_bernoulli(VelArgs V);
 __global__ void k_velocity_node1(VelArgs V);
