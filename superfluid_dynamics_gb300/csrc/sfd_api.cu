@@ -265,8 +265,8 @@ int enqueue_precond(sfd_engine* e) {
               k_gj_update<<<dim3(4 * tiles - 4, 1, e->nsurf), 256, 0, e->stream>>>(
                   e->d_surf, e->nsurf, kb, e->m32, e->pbuf, e->rbuf, e->cbuf, e->d_poff, 1));
       LAUNCHC(e, SFD_K_UPDATE_TC,
-              sfd_launch_gj_update_tc(e->d_surf, e->nsurf, kb, e->max_np, e->m32, e->cparts, e->rparts,
-                                      e->panel_elems, e->d_poff, e->status, e->stream));
+              sfd_launch_gj_update_tc(&e->tmap_c, &e->tmap_r, e->d_tmap_out, e->d_surf, e->nsurf, kb, e->max_np,
+                                      e->tc_groups, e->d_poff, e->status, e->stream));
     } else {
       LAUNCHC(e, SFD_K_UPDATE,
               k_gj_update<<<dim3(tiles, tiles, e->nsurf), 256, 0, e->stream>>>(
@@ -649,8 +649,8 @@ int bg_start(sfd_engine* e) {
                                                             e->d_poff, e->cparts, e->rparts, e->panel_elems);
     k_gj_update<<<dim3(4 * tiles - 4, 1, e->nsurf), 256, 0, side>>>(e->d_surf, e->nsurf, kb, e->m32, e->pbuf, e->rbuf,
                                                                      e->cbuf, e->d_poff, 1);
-    CK(sfd_launch_gj_update_tc(e->d_surf, e->nsurf, kb, e->max_np, e->m32, e->cparts, e->rparts, e->panel_elems,
-                               e->d_poff, e->status, side));
+    CK(sfd_launch_gj_update_tc(&e->tmap_c, &e->tmap_r, e->d_tmap_out, e->d_surf, e->nsurf, kb, e->max_np,
+                               e->tc_groups, e->d_poff, e->status, side));
   }
   k_precond_to_half<<<e->ngemv, 256, 0, side>>>(e->d_surf, e->d_gemv_rows, e->m32, B.m16_next, B.rscale_next);
   CK(cudaGetLastError());
@@ -763,7 +763,8 @@ void free_engine(sfd_engine* e) {
                   e->r, e->delta, e->phi_im, e->nd.w, e->nd.p, e->nd.wdf, e->nd.pdf, e->adf, e->ddf, e->nd.mdiag, e->nd.v1low, e->nd.v1up, e->nd.v2,
                   e->cacc, e->dacc, e->vel_low1, e->status, e->lmax, e->rnorm, e->rslot, e->bnorm, e->rrel,
                   e->extra_count,
-                  e->inv_out, e->m64, e->m32, e->m16, e->rscale, e->fc_in, e->fc_out, e->rf, e->phipf, e->pbuf, e->rbuf, e->cbuf, e->cparts, e->rparts};
+                  e->inv_out, e->m64, e->m32, e->m16, e->rscale, e->fc_in, e->fc_out, e->rf, e->phipf, e->pbuf, e->rbuf, e->cbuf, e->cparts, e->rparts,
+                  e->d_tmap_out};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   {
@@ -1232,6 +1233,24 @@ int sfd_create_driven(const int* n, int nsurf, const sfd_problem* problems, cons
       CKE(dalloc(&e->cparts, 3 * e->panel_elems));
       CKE(dalloc(&e->rparts, 3 * e->panel_elems));
       CKE(sfd_tc_configure());
+      CKE(sfd_tc_make_map(&e->tmap_c, e->cparts, e->panel_elems / 128, e->panel_elems));
+      CKE(sfd_tc_make_map(&e->tmap_r, e->rparts, e->panel_elems / 128, e->panel_elems));
+      {
+        std::vector<sfd_engine::TensorMap> maps(nsurf);
+        for (int s = 0; s < nsurf; ++s) CKE(sfd_tc_make_out_map(&maps[s], e->m32 + e->hs[s].moff, pad_n(e->hs[s].n)));
+        CKE(dalloc(&e->d_tmap_out, nsurf));
+        CKE(cudaMemcpy(e->d_tmap_out, maps.data(), nsurf * sizeof(sfd_engine::TensorMap), cudaMemcpyHostToDevice));
+      }
+      // row groups per tile column: a single surface spreads its columns'
+      // rows over the SMs; a batch has columns enough
+      long long cols = 0;
+      int max_nt = 1;
+      for (int s = 0; s < nsurf; ++s) {
+        const int ntile = pad_n(e->hs[s].n) / 128;
+        cols += std::max(1, ntile - 1);
+        max_nt = std::max(max_nt, ntile);
+      }
+      e->tc_groups = cols >= e->nsm ? 1 : (int)std::max(1LL, std::min<long long>(max_nt, e->nsm / std::max(1LL, cols)));
     }
   }
   CKE(sfd_fft_configure());

@@ -116,6 +116,13 @@ struct sfd_engine {
   float* rscale = nullptr;   // per-row inverse scales of m16
   float *pbuf = nullptr, *rbuf = nullptr, *cbuf = nullptr;
   __nv_bfloat16 *cparts = nullptr, *rparts = nullptr;  // tensor-core operands: 3 bf16 parts, panel_elems apart
+  // TMA tensor maps of cparts / rparts (opaque 128-byte descriptors) and the
+  // row groups per tile column of the tensor-core update
+  struct alignas(64) TensorMap {
+    unsigned char bytes[128];
+  } tmap_c{}, tmap_r{};
+  TensorMap* d_tmap_out = nullptr;  // per surface: its FP32 matrix, the target of the update's reduce-adds
+  int tc_groups = 1;
   // graphs
   cudaGraphExec_t g_step[2] = {nullptr, nullptr};
   double g_dt = 0.0;

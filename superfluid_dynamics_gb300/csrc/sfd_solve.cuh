@@ -48,8 +48,17 @@ __global__ void k_precond_to_half(const SurfaceDesc* surf, const int2* rowblk, c
 __global__ void k_gemv_h(const SurfaceDesc* surf, const int2* rowblk, const __half* mat16, const float* rscale,
                          const float* v, double* y, float2* ydf, double* acc, float2* accdf, Gate gate);
 cudaError_t sfd_tc_configure();
-cudaError_t sfd_launch_gj_update_tc(const SurfaceDesc* surf, int nsurf, int kb, int max_np, float* mat,
-                                    const __nv_bfloat16* cparts, const __nv_bfloat16* rparts, long long part_stride,
+// TMA tensor map (128 bytes, written to map_out) of three bf16 part arrays of
+// `rows` rows x 128 K-major values, parts `part_stride` elements apart.
+cudaError_t sfd_tc_make_map(void* map_out, const __nv_bfloat16* parts, long long rows, long long part_stride);
+// TMA tensor map (128 bytes) of one surface's np x np FP32 matrix at `mat`.
+cudaError_t sfd_tc_make_out_map(void* map_out, float* mat, int np);
+// Tensor-core trailing update of Gauss-Jordan step kb: grid (tile columns,
+// ngroups row groups, surfaces), operands through the two tensor maps, the
+// update reduce-added into each surface's matrix through maps_out (device
+// array of one 128-byte map per surface, 64-byte aligned).
+cudaError_t sfd_launch_gj_update_tc(const void* map_c, const void* map_r, const void* maps_out,
+                                    const SurfaceDesc* surf, int nsurf, int kb, int max_np, int ngroups,
                                     const long long* poff, unsigned int* status, cudaStream_t st);
 __global__ void k_gemv(const SurfaceDesc* surf, const int2* rowblk, const float* mat, const float* v, double* y,
                        float2* ydf, double* acc, float2* accdf, Gate gate);
