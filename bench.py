@@ -397,7 +397,8 @@ def fp64_and_accuracy(args, opts_mixed, device, stream, checkpoints=(25, 50, 100
 
 
 def helium_batch_summary(args, device, stream, timed_steps=50):
-    """512 uneven helium films (N = 32 U{4..64}, seed 3) in one mixed engine:
+    """512 uneven helium films (N = 32 U{4..64}, seed 3) in one mixed engine
+    with the headline's solver settings (background rebuild included):
     surface-steps/s over `timed_steps` steps after 5 checked ones, error of
     those 5 steps against the FP64 engine, per-surface status counts."""
     import superfluid_dynamics_gb300 as sfd
@@ -410,7 +411,7 @@ def helium_batch_summary(args, device, stream, timed_steps=50):
     ph = np.concatenate([sf.phi for sf in surfs])
     dt = 1e-3
     opt = sfd.Options(precision=sfd.PRECISION_MIXED, refine_iters=args.refine_iters, pre_iters=args.pre_iters,
-                      refactor_every=args.refactor_every, device=device)
+                      refactor_every=args.refactor_every, refactor_lag=args.refactor_lag, device=device)
     eng = sfd.Engine(ns, phys, opt)
     eng.set_stream(stream.cuda_stream)
     eng.set_state(x, y, ph)
@@ -680,7 +681,7 @@ def run_workload(args, rank, world, local_rank):
     torch.cuda.set_device(local_rank)
     stream = torch.cuda.Stream()
     mixed = sfd.Options(precision=sfd.PRECISION_MIXED, refine_iters=args.refine_iters, pre_iters=args.pre_iters,
-                        refactor_every=args.refactor_every, device=local_rank)
+                        refactor_every=args.refactor_every, refactor_lag=args.refactor_lag, device=local_rank)
     fp64 = sfd.Options(precision=sfd.PRECISION_FP64, device=local_rank)
     line = {"workload": args.workload, "unit": "steps/s", "higher_is_better": True,
             "config": {"precision": "mixed", "pre_iters": args.pre_iters, "refine_iters": args.refine_iters,

@@ -233,11 +233,15 @@ int enqueue_gemv(sfd_engine* e, const float* vf, double* y, float2* ydf, double*
     const int wave = 2 * e->nsm, need = (e->max_n + kGemvRows - 1) / kGemvRows;
     const int grid = (need + wave - 1) / wave * wave;
     LAUNCHC(e, cls, sfd_launch(k_gemv_h, dim3(grid), dim3(512), e->max_np * sizeof(float), e->stream, true,
-                                      e->d_surf, (const int2*)nullptr, e->m16, e->rscale, vf, y, ydf, acc, accdf, G));
-  } else if (e->m16)
-    LAUNCHC(e, cls, sfd_launch(k_gemv_h, dim3(e->ngemv), dim3(512), e->max_np * sizeof(float), e->stream, true,
-                                      e->d_surf, e->d_gemv_rows, e->m16, e->rscale, vf, y, ydf, acc, accdf, G));
-  else
+                                      e->d_surf, (const int2*)nullptr, 0, e->m16, e->rscale, vf, y, ydf, acc, accdf,
+                                      G));
+  } else if (e->m16) {
+    // a batch: persistent CTAs (two per SM) over the (surface, row block) entries
+    const int grid = e->nsm > 0 ? std::min(e->ngemv, 2 * e->nsm) : e->ngemv;
+    LAUNCHC(e, cls, sfd_launch(k_gemv_h, dim3(grid), dim3(512), e->max_np * sizeof(float), e->stream, true,
+                                      e->d_surf, e->d_gemv_rows, e->ngemv, e->m16, e->rscale, vf, y, ydf, acc, accdf,
+                                      G));
+  } else
     LAUNCHC(e, cls, sfd_launch(k_gemv, dim3(e->ngemv), dim3(256), e->max_np * sizeof(float), e->stream, true,
                                       e->d_surf, e->d_gemv_rows, e->m32, vf, y, ydf, acc, accdf, G));
   return 0;

@@ -908,66 +908,72 @@ __global__ void __launch_bounds__(256) k_precond_to_half(const SurfaceDesc* surf
 // (8 entries) of the row in batches of four, software-pipelined one batch
 // ahead; the first batch is issued before v is staged, so the staging
 // latency overlaps the first matrix loads.
-__global__ void __launch_bounds__(512) k_gemv_h(const SurfaceDesc* surf, const int2* rowblk, const __half* mat16,
-                                                const float* rscale, const float* v, double* y, float2* ydf,
-                                                double* accv, float2* accdf, Gate gate) {
+// Row blocks (rowblk, nblk entries of (surface, first row), batches): the CTAs
+// are persistent and take blocks blockIdx.x, blockIdx.x + gridDim.x, ...; a
+// batch of small surfaces would otherwise run as tens of thousands of short
+// CTAs.  rowblk null (one surface): rows interleaved over the grid,
+// r = block + grid * warp, so every SM gets the same number of rows within one.
+__global__ void __launch_bounds__(512) k_gemv_h(const SurfaceDesc* surf, const int2* rowblk, int nblk,
+                                                const __half* mat16, const float* rscale, const float* v, double* y,
+                                                float2* ydf, double* accv, float2* accdf, Gate gate) {
   sfd_pdl_begin();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  // row blocks from the list, or (rowblk null: one surface) rows interleaved
-  // over the grid, r = block + grid * warp, so every SM gets the same number
-  // of rows within one
-  int sidx, r;
-  if (rowblk) {
-    const int2 rb = rowblk[blockIdx.x];
-    sidx = rb.x;
-    r = rb.y + warp;
-  } else {
-    sidx = 0;
-    r = blockIdx.x + gridDim.x * warp;
-  }
-  if (!gate_open(gate, sidx)) return;
-  const SurfaceDesc& S = surf[sidx];
-  const int n = S.n, np = pad_n(n), off = S.off;
   extern __shared__ float4 vsh[];
-  const bool live = r < n;
-  const int n8 = (n + 7) & ~7;
-  const int nq = n8 / 8;
-  const int per_lane = lane < nq ? (nq - lane + 31) / 32 : 0;  // chunks q = lane + 32 i, i < per_lane
-  const uint4* xr = reinterpret_cast<const uint4*>(mat16 + S.moff + (long long)(live ? r : 0) * np) + lane;
-  uint4 cur[4], nxt[4];
-#pragma unroll
-  for (int i = 0; i < 4; ++i) cur[i] = (live && i < per_lane) ? __ldg(xr + 32 * i) : make_uint4(0, 0, 0, 0);
-  stage_vector_f<512>(reinterpret_cast<float*>(vsh), v + off, n, n8);
-  __syncthreads();
-  if (!live) return;
-  auto dot8 = [&](uint4 h, int q, float acc) {
-    const __half2* hp = reinterpret_cast<const __half2*>(&h);
-    const float4 va = vsh[2 * q], vb = vsh[2 * q + 1];
-    float2 f0 = __half22float2(hp[0]), f1 = __half22float2(hp[1]), f2 = __half22float2(hp[2]),
-           f3 = __half22float2(hp[3]);
-    acc = fmaf(f0.x, va.x, fmaf(f0.y, va.y, fmaf(f1.x, va.z, fmaf(f1.y, va.w, acc))));
-    return fmaf(f2.x, vb.x, fmaf(f2.y, vb.y, fmaf(f3.x, vb.z, fmaf(f3.y, vb.w, acc))));
-  };
-  float acc0 = 0.f, acc1 = 0.f;
-  for (int b = 0; 4 * b < per_lane; ++b) {
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const int idx = 4 * (b + 1) + i;
-      nxt[i] = idx < per_lane ? __ldg(xr + 32 * idx) : make_uint4(0, 0, 0, 0);
+  const int nit = rowblk ? nblk : 1;
+  for (int blk = rowblk ? (int)blockIdx.x : 0; blk < nit; blk += rowblk ? (int)gridDim.x : 1) {
+    int sidx, r;
+    if (rowblk) {
+      const int2 rb = rowblk[blk];
+      sidx = rb.x;
+      r = rb.y + warp;
+    } else {
+      sidx = 0;
+      r = blockIdx.x + gridDim.x * warp;
     }
+    if (!gate_open(gate, sidx)) continue;  // uniform over the CTA
+    const SurfaceDesc& S = surf[sidx];
+    const int n = S.n, np = pad_n(n), off = S.off;
+    const bool live = r < n;
+    const int n8 = (n + 7) & ~7;
+    const int nq = n8 / 8;
+    const int per_lane = lane < nq ? (nq - lane + 31) / 32 : 0;  // chunks q = lane + 32 i, i < per_lane
+    const uint4* xr = reinterpret_cast<const uint4*>(mat16 + S.moff + (long long)(live ? r : 0) * np) + lane;
+    uint4 cur[4], nxt[4];
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const int idx = 4 * b + i;
-      if (idx < per_lane) {
-        if (i & 1) acc1 = dot8(cur[i], lane + 32 * idx, acc1);
-        else acc0 = dot8(cur[i], lane + 32 * idx, acc0);
+    for (int i = 0; i < 4; ++i) cur[i] = (live && i < per_lane) ? __ldg(xr + 32 * i) : make_uint4(0, 0, 0, 0);
+    __syncthreads();  // the previous block's readers of vsh are done
+    stage_vector_f<512>(reinterpret_cast<float*>(vsh), v + off, n, n8);
+    __syncthreads();
+    if (!live) continue;
+    auto dot8 = [&](uint4 h, int q, float acc) {
+      const __half2* hp = reinterpret_cast<const __half2*>(&h);
+      const float4 va = vsh[2 * q], vb = vsh[2 * q + 1];
+      float2 f0 = __half22float2(hp[0]), f1 = __half22float2(hp[1]), f2 = __half22float2(hp[2]),
+             f3 = __half22float2(hp[3]);
+      acc = fmaf(f0.x, va.x, fmaf(f0.y, va.y, fmaf(f1.x, va.z, fmaf(f1.y, va.w, acc))));
+      return fmaf(f2.x, vb.x, fmaf(f2.y, vb.y, fmaf(f3.x, vb.z, fmaf(f3.y, vb.w, acc))));
+    };
+    float acc0 = 0.f, acc1 = 0.f;
+    for (int b = 0; 4 * b < per_lane; ++b) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int idx = 4 * (b + 1) + i;
+        nxt[i] = idx < per_lane ? __ldg(xr + 32 * idx) : make_uint4(0, 0, 0, 0);
       }
-    }
 #pragma unroll
-    for (int i = 0; i < 4; ++i) cur[i] = nxt[i];
+      for (int i = 0; i < 4; ++i) {
+        const int idx = 4 * b + i;
+        if (idx < per_lane) {
+          if (i & 1) acc1 = dot8(cur[i], lane + 32 * idx, acc1);
+          else acc0 = dot8(cur[i], lane + 32 * idx, acc0);
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i) cur[i] = nxt[i];
+    }
+    float acc = acc0 + acc1;
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) gemv_store(acc * rscale[off + r], off + r, y, ydf, accv, accdf);
   }
-  float acc = acc0 + acc1;
-  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-  if (lane == 0) gemv_store(acc * rscale[off + r], off + r, y, ydf, accv, accdf);
 }
 

@@ -45,7 +45,7 @@ __global__ void k_gj_update(const SurfaceDesc* surf, int nsurf, int kb, float* m
 __global__ void k_precond_to_half(const SurfaceDesc* surf, const int2* rowblk, const float* mat, __half* mat16,
                                   float* rscale);
 // y = X v (v FP32); optional double-float copy of y and in-place acc += y
-__global__ void k_gemv_h(const SurfaceDesc* surf, const int2* rowblk, const __half* mat16, const float* rscale,
+__global__ void k_gemv_h(const SurfaceDesc* surf, const int2* rowblk, int nblk, const __half* mat16, const float* rscale,
                          const float* v, double* y, float2* ydf, double* acc, float2* accdf, Gate gate);
 cudaError_t sfd_tc_configure();
 // TMA tensor map (128 bytes, written to map_out) of three bf16 part arrays of

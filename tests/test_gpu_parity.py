@@ -309,10 +309,12 @@ def test_batch_mixing_cluster_and_single_cta_transforms(prec):
         assert rel(parts[2][i], op) < TOL[prec]
 
 
-@pytest.mark.parametrize("n", [256, 640, 1024])
+@pytest.mark.parametrize("n", [256, 640, 1024, 3072])
 def test_tensor_core_preconditioner(n):
     # The tcgen05 (3 x bf16-split) Gauss-Jordan update must give a usable inverse on
     # its own (no refinement: a = X phi' to ~1e-4), and the refined result must match.
+    # n = 3072: four tiles per CTA of the update, so its stage ring and both tensor-memory
+    # accumulators are reused.
     s = W.random_modes(n, seed=11)
     (ox, oy, op, oa, _, _), _ = O.rhs(O.Problem(), s.x, s.y, s.phi, diagnostics=True)
     for tc in (True, False):
