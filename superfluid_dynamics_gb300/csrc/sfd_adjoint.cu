@@ -307,7 +307,7 @@ __global__ void __launch_bounds__(kAdjThreads) k_lu_solve_t(int n, int np, const
 // and the corrections the solve ran (maxima over the solves of a call).
 __global__ void k_adj_node2(AdjConst K, AdjStage st, const double* lambda, cd* cbar, cd* dbar, double* zpb_re,
                             double* zpb_im, double* zppb_re, double* zppb_im, const double* rmax, int last,
-                            double tol, unsigned int* status, double* diag_rel, unsigned int* diag_corr) {
+                            double tol, unsigned int* status, double* diag_rel, unsigned int* diag_corr, cd* bq) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (rmax && k == 0) {
     const double b = rmax[0], rl = rmax[last];
@@ -323,7 +323,9 @@ __global__ void k_adj_node2(AdjConst K, AdjStage st, const double* lambda, cd* c
   const double rho = -lambda[k];
   const cd zp = st.zp[k], zpp = st.zpp[k];
   const cd izp = crcp(zp);
-  cbar[k] = cbar[k] + cmul_i(K.c1 * rho * cconj(zp));
+  const cd cb = cbar[k] + cmul_i(K.c1 * rho * cconj(zp));
+  cbar[k] = cb;
+  if (bq) bq[k] = st.w[k] * cconj(cb);  // the weight w_j conj(gC_j) of the second-order sums
   if (K.image) dbar[k] = dbar[k] + cmul_i(cd{-K.cI * rho, 0.0});
   // Mdiag = 1/2 + c1 Im(z''/z'):  gR = i c1 gMdiag,  gMdiag = rho a
   const cd Rb = cmul_i(cd{K.c1 * rho * st.a[k], 0.0});
@@ -386,18 +388,66 @@ __global__ void k_adj_sums2(AdjConst K, AdjStage st, const cd* cbar, const cd* d
 // ------------------------------------------------ mixed-precision reverse sweep
 // Pair reciprocals of one stage, row j = target: R_jk = 1 / (w_j - w_k)
 // (0 on the diagonal), Rb_jk = bw_k R_jk with bw = -i c1 w z' (the weights of
-// M^T lambda) and, with the image, I_jk = 1 / (1 - p_j conj p_k).
-// One thread per pair; consecutive threads write consecutive k.
-__global__ void k_adj_pairs(AdjConst K, const cd* w, const cd* p, const cd* zp, cd* R, cd* Rb, cd* I) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long long nn = (long long)K.n * K.n;
-  if (t >= nn) return;
-  const int j = (int)(t / K.n), k = (int)(t - (long long)j * K.n);
-  const cd wk = w[k];
-  const cd r = j == k ? cd{0.0, 0.0} : crcp(w[j] - wk);
-  R[t] = r;
-  Rb[t] = cmul_i(-K.c1 * (wk * zp[k])) * r;
-  if (K.image) I[t] = crcp(cd{1.0, 0.0} - p[j] * cconj(p[k]));
+// M^T lambda) and, with the image, I_jk = 1 / (1 - p_j conj p_k).  R is
+// antisymmetric and I Hermitian, so one CTA computes the 32 x 32 block (J, K),
+// J <= K, once and writes it and its mirror (K, J) (through shared memory, so
+// that both writes are coalesced): half the FP64 divisions of a full pass.
+__device__ __forceinline__ cd adj_bw(const AdjConst& K, cd w, cd zp) { return cmul_i(-K.c1 * (w * zp)); }
+__global__ void __launch_bounds__(256) k_adj_pairs(AdjConst K, const cd* w, const cd* p, const cd* zp, cd* R,
+                                                   cd* Rb, cd* I) {
+  __shared__ cd sr[32][33], si[32][33];
+  __shared__ cd wJ[32], wK[32], pJ[32], pK[32], bJ[32], bK[32];
+  const int n = K.n;
+  // triangular block index t = Kb (Kb + 1) / 2 + Jb, Jb <= Kb
+  const int t = blockIdx.x;
+  int Kb = (int)((sqrt(8.0 * t + 1.0) - 1.0) * 0.5);
+  while ((Kb + 1) * (Kb + 2) / 2 <= t) ++Kb;
+  while (Kb * (Kb + 1) / 2 > t) --Kb;
+  const int Jb = t - Kb * (Kb + 1) / 2;
+  const int j0 = 32 * Jb, k0 = 32 * Kb;
+  if (threadIdx.x < 32) {
+    const int i = threadIdx.x;
+    const int j = min(j0 + i, n - 1), k = min(k0 + i, n - 1);
+    wJ[i] = w[j];
+    wK[i] = w[k];
+    bJ[i] = adj_bw(K, w[j], zp[j]);
+    bK[i] = adj_bw(K, w[k], zp[k]);
+    pJ[i] = K.image ? p[j] : cd{0.0, 0.0};
+    pK[i] = K.image ? p[k] : cd{0.0, 0.0};
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < 32 * 32; e += 256) {
+    const int jj = e >> 5, kk = e & 31;
+    const int j = j0 + jj, k = k0 + kk;
+    cd r = {0.0, 0.0}, q = {0.0, 0.0};
+    if (j < n && k < n) {
+      r = j == k ? cd{0.0, 0.0} : crcp(wJ[jj] - wK[kk]);
+      const long long o = (long long)j * n + k;
+      R[o] = r;
+      Rb[o] = bK[kk] * r;
+      if (K.image) {
+        q = crcp(cd{1.0, 0.0} - pJ[jj] * cconj(pK[kk]));
+        I[o] = q;
+      }
+    }
+    sr[jj][kk] = r;
+    si[jj][kk] = q;
+  }
+  if (Jb == Kb) return;  // uniform over the CTA
+  __syncthreads();
+  // mirror: row k = k0 + a, column j = j0 + b: R_kj = -R_jk, I_kj = conj I_jk
+  for (int e = threadIdx.x; e < 32 * 32; e += 256) {
+    const int a = e >> 5, b = e & 31;
+    const int k = k0 + a, j = j0 + b;
+    if (k < n && j < n) {
+      const cd r = sr[b][a];
+      const cd rr = {-r.re, -r.im};
+      const long long o = (long long)k * n + j;
+      R[o] = rr;
+      Rb[o] = bJ[b] * rr;
+      if (K.image) I[o] = cconj(si[b][a]);
+    }
+  }
 }
 
 // The pair sums below give each target kWpt warps (a CTA holds kTpc targets):
@@ -472,7 +522,8 @@ __global__ void __launch_bounds__(kPairThreads) k_adj_sums1m(AdjConst K, const c
 // k_adj_sums2 from the pair reciprocals: R_kj = 1 / (w_k - w_j),
 // I_kj = 1 / (1 - p_k conj p_j).
 __global__ void __launch_bounds__(kPairThreads) k_adj_sums2m(AdjConst K, AdjStage st, const cd* R, const cd* I,
-                                                            const cd* cbar, const cd* dbar, double* gY) {
+                                                            const cd* cbar, const cd* dbar, const cd* bq,
+                                                            double* gY) {
   __shared__ cd sh[kTpc][kWpt][5];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int k = blockIdx.x * kTpc + warp / kWpt;
@@ -490,7 +541,7 @@ __global__ void __launch_bounds__(kPairThreads) k_adj_sums2m(AdjConst K, AdjStag
       const cd inv2 = inv * inv;
       acc[0] = cadd(acc[0], aj * inv);
       acc[1] = cadd(acc[1], aj * inv2);
-      acc[2] = cadd(acc[2], (w[j] * cconj(cbar[j])) * inv2);
+      acc[2] = cadd(acc[2], bq[j] * inv2);  // bq = w conj(gC)
       if (K.image) {
         const cd ie = Ik[j];
         const cd ie2c = (ie * ie) * cconj(p[j]);
@@ -716,7 +767,7 @@ struct AdjWork {
   // the image only), the transposed solve's node weights, FP32 product input
   // and residual slots, and the engine state saved around a recording
   bool mixed = false;
-  cd *R = nullptr, *Rb = nullptr, *I = nullptr;
+  cd *R = nullptr, *Rb = nullptr, *I = nullptr, *bq = nullptr;
   cd* part = nullptr;          // per-CTA partial sums of the X^T product (2 per CTA)
   float* v = nullptr;
   float* xt = nullptr;         // transpose of the FP32 approximate inverse (np x np)
@@ -728,6 +779,9 @@ struct AdjWork {
   // plan a' (the a' cotangent) and plan 3 (z', z'' and lambda cotangents)
   F4Plan f4_ap, f4_3;
   cd* f4_scr = nullptr;
+  // fork / join of the reverse sweep's independent branches onto the
+  // engine's auxiliary stream (mixed engines)
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int2* jobs = nullptr;        // {0, RAW}, {0, RAW2}
   std::vector<void*> allocs;
   // captured steps of sfd_rk4_vjp (engines with use_graphs): for step slot i
@@ -758,6 +812,8 @@ void sfd_adjoint_free(sfd_engine* e) {
   if (!e || !e->adj) return;
   adj_destroy_graphs(e->adj);
   if (e->adj->xt) cudaFree(e->adj->xt);
+  if (e->adj->ev_fork) cudaEventDestroy(e->adj->ev_fork);
+  if (e->adj->ev_join) cudaEventDestroy(e->adj->ev_join);
   for (void* p : e->adj->allocs) cudaFree(p);
   if (e->adj->slot_mem) cudaFree(e->adj->slot_mem);
   if (e->adj->ckpt) cudaFree(e->adj->ckpt);
@@ -830,12 +886,15 @@ int ensure_work(sfd_engine* e, int steps) {
       const AdjConst K = adj_const(e->hs[0]);
       ACK(adj_alloc(W, &W->R, (size_t)n * n));
       ACK(adj_alloc(W, &W->Rb, (size_t)n * n));
+      ACK(adj_alloc(W, &W->bq, (size_t)n));
       if (K.image) ACK(adj_alloc(W, &W->I, (size_t)n * n));
       ACK(adj_alloc(W, &W->part, 2 * (size_t)((n + kGtRows - 1) / kGtRows)));
       ACK(adj_alloc(W, &W->v, (size_t)n));
       ACK(adj_alloc(W, &W->rmax, (size_t)kAdjtIters + 1));
       ACK(adj_alloc(W, &W->ysave, n3));
 
+      ACK(cudaEventCreateWithFlags(&W->ev_fork, cudaEventDisableTiming));
+      ACK(cudaEventCreateWithFlags(&W->ev_join, cudaEventDisableTiming));
       ACK(adj_alloc(W, &W->diag_rel, 1));
       ACK(adj_alloc(W, &W->diag_corr, 1));
     }
@@ -923,19 +982,20 @@ int record_rhs(sfd_engine* e, AdjWork* W, AdjStage& st, bool refactor = true) {
   return 0;
 }
 
-int spectral(sfd_engine* e, AdjWork* W, int job, const double* re, const double* im, cd* out) {
+int spectral(sfd_engine* e, AdjWork* W, int job, const double* re, const double* im, cd* out,
+             cudaStream_t st = nullptr) {
   DerivArgs D{e->d_surf, 1, re, im, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, out, nullptr};
-  cudaError_t err = sfd_launch_spectral(D, W->jobs + job, 1, W->n, e->stream);
+  cudaError_t err = sfd_launch_spectral(D, W->jobs + job, 1, W->n, st ? st : e->stream);
   if (err != cudaSuccess) return sfd_internal_cuda(err, "spectral derivative");
   return 0;
 }
 
 // The jobs of a four-step plan (unscaled first / second derivatives of the
 // jobs' own inputs) in its three launches.
-int spectral_f4(sfd_engine* e, AdjWork* W, const F4Plan& P) {
+int spectral_f4(sfd_engine* e, AdjWork* W, const F4Plan& P, cudaStream_t st = nullptr) {
   DerivArgs D{e->d_surf, 1, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   for (int ph = 1; ph <= 3; ++ph) {
-    cudaError_t err = sfd_launch_f4(D, P, W->f4_scr, e->stream, ph);
+    cudaError_t err = sfd_launch_f4(D, P, W->f4_scr, st ? st : e->stream, ph);
     if (err != cudaSuccess) return sfd_internal_cuda(err, "four-step transform");
   }
   return 0;
@@ -972,22 +1032,34 @@ int rhs_vjp(sfd_engine* e, AdjWork* W, const AdjStage& st, double alpha, const d
                                        W->abar, W->zpb_re, W->zpb_im, W->zppb_re, W->zppb_im, W->pbar,
                                        W->mixed ? W->rmax : nullptr);
   ACK(cudaGetLastError());
+  // Mixed engines fork independent work onto the auxiliary stream (captured
+  // graphs keep the fork as parallel branches): the pair reciprocals and the
+  // gC / gD totals beside the a' cotangent's transform, and later the
+  // cotangents' transforms beside the second-order pair sums.
+  const bool fork = W->mixed && e->aux && !e->profile;
+  cudaStream_t x = fork ? e->aux : s;
+  const int T = (n + 31) / 32;
+  if (fork) {
+    ACK(cudaEventRecord(W->ev_fork, s));
+    ACK(cudaStreamWaitEvent(x, W->ev_fork, 0));
+  }
+  if (W->mixed) k_adj_pairs<<<T * (T + 1) / 2, 256, 0, x>>>(K, st.w, st.p, st.zp, W->R, W->Rb, W->I);
+  k_adj_sum_cd<<<1, kAdjThreads, 0, x>>>(n, W->cbar, W->dbar, W->sums);
+  if (fork) ACK(cudaEventRecord(W->ev_join, x));
   int rc = W->f4_ap.njobs ? spectral_f4(e, W, W->f4_ap) : spectral(e, W, 0, W->apb_re, W->apb_im, W->t1);
   if (rc) return rc;
-  k_adj_sum_cd<<<1, kAdjThreads, 0, s>>>(n, W->cbar, W->dbar, W->sums);
+  if (fork) ACK(cudaStreamWaitEvent(s, W->ev_join, 0));
   if (!W->mixed) {
     k_adj_sums1<<<nw, kAdjThreads, 0, s>>>(K, st.w, st.p, W->cbar, W->dbar, W->sb, W->tb);
     k_adj_a<<<nb, kAdjThreads, 0, s>>>(K, W->sums, W->t1, W->cbar, W->sb, W->tb, W->abar);
     k_lu_solve_t<<<1, kAdjThreads, K.np * sizeof(double), s>>>(n, K.np, st.lu, W->abar, W->lam);
     k_adj_node2<<<nb, kAdjThreads, 0, s>>>(K, st, W->lam, W->cbar, W->dbar, W->zpb_re, W->zpb_im, W->zppb_re,
-                                           W->zppb_im, nullptr, 0, 0.0, nullptr, nullptr, nullptr);
+                                           W->zppb_im, nullptr, 0, 0.0, nullptr, nullptr, nullptr, nullptr);
     k_adj_sums2<<<nw, kAdjThreads, 0, s>>>(K, st, W->cbar, W->dbar, gYout);
   } else {
-    const long long nn = (long long)n * n;
     const int np_blocks = (n + kTpc - 1) / kTpc;
     const int gt_blocks = (n + kGtRows - 1) / kGtRows;
     const size_t gt_smem = (size_t)((n + 3) & ~3) * sizeof(float);
-    k_adj_pairs<<<nblocks(nn, kAdjThreads), kAdjThreads, 0, s>>>(K, st.w, st.p, st.zp, W->R, W->Rb, W->I);
     // Sb, Tb and the solve's right-hand side ga (k_adj_a), lambda = 0, v = ga
     k_adj_sums1m<<<np_blocks, kPairThreads, 0, s>>>(K, st.w, W->R, W->I, W->cbar, W->dbar, W->sums, W->t1,
                                                     W->abar, W->lam, W->v, W->rmax);
@@ -1005,8 +1077,13 @@ int rhs_vjp(sfd_engine* e, AdjWork* W, const AdjStage& st, double alpha, const d
                                                     W->rmax, kAdjtIters);
     k_adj_node2<<<nb, kAdjThreads, 0, s>>>(K, st, W->lam, W->cbar, W->dbar, W->zpb_re, W->zpb_im, W->zppb_re,
                                            W->zppb_im, W->rmax, kAdjtIters, e->opt.refine_tol, e->status,
-                                           W->diag_rel, W->diag_corr);
-    k_adj_sums2m<<<np_blocks, kPairThreads, 0, s>>>(K, st, W->R, W->I, W->cbar, W->dbar, gYout);
+                                           W->diag_rel, W->diag_corr, W->bq);
+    if (fork) {
+      ACK(cudaEventRecord(W->ev_fork, s));
+      ACK(cudaStreamWaitEvent(x, W->ev_fork, 0));
+    }
+    k_adj_sums2m<<<np_blocks, kPairThreads, 0, x>>>(K, st, W->R, W->I, W->cbar, W->dbar, W->bq, gYout);
+    if (fork) ACK(cudaEventRecord(W->ev_join, x));
   }
   ACK(cudaGetLastError());
   if (W->f4_3.njobs) {
@@ -1017,6 +1094,7 @@ int rhs_vjp(sfd_engine* e, AdjWork* W, const AdjStage& st, double alpha, const d
     if (!rc) rc = spectral(e, W, 0, W->lam, nullptr, W->t3);
   }
   if (rc) return rc;
+  if (fork) ACK(cudaStreamWaitEvent(s, W->ev_join, 0));
   // parameter: d/dA3 = d/dvdw / h^3 (helium), d/dg (water)
   const double scale = K.physics == 1 ? 1.0 / (K.depth * K.depth * K.depth) : 1.0;
   k_adj_final<<<nb, kAdjThreads, 0, s>>>(K, W->t1, W->t2, W->t3, gYout, W->pbar, scale, W->gparam);
