@@ -1340,7 +1340,9 @@ extern "C" int sfd_rk4_vjp(sfd_engine* e, const double* cot_final, double* grad_
       AdjStage* rec = &W->slots[4 * (size_t)k];
       const bool rebuild = k % kXtEvery == 0;
       auto body = [&] {
+        e->allow_warm = true;  // a recomputed RK4 trajectory: evaluations may start warm
         int r = adj_step(e, W, W->dt, rec, rebuild);
+        e->allow_warm = false;
         return (!r && rebuild) ? refresh_xt(e, W, rec[0]) : r;
       };
       rc = graphs ? run_captured(e, &W->g_rec[k], &W->g_rec_nodes[k], body) : body();

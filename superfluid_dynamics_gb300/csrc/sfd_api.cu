@@ -224,10 +224,8 @@ int enqueue_sums(sfd_engine* e, int prec, const double* weights, const float2* w
 // y = X v with the current preconditioner (FP16 copy or FP32); ydf: optional
 // double-float copy of y; gate >= 0: only where that residual slot is above
 // the tolerance.
-int enqueue_gemv(sfd_engine* e, const float* vf, double* y, float2* ydf, double* acc, float2* accdf,
-                 int gate = -1) {
-  const Gate G = make_gate(e, gate);
-  const int cls = gate >= 0 ? SFD_K_EXTRA : SFD_K_GEMV;
+int enqueue_gemv_gated(sfd_engine* e, const float* vf, double* y, float2* ydf, double* acc, float2* accdf,
+                       const Gate& G, int cls) {
   if (e->m16 && e->nsurf == 1 && e->nsm > 0) {
     // one surface: a whole number of waves of two CTAs per SM, rows interleaved
     const int wave = 2 * e->nsm, need = (e->max_n + kGemvRows - 1) / kGemvRows;
@@ -245,6 +243,10 @@ int enqueue_gemv(sfd_engine* e, const float* vf, double* y, float2* ydf, double*
     LAUNCHC(e, cls, sfd_launch(k_gemv, dim3(e->ngemv), dim3(256), e->max_np * sizeof(float), e->stream, true,
                                       e->d_surf, e->d_gemv_rows, e->m32, vf, y, ydf, acc, accdf, G));
   return 0;
+}
+int enqueue_gemv(sfd_engine* e, const float* vf, double* y, float2* ydf, double* acc, float2* accdf,
+                 int gate = -1) {
+  return enqueue_gemv_gated(e, vf, y, ydf, acc, accdf, make_gate(e, gate), gate >= 0 ? SFD_K_EXTRA : SFD_K_GEMV);
 }
 
 int bg_flush(sfd_engine* e);
@@ -401,6 +403,8 @@ int enqueue_solve(sfd_engine* e, const double* st, const double* phi_im, bool re
       int rc = enqueue_precond(e);
       if (rc) return rc;
       e->have_precond = true;
+      // cold starts after a rebuild: every byte 0x7F is a large positive double, an open gate
+      if (e->warm) CK(cudaMemsetAsync(e->warm, 0x7F, (size_t)e->nsurf * sizeof(double), e->stream));
     }
     // a0 = X phi'; FP32 pre-iterations (full residual in FP32) bring a within
     // ~1e-7 of the solution; one double-float pass then gives the accurate
@@ -408,7 +412,10 @@ int enqueue_solve(sfd_engine* e, const double* st, const double* phi_im, bool re
     // The products read FP32 copies of phi' and r written by their producers;
     // the updates a += delta run in the product's epilogue.
     // a is final after the last product: a' forks from there
-    int rc = enqueue_gemv(e, e->phipf, e->a, e->adf, nullptr, nullptr);
+    // a0 = X phi' where the surface's previous solve did not converge (or
+    // there is none); elsewhere the previous solution a is the start
+    const Gate cold = (e->warm && e->allow_warm && sfd_warm_enabled()) ? Gate{e->warm, e->warm, 1, 0.0} : Gate{};
+    int rc = enqueue_gemv_gated(e, e->phipf, e->a, e->adf, nullptr, nullptr, cold, SFD_K_GEMV);
     if (rc) return rc;
     for (int it = 0; it < e->opt.pre_iters; ++it) {
       rc = enqueue_sums(e, SFD_PREC_F32, e->a, e->adf, 0, -1);
@@ -423,7 +430,7 @@ int enqueue_solve(sfd_engine* e, const double* st, const double* phi_im, bool re
     rc = enqueue_sums(e, SFD_PREC_DF, e->a, e->adf, 0, e->opt.refine_iters == 0 ? 0 : -1);
     if (rc) return rc;
     for (int it = 0; it < e->opt.refine_iters; ++it) {
-      rc = enqueue_gemv(e, e->rf, e->delta, e->ddf, e->a, nullptr);
+      rc = enqueue_gemv(e, e->rf, e->delta, e->ddf, e->a, e->adf);
       if (rc) return rc;
       if (fork_ap && it == e->opt.refine_iters - 1) {
         rc = enqueue_ap(e, true);
@@ -435,7 +442,7 @@ int enqueue_solve(sfd_engine* e, const double* st, const double* phi_im, bool re
     // extra corrections where the residual of the regular passes is above the
     // tolerance (a stale or inaccurate preconditioner)
     for (int i = 1; i <= extra; ++i) {
-      rc = enqueue_gemv(e, e->rf, e->delta, e->ddf, e->a, nullptr, i - 1);
+      rc = enqueue_gemv(e, e->rf, e->delta, e->ddf, e->a, e->adf, i - 1);
       if (rc) return rc;
       rc = enqueue_sums(e, SFD_PREC_F32, e->delta, e->ddf, 1, i, i - 1);
       if (rc) return rc;
@@ -473,7 +480,7 @@ int enqueue_rhs(sfd_engine* e, const double* st, double* out, bool refactor) {
             e->nd.v2, y, st, e->nblk == 4 ? st + 3 * nt : nullptr, e->nblk == 4 ? out + 3 * nt : nullptr,
             e->zp, e->zpp, e->vel_low1, out, out + nt, out + 2 * nt, e->status,
             e->rslot, 1 + extra, e->bnorm, e->opt.refine_tol, e->rnorm, e->rrel, e->extra_count,
-            e->opt.precision == SFD_PRECISION_MIXED ? e->stall_dev : nullptr};
+            e->opt.precision == SFD_PRECISION_MIXED ? e->stall_dev : nullptr, e->warm};
   if (e->any_rho) LAUNCHC(e, SFD_K_VELOCITY, sfd_launch(k_velocity_node1, dim3(1), dim3(32), 0, e->stream, true, V));
   LAUNCHC(e, SFD_K_VELOCITY,
           sfd_launch(k_velocity_bernoulli, dim3(blocks_for(nt, 32)), dim3(32), 0, e->stream, true, V));
@@ -690,7 +697,15 @@ int bg_flush(sfd_engine* e) {
   return bg_swap(e);
 }
 
+int run_steps_body(sfd_engine* e, double dt, int steps);
+// Fixed-step RK4 on the resident state; its evaluations may start warm.
 int run_steps(sfd_engine* e, double dt, int steps) {
+  e->allow_warm = true;
+  const int rc = run_steps_body(e, dt, steps);
+  e->allow_warm = false;
+  return rc;
+}
+int run_steps_body(sfd_engine* e, double dt, int steps) {
   if (steps < 0) return set_error(SFD_ERR_INVALID, "negative step count");
   if (!std::isfinite(dt)) return set_error(SFD_ERR_INVALID, "time step must be finite");
   CK(cudaSetDevice(e->device));
@@ -768,7 +783,7 @@ void free_engine(sfd_engine* e) {
                   e->cacc, e->dacc, e->vel_low1, e->status, e->lmax, e->rnorm, e->rslot, e->bnorm, e->rrel,
                   e->extra_count,
                   e->inv_out, e->m64, e->m32, e->m16, e->rscale, e->fc_in, e->fc_out, e->rf, e->phipf, e->pbuf, e->rbuf, e->cbuf, e->cparts, e->rparts,
-                  e->d_tmap_out};
+                  e->d_tmap_out, e->warm};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   {
@@ -867,6 +882,13 @@ int sfd_internal_rhs_ex(sfd_engine* e, const double* st, double* out, bool refac
   return enqueue_rhs(e, st, out, refactor);
 }
 int sfd_internal_bg_flush(sfd_engine* e) { return bg_flush(e); }
+bool sfd_warm_enabled() {
+  static const bool on = [] {
+    const char* v = std::getenv("SFD_WARM");
+    return !(v && v[0] == '0');
+  }();
+  return on;
+}
 
 // ====================================================================== C ABI
 extern "C" {
@@ -1214,6 +1236,8 @@ int sfd_create_driven(const int* n, int nsurf, const sfd_problem* problems, cons
   CKE(cudaMemset(e->rrel, 0, nsurf * sizeof(double)));
   CKE(cudaMemset(e->extra_count, 0, nsurf * sizeof(unsigned long long)));
   if (e->opt.precision == SFD_PRECISION_MIXED) {
+    CKE(dalloc(&e->warm, nsurf));
+    CKE(cudaMemset(e->warm, 0x7F, nsurf * sizeof(double)));  // cold: no previous solve
     CKE(cudaHostAlloc(reinterpret_cast<void**>(&e->stall_host), sizeof(unsigned int), cudaHostAllocMapped));
     *e->stall_host = 0u;
     CKE(cudaHostGetDevicePointer(reinterpret_cast<void**>(&e->stall_dev), e->stall_host, 0));

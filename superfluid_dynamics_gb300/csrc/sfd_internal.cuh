@@ -108,6 +108,14 @@ struct sfd_engine {
   // preconditioner in-step
   unsigned int* stall_host = nullptr;
   unsigned int* stall_dev = nullptr;
+  // mixed mode: per surface 0 when the last solve converged, 1e300 otherwise
+  // (written by the velocity kernel).  During fixed-step RK4 stepping
+  // (allow_warm) a converged solve's a is the starting point of the next one
+  // (the product a0 = X phi' is gated off for that surface); every other
+  // evaluation, and every evaluation that rebuilds the preconditioner, starts
+  // cold.  SFD_WARM=0 in the environment turns warm starts off.
+  double* warm = nullptr;
+  bool allow_warm = false;
   long long stall_rebuilds = 0;
   // matrices
   double* m64 = nullptr;
@@ -198,6 +206,8 @@ int sfd_internal_rhs(sfd_engine* e, const double* st, double* out);
 // As sfd_internal_rhs, for either precision; refactor = rebuild the mixed
 // preconditioner at this evaluation (it is built anyway if there is none).
 int sfd_internal_rhs_ex(sfd_engine* e, const double* st, double* out, bool refactor);
+// Whether warm starts are enabled (SFD_WARM=0 in the environment: off; read once).
+bool sfd_warm_enabled();
 // Switch in a pending background preconditioner rebuild now (not allowed
 // while the engine stream is being captured).
 int sfd_internal_bg_flush(sfd_engine* e);

@@ -1193,6 +1193,7 @@ __global__ void k_velocity_bernoulli(VelArgs V) {
       atomicOr(V.status + s, SFD_ST_REFINE_STALL);
       if (V.stall_host) *reinterpret_cast<volatile unsigned int*>(V.stall_host) = 1u;
     }
+    if (V.warm) V.warm[s] = (V.tol > 0.0 && fin <= lim) ? 0.0 : 1e300;
   }
 }
 

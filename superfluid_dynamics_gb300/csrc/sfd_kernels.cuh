@@ -112,6 +112,8 @@ struct VelArgs {
   double* rrel;         // the same relative to max |phi'|
   unsigned long long* extra_count;  // per-surface count of extra corrections run
   unsigned int* stall_host;         // host-mapped word set on a refinement stall (nullable)
+  double* warm;                     // mixed solves: per surface 0 when this solve converged (the next may
+                                    // start from its solution), 1e300 otherwise (nullable)
 };
 
 __global__ void k_node_prep(const SurfaceDesc* surf, const int* node_surf, int ntot, const double* x,
