@@ -42,17 +42,19 @@
 //  * FP64 engines record the LU factors of M per stage and solve M^T lambda = ga
 //    with them (U^T then L^T).
 //  * Mixed engines record O(n) data only.  The transposed solve is iterative
-//    refinement preconditioned by the transpose of the engine's approximate
-//    inverse X (FP16, row-scaled: X = diag(s) H, so X^T r = H^T (s r)):
+//    refinement preconditioned by X^T, the transpose of the engine's FP32
+//    approximate inverse X (kept as an FP32 transposed copy per block of
+//    recomputed steps):
 //      lambda_0 = X^T ga;  r = ga - M^T lambda (FP64, matrix-free);  lambda += X^T r
 //    where, with gC = i c1 conj(z') lambda and gD = -i cI lambda,
 //      (M^T lambda)_j = Mdiag_j lambda_j + Re(i (sum gC - gC_j) + 2 i conj(Sb_j)) + Re(-i sum gD + 2 i Tb_j)
 //    (Sb, Tb as in the ga line above, here with b_k = -i c1 w_k z'_k lambda_k).
-//    The iterations are gated on the residual (they return at once once
-//    max |r| <= 1e-13 max |ga|); a final residual above the engine's
-//    refine_tol raises SFD_ST_REFINE_STALL.  Every pair sum of one stage reads
-//    the pair reciprocals R_jk = 1 / (w_j - w_k) and I_jk = 1 / (1 - p_j conj p_k),
-//    computed once per stage in FP64 into two n x n complex matrices.
+//    The corrections are gated on the residual (they return at once once
+//    max |r| <= 1e-13 max |ga|, or once a correction gained less than a factor
+//    4); a final residual above the engine's refine_tol raises
+//    SFD_ST_REFINE_STALL.  Every pair sum of one stage reads the pair
+//    reciprocals R_jk = 1 / (w_j - w_k), bw_k R_jk and I_jk = 1 / (1 - p_j conj p_k),
+//    computed once per stage in FP64 into n x n complex matrices.
 #include <algorithm>
 #include <cstring>
 
@@ -75,9 +77,10 @@ constexpr int kAdjThreads = 256;
 // Transposed solve of mixed engines: residual checks (each but the last
 // followed by a correction, gated on the residual), and the relative residual
 // below which the remaining checks and corrections return at once.  They also
-// stop once a correction gained less than a factor kAdjtStagnation: the
-// residual has reached the noise floor of its FP64 evaluation (a few 1e-12
-// relative at n = 512), where further corrections change nothing.
+// stop once a correction gained less than a factor 1 / kAdjtStagnation: the
+// residual has reached the noise floor of its FP64 evaluation (about 3e-15
+// relative on the fit film at n = 512), where further corrections change
+// nothing.
 constexpr int kAdjtIters = 5;
 constexpr double kAdjtGateTol = 1e-13;
 constexpr double kAdjtStagnation = 0.25;
@@ -706,8 +709,8 @@ __global__ void __launch_bounds__(kPairThreads) k_adjt_resid(AdjConst K, AdjStag
 }
 
 // spectral part: gZ = -s1 R1(gz') + s2 R2(gz''); gphi = -s1 Re R1(lambda)
-// Block 0 also adds scale * sum pbar to *acc (the parameter cotangent, fixed
-// order; k_adj_sum_param's work).
+// Block 0 also adds scale * sum pbar to *acc (the parameter cotangent, summed
+// in a fixed order).
 __global__ void __launch_bounds__(kAdjThreads) k_adj_final(AdjConst K, const cd* r1zpb, const cd* r2zppb,
                                                           const cd* r1lam, double* gY, const double* pbar,
                                                           double scale, double* acc) {
