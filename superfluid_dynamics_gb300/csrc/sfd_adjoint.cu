@@ -395,6 +395,9 @@ __global__ void k_adj_sums2(AdjConst K, AdjStage st, const cd* cbar, const cd* d
 // antisymmetric and I Hermitian, so one CTA computes the 32 x 32 block (J, K),
 // J <= K, once and writes it and its mirror (K, J) (through shared memory, so
 // that both writes are coalesced): half the FP64 divisions of a full pass.
+// The mirrored R is bitwise the direct one; the mirrored I may differ from a
+// direct evaluation in the last bit (p_k conj p_j and p_j conj p_k round
+// separately).
 __device__ __forceinline__ cd adj_bw(const AdjConst& K, cd w, cd zp) { return cmul_i(-K.c1 * (w * zp)); }
 __global__ void __launch_bounds__(256) k_adj_pairs(AdjConst K, const cd* w, const cd* p, const cd* zp, cd* R,
                                                    cd* Rb, cd* I) {
