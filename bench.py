@@ -524,9 +524,9 @@ def run_ours(args, rank, world, local_rank):
     # ---- end to end through the C ABI with host buffers: every step is one
     # sfd_rk4_steps_host call that copies the state in from pinned host memory,
     # steps, and copies the result back into the same buffers
-    x = torch.from_numpy(s.x.copy()).pin_memory().numpy()
-    y = torch.from_numpy(s.y.copy()).pin_memory().numpy()
-    p = torch.from_numpy(s.phi.copy()).pin_memory().numpy()
+    # one pinned [x | y | phi] buffer: the state moves in one copy each way
+    buf = torch.from_numpy(np.concatenate([s.x, s.y, s.phi])).pin_memory().numpy()
+    x, y, p = buf[:s.x.size], buf[s.x.size:2 * s.x.size], buf[2 * s.x.size:]
     align()
     torch.cuda.synchronize()
     t0 = time.perf_counter()

@@ -171,7 +171,9 @@ int sfd_rhs_device(sfd_engine* e, const void* state_in, void* rhs_out);
 int sfd_rk4_steps(sfd_engine* e, double dt, int steps);
 /* Host-buffer stepping in one call: copy the state [x | y | phi] (ntot each)
  * in, run `steps` RK4 steps, copy it back out into the same arrays, with one
- * synchronisation.  Pinned host arrays make the copies asynchronous. */
+ * synchronisation.  Pinned host arrays make the copies asynchronous; arrays
+ * that are consecutive parts of one buffer (y = x + ntot, phi = y + ntot)
+ * move in one copy each way. */
 int sfd_rk4_steps_host(sfd_engine* e, double* x, double* y, double* phi, double dt, int steps);
 /* Enqueue without waiting for completion (timed loops). */
 int sfd_rk4_steps_async(sfd_engine* e, double dt, int steps);

@@ -1483,6 +1483,9 @@ int sfd_rk4_steps(sfd_engine* e, double dt, int steps) {
 // engine stream.
 static cudaError_t copy_state_host(sfd_engine* e, double* x, double* y, double* phi, bool to_device) {
   const size_t b = (size_t)e->ntot * sizeof(double);
+  if (y == x + e->ntot && phi == y + e->ntot)  // one [x | y | phi] buffer: one copy
+    return to_device ? cudaMemcpyAsync(e->y0, x, 3 * b, cudaMemcpyHostToDevice, e->stream)
+                     : cudaMemcpyAsync(x, e->y0, 3 * b, cudaMemcpyDeviceToHost, e->stream);
   double* h[3] = {x, y, phi};
   for (int k = 0; k < 3; ++k) {
     double* d = e->y0 + (size_t)k * e->ntot;

@@ -79,4 +79,11 @@ def test_step_host_matches_resident_stepping():
             e.step_host(x, y, p, 0.005, 1)
         got = np.concatenate([x, y, p])
     assert np.array_equal(got, ref)
+    # the three blocks as consecutive parts of one buffer (one copy each way)
+    with sfd.Engine(n, sfd.WaterBoundaryProblem(), opt) as e:
+        buf = np.concatenate([s.x, s.y, s.phi])
+        x, y, p = buf[:n], buf[n:2 * n], buf[2 * n:]
+        for _ in range(7):
+            e.step_host(x, y, p, 0.005, 1)
+    assert np.array_equal(buf, ref)
 
