@@ -194,11 +194,18 @@ def kernel_traffic(kernel: str, n: int):
 #   boundary_sums_fp64 : per pair, water: 11 FP64 FLOP
 #   gemv               : per product: 2 n^2 bytes (the FP16 preconditioner)
 #   fft4_columns, fft4_rows, fft4_inverse_columns (four-step transforms of a
-#                        power-of-two n = 64 N2; per RK stage z is transformed
-#                        forward once and back twice, phi and a forward and
-#                        back once): 5 L log2 L FP64 FLOP per length-L FFT,
-#                        3 x 64 forward columns (L = N2), 7 x N2 rows
-#                        (L = 64), 4 x 64 inverse columns per stage
+#                        power-of-two n = 64 N2 on the step's critical path;
+#                        per RK stage z is transformed forward once and back
+#                        twice, phi forward and back once): 5 L log2 L FP64
+#                        FLOP per length-L FFT, 2 x 64 forward columns
+#                        (L = N2), 5 x N2 rows (L = 64), 3 x 64 inverse
+#                        columns per stage
+#   ap_transform       : the a' transform of each stage (forked beside the
+#                        last boundary-sum pass while stepping on graphs):
+#                        four-step, 64 forward columns, 2 x N2 rows, 64
+#                        inverse columns; otherwise 10 n log2 n per stage
+#   start_product      : a0 = X phi', returning at once on warm starts:
+#                        reported by time only
 #   node_prep, velocity_bernoulli, rk4_combine: O(n), reported by time only
 #   extra_corrections, ap_redo: the gated extra corrections and the a'
 #                        transform repeated after them; they return at once
@@ -212,7 +219,8 @@ def fft4_work_per_step(cls: str, n: int) -> float:
     n2 = n // 64
     col = 5.0 * n2 * math.log2(n2)
     row = 5.0 * 64 * 6
-    return 4 * {"fft4_columns": 3 * 64 * col, "fft4_rows": 7 * n2 * row, "fft4_inverse_columns": 4 * 64 * col}[cls]
+    return 4 * {"fft4_columns": 2 * 64 * col, "fft4_rows": 5 * n2 * row, "fft4_inverse_columns": 3 * 64 * col,
+                "ap_transform": 2 * 64 * col + 2 * n2 * row}[cls]
 
 
 def class_roofline(prof: dict, prof_steps: int, n: int, sums_per_step: dict, jobs_per_step: int,
@@ -230,8 +238,12 @@ def class_roofline(prof: dict, prof_steps: int, n: int, sums_per_step: dict, job
             work = jobs_per_step * 10.0 * n * math.log2(n)
             c.update(bound="fp64", unit="TFLOP/s", work_per_step=work, achieved=work / sec / 1e12,
                      peak=pk["fp64_tflops"])
-        elif name.startswith("fft4_"):
+        elif name.startswith("fft4_") or (name == "ap_transform" and n >= 512 and (n & (n - 1)) == 0):
             work = fft4_work_per_step(name, n)
+            c.update(bound="fp64", unit="TFLOP/s", work_per_step=work, achieved=work / sec / 1e12,
+                     peak=pk["fp64_tflops"])
+        elif name == "ap_transform":
+            work = 4 * 10.0 * n * math.log2(n)
             c.update(bound="fp64", unit="TFLOP/s", work_per_step=work, achieved=work / sec / 1e12,
                      peak=pk["fp64_tflops"])
         elif name in FLOP_PER_PAIR:
@@ -587,13 +599,13 @@ def run_ours(args, rank, world, local_rank):
         pk.update({"hbm_gbs": hbm, "bf16_tflops": bf16, "source_hbm_bf16": peak_kind})
         passes = {"boundary_sums_fp32": 4 * (args.pre_iters + args.refine_iters) if mixed else 0,
                   "boundary_sums_df": 4 if mixed else 0, "boundary_sums_fp64": 0 if mixed else 4}
-        gemv = 4 * (1 + args.pre_iters + args.refine_iters) if mixed else 0
+        gemv = 4 * (args.pre_iters + args.refine_iters) if mixed else 0  # a0 = X phi' is its own class
         f4 = n >= 512 and n <= 8192 and (n & (n - 1)) == 0  # four-step transforms instead of per-job ones
-        classes = class_roofline(prof, prof_steps, n, passes, 0 if f4 else 16, gemv, pk)
+        classes = class_roofline(prof, prof_steps, n, passes, 0 if f4 else 12, gemv, pk)
         dom = max(classes, key=lambda k: classes[k]["ms_per_step"])
         d = classes[dom]
         kname = {"spectral_deriv": "k_spectral_cluster", "boundary_sums_fp32": "k_sums_f32",
-                 "boundary_sums_df": "k_boundary_sums<DF>", "gemv": "k_gemv_h", "fft4_columns": "k_fft4<1>",
+                 "boundary_sums_df": "k_sums_dfs", "gemv": "k_gemv_h", "fft4_columns": "k_fft4<1>",
                  "fft4_rows": "k_fft4<2>", "fft4_inverse_columns": "k_fft4<3>"}.get(dom, dom)
         per_launch_work = d.get("work_per_step", 0.0) / max(d["launches_per_step"], 1e-9)
         traffic = kernel_traffic(kname, n)
@@ -607,9 +619,11 @@ def run_ours(args, rank, world, local_rank):
                             f"{peak_kind} HBM copy"),
             "peaks": pk, "classes": classes,
             "note": "achieved = algorithmic work of the class per step / its event-timed device time per step "
-                    "(eager pass over one preconditioner period, graphs off); the gated extra corrections and the "
-                    "repeated a' transform are the classes extra_corrections and ap_redo, timed but counted as no "
-                    "work; the step is neither HBM- nor tensor-bound: the boundary sums run on the FP32 pipes, "
+                    "(eager pass over one preconditioner period, graphs off); the gated extra corrections, the "
+                    "repeated a' transform and the starting product a0 = X phi' (returning at once on warm starts) "
+                    "are the classes extra_corrections, ap_redo and start_product, timed but counted as no work; "
+                    "ap_transform is the a' transform, which the graphs run beside the last boundary-sum pass; "
+                    "the step is neither HBM- nor tensor-bound: the boundary sums run on the FP32 pipes, "
                     "the transforms on the FP64 pipe"}
 
     if not args.no_adjoint:

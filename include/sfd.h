@@ -207,11 +207,13 @@ long long sfd_kernel_launches(const sfd_engine* e);
 /* Per-kernel-class device time: while enabled, RK4 steps run eagerly (no
  * graph) and every kernel launch is bracketed by CUDA events on the engine
  * stream; sfd_profile_read returns accumulated milliseconds and launch counts
- * per class (names from sfd_profile_class_name; 21 classes).  The gated extra
- * corrections and the a' transform repeated after them have classes of their
- * own ("extra_corrections", "ap_redo"), so the other classes hold working
- * launches only. */
-#define SFD_PROFILE_CLASSES 21
+ * per class (names from sfd_profile_class_name; 23 classes).  The gated extra
+ * corrections, the a' transform repeated after them and the starting product
+ * a0 = X phi' (which returns at once on warm starts) have classes of their
+ * own ("extra_corrections", "ap_redo", "start_product"), so the other classes
+ * hold working launches only; the a' transform, which stepping on graphs runs
+ * beside the last boundary-sum pass, is "ap_transform". */
+#define SFD_PROFILE_CLASSES 23
 int sfd_profile(sfd_engine* e, int enable);
 int sfd_profile_read(sfd_engine* e, double* ms, long long* counts, int nclass);
 const char* sfd_profile_class_name(int cls);

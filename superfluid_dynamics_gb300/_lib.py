@@ -22,7 +22,7 @@ STATUS_PIVOT_SWAP = 0x2
 STATUS_ZERO_PIVOT = 0x4
 STATUS_REFINE_STALL = 0x8
 STATUS_TIMEOUT = 0x20
-PROFILE_CLASSES = 21
+PROFILE_CLASSES = 23
 
 
 class SfdProblem(ctypes.Structure):

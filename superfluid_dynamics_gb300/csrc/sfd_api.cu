@@ -316,18 +316,20 @@ cudaError_t launch_transforms(const sfd_engine* e, const DerivArgs& D, bool firs
 int enqueue_transforms(sfd_engine* e, const DerivArgs& D, bool first) {
   const int nj = first ? e->njobs_first : e->njobs_ap, ncj = first ? e->ncjobs_first : e->ncjobs_ap;
   const bool redo = D.gate.slot != nullptr;  // gated a' after extra corrections: a class of its own
+  // the a' transform has a class of its own too (off the step's critical path on graphs)
+  const int c_single = redo ? SFD_K_AP_REDO : first ? SFD_K_SPECTRAL : SFD_K_AP;
   if (nj)
-    LAUNCHC(e, redo ? SFD_K_AP_REDO : SFD_K_SPECTRAL,
+    LAUNCHC(e, c_single,
             sfd_launch_spectral(D, first ? e->d_jobs_first : e->d_jobs_ap, nj, e->max_n_single, e->stream));
   if (ncj)
-    LAUNCHC(e, redo ? SFD_K_AP_REDO : SFD_K_SPECTRAL,
+    LAUNCHC(e, c_single,
             sfd_launch_spectral_cluster(D, first ? e->d_cjobs_first : e->d_cjobs_ap, ncj, e->max_n_cluster,
                                         e->stream));
   const F4Plan& p = first ? e->f4_first : e->f4_ap;
   if (p.njobs) {
-    LAUNCHC(e, redo ? SFD_K_AP_REDO : SFD_K_F4_COLS, sfd_launch_f4(D, p, e->f4_scr, e->stream, 1));
-    LAUNCHC(e, redo ? SFD_K_AP_REDO : SFD_K_F4_ROWS, sfd_launch_f4(D, p, e->f4_scr, e->stream, 2));
-    LAUNCHC(e, redo ? SFD_K_AP_REDO : SFD_K_F4_ICOLS, sfd_launch_f4(D, p, e->f4_scr, e->stream, 3));
+    LAUNCHC(e, first ? SFD_K_F4_COLS : c_single, sfd_launch_f4(D, p, e->f4_scr, e->stream, 1));
+    LAUNCHC(e, first ? SFD_K_F4_ROWS : c_single, sfd_launch_f4(D, p, e->f4_scr, e->stream, 2));
+    LAUNCHC(e, first ? SFD_K_F4_ICOLS : c_single, sfd_launch_f4(D, p, e->f4_scr, e->stream, 3));
   }
   return 0;
 }
@@ -415,7 +417,7 @@ int enqueue_solve(sfd_engine* e, const double* st, const double* phi_im, bool re
     // a0 = X phi' where the surface's previous solve did not converge (or
     // there is none); elsewhere the previous solution a is the start
     const Gate cold = (e->warm && e->allow_warm && sfd_warm_enabled()) ? Gate{e->warm, e->warm, 1, 0.0} : Gate{};
-    int rc = enqueue_gemv_gated(e, e->phipf, e->a, e->adf, nullptr, nullptr, cold, SFD_K_GEMV);
+    int rc = enqueue_gemv_gated(e, e->phipf, e->a, e->adf, nullptr, nullptr, cold, SFD_K_GEMV0);
     if (rc) return rc;
     for (int it = 0; it < e->opt.pre_iters; ++it) {
       rc = enqueue_sums(e, SFD_PREC_F32, e->a, e->adf, 0, -1);
@@ -1469,7 +1471,7 @@ const char* sfd_profile_class_name(int cls) {
                                           "factor_diag", "factor_panel", "factor_update", "lu_trsv", "gemv",
                                           "velocity_bernoulli", "rk4_combine", "factor_update_tcgen05",
                                           "fft4_columns", "fft4_rows", "fft4_inverse_columns", "extra_corrections",
-                                          "ap_redo"};
+                                          "ap_redo", "ap_transform", "start_product"};
   return (cls >= 0 && cls < SFD_NCLASS) ? names[cls] : "";
 }
 

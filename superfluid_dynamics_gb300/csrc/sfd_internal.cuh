@@ -37,6 +37,8 @@ enum {
   SFD_K_F4_ICOLS,  // inverse column FFTs and outputs
   SFD_K_EXTRA,     // extra corrections (gated: they return at once where the residual is converged)
   SFD_K_AP_REDO,   // a' transformed again after extra corrections (gated likewise)
+  SFD_K_AP,        // the a' transform (forked beside the last pass while stepping on graphs)
+  SFD_K_GEMV0,     // the starting product a0 = X phi' (returns at once on warm starts)
   SFD_NCLASS
 };
 

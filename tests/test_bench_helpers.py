@@ -29,11 +29,14 @@ def test_class_roofline_counts_the_work_actually_run():
 
 
 def test_fft4_work_counts_five_n_log_n_per_transform():
-    n = 4096  # N2 = 64: per stage 3 forward column sets, 7 row sets, 4 inverse column sets of 64 FFTs of 64 points
+    # N2 = 64: per stage, z and phi: 2 forward column sets, 5 row sets, 3 inverse column sets of
+    # 64 FFTs of 64 points; a': 1 forward column set, 2 row sets, 1 inverse column set
+    n = 4096
     per_fft = 5.0 * 64 * 6
-    assert math.isclose(bench.fft4_work_per_step("fft4_columns", n), 4 * 3 * 64 * per_fft)
-    assert math.isclose(bench.fft4_work_per_step("fft4_rows", n), 4 * 7 * 64 * per_fft)
-    assert math.isclose(bench.fft4_work_per_step("fft4_inverse_columns", n), 4 * 4 * 64 * per_fft)
+    assert math.isclose(bench.fft4_work_per_step("fft4_columns", n), 4 * 2 * 64 * per_fft)
+    assert math.isclose(bench.fft4_work_per_step("fft4_rows", n), 4 * 5 * 64 * per_fft)
+    assert math.isclose(bench.fft4_work_per_step("fft4_inverse_columns", n), 4 * 3 * 64 * per_fft)
+    assert math.isclose(bench.fft4_work_per_step("ap_transform", n), 4 * 4 * 64 * per_fft)
 
 
 def test_traffic_lookup_misses_cleanly():
