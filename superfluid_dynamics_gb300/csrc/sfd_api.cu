@@ -226,19 +226,28 @@ int enqueue_sums(sfd_engine* e, int prec, const double* weights, const float2* w
 // the tolerance.
 int enqueue_gemv_gated(sfd_engine* e, const float* vf, double* y, float2* ydf, double* acc, float2* accdf,
                        const Gate& G, int cls) {
-  if (e->m16 && e->nsurf == 1 && e->nsm > 0) {
+  // the first rows may be requested before the wait on the preceding kernel
+  // unless the launch is gated or that kernel wrote the matrix
+  const bool prefetch = !G.slot && !e->m16_written && sfd_gemv_prefetch_enabled();
+  if (e->m16 && e->gemv_spw > 0) {
+    // one surface: rows streamed into shared memory, one CTA per SM
+    LAUNCHC(e, cls, sfd_launch_gemv_stream(e->d_surf, e->nsm, e->gemv_spw, e->gemv_smem, prefetch, e->m16, e->rscale,
+                                           vf, y, ydf, acc, accdf, G, e->status, e->stream));
+    e->m16_written = false;
+  } else if (e->m16 && e->nsurf == 1 && e->nsm > 0) {
     // one surface: a whole number of waves of two CTAs per SM, rows interleaved
     const int wave = 2 * e->nsm, need = (e->max_n + kGemvRows - 1) / kGemvRows;
     const int grid = (need + wave - 1) / wave * wave;
     LAUNCHC(e, cls, sfd_launch(k_gemv_h, dim3(grid), dim3(512), e->max_np * sizeof(float), e->stream, true,
                                       e->d_surf, (const int2*)nullptr, 0, e->m16, e->rscale, vf, y, ydf, acc, accdf,
-                                      G));
+                                      G, prefetch ? 1 : 0));
+    e->m16_written = false;
   } else if (e->m16) {
     // a batch: persistent CTAs (two per SM) over the (surface, row block) entries
     const int grid = e->nsm > 0 ? std::min(e->ngemv, 2 * e->nsm) : e->ngemv;
     LAUNCHC(e, cls, sfd_launch(k_gemv_h, dim3(grid), dim3(512), e->max_np * sizeof(float), e->stream, true,
                                       e->d_surf, e->d_gemv_rows, e->ngemv, e->m16, e->rscale, vf, y, ydf, acc, accdf,
-                                      G));
+                                      G, 0));
   } else
     LAUNCHC(e, cls, sfd_launch(k_gemv, dim3(e->ngemv), dim3(256), e->max_np * sizeof(float), e->stream, true,
                                       e->d_surf, e->d_gemv_rows, e->m32, vf, y, ydf, acc, accdf, G));
@@ -279,9 +288,11 @@ int enqueue_precond(sfd_engine* e) {
                   e->d_surf, e->nsurf, kb, e->m32, e->pbuf, e->rbuf, e->cbuf, e->d_poff, 0));
     }
   }
-  if (e->m16)
+  if (e->m16) {
     LAUNCHC(e, SFD_K_GEMV, k_precond_to_half<<<e->ngemv, 256, 0, e->stream>>>(e->d_surf, e->d_gemv_rows, e->m32,
                                                                               e->m16, e->rscale));
+    e->m16_written = true;  // the next product reads it only after its wait
+  }
   return 0;
 }
 
@@ -678,6 +689,7 @@ int bg_swap(sfd_engine* e) {
   auto& B = e->bg;
   CK(cudaStreamWaitEvent(e->stream, B.ev_done, 0));
   CK(cudaMemcpyAsync(e->m16, B.m16_next, (size_t)e->mat_elems * sizeof(__half), cudaMemcpyDeviceToDevice, e->stream));
+  e->m16_written = true;
   CK(cudaMemcpyAsync(e->rscale, B.rscale_next, (size_t)e->ntot * sizeof(float), cudaMemcpyDeviceToDevice, e->stream));
   B.swap_at = -1;
   return 0;
@@ -884,6 +896,20 @@ int sfd_internal_rhs_ex(sfd_engine* e, const double* st, double* out, bool refac
   return enqueue_rhs(e, st, out, refactor);
 }
 int sfd_internal_bg_flush(sfd_engine* e) { return bg_flush(e); }
+bool sfd_gemv_prefetch_enabled() {
+  static const bool on = [] {
+    const char* v = std::getenv("SFD_GEMV_PREFETCH");
+    return !(v && v[0] == '0');
+  }();
+  return on;
+}
+int sfd_gemv_stream_cap() {
+  static const int cap = [] {
+    const char* v = std::getenv("SFD_GEMV_SPW");
+    return v ? std::max(0, std::atoi(v)) : kGemvSDefaultSpw;
+  }();
+  return cap;
+}
 bool sfd_warm_enabled() {
   static const bool on = [] {
     const char* v = std::getenv("SFD_WARM");
@@ -1255,6 +1281,12 @@ int sfd_create_driven(const int* n, int nsurf, const sfd_problem* problems, cons
     if (e->opt.precond_half) {
       CKE(dalloc(&e->m16, e->mat_elems));
       CKE(dalloc(&e->rscale, nt));
+      if (nsurf == 1 && e->nsm > 0 && e->hs[0].moff % 8 == 0 && sfd_gemv_stream_cap() > 0) {
+        int smem_max = 0;
+        CKE(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, e->device));
+        sfd_gemv_stream_plan(e->hs[0].n, e->nsm, smem_max, sfd_gemv_stream_cap(), &e->gemv_spw, &e->gemv_smem);
+        if (e->gemv_spw > 0) CKE(sfd_gemv_stream_configure(e->gemv_smem));
+      }
     }
     CKE(dalloc(&e->pbuf, (long long)nsurf * 128 * 128));
     CKE(dalloc(&e->rbuf, e->panel_elems));

@@ -124,6 +124,9 @@ struct sfd_engine {
   float* m32 = nullptr;
   __half* m16 = nullptr;     // FP16 copy of the preconditioner (rows scaled by powers of two)
   float* rscale = nullptr;   // per-row inverse scales of m16
+  int gemv_spw = 0;          // streamed product (one surface): row slots per warp, 0 = register-pipelined
+  int gemv_smem = 0;         // its dynamic shared memory
+  bool m16_written = false;  // the last kernel enqueued wrote m16: the next product may not prefetch it
   float *pbuf = nullptr, *rbuf = nullptr, *cbuf = nullptr;
   __nv_bfloat16 *cparts = nullptr, *rparts = nullptr;  // tensor-core operands: 3 bf16 parts, panel_elems apart
   // TMA tensor maps of cparts / rparts (opaque 128-byte descriptors) and the
@@ -210,6 +213,13 @@ int sfd_internal_rhs(sfd_engine* e, const double* st, double* out);
 int sfd_internal_rhs_ex(sfd_engine* e, const double* st, double* out, bool refactor);
 // Whether warm starts are enabled (SFD_WARM=0 in the environment: off; read once).
 bool sfd_warm_enabled();
+// Row slots per warp of the streamed single-surface product at most
+// (SFD_GEMV_SPW in the environment, default kGemvSDefaultSpw; 0: the
+// register-pipelined product; read once).
+int sfd_gemv_stream_cap();
+// Whether the streamed product requests its first rows before waiting on its
+// predecessor (SFD_GEMV_PREFETCH=0: never; read once).
+bool sfd_gemv_prefetch_enabled();
 // Switch in a pending background preconditioner rebuild now (not allowed
 // while the engine stream is being captured).
 int sfd_internal_bg_flush(sfd_engine* e);

@@ -20,9 +20,12 @@
 //  * mixed mode: FP32 matrix, blocked in-place Gauss-Jordan inverse (nb = 128),
 //    applied as a GEMV inside the FP64-accurate refinement loop.
 #include "sfd_engine.cuh"
+#include "sfd_mbar.cuh"
 #include "sfd_solve.cuh"
 
 #include <cuda_fp16.h>
+
+#include <algorithm>
 
 #include <cuda_bf16.h>
 
@@ -903,6 +906,16 @@ __global__ void __launch_bounds__(256) k_precond_to_half(const SurfaceDesc* surf
   }
 }
 
+// acc + (8 FP16 entries of a row, chunk q) . (v[8q .. 8q + 8) staged as float4s)
+__device__ __forceinline__ float dot8h(uint4 h, const float4* vsh, int q, float acc) {
+  const __half2* hp = reinterpret_cast<const __half2*>(&h);
+  const float4 va = vsh[2 * q], vb = vsh[2 * q + 1];
+  float2 f0 = __half22float2(hp[0]), f1 = __half22float2(hp[1]), f2 = __half22float2(hp[2]),
+         f3 = __half22float2(hp[3]);
+  acc = fmaf(f0.x, va.x, fmaf(f0.y, va.y, fmaf(f1.x, va.z, fmaf(f1.y, va.w, acc))));
+  return fmaf(f2.x, vb.x, fmaf(f2.y, vb.y, fmaf(f3.x, vb.z, fmaf(f3.y, vb.w, acc))));
+}
+
 // y = X v with the FP16 copy (FP32 accumulation), y scaled back per row.
 // 16 warps per CTA, one row per warp.  Each lane streams its 16-byte chunks
 // (8 entries) of the row in batches of four, software-pipelined one batch
@@ -913,11 +926,26 @@ __global__ void __launch_bounds__(256) k_precond_to_half(const SurfaceDesc* surf
 // batch of small surfaces would otherwise run as tens of thousands of short
 // CTAs.  rowblk null (one surface): rows interleaved over the grid,
 // r = block + grid * warp, so every SM gets the same number of rows within one.
+// prefetch != 0 (one surface, ungated launches whose immediate predecessor
+// does not write the matrix): each warp loads its first batch of the row
+// before the wait on the preceding kernel (programmatic dependent launch); by
+// then every earlier kernel of the stream has completed.
 __global__ void __launch_bounds__(512) k_gemv_h(const SurfaceDesc* surf, const int2* rowblk, int nblk,
                                                 const __half* mat16, const float* rscale, const float* v, double* y,
-                                                float2* ydf, double* accv, float2* accdf, Gate gate) {
-  sfd_pdl_begin();
+                                                float2* ydf, double* accv, float2* accdf, Gate gate, int prefetch) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  uint4 cur[4], nxt[4];
+  bool have = false;  // cur holds the first batch already
+  if (prefetch && !rowblk) {
+    const SurfaceDesc& S = surf[0];  // written once at set-up
+    const int n = S.n, r = blockIdx.x + gridDim.x * warp, nq = ((n + 7) & ~7) / 8;
+    const int per_lane = lane < nq ? (nq - lane + 31) / 32 : 0;
+    const uint4* xr = reinterpret_cast<const uint4*>(mat16 + S.moff + (long long)(r < n ? r : 0) * pad_n(n)) + lane;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) cur[i] = (r < n && i < per_lane) ? __ldg(xr + 32 * i) : make_uint4(0, 0, 0, 0);
+    have = true;
+  }
+  sfd_pdl_begin();
   extern __shared__ float4 vsh[];
   const int nit = rowblk ? nblk : 1;
   for (int blk = rowblk ? (int)blockIdx.x : 0; blk < nit; blk += rowblk ? (int)gridDim.x : 1) {
@@ -938,21 +966,16 @@ __global__ void __launch_bounds__(512) k_gemv_h(const SurfaceDesc* surf, const i
     const int nq = n8 / 8;
     const int per_lane = lane < nq ? (nq - lane + 31) / 32 : 0;  // chunks q = lane + 32 i, i < per_lane
     const uint4* xr = reinterpret_cast<const uint4*>(mat16 + S.moff + (long long)(live ? r : 0) * np) + lane;
-    uint4 cur[4], nxt[4];
+    if (!have) {
 #pragma unroll
-    for (int i = 0; i < 4; ++i) cur[i] = (live && i < per_lane) ? __ldg(xr + 32 * i) : make_uint4(0, 0, 0, 0);
+      for (int i = 0; i < 4; ++i) cur[i] = (live && i < per_lane) ? __ldg(xr + 32 * i) : make_uint4(0, 0, 0, 0);
+    }
+    have = false;
     __syncthreads();  // the previous block's readers of vsh are done
     stage_vector_f<512>(reinterpret_cast<float*>(vsh), v + off, n, n8);
     __syncthreads();
     if (!live) continue;
-    auto dot8 = [&](uint4 h, int q, float acc) {
-      const __half2* hp = reinterpret_cast<const __half2*>(&h);
-      const float4 va = vsh[2 * q], vb = vsh[2 * q + 1];
-      float2 f0 = __half22float2(hp[0]), f1 = __half22float2(hp[1]), f2 = __half22float2(hp[2]),
-             f3 = __half22float2(hp[3]);
-      acc = fmaf(f0.x, va.x, fmaf(f0.y, va.y, fmaf(f1.x, va.z, fmaf(f1.y, va.w, acc))));
-      return fmaf(f2.x, vb.x, fmaf(f2.y, vb.y, fmaf(f3.x, vb.z, fmaf(f3.y, vb.w, acc))));
-    };
+    auto dot8 = [&](uint4 h, int q, float acc) { return dot8h(h, vsh, q, acc); };
     float acc0 = 0.f, acc1 = 0.f;
     for (int b = 0; 4 * b < per_lane; ++b) {
 #pragma unroll
@@ -977,3 +1000,156 @@ __global__ void __launch_bounds__(512) k_gemv_h(const SurfaceDesc* surf, const i
   }
 }
 
+
+// ------------------------------------------------ streamed product, one surface
+// y = X v for one surface with the FP16 rows streamed into shared memory by
+// the copy engine.  One persistent CTA per SM takes the rows r = block +
+// grid * i; CTA row i belongs to warp i % 8, and each warp owns `spw` row
+// slots: it keeps up to spw whole rows of its own in flight as bulk copies
+// (cp.async.bulk, one mbarrier per slot) and refills a slot with its next row
+// as soon as it has consumed the row in it.  At N = 4096 that is 24 rows
+// (192 KB) in flight per SM, against the 2 KB per warp that the
+// register-pipelined k_gemv_h keeps: the product is bound by L2 / DRAM
+// bandwidth instead of by load latency.  The arithmetic is k_gemv_h's entry
+// for entry (each lane's chunks in the same order, the same two accumulators,
+// the same reduction), so both give the same bits.  A slot is only ever waited
+// on and refilled by its own warp, so a wait is never more than one phase
+// ahead of the barrier.  A wait that runs out (1 << 22 probes) sets
+// SFD_ST_TIMEOUT in the surface status; the warp then stops, waits (bounded)
+// for its copies in flight and returns.
+// prefetch != 0: the first rows are requested before the wait on the
+// preceding kernel of the stream (programmatic dependent launch), so they
+// arrive while that kernel finishes.  Only for ungated launches whose
+// immediate predecessor does not write the matrix: by then every earlier
+// kernel of the stream has completed (each waits on its own predecessor
+// before it lets the next one start).
+__global__ void __launch_bounds__(32 * kGemvSWarps, 1)
+    k_gemv_hs(const SurfaceDesc* surf, int spw, int prefetch, const __half* mat16, const float* rscale,
+              const float* v, double* y, float2* ydf, double* accv, float2* accdf, Gate gate,
+              unsigned int* status) {
+  using namespace sfd_async;
+  constexpr unsigned kSpin = 1u << 22;
+  const SurfaceDesc& S = surf[0];  // written once at set-up
+  const int n = S.n, np = pad_n(n), off = S.off, n8 = (n + 7) & ~7;
+  const int G = gridDim.x, b = blockIdx.x;
+  const int rows = b < n ? (n - 1 - b) / G + 1 : 0;  // CTA rows i: matrix rows b + G i < n
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int wrows = warp < rows ? (rows - 1 - warp) / kGemvSWarps + 1 : 0;  // warp rows j: i = warp + 8 j
+  const uint32_t rb = (uint32_t)n8 * 2u;  // bytes per row copy (a multiple of 16)
+  extern __shared__ __align__(128) unsigned char gsm[];
+  uint64_t* bar = reinterpret_cast<uint64_t*>(gsm) + warp * kGemvSMaxSpw;
+  float4* vsh = reinterpret_cast<float4*>(gsm + kGemvSHead);
+  unsigned char* slots = gsm + kGemvSHead + ((n8 * 4 + 127) & ~127) + (size_t)warp * spw * rb;
+  const char* xrow = reinterpret_cast<const char*>(mat16 + S.moff + (long long)b * np);
+  const long long xstride = (long long)G * np * 2;  // bytes from one CTA row to the next
+  auto issue = [&](int j) {
+    const uint32_t mb = smem_u32(bar + j % spw);
+    mbar_expect_tx(mb, rb);
+    bulk_g2s(smem_u32(slots + (size_t)(j % spw) * rb), xrow + (long long)(warp + kGemvSWarps * j) * xstride, rb,
+             mb);
+  };
+  const int first = min(spw, wrows);
+  auto start = [&] {
+    if (lane == 0 && first > 0) {
+      for (int k = 0; k < first; ++k) mbar_init(smem_u32(bar + k), 1);
+      mbar_init_fence();
+      for (int j = 0; j < first; ++j) issue(j);
+    }
+  };
+  if (prefetch) start();
+  sfd_pdl_begin();
+  if (rows == 0) return;
+  if (!prefetch) {
+    if (!gate_open(gate, 0)) return;  // uniform over the grid
+    start();
+  }
+  // stage v (zero from n to n8) while the first rows are in flight
+  {
+    const float* vs = v + off;
+    if ((n & 3) == 0 && (reinterpret_cast<uintptr_t>(vs) & 15) == 0) {
+      const float4* v4 = reinterpret_cast<const float4*>(vs);
+      for (int q = threadIdx.x; q < n8 / 4; q += blockDim.x)
+        vsh[q] = 4 * q < n ? v4[q] : make_float4(0.f, 0.f, 0.f, 0.f);
+    } else {
+      float* vf = reinterpret_cast<float*>(vsh);
+      for (int q = threadIdx.x; q < n8; q += blockDim.x) vf[q] = q < n ? vs[q] : 0.f;
+    }
+  }
+  __syncthreads();
+  const int nq = n8 / 8;
+  const int per_lane = lane < nq ? (nq - lane + 31) / 32 : 0;  // chunks q = lane + 32 t, t < per_lane
+  int j = 0;
+  for (; j < wrows; ++j) {
+    const uint32_t mb = smem_u32(bar + j % spw);
+    const uint32_t parity = (uint32_t)(j / spw) & 1u;
+    unsigned it = 0;
+    while (!mbar_try(mb, parity) && ++it < kSpin) {
+    }
+    if (!__all_sync(0xffffffffu, it < kSpin)) {
+      if (lane == 0) atomicOr(status, SFD_ST_TIMEOUT);
+      break;
+    }
+    const uint4* xs = reinterpret_cast<const uint4*>(slots + (size_t)(j % spw) * rb);
+    float acc0 = 0.f, acc1 = 0.f;
+    int t = 0;
+#pragma unroll 4
+    for (; t + 1 < per_lane; t += 2) {
+      const int q0 = lane + 32 * t, q1 = q0 + 32;
+      const uint4 h0 = xs[q0], h1 = xs[q1];
+      acc0 = dot8h(h0, vsh, q0, acc0);
+      acc1 = dot8h(h1, vsh, q1, acc1);
+    }
+    if (t < per_lane) acc0 = dot8h(xs[lane + 32 * t], vsh, lane + 32 * t, acc0);
+    float acc = acc0 + acc1;
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    __syncwarp();  // every lane's reads of the slot are done
+    if (lane == 0) {
+      const int g = off + b + G * (warp + kGemvSWarps * j);
+      gemv_store(acc * rscale[g], g, y, ydf, accv, accdf);
+      if (j + spw < wrows) {
+        fence_proxy_async_smem();
+        issue(j + spw);
+      }
+    }
+  }
+  if (j < wrows && lane == 0) {
+    // gave up at row j: let the copies in flight (rows j .. j + spw - 1 that
+    // were issued) land before the CTA's shared memory is released
+    for (int jj = j; jj < min(wrows, j + spw); ++jj) {
+      const uint32_t mb = smem_u32(bar + jj % spw);
+      for (unsigned w = 0; w < kSpin && !mbar_try(mb, (uint32_t)(jj / spw) & 1u); ++w) {
+      }
+    }
+  }
+}
+
+// Plan of the streamed product for one surface of n nodes on `nsm` SMs with
+// `smem_max` bytes of shared memory per CTA: row slots per warp (capped at
+// cap, and at the rows a warp gets) and the dynamic shared memory; spw = 0
+// when one row per warp does not fit.
+void sfd_gemv_stream_plan(int n, int nsm, int smem_max, int cap, int* spw, int* smem) {
+  *spw = 0;
+  *smem = 0;
+  if (n < 1 || nsm < 1) return;
+  const long long n8 = (n + 7) & ~7, rb = 2 * n8, vbytes = (4 * n8 + 127) & ~127LL;
+  const long long room = (long long)smem_max - kGemvSHead - vbytes;
+  const int rows_cta = (n + nsm - 1) / nsm, rows_warp = (rows_cta + kGemvSWarps - 1) / kGemvSWarps;
+  long long k = room / (kGemvSWarps * rb);
+  k = std::min<long long>(k, std::min(kGemvSMaxSpw, std::min(cap, rows_warp)));
+  if (k < 1) return;
+  *spw = (int)k;
+  *smem = (int)(kGemvSHead + vbytes + kGemvSWarps * k * rb);
+}
+
+cudaError_t sfd_launch_gemv_stream(const SurfaceDesc* surf, int nsm, int spw, int smem, bool prefetch,
+                                   const __half* mat16, const float* rscale, const float* v, double* y, float2* ydf,
+                                   double* acc, float2* accdf, const Gate& gate, unsigned int* status,
+                                   cudaStream_t st) {
+  if (prefetch && gate.slot) return cudaErrorInvalidValue;  // a gated launch may not prefetch
+  return sfd_launch(k_gemv_hs, dim3(nsm), dim3(32 * kGemvSWarps), (size_t)smem, st, true, surf, spw,
+                    prefetch ? 1 : 0, mat16, rscale, v, y, ydf, acc, accdf, gate, status);
+}
+
+cudaError_t sfd_gemv_stream_configure(int smem) {
+  return cudaFuncSetAttribute(k_gemv_hs, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+}

@@ -44,9 +44,30 @@ __global__ void k_gj_update(const SurfaceDesc* surf, int nsurf, int kb, float* m
                             const float* rbuf, const float* cbuf, const long long* poff, int k_lines_only);
 __global__ void k_precond_to_half(const SurfaceDesc* surf, const int2* rowblk, const float* mat, __half* mat16,
                                   float* rscale);
-// y = X v (v FP32); optional double-float copy of y and in-place acc += y
+// y = X v (v FP32); optional double-float copy of y and in-place acc += y;
+// prefetch: one surface (rowblk null), ungated, predecessor not writing mat16
 __global__ void k_gemv_h(const SurfaceDesc* surf, const int2* rowblk, int nblk, const __half* mat16, const float* rscale,
-                         const float* v, double* y, float2* ydf, double* acc, float2* accdf, Gate gate);
+                         const float* v, double* y, float2* ydf, double* acc, float2* accdf, Gate gate, int prefetch);
+// y = X v for one surface with the FP16 rows streamed into shared memory
+// (k_gemv_hs): kGemvSWarps warps per CTA, one CTA per SM, spw row slots per
+// warp; the plan gives spw and the dynamic shared memory (spw = 0: the rows do
+// not fit, use k_gemv_h); configure sets the kernel's shared-memory limit.
+constexpr int kGemvSWarps = 8;
+constexpr int kGemvSMaxSpw = 8;
+// Default cap on the slots per warp.  At N = 4096 (27 rows per CTA) two slots
+// (16 rows, 148 KB in flight per SM) stepped faster than three (214 KB) or
+// one: the smaller footprint leaves room on the SM for the next kernel's CTAs,
+// which programmatic dependent launch places there early.
+constexpr int kGemvSDefaultSpw = 2;
+constexpr int kGemvSHead = 1024;  // mbarriers (kGemvSWarps x kGemvSMaxSpw x 8 B), padded
+void sfd_gemv_stream_plan(int n, int nsm, int smem_max, int cap, int* spw, int* smem);
+cudaError_t sfd_gemv_stream_configure(int smem);
+// prefetch: request the first rows before waiting on the preceding kernel
+// (ungated launches whose predecessor does not write mat16 only).
+cudaError_t sfd_launch_gemv_stream(const SurfaceDesc* surf, int nsm, int spw, int smem, bool prefetch,
+                                   const __half* mat16, const float* rscale, const float* v, double* y, float2* ydf,
+                                   double* acc, float2* accdf, const Gate& gate, unsigned int* status,
+                                   cudaStream_t st);
 cudaError_t sfd_tc_configure();
 // TMA tensor map (128 bytes, written to map_out) of three bf16 part arrays of
 // `rows` rows x 128 K-major values, parts `part_stride` elements apart.

@@ -40,9 +40,11 @@
 #include <cuda_bf16.h>
 
 #include "sfd_engine.cuh"
+#include "sfd_mbar.cuh"
 #include "sfd_solve.cuh"
 
 namespace {
+using namespace sfd_async;
 
 constexpr int kTile = 128;                       // M = N = K of one tile update
 constexpr int kParts = 3;                        // bf16 parts per operand
@@ -55,10 +57,6 @@ constexpr int kThreads = 32 * (2 + kEpiWarps);   // producer, MMA issuer, 4 epil
 constexpr int kBoxBytes = 32 * 32 * 4;           // epilogue staging box: 32 rows x 32 FP32 (128-byte rows)
 constexpr int kSmemBytes = kRBytes + kStages * kStageBytes + kEpiWarps * 2 * kBoxBytes + 1024;
 constexpr unsigned kSpinLimit = 1u << 22;
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
 
 // Shared-memory matrix descriptor (tcgen05 format): start address, leading
 // byte offset (unused for swizzled K-major: 16 B), stride byte offset (1024 B
@@ -86,18 +84,6 @@ __device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b
       "l"(a), "l"(b), "r"(kIdesc), "r"(acc));
 }
 
-__device__ __forceinline__ bool mbar_try(uint32_t mbar, uint32_t parity) {
-  uint32_t done;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}\n"
-      : "=r"(done)
-      : "r"(mbar), "r"(parity)
-      : "memory");
-  return done != 0;
-}
-
 // Bounded wait that also gives up once another role of the CTA aborted.  A
 // wait that runs out raises the abort flag and the timeout status bit.
 __device__ __forceinline__ bool wait_or_abort(uint32_t mbar, uint32_t parity, volatile int* abort_flag,
@@ -117,15 +103,6 @@ __device__ __forceinline__ bool wait_bounded(uint32_t mbar, uint32_t parity) {
   return false;
 }
 
-__device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(mbar), "r"(count));
-}
-__device__ __forceinline__ void mbar_expect_tx(uint32_t mbar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(mbar), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(mbar) : "memory");
-}
 // One K-half box (128 rows x 64 bf16) of part `part` at row `row`, K offset
 // `k0` (0 or 64: k0 x 2 bytes is a multiple of 16).
 __device__ __forceinline__ void tma_load_half(uint32_t sdst, const CUtensorMap* map, int k0, int row, int part,
@@ -197,7 +174,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       mbar_init(smem_u32(&bar_afull[b]), 1);
       mbar_init(smem_u32(&bar_aempty[b]), kEpiWarps);
     }
-    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    mbar_init_fence();
   }
   // tensor memory: two FP32 accumulators of 128 columns (128 lanes = rows)
   if (warp == 1) {
