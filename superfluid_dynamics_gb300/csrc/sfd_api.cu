@@ -207,6 +207,8 @@ int enqueue_sums(sfd_engine* e, int prec, const double* weights, const float2* w
             (mode == 0 && e->rslot) ? e->bnorm : nullptr, make_gate(e, gate),
             e->d_f32_work, e->f32_part, e->f32_wsum, e->f32_count};
   if (prec == SFD_PREC_F32 && e->d_f32_work) {
+    // node data staged before the wait unless the preceding kernel wrote them
+    A.prefetch = (gate < 0 && !e->node_written && sfd_sums_prefetch_enabled()) ? 1 : 0;
     LAUNCHC(e, gate >= 0 ? SFD_K_EXTRA : SFD_K_SUMS32, sfd_launch_sums_f32(A, e->nf32, e->f32_max_per, e->stream));
     return 0;
   }
@@ -251,6 +253,7 @@ int enqueue_gemv_gated(sfd_engine* e, const float* vf, double* y, float2* ydf, d
   } else
     LAUNCHC(e, cls, sfd_launch(k_gemv, dim3(e->ngemv), dim3(256), e->max_np * sizeof(float), e->stream, true,
                                       e->d_surf, e->d_gemv_rows, e->m32, vf, y, ydf, acc, accdf, G));
+  e->node_written = false;  // node data are at least two kernels back from the next pass
   return 0;
 }
 int enqueue_gemv(sfd_engine* e, const float* vf, double* y, float2* ydf, double* acc, float2* accdf,
@@ -381,6 +384,7 @@ int enqueue_solve(sfd_engine* e, const double* st, const double* phi_im, bool re
   }
   LAUNCHC(e, SFD_K_NODE, sfd_launch(k_node_prep, dim3(blocks_for(nt, 32)), dim3(64), 0, e->stream, true, e->d_surf,
                                     e->d_node_surf, nt, x, y, e->zp, e->zpp, e->nd, e->rslot, e->bnorm));
+  e->node_written = true;  // the next boundary-sum pass stages them only after its wait
   const int extra = extra_iters(e);
   if (e->opt.precision == SFD_PRECISION_FP64) {
     LAUNCHC(e, SFD_K_ASSEMBLE, sfd_launch_assemble64(e->d_surf, e->d_asm_tiles, e->nasm, e->nd.w, e->nd.p, e->zp, e->nd.mdiag,
@@ -896,6 +900,13 @@ int sfd_internal_rhs_ex(sfd_engine* e, const double* st, double* out, bool refac
   return enqueue_rhs(e, st, out, refactor);
 }
 int sfd_internal_bg_flush(sfd_engine* e) { return bg_flush(e); }
+bool sfd_sums_prefetch_enabled() {
+  static const bool on = [] {
+    const char* v = std::getenv("SFD_SUMS_PREFETCH");
+    return !(v && v[0] == '0');
+  }();
+  return on;
+}
 bool sfd_gemv_prefetch_enabled() {
   static const bool on = [] {
     const char* v = std::getenv("SFD_GEMV_PREFETCH");

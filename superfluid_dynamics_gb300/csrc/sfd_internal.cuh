@@ -127,6 +127,7 @@ struct sfd_engine {
   int gemv_spw = 0;          // streamed product (one surface): row slots per warp, 0 = register-pipelined
   int gemv_smem = 0;         // its dynamic shared memory
   bool m16_written = false;  // the last kernel enqueued wrote m16: the next product may not prefetch it
+  bool node_written = false; // node data written since the last product: FP32 passes may not prefetch them
   float *pbuf = nullptr, *rbuf = nullptr, *cbuf = nullptr;
   __nv_bfloat16 *cparts = nullptr, *rparts = nullptr;  // tensor-core operands: 3 bf16 parts, panel_elems apart
   // TMA tensor maps of cparts / rparts (opaque 128-byte descriptors) and the
@@ -220,6 +221,9 @@ int sfd_gemv_stream_cap();
 // Whether the streamed product requests its first rows before waiting on its
 // predecessor (SFD_GEMV_PREFETCH=0: never; read once).
 bool sfd_gemv_prefetch_enabled();
+// Whether the FP32 boundary-sum passes stage the node data before waiting on
+// their predecessor (SFD_SUMS_PREFETCH=0: never; read once).
+bool sfd_sums_prefetch_enabled();
 // Switch in a pending background preconditioner rebuild now (not allowed
 // while the engine stream is being captured).
 int sfd_internal_bg_flush(sfd_engine* e);

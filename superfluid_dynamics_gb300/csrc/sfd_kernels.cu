@@ -721,13 +721,12 @@ struct __align__(16) F32Epi {
   cd zp;     // z'
   double a, md, b;  // weight, M diagonal, phi' (first pass) or r (correction)
   double pad;
+  cd c, d;   // corrections: the accumulated C and D
 };
 
 __global__ void __launch_bounds__(kF32Threads, 8) k_sums_f32(SumArgs A) {
-  sfd_pdl_begin();
-  const F32Work wk = A.swork[blockIdx.x];
+  const F32Work wk = A.swork[blockIdx.x];  // written once at set-up
   const int sidx = wk.sidx, t0 = wk.t0;
-  if (!gate_open(A.gate, sidx)) return;  // every slice of the tile skips together
   const int n = wk.n, off = wk.off;
   const bool image = wk.image != 0;
   const int per = (n + wk.nsl - 1) / wk.nsl;
@@ -737,6 +736,20 @@ __global__ void __launch_bounds__(kF32Threads, 8) k_sums_f32(SumArgs A) {
   __shared__ df wred[kF32Groups];
   __shared__ int last;
   const int tid = threadIdx.x, lane = tid & 31, grp = tid >> 5;
+  const int tk0 = t0 + lane, tk1 = t0 + 32 + lane;
+  float T0[6], T1[6];
+  // The node data (w, p) do not change during the solve: where the preceding
+  // kernel does not write them, they are staged and the targets loaded
+  // before the wait on that kernel, so they arrive while it finishes.
+  const bool pre = A.prefetch && !A.gate.slot;
+  if (pre) {
+    for (int jj = tid; jj < jn; jj += kF32Threads) cp_async16(&f32_src[2 * jj], A.wdf + off + j_lo + jj);
+    cp_async_commit();
+    load_target(A, off + (tk0 < n ? tk0 : 0), image, T0);
+    load_target(A, off + (tk1 < n ? tk1 : 0), image, T1);
+  }
+  sfd_pdl_begin();
+  if (!gate_open(A.gate, sidx)) return;  // every slice of the tile skips together
 
   // ---- stage this slice's sources and its weight sum
   df wpart{0.f, 0.f};
@@ -745,7 +758,7 @@ __global__ void __launch_bounds__(kF32Threads, 8) k_sums_f32(SumArgs A) {
     const float2 ad = A.adf[g];
     const float4 p = image ? A.pdf[g] : make_float4(0.f, 0.f, 0.f, 0.f);
     wpart = df_add(wpart, df{ad.x, ad.y});
-    f32_src[2 * jj] = A.wdf[g];
+    if (!pre) f32_src[2 * jj] = A.wdf[g];
     f32_src[2 * jj + 1] = make_float4(ad.x, p.x, p.z, 0.f);
   }
   for (int o = 16; o > 0; o >>= 1)
@@ -753,10 +766,11 @@ __global__ void __launch_bounds__(kF32Threads, 8) k_sums_f32(SumArgs A) {
   if (lane == 0) wred[grp] = wpart;
 
   // ---- targets t0 + lane and t0 + 32 + lane
-  const int tk0 = t0 + lane, tk1 = t0 + 32 + lane;
-  float T0[6], T1[6];
-  load_target(A, off + (tk0 < n ? tk0 : 0), image, T0);
-  load_target(A, off + (tk1 < n ? tk1 : 0), image, T1);
+  if (!pre) {
+    load_target(A, off + (tk0 < n ? tk0 : 0), image, T0);
+    load_target(A, off + (tk1 < n ? tk1 : 0), image, T1);
+  }
+  if (pre) cp_async_wait_all();  // this thread's staged w; the barrier publishes them
   __syncthreads();
   // only the sources of the tile's own nodes need the j == k test
   int lo = jn, hi = jn;
@@ -821,6 +835,10 @@ __global__ void __launch_bounds__(kF32Threads, 8) k_sums_f32(SumArgs A) {
     cp_async8(&E.a, A.a + ge);
     cp_async8(&E.md, A.mdiag + ge);
     cp_async8(&E.b, (A.mode == 0 ? A.phip : A.r) + ge);
+    if (A.mode != 0) {
+      cp_async16(&E.c, A.cacc + ge);
+      if (image) cp_async16(&E.d, A.dacc + ge);
+    }
     cp_async_commit();
   }
   df sr{0.f, 0.f}, si{0.f, 0.f}, tr{0.f, 0.f}, ti{0.f, 0.f}, aw{0.f, 0.f};
@@ -887,10 +905,10 @@ __global__ void __launch_bounds__(kF32Threads, 8) k_sums_f32(SumArgs A) {
       if (image) A.dacc[g] = cd{(double)Dr, (double)Di};
       rnew = eb - (double)ma;
     } else {
-      const cd c = A.cacc[g];
+      const cd c = E.c;
       A.cacc[g] = cd{c.re + (double)Cr, c.im + (double)Ci};
       if (image) {
-        const cd d = A.dacc[g];
+        const cd d = E.d;
         A.dacc[g] = cd{d.re + (double)Dr, d.im + (double)Di};
       }
       rnew = eb - (double)ma;

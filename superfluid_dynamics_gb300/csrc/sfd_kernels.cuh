@@ -52,6 +52,10 @@ struct SumArgs {
   float4* spart;        // per work entry: 64 target partials (S re, S im, T re, T im)
   float2* swsum;        // per work entry: weight-sum partial (double-float)
   unsigned int* scount; // per item: slices finished (the last one resets it)
+  // k_sums_f32, ungated: stage the node data (w, p: written by the node kernel
+  // at the start of the evaluation) before the wait on the preceding kernel.
+  // Only where that kernel is not the one that writes them.
+  int prefetch;
 };
 
 // One CTA of the FP32 pass: everything it needs before its first source
