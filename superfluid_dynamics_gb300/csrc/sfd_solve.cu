@@ -1007,10 +1007,13 @@ __global__ void __launch_bounds__(512) k_gemv_h(const SurfaceDesc* surf, const i
 // grid * i; CTA row i belongs to warp i % 8, and each warp owns `spw` row
 // slots: it keeps up to spw whole rows of its own in flight as bulk copies
 // (cp.async.bulk, one mbarrier per slot) and refills a slot with its next row
-// as soon as it has consumed the row in it.  At N = 4096 that is 24 rows
-// (192 KB) in flight per SM, against the 2 KB per warp that the
-// register-pipelined k_gemv_h keeps: the product is bound by L2 / DRAM
-// bandwidth instead of by load latency.  The arithmetic is k_gemv_h's entry
+// as soon as it has consumed the row in it.  At N = 4096 with the default two
+// slots that is 16 rows (128 KB) in flight per SM, against the 2 KB per warp
+// that the register-pipelined k_gemv_h keeps.  Stand-alone it is not faster
+// (the copies arrive at about 2 TB/s from DRAM); its gain in the step comes
+// from requesting the first rows before the wait on the preceding kernel
+// (prefetch below), which a register pipeline can only do for one small
+// batch.  The arithmetic is k_gemv_h's entry
 // for entry (each lane's chunks in the same order, the same two accumulators,
 // the same reduction), so both give the same bits.  A slot is only ever waited
 // on and refilled by its own warp, so a wait is never more than one phase
