@@ -467,7 +467,7 @@ def run_ours(args, rank, world, local_rank):
     prec = sfd.PRECISION_MIXED if args.precision == "mixed" else sfd.PRECISION_FP64
     opts = sfd.Options(precision=prec, refine_iters=args.refine_iters, refactor_every=args.refactor_every,
                        pre_iters=args.pre_iters, device=local_rank, precond_half=not args.precond_fp32,
-                       refactor_lag=args.refactor_lag)
+                       refactor_lag=args.refactor_lag, extra_iters=args.extra_iters)
     eng = sfd.Engine(args.n, sfd.WaterBoundaryProblem(), opts)
     stream = torch.cuda.Stream(device=dev)
     eng.set_stream(stream.cuda_stream)
@@ -830,7 +830,7 @@ def run_profile_window(args, local_rank):
     s = workloads.random_modes(args.n, seed=2)
     opts = sfd.Options(precision=sfd.PRECISION_MIXED, refine_iters=args.refine_iters,
                        refactor_every=args.refactor_every, pre_iters=args.pre_iters, device=local_rank,
-                       refactor_lag=args.refactor_lag)
+                       refactor_lag=args.refactor_lag, extra_iters=args.extra_iters)
     with sfd.Engine(args.n, sfd.WaterBoundaryProblem(), opts) as eng:
         eng.set_state(s.x, s.y, s.phi)
         eng.step(DT, 60)
@@ -855,6 +855,8 @@ def main():
     ap.add_argument("--refine-iters", type=int, default=2)
     ap.add_argument("--pre-iters", type=int, default=2)
     ap.add_argument("--refactor-every", type=int, default=50)
+    ap.add_argument("--extra-iters", type=int, default=2,
+                    help="gated extra corrections of each solve (run only above the residual tolerance)")
     ap.add_argument("--refactor-lag", type=int, default=8,
                     help="rebuild the preconditioner on a side stream and switch to it this many steps later")
     ap.add_argument("--no-cpu", action="store_true")
