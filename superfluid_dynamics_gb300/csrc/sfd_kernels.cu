@@ -687,6 +687,71 @@ __device__ __forceinline__ void f32_slice_loop(const float4* src, int jn, int gr
   acc1 = make_float4(sr.y, si.y, tr.y, ti.y);
 }
 
+// Water (no image sums): the sources of a slice are staged in pairs (2m,
+// 2m + 1) as {w.re hi, w.re hi', w.re lo, w.re lo'}, {w.im hi, w.im hi',
+// w.im lo, w.im lo'} and {a, a'}, so one FP32x2 instruction works on two
+// sources of one target with register pairs straight from the shared-memory
+// loads (no per-source broadcasts), and the target's values are broadcast
+// once, outside the loop.  Pairs holding a node of the tile itself take the
+// per-source path with the j == k test.  The imaginary part is accumulated
+// negated (exact) and the lanes summed at the end.
+struct F32Tgt2 {
+  float2 rh, rl, ih, il;  // the target's w parts, broadcast to both lanes
+};
+__device__ __forceinline__ void f32_pair_src2(const F32Tgt2& T, float4 A, float4 B, float2 a, float2& sr,
+                                              float2& sin) {
+  const float2 dr = add2(sub2(T.rh, make_float2(A.x, A.y)), sub2(T.rl, make_float2(A.z, A.w)));
+  const float2 di = add2(sub2(T.ih, make_float2(B.x, B.y)), sub2(T.il, make_float2(B.z, B.w)));
+  const float2 d2 = fma2(dr, dr, mul2(di, di));
+  const float2 inv = mul2(a, make_float2(rcp_approx(d2.x), rcp_approx(d2.y)));
+  sr = fma2(inv, dr, sr);
+  sin = fma2(inv, di, sin);
+}
+__device__ __forceinline__ void f32_water_pairs(const float4* P0, const float4* P1, const float2* P2, int npairs,
+                                                int grp, int plo, int phi, int jn, int self0, int self1,
+                                                const float (&T0)[6], const float (&T1)[6], float4& acc0,
+                                                float4& acc1) {
+  auto first = [&](int a) { return a + ((grp - a) % kF32Groups + kF32Groups) % kF32Groups; };
+  const F32Tgt2 U0{{T0[0], T0[0]}, {T0[1], T0[1]}, {T0[2], T0[2]}, {T0[3], T0[3]}};
+  const F32Tgt2 U1{{T1[0], T1[0]}, {T1[1], T1[1]}, {T1[2], T1[2]}, {T1[3], T1[3]}};
+  // the per-source path reads the targets from the broadcast pairs' first lanes
+  const float V0[6] = {U0.rh.x, U0.rl.x, U0.ih.x, U0.il.x, 0.f, 0.f};
+  const float V1[6] = {U1.rh.x, U1.rl.x, U1.ih.x, U1.il.x, 0.f, 0.f};
+  float2 sr0 = {0.f, 0.f}, si0 = sr0, sr1 = sr0, si1 = sr0;
+  int m = grp;
+#pragma unroll 2
+  for (; m < plo; m += kF32Groups) {
+    const float4 A = P0[m], B = P1[m];
+    const float2 a = P2[m];
+    f32_pair_src2(U0, A, B, a, sr0, si0);
+    f32_pair_src2(U1, A, B, a, sr1, si1);
+  }
+  // pairs holding a node of the tile: per source, j == k skipped per target
+  for (m = first(plo); m < phi; m += kF32Groups) {
+    const float4 A = P0[m], B = P1[m];
+    const float2 a = P2[m];
+    for (int e = 0; e < 2; ++e) {
+      const int jj = 2 * m + e;
+      if (jj >= jn) break;
+      const float4 s0 = e ? make_float4(A.y, A.w, B.y, B.w) : make_float4(A.x, A.z, B.x, B.z);
+      const float aj = e ? a.y : a.x;
+      if (jj != self0) f32_s(V0, s0, aj, acc0);
+      if (jj != self1) f32_s(V1, s0, aj, acc1);
+    }
+  }
+#pragma unroll 2
+  for (m = first(phi); m < npairs; m += kF32Groups) {
+    const float4 A = P0[m], B = P1[m];
+    const float2 a = P2[m];
+    f32_pair_src2(U0, A, B, a, sr0, si0);
+    f32_pair_src2(U1, A, B, a, sr1, si1);
+  }
+  acc0.x += sr0.x + sr0.y;
+  acc0.y -= si0.x + si0.y;
+  acc1.x += sr1.x + sr1.y;
+  acc1.y -= si1.x + si1.y;
+}
+
 __device__ __forceinline__ void load_target(const SumArgs& A, int g, bool image, float (&T)[6]) {
   const float4 w = A.wdf[g];
   T[0] = w.x; T[1] = w.y; T[2] = w.z; T[3] = w.w;
@@ -724,7 +789,7 @@ struct __align__(16) F32Epi {
   cd c, d;   // corrections: the accumulated C and D
 };
 
-__global__ void __launch_bounds__(kF32Threads, 8) k_sums_f32(SumArgs A) {
+__global__ void __launch_bounds__(kF32Threads, 7) k_sums_f32(SumArgs A) {
   const F32Work wk = A.swork[blockIdx.x];  // written once at set-up
   const int sidx = wk.sidx, t0 = wk.t0;
   const int n = wk.n, off = wk.off;
@@ -742,9 +807,28 @@ __global__ void __launch_bounds__(kF32Threads, 8) k_sums_f32(SumArgs A) {
   // kernel does not write them, they are staged and the targets loaded
   // before the wait on that kernel, so they arrive while it finishes.
   const bool pre = A.prefetch && !A.gate.slot;
+  // water: sources in pairs (P0, P1: w parts; P2: weights), see f32_water_pairs;
+  // the second source of an odd slice's last pair is a far node of weight 0
+  const int npairs = (jn + 1) >> 1;
+  float4* P0 = f32_src;
+  float4* P1 = f32_src + npairs;
+  float2* P2 = reinterpret_cast<float2*>(f32_src + 2 * npairs);
+  auto stage_w_pairs = [&] {
+    for (int m = tid; m < npairs; m += kF32Threads) {
+      const int g = off + j_lo + 2 * m;
+      const float4 w0 = A.wdf[g];
+      const float4 w1 = 2 * m + 1 < jn ? A.wdf[g + 1] : make_float4(1e4f, 0.f, 0.f, 0.f);
+      P0[m] = make_float4(w0.x, w1.x, w0.y, w1.y);
+      P1[m] = make_float4(w0.z, w1.z, w0.w, w1.w);
+    }
+  };
   if (pre) {
-    for (int jj = tid; jj < jn; jj += kF32Threads) cp_async16(&f32_src[2 * jj], A.wdf + off + j_lo + jj);
-    cp_async_commit();
+    if (image) {
+      for (int jj = tid; jj < jn; jj += kF32Threads) cp_async16(&f32_src[2 * jj], A.wdf + off + j_lo + jj);
+      cp_async_commit();
+    } else {
+      stage_w_pairs();
+    }
     load_target(A, off + (tk0 < n ? tk0 : 0), image, T0);
     load_target(A, off + (tk1 < n ? tk1 : 0), image, T1);
   }
@@ -753,13 +837,25 @@ __global__ void __launch_bounds__(kF32Threads, 8) k_sums_f32(SumArgs A) {
 
   // ---- stage this slice's sources and its weight sum
   df wpart{0.f, 0.f};
-  for (int jj = tid; jj < jn; jj += kF32Threads) {
-    const int g = off + j_lo + jj;
-    const float2 ad = A.adf[g];
-    const float4 p = image ? A.pdf[g] : make_float4(0.f, 0.f, 0.f, 0.f);
-    wpart = df_add(wpart, df{ad.x, ad.y});
-    if (!pre) f32_src[2 * jj] = A.wdf[g];
-    f32_src[2 * jj + 1] = make_float4(ad.x, p.x, p.z, 0.f);
+  if (image) {
+    for (int jj = tid; jj < jn; jj += kF32Threads) {
+      const int g = off + j_lo + jj;
+      const float2 ad = A.adf[g];
+      const float4 p = A.pdf[g];
+      wpart = df_add(wpart, df{ad.x, ad.y});
+      if (!pre) f32_src[2 * jj] = A.wdf[g];
+      f32_src[2 * jj + 1] = make_float4(ad.x, p.x, p.z, 0.f);
+    }
+  } else {
+    if (!pre) stage_w_pairs();
+    for (int m = tid; m < npairs; m += kF32Threads) {
+      const int g = off + j_lo + 2 * m;
+      const float2 a0 = A.adf[g];
+      const float2 a1 = 2 * m + 1 < jn ? A.adf[g + 1] : make_float2(0.f, 0.f);
+      wpart = df_add(wpart, df{a0.x, a0.y});
+      wpart = df_add(wpart, df{a1.x, a1.y});
+      P2[m] = make_float2(a0.x, a1.x);
+    }
   }
   for (int o = 16; o > 0; o >>= 1)
     wpart = df_add(wpart, df{__shfl_xor_sync(0xffffffffu, wpart.hi, o), __shfl_xor_sync(0xffffffffu, wpart.lo, o)});
@@ -781,7 +877,7 @@ __global__ void __launch_bounds__(kF32Threads, 8) k_sums_f32(SumArgs A) {
   const int self0 = tk0 < n ? tk0 - j_lo : -1, self1 = tk1 < n ? tk1 - j_lo : -1;
   float4 acc0 = make_float4(0.f, 0.f, 0.f, 0.f), acc1 = acc0;
   if (image) f32_slice_loop<true>(f32_src, jn, grp, lo, hi, self0, self1, T0, T1, acc0, acc1);
-  else f32_slice_loop<false>(f32_src, jn, grp, lo, hi, self0, self1, T0, T1, acc0, acc1);
+  else f32_water_pairs(P0, P1, P2, npairs, grp, lo >> 1, (hi + 1) >> 1, jn, self0, self1, T0, T1, acc0, acc1);
   red[grp][lane] = acc0;
   red[grp][32 + lane] = acc1;
   __syncthreads();
@@ -934,7 +1030,10 @@ __global__ void __launch_bounds__(kF32Threads, 8) k_sums_f32(SumArgs A) {
   if (A.bnorm) warp_max_to(bv, A.bnorm + sidx);
 }
 
-static size_t f32_smem(int max_per) { return (size_t)std::max(1, max_per) * 2 * sizeof(float4); }
+// two float4 per source (image layout), or per pair of sources two float4
+// and one float2 (water layout: 40 bytes per pair, at most 32 per source
+// from two sources on, plus the slack of a one-source slice)
+static size_t f32_smem(int max_per) { return (size_t)std::max(1, max_per) * 2 * sizeof(float4) + 16; }
 
 cudaError_t sfd_f32_ctas_per_sm(int max_per, int* ctas) {
   const size_t smem = f32_smem(max_per);
