@@ -789,6 +789,8 @@ struct __align__(16) F32Epi {
   cd c, d;   // corrections: the accumulated C and D
 };
 
+// 72 registers (7 CTAs per SM): the water pair loop spills under 64, and the
+// 1024 CTAs of N = 4096 still fit one wave on 152 SMs.
 __global__ void __launch_bounds__(kF32Threads, 7) k_sums_f32(SumArgs A) {
   const F32Work wk = A.swork[blockIdx.x];  // written once at set-up
   const int sidx = wk.sidx, t0 = wk.t0;
